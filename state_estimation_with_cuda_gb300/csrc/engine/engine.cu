@@ -1,0 +1,794 @@
+#include "engine.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace sle_gb300 {
+
+cudaError_t launch_gain_export(const DevNet& net, const DevFactor& f, const DevWork& w, int32_t n_tgt, double* out,
+                               cudaStream_t st);
+
+namespace {
+
+// Sub-allocates one device arena with 256-byte alignment.
+struct Carver {
+    char* base;
+    size_t off = 0;
+    explicit Carver(void* b) : base(static_cast<char*>(b)) {}
+    template <typename T>
+    T* take(size_t n) {
+        off = (off + 255) & ~static_cast<size_t>(255);
+        T* p = reinterpret_cast<T*>(base + off);
+        off += std::max<size_t>(n, 1) * sizeof(T);
+        return p;
+    }
+};
+
+template <typename T>
+cudaError_t put(T* dst, const std::vector<T>& src, cudaStream_t st) {
+    if (src.empty()) return cudaSuccess;
+    return cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+inline int nblk(int n) { return (n + 255) / 256; }
+
+}  // namespace
+
+Engine::~Engine() {
+    release_device();
+    if (st_) cudaStreamDestroy(st_);
+    if (ev0_) cudaEventDestroy(ev0_);
+    if (ev1_) cudaEventDestroy(ev1_);
+    if (h_status_) cudaFreeHost(h_status_);
+    if (h_stage_) cudaFreeHost(h_stage_);
+    if (d_slots_) cudaFree(d_slots_);
+    if (d_scratch_) cudaFree(d_scratch_);
+    if (tm0_) cudaEventDestroy(tm0_);
+    if (tm1_) cudaEventDestroy(tm1_);
+    for (cudaEvent_t e : ev_pool_) cudaEventDestroy(e);
+}
+
+void Engine::release_device() {
+    if (d_slots_) cudaFree(d_slots_);
+    d_slots_ = nullptr;
+    n_slots_ = 0;
+    if (arena_) cudaFree(arena_);
+    arena_ = nullptr;
+    arena_bytes_ = 0;
+    uploaded_ = false;
+    factor_valid_ = false;
+}
+
+int32_t Engine::set_cuda_error(cudaError_t e, const char* where) {
+    last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return -3;
+}
+
+std::string Engine::device_info() {
+    cudaDeviceProp p{};
+    if (cudaGetDeviceProperties(&p, cfg.device_id) != cudaSuccess) return "no CUDA device";
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s (sm_%d%d, %d SMs, %.1f GiB)", p.name, p.major, p.minor, p.multiProcessorCount,
+             static_cast<double>(p.totalGlobalMem) / (1024.0 * 1024.0 * 1024.0));
+    return buf;
+}
+
+int32_t Engine::initialize() {
+    if (init_) return 0;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        last_error = "no CUDA device available";
+        return -3;
+    }
+    if (cfg.device_id < 0 || cfg.device_id >= n) {
+        last_error = "device_id out of range";
+        return -4;
+    }
+    if ((e = cudaSetDevice(cfg.device_id)) != cudaSuccess) return set_cuda_error(e, "cudaSetDevice");
+    if ((e = cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking)) != cudaSuccess) return set_cuda_error(e, "stream");
+    cudaEventCreate(&ev0_);
+    cudaEventCreate(&ev1_);
+    if ((e = cudaMallocHost(&h_status_, sizeof(DevStatus))) != cudaSuccess) return set_cuda_error(e, "cudaMallocHost");
+    init_ = true;
+    return 0;
+}
+
+int32_t Engine::analyze() {
+    std::string err;
+    if (!model.validate(err)) {
+        last_error = err;
+        return -5;
+    }
+    Topology t;
+    t.n_bus = model.n_bus();
+    t.n_branch = model.n_branch();
+    t.n_meas = model.n_meas();
+    t.slack = model.slack;
+    t.br_from = model.br_from.data();
+    t.br_to = model.br_to.data();
+    t.br_closed = model.br_closed.data();
+    t.m_type = model.m_type.data();
+    t.m_loc = model.m_loc.data();
+    t.m_end = model.m_end.data();
+    t.m_active = model.m_active.data();
+    SymbolicParams sp;
+    sp.ordering = cfg.ordering;
+    if (!build_plan(t, sp, plan_, err)) {
+        last_error = "symbolic analysis: " + err;
+        analyzed_ = false;
+        return -5;
+    }
+    analyzed_ = true;
+    return 0;
+}
+
+int32_t Engine::upload() {
+    int32_t rc = initialize();
+    if (rc) return rc;
+    cudaSetDevice(cfg.device_id);
+    // keep the hot-start state across re-uploads
+    if (uploaded_) download_results();
+    rc = analyze();
+    if (rc) return rc;
+    const int32_t n = model.n_bus(), nbr = model.n_branch(), m = model.n_meas();
+    const Plan& P = plan_;
+    // level schedule
+    sch_small_ptr_.assign(P.n_levels + 1, 0);
+    sch_big_ptr_.assign(P.n_levels + 1, 0);
+    sch_all_ptr_.assign(P.n_levels + 1, 0);
+    sch_small_.clear();
+    sch_big_.clear();
+    sch_all_.clear();
+    sch_maxf_.assign(P.n_levels, 0);
+    big_off_.assign(P.n_super + 1, -1);
+    int64_t big_total = 0;
+    int32_t max_small = 1;
+    for (int32_t l = 0; l < P.n_levels; ++l) {
+        for (int32_t x = P.lvl_ptr[l]; x < P.lvl_ptr[l + 1]; ++x) {
+            const int32_t s = P.lvl_sn[x];
+            const int32_t f = P.sn_f[s];
+            sch_all_.push_back(s);
+            sch_maxf_[l] = std::max(sch_maxf_[l], f);
+            if (f <= kSmallFrontMax) {
+                sch_small_.push_back(s);
+                max_small = std::max(max_small, f);
+            } else {
+                sch_big_.push_back(s);
+                big_off_[s] = big_total;
+                big_total += static_cast<int64_t>(f) * f;
+            }
+        }
+        sch_small_ptr_[l + 1] = static_cast<int32_t>(sch_small_.size());
+        sch_big_ptr_[l + 1] = static_cast<int32_t>(sch_big_.size());
+        sch_all_ptr_[l + 1] = static_cast<int32_t>(sch_all_.size());
+    }
+    const int64_t nnz_h = static_cast<int64_t>(P.h_col.size());
+    const int64_t nnz_y = static_cast<int64_t>(P.y_col.size());
+    const int32_t ns = P.n_super;
+    const int32_t nparts = std::max(nblk(std::max(m, 1)), nblk(n)) + 1;
+
+    auto layout = [&](Carver& c) {
+        // network
+        net_.bus_type = c.take<int32_t>(n);
+        net_.v_setpoint = c.take<double>(n);
+        net_.br_from = c.take<int32_t>(nbr);
+        net_.br_to = c.take<int32_t>(nbr);
+        net_.br_r = c.take<double>(nbr);
+        net_.br_x = c.take<double>(nbr);
+        net_.br_bch = c.take<double>(nbr);
+        net_.br_tap = c.take<double>(nbr);
+        net_.br_shift = c.take<double>(nbr);
+        net_.br_closed = c.take<uint8_t>(nbr);
+        net_.br_g = c.take<double>(nbr);
+        net_.br_b = c.take<double>(nbr);
+        net_.br_bsf = c.take<double>(nbr);
+        net_.br_bst = c.take<double>(nbr);
+        net_.y_ptr = c.take<int32_t>(n + 1);
+        net_.y_col = c.take<int32_t>(nnz_y);
+        net_.y_src = c.take<int32_t>(nnz_y);
+        net_.y_g = c.take<double>(nnz_y);
+        net_.y_b = c.take<double>(nnz_y);
+        net_.y_hpos_t = c.take<int32_t>(nnz_y);
+        net_.y_hpos_v = c.take<int32_t>(nnz_y);
+        net_.m_type = c.take<int32_t>(m);
+        net_.m_loc = c.take<int32_t>(m);
+        net_.m_end = c.take<int32_t>(m);
+        net_.m_kind = c.take<int32_t>(m);
+        net_.m_fpos = c.take<int32_t>(m);
+        net_.m_active = c.take<uint8_t>(m);
+        net_.m_sigma = c.take<double>(m);
+        net_.m_w = c.take<double>(m);
+        net_.h_ptr = c.take<int32_t>(m + 1);
+        net_.h_row = c.take<int32_t>(nnz_h);
+        // factor plan
+        fac_.sn_c0 = c.take<int32_t>(ns + 1);
+        fac_.sn_f = c.take<int32_t>(ns);
+        fac_.sn_rows_off = c.take<int64_t>(ns + 1);
+        fac_.sn_rows = c.take<int32_t>(P.sn_rows.size());
+        fac_.sn_lx_off = c.take<int64_t>(ns + 1);
+        fac_.sn_u_off = c.take<int64_t>(ns + 1);
+        fac_.sn_su_off = c.take<int64_t>(ns + 1);
+        fac_.sn_child_ptr = c.take<int32_t>(ns + 1);
+        fac_.sn_child = c.take<int32_t>(P.sn_child.size());
+        fac_.sn_relmap = c.take<int32_t>(P.sn_relmap.size());
+        fac_.sn_tgt_ptr = c.take<int32_t>(ns + 1);
+        fac_.tgt_local = c.take<int32_t>(P.tgt_local.size());
+        fac_.tgt_pair_ptr = c.take<int64_t>(P.tgt_pair_ptr.size());
+        fac_.pair_a = c.take<int32_t>(P.pair_a.size());
+        fac_.pair_b = c.take<int32_t>(P.pair_b.size());
+        fac_.rhs_ptr = c.take<int32_t>(P.rhs_ptr.size());
+        fac_.rhs_h = c.take<int32_t>(P.rhs_h.size());
+        fac_.bus_ps_theta = c.take<int32_t>(n);
+        fac_.bus_ps_v = c.take<int32_t>(n);
+        fac_.sn_big_off = c.take<int64_t>(ns + 1);
+        d_small_ = c.take<int32_t>(sch_small_.size());
+        d_all_ = c.take<int32_t>(sch_all_.size());
+        // work
+        work_.v = c.take<double>(n);
+        work_.th = c.take<double>(n);
+        work_.z = c.take<double>(m);
+        work_.h = c.take<double>(m);
+        work_.r = c.take<double>(m);
+        work_.w_eff = c.take<double>(m);
+        work_.wr = c.take<double>(m);
+        work_.hval = c.take<double>(nnz_h);
+        work_.rhs = c.take<double>(P.n_state);
+        work_.sol = c.take<double>(P.n_state);
+        work_.lx = c.take<double>(P.lx_size);
+        work_.u = c.take<double>(P.u_size);
+        work_.su = c.take<double>(P.su_size);
+        work_.big = c.take<double>(big_total);
+        work_.p_inj = c.take<double>(n);
+        work_.q_inj = c.take<double>(n);
+        work_.pf = c.take<double>(nbr);
+        work_.qf = c.take<double>(nbr);
+        work_.pt = c.take<double>(nbr);
+        work_.qt = c.take<double>(nbr);
+        work_.part = c.take<double>(nparts);
+        work_.status = c.take<DevStatus>(1);
+    };
+    Carver dry(nullptr);
+    layout(dry);
+    const size_t need = dry.off + 256;
+    cudaError_t e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "stream sync");
+    release_device();
+    e = cudaMalloc(&arena_, need);
+    if (e != cudaSuccess) {
+        arena_ = nullptr;
+        last_error = "device allocation of " + std::to_string(need) + " bytes failed";
+        return -10;
+    }
+    arena_bytes_ = need;
+    Carver real(arena_);
+    layout(real);
+    net_.n_bus = n;
+    net_.n_branch = nbr;
+    net_.n_meas = m;
+    net_.n_state = P.n_state;
+    net_.slack = model.slack;
+    fac_.n_super = ns;
+    fac_.n_state = P.n_state;
+
+    std::vector<uint8_t> act(model.m_active);
+    std::vector<int32_t> btype(model.bus_type);
+    auto chk = [&](cudaError_t ee) { if (ee != cudaSuccess && e == cudaSuccess) e = ee; };
+    chk(put(const_cast<int32_t*>(net_.bus_type), model.bus_type, st_));
+    chk(put(const_cast<double*>(net_.v_setpoint), model.bus_vset, st_));
+    chk(put(const_cast<int32_t*>(net_.br_from), model.br_from, st_));
+    chk(put(const_cast<int32_t*>(net_.br_to), model.br_to, st_));
+    chk(put(const_cast<double*>(net_.br_r), model.br_r, st_));
+    chk(put(const_cast<double*>(net_.br_x), model.br_x, st_));
+    chk(put(const_cast<double*>(net_.br_bch), model.br_b, st_));
+    chk(put(const_cast<double*>(net_.br_tap), model.br_tap, st_));
+    chk(put(const_cast<double*>(net_.br_shift), model.br_shift, st_));
+    chk(put(const_cast<uint8_t*>(net_.br_closed), model.br_closed, st_));
+    chk(put(const_cast<int32_t*>(net_.y_ptr), P.y_ptr, st_));
+    chk(put(const_cast<int32_t*>(net_.y_col), P.y_col, st_));
+    chk(put(const_cast<int32_t*>(net_.y_src), P.y_src, st_));
+    chk(put(const_cast<int32_t*>(net_.y_hpos_t), P.y_hpos_t, st_));
+    chk(put(const_cast<int32_t*>(net_.y_hpos_v), P.y_hpos_v, st_));
+    chk(put(const_cast<int32_t*>(net_.m_type), model.m_type, st_));
+    chk(put(const_cast<int32_t*>(net_.m_loc), model.m_loc, st_));
+    chk(put(const_cast<int32_t*>(net_.m_end), model.m_end, st_));
+    chk(put(const_cast<int32_t*>(net_.m_kind), P.m_kind, st_));
+    chk(put(const_cast<int32_t*>(net_.m_fpos), P.m_fpos, st_));
+    chk(put(const_cast<uint8_t*>(net_.m_active), model.m_active, st_));
+    chk(put(const_cast<double*>(net_.m_sigma), model.m_sigma, st_));
+    chk(put(const_cast<double*>(net_.m_w), model.m_w, st_));
+    chk(put(const_cast<int32_t*>(net_.h_ptr), P.h_ptr, st_));
+    chk(put(const_cast<int32_t*>(net_.h_row), P.h_row, st_));
+    chk(put(const_cast<int32_t*>(fac_.sn_c0), P.sn_c0, st_));
+    chk(put(const_cast<int32_t*>(fac_.sn_f), P.sn_f, st_));
+    chk(put(const_cast<int64_t*>(fac_.sn_rows_off), P.sn_rows_off, st_));
+    chk(put(const_cast<int32_t*>(fac_.sn_rows), P.sn_rows, st_));
+    chk(put(const_cast<int64_t*>(fac_.sn_lx_off), P.sn_lx_off, st_));
+    chk(put(const_cast<int64_t*>(fac_.sn_u_off), P.sn_u_off, st_));
+    chk(put(const_cast<int64_t*>(fac_.sn_su_off), P.sn_su_off, st_));
+    chk(put(const_cast<int32_t*>(fac_.sn_child_ptr), P.sn_child_ptr, st_));
+    chk(put(const_cast<int32_t*>(fac_.sn_child), P.sn_child, st_));
+    chk(put(const_cast<int32_t*>(fac_.sn_relmap), P.sn_relmap, st_));
+    chk(put(const_cast<int32_t*>(fac_.sn_tgt_ptr), P.sn_tgt_ptr, st_));
+    chk(put(const_cast<int32_t*>(fac_.tgt_local), P.tgt_local, st_));
+    chk(put(const_cast<int64_t*>(fac_.tgt_pair_ptr), P.tgt_pair_ptr, st_));
+    chk(put(const_cast<int32_t*>(fac_.pair_a), P.pair_a, st_));
+    chk(put(const_cast<int32_t*>(fac_.pair_b), P.pair_b, st_));
+    chk(put(const_cast<int32_t*>(fac_.rhs_ptr), P.rhs_ptr, st_));
+    chk(put(const_cast<int32_t*>(fac_.rhs_h), P.rhs_h, st_));
+    chk(put(const_cast<int32_t*>(fac_.bus_ps_theta), P.bus_ps_theta, st_));
+    chk(put(const_cast<int32_t*>(fac_.bus_ps_v), P.bus_ps_v, st_));
+    chk(put(const_cast<int64_t*>(fac_.sn_big_off), big_off_, st_));
+    chk(put(d_small_, sch_small_, st_));
+    chk(put(d_all_, sch_all_, st_));
+    chk(put(work_.v, model.bus_v, st_));
+    chk(put(work_.th, model.bus_th, st_));
+    chk(put(work_.z, model.m_value, st_));
+    chk(cudaMemsetAsync(work_.status, 0, sizeof(DevStatus), st_));
+    chk(launch_admittance_and_ybus(net_, st_));
+    chk(cudaStreamSynchronize(st_));
+    if (e != cudaSuccess) return set_cuda_error(e, "upload");
+
+    sched_.n_levels = P.n_levels;
+    sched_.h_small_ptr = sch_small_ptr_.data();
+    sched_.d_small = d_small_;
+    sched_.h_big_ptr = sch_big_ptr_.data();
+    sched_.h_big = sch_big_.data();
+    sched_.h_all_ptr = sch_all_ptr_.data();
+    sched_.d_all = d_all_;
+    sched_.h_lvl_maxf = sch_maxf_.data();
+    sched_.h_sn_f = plan_.sn_f.data();
+    sched_.h_sn_c0 = plan_.sn_c0.data();
+    sched_.h_big_off = big_off_.data();
+    sched_.h_tgt_ptr = plan_.sn_tgt_ptr.data();
+    sched_.h_child_ptr = plan_.sn_child_ptr.data();
+    sched_.h_child = plan_.sn_child.data();
+    sched_.max_small_f = max_small;
+
+    if (h_stage_n_ < static_cast<size_t>(m)) {
+        if (h_stage_) cudaFreeHost(h_stage_);
+        h_stage_ = nullptr;
+        h_stage_n_ = 0;
+        if (cudaMallocHost(&h_stage_, std::max<size_t>(m, 1) * sizeof(double)) == cudaSuccess) h_stage_n_ = m;
+    }
+    p_inj.assign(n, 0.0);
+    q_inj.assign(n, 0.0);
+    pf.assign(nbr, 0.0);
+    qf.assign(nbr, 0.0);
+    pt.assign(nbr, 0.0);
+    qt.assign(nbr, 0.0);
+    uploaded_ = true;
+    factor_valid_ = false;
+    stale_ = 0;
+    model.structure_dirty = false;
+    model.values_dirty = false;
+    return 0;
+}
+
+int32_t Engine::update_telemetry(const double* z, int32_t count) {
+    if (count != model.n_meas()) {
+        last_error = "telemetry count does not match the measurement count";
+        return -4;
+    }
+    std::memcpy(model.m_value.data(), z, sizeof(double) * count);
+    if (!uploaded_ || model.structure_dirty) {
+        model.values_dirty = true;
+        return 0;
+    }
+    cudaError_t e;
+    if (h_stage_ && h_stage_n_ >= static_cast<size_t>(count)) {
+        // wait for the previous staged copy before overwriting the staging buffer
+        e = cudaStreamSynchronize(st_);
+        if (e != cudaSuccess) return set_cuda_error(e, "telemetry");
+        std::memcpy(h_stage_, z, sizeof(double) * count);
+        e = cudaMemcpyAsync(work_.z, h_stage_, sizeof(double) * count, cudaMemcpyHostToDevice, st_);
+    } else {
+        e = cudaMemcpyAsync(work_.z, z, sizeof(double) * count, cudaMemcpyHostToDevice, st_);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    }
+    if (e != cudaSuccess) return set_cuda_error(e, "telemetry");
+    model.values_dirty = false;
+    return 0;
+}
+
+int32_t Engine::sync_measurements() {
+    if (!uploaded_) return 0;
+    return update_telemetry(model.m_value.data(), model.n_meas());
+}
+
+int32_t Engine::flat_start() {
+    for (int32_t i = 0; i < model.n_bus(); ++i) {
+        const int32_t t = model.bus_type[i];
+        model.bus_v[i] = (t == 1 || t == 2) ? model.bus_vset[i] : 1.0;
+        model.bus_th[i] = 0.0;
+    }
+    if (!uploaded_) return 0;
+    cudaError_t e = launch_flat_start(net_, work_, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "flat start");
+    return 0;
+}
+
+SolveParams Engine::params(const SolveRequest& rq) const {
+    SolveParams sp{};
+    sp.exact_jacobian = cfg.exact_jacobian;
+    sp.robust = rq.robust;
+    sp.huber_gamma = rq.huber_gamma;
+    sp.tol = rq.tolerance;
+    sp.vmin = cfg.voltage_min_pu;
+    sp.vmax = cfg.voltage_max_pu;
+    return sp;
+}
+
+int32_t Engine::stage_begin(int32_t stage) {
+    if (!cfg.enable_profiling) return -1;
+    while (ev_pool_.size() < ev_used_ + 2) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        ev_pool_.push_back(e);
+    }
+    const int32_t mark = static_cast<int32_t>(ev_used_);
+    ev_used_ += 2;
+    cudaEventRecord(ev_pool_[mark], st_);
+    ev_marks_.push_back({stage, mark});
+    return mark;
+}
+
+void Engine::stage_end(int32_t stage, int32_t mark, int64_t launches_before) {
+    stats.launches[stage] += g_kernel_launches.load() - launches_before;
+    stats.calls[stage] += 1;
+    if (mark >= 0) cudaEventRecord(ev_pool_[mark + 1], st_);
+}
+
+void Engine::collect_stage_times() {
+    for (auto& m : ev_marks_) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, ev_pool_[m.second], ev_pool_[m.second + 1]) == cudaSuccess)
+            stats.ms[m.first] += ms;
+    }
+    ev_marks_.clear();
+    ev_used_ = 0;
+}
+
+int32_t Engine::run_iteration(const SolveParams& sp, bool refactor) {
+    cudaError_t e = cudaMemsetAsync(&work_.status->flags, 0, sizeof(uint32_t), st_);
+    int64_t l0 = g_kernel_launches.load();
+    int32_t mk = stage_begin(ST_EVALUATE);
+    if (e == cudaSuccess) e = launch_evaluate(net_, work_, sp, st_);
+    stage_end(ST_EVALUATE, mk, l0);
+    if (e == cudaSuccess && refactor) {
+        l0 = g_kernel_launches.load();
+        mk = stage_begin(ST_FACTOR);
+        e = launch_factor(net_, fac_, work_, sched_, st_);
+        stage_end(ST_FACTOR, mk, l0);
+    }
+    l0 = g_kernel_launches.load();
+    mk = stage_begin(ST_RHS);
+    if (e == cudaSuccess) e = launch_rhs(net_, fac_, work_, st_);
+    stage_end(ST_RHS, mk, l0);
+    l0 = g_kernel_launches.load();
+    mk = stage_begin(ST_SOLVE);
+    if (e == cudaSuccess) e = launch_solve(fac_, work_, sched_, st_);
+    stage_end(ST_SOLVE, mk, l0);
+    l0 = g_kernel_launches.load();
+    mk = stage_begin(ST_UPDATE);
+    if (e == cudaSuccess) e = launch_update(net_, fac_, work_, sp, st_);
+    stage_end(ST_UPDATE, mk, l0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_status_, work_.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    ++stats.iterations;
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "iteration");
+        return -3;
+    }
+    return 0;
+}
+
+int32_t Engine::solve(const SolveRequest& rq, SolveResult& out) {
+    out = SolveResult();
+    if (!init_ || !uploaded_ || model.structure_dirty) {
+        const int32_t rc = upload();
+        if (rc) {
+            out.status = CONV_NOTOBS;
+            last_ = out;
+            return rc;
+        }
+    }
+    cudaSetDevice(cfg.device_id);
+    if (model.values_dirty) {
+        const int32_t rc = sync_measurements();
+        if (rc) return rc;
+    }
+    const SolveParams sp = params(rq);
+    cudaEventRecord(ev0_, st_);
+    if (rq.flat_start) launch_flat_start(net_, work_, st_);
+    const int32_t max_iter = rq.max_iterations;
+    bool converged = false, diverged = false, retry = false;
+    int32_t retries = 0;
+    out.status = CONV_RUNNING;
+    do {
+        if (retry) {
+            launch_flat_start(net_, work_, st_);
+            converged = diverged = retry = false;
+            factor_valid_ = false;
+        }
+        for (int32_t it = 0; it < max_iter && !converged && !diverged; ++it) {
+            const bool refactor = !factor_valid_ || rq.robust || cfg.gain_policy == 0;
+            if (run_iteration(sp, refactor) != 0) {
+                out.status = CONV_SINGULAR;  // wls_solver.cu:296-300
+                diverged = true;
+                break;
+            }
+            const uint32_t fl = h_status_->flags;
+            if (fl & FLAG_SINGULAR) {
+                out.status = CONV_SINGULAR;
+                factor_valid_ = false;
+                diverged = true;
+                break;
+            }
+            if (refactor) factor_valid_ = true;
+            out.max_mismatch = h_status_->max_mismatch;
+            converged = (fl & FLAG_CONVERGED) != 0;
+            diverged = (fl & FLAG_NONFINITE) != 0;
+            out.iterations = it + 1;
+            if (rq.mode == Mode::REALTIME && rq.time_limit_ms > 0.0) {
+                cudaEventRecord(ev1_, st_);
+                cudaEventSynchronize(ev1_);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ev0_, ev1_);
+                if (ms > rq.time_limit_ms && !converged && !diverged) {
+                    out.status = CONV_MAXIT;
+                    break;
+                }
+            }
+        }
+        if (diverged && retries < 2 && rq.mode != Mode::REALTIME) {  // wls_solver.cu:326-332
+            retry = true;
+            ++retries;
+            out.iterations = 0;
+            if (out.status == CONV_RUNNING) {
+                // retry from a flat start
+            }
+        }
+    } while (retry);
+    if (out.status == CONV_RUNNING) out.status = converged ? CONV_OK : (diverged ? CONV_DIVERGED : CONV_MAXIT);
+    if (diverged) factor_valid_ = false;
+    // final evaluation at the returned state: objective, residuals, bad data
+    {
+        const int64_t l0 = g_kernel_launches.load();
+        const int32_t mk = stage_begin(ST_OTHER);
+        launch_evaluate(net_, work_, sp, st_);
+        launch_objective(net_, work_, cfg.bad_data_threshold, st_);
+        stage_end(ST_OTHER, mk, l0);
+    }
+    cudaEventRecord(ev1_, st_);
+    cudaMemcpyAsync(h_status_, work_.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st_);
+    cudaError_t e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "solve");
+        out.status = CONV_SINGULAR;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    out.time_ms = ms;
+    out.objective = h_status_->objective;
+    out.largest_residual = h_status_->largest_residual;
+    out.largest_idx = h_status_->largest_idx;
+    out.bad_count = h_status_->bad_count;
+    stale_ = DL_ALL;
+    last_ = out;
+    ++stats.solves;
+    collect_stage_times();
+    return 0;
+}
+
+int32_t Engine::download_results(int32_t what) {
+    what &= stale_;
+    if (!uploaded_ || !what) return 0;
+    const int32_t n = model.n_bus(), m = model.n_meas(), nbr = model.n_branch();
+    cudaError_t e = cudaSuccess;
+    auto get = [&](double* dst, const double* src, int32_t cnt) {
+        if (cnt > 0 && e == cudaSuccess) e = cudaMemcpyAsync(dst, src, sizeof(double) * cnt, cudaMemcpyDeviceToHost, st_);
+    };
+    if (what & DL_STATE) {
+        get(model.bus_v.data(), work_.v, n);
+        get(model.bus_th.data(), work_.th, n);
+    }
+    if (what & DL_MEAS) {
+        get(model.m_est.data(), work_.h, m);
+        get(model.m_res.data(), work_.r, m);
+    }
+    if (what & DL_FLOWS) {
+        e = launch_results(net_, work_, st_);
+        get(p_inj.data(), work_.p_inj, n);
+        get(q_inj.data(), work_.q_inj, n);
+        get(pf.data(), work_.pf, nbr);
+        get(qf.data(), work_.qf, nbr);
+        get(pt.data(), work_.pt, nbr);
+        get(qt.data(), work_.qt, nbr);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "download");
+    stale_ &= ~what;
+    return 0;
+}
+
+int32_t Engine::evaluate_at(const double* v, const double* th, int32_t exact) {
+    if (!uploaded_ || model.structure_dirty) {
+        const int32_t rc = upload();
+        if (rc) return rc;
+    }
+    if (model.values_dirty) sync_measurements();
+    const int32_t n = model.n_bus();
+    cudaError_t e = cudaMemcpyAsync(work_.v, v, sizeof(double) * n, cudaMemcpyHostToDevice, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(work_.th, th, sizeof(double) * n, cudaMemcpyHostToDevice, st_);
+    SolveParams sp{};
+    sp.exact_jacobian = exact;
+    sp.robust = 0;
+    sp.huber_gamma = cfg.huber_gamma;
+    sp.tol = cfg.convergence_tolerance;
+    sp.vmin = cfg.voltage_min_pu;
+    sp.vmax = cfg.voltage_max_pu;
+    if (e == cudaSuccess) e = launch_evaluate(net_, work_, sp, st_);
+    if (e == cudaSuccess) e = launch_objective(net_, work_, cfg.bad_data_threshold, st_);
+    if (e == cudaSuccess) e = launch_rhs(net_, fac_, work_, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "evaluate");
+    stale_ = DL_ALL;
+    factor_valid_ = false;
+    return 0;
+}
+
+int32_t Engine::export_gain(std::vector<int32_t>& rows, std::vector<int32_t>& cols, std::vector<double>& vals) {
+    const Plan& P = plan_;
+    const int32_t nt = static_cast<int32_t>(P.tgt_local.size());
+    double* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(double) * std::max(nt, 1));
+    if (e != cudaSuccess) return set_cuda_error(e, "export gain");
+    e = launch_gain_export(net_, fac_, work_, nt, d, st_);
+    vals.assign(nt, 0.0);
+    if (e == cudaSuccess && nt > 0) e = cudaMemcpyAsync(vals.data(), d, sizeof(double) * nt, cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    cudaFree(d);
+    if (e != cudaSuccess) return set_cuda_error(e, "export gain");
+    rows.resize(nt);
+    cols.resize(nt);
+    for (int32_t s = 0; s < P.n_super; ++s) {
+        const int32_t f = P.sn_f[s];
+        for (int32_t tg = P.sn_tgt_ptr[s]; tg < P.sn_tgt_ptr[s + 1]; ++tg) {
+            const int32_t lr = P.tgt_local[tg] % f, lc = P.tgt_local[tg] / f;
+            rows[tg] = P.state_of_ps[P.sn_rows[P.sn_rows_off[s] + lr]];
+            cols[tg] = P.state_of_ps[P.sn_c0[s] + lc];
+        }
+    }
+    return 0;
+}
+
+int32_t Engine::factor_and_solve(const double* rhs_orig, double* x_orig) {
+    const Plan& P = plan_;
+    std::vector<double> b(P.n_state);
+    for (int32_t p = 0; p < P.n_state; ++p) b[p] = rhs_orig[P.state_of_ps[p]];
+    cudaError_t e = cudaMemsetAsync(&work_.status->flags, 0, sizeof(uint32_t), st_);
+    if (e == cudaSuccess) e = launch_factor(net_, fac_, work_, sched_, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(work_.rhs, b.data(), sizeof(double) * P.n_state, cudaMemcpyHostToDevice, st_);
+    if (e == cudaSuccess) e = launch_solve(fac_, work_, sched_, st_);
+    std::vector<double> x(P.n_state);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(x.data(), work_.sol, sizeof(double) * P.n_state, cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_status_, work_.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "factor/solve");
+    for (int32_t p = 0; p < P.n_state; ++p) x_orig[P.state_of_ps[p]] = x[p];
+    factor_valid_ = false;
+    return (h_status_->flags & FLAG_SINGULAR) ? -7 : 0;
+}
+
+int32_t Engine::export_ybus(std::vector<double>& g, std::vector<double>& b) {
+    const size_t nnz = plan_.y_col.size();
+    g.assign(nnz, 0.0);
+    b.assign(nnz, 0.0);
+    cudaError_t e = cudaMemcpyAsync(g.data(), net_.y_g, sizeof(double) * nnz, cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b.data(), net_.y_b, sizeof(double) * nnz, cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "export ybus");
+    return 0;
+}
+
+int32_t Engine::export_eval(double* hval, double* hx, double* rhs_orig) {
+    const Plan& P = plan_;
+    std::vector<double> b(P.n_state);
+    cudaError_t e = cudaSuccess;
+    if (hval && !P.h_col.empty())
+        e = cudaMemcpyAsync(hval, work_.hval, sizeof(double) * P.h_col.size(), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess && hx && P.n_meas > 0)
+        e = cudaMemcpyAsync(hx, work_.h, sizeof(double) * P.n_meas, cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess && rhs_orig)
+        e = cudaMemcpyAsync(b.data(), work_.rhs, sizeof(double) * P.n_state, cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "export eval");
+    if (rhs_orig)
+        for (int32_t p = 0; p < P.n_state; ++p) rhs_orig[P.state_of_ps[p]] = b[p];
+    return 0;
+}
+
+int32_t Engine::stage_telemetry(const double* z, int32_t count, int32_t slot) {
+    if (!uploaded_ || model.structure_dirty) {
+        const int32_t rc = upload();
+        if (rc) return rc;
+    }
+    const int32_t m = model.n_meas();
+    if (count != m || slot < 0 || slot >= 4096) {
+        last_error = "telemetry count or slot out of range";
+        return -4;
+    }
+    if (slot >= n_slots_) {
+        const int32_t ns = std::max(slot + 1, std::max(2 * n_slots_, 8));
+        double* d = nullptr;
+        cudaError_t e = cudaMalloc(&d, sizeof(double) * static_cast<size_t>(ns) * std::max(m, 1));
+        if (e != cudaSuccess) return set_cuda_error(e, "telemetry slots");
+        if (d_slots_) {
+            cudaMemcpyAsync(d, d_slots_, sizeof(double) * static_cast<size_t>(n_slots_) * m, cudaMemcpyDeviceToDevice, st_);
+            cudaStreamSynchronize(st_);
+            cudaFree(d_slots_);
+        }
+        d_slots_ = d;
+        n_slots_ = ns;
+    }
+    cudaError_t e = cudaMemcpyAsync(d_slots_ + static_cast<size_t>(slot) * m, z, sizeof(double) * m,
+                                    cudaMemcpyHostToDevice, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "stage telemetry");
+    return 0;
+}
+
+int32_t Engine::use_telemetry(int32_t slot) {
+    if (slot < 0 || slot >= n_slots_ || !uploaded_) {
+        last_error = "telemetry slot not staged";
+        return -4;
+    }
+    const int32_t m = model.n_meas();
+    cudaError_t e = cudaMemcpyAsync(work_.z, d_slots_ + static_cast<size_t>(slot) * m, sizeof(double) * m,
+                                    cudaMemcpyDeviceToDevice, st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "use telemetry");
+    model.values_dirty = false;
+    return 0;
+}
+
+int32_t Engine::flush_l2(size_t bytes) {
+    int32_t rc = initialize();
+    if (rc) return rc;
+    if (bytes > scratch_bytes_) {
+        if (d_scratch_) cudaFree(d_scratch_);
+        d_scratch_ = nullptr;
+        scratch_bytes_ = 0;
+        cudaError_t e = cudaMalloc(&d_scratch_, bytes);
+        if (e != cudaSuccess) return set_cuda_error(e, "l2 flush buffer");
+        scratch_bytes_ = bytes;
+    }
+    static int salt = 0;
+    cudaError_t e = cudaMemsetAsync(d_scratch_, (++salt) & 0xFF, bytes, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "l2 flush");
+    return 0;
+}
+
+int32_t Engine::timer(int32_t op, double* ms) {
+    int32_t rc = initialize();
+    if (rc) return rc;
+    if (!tm0_) {
+        cudaEventCreate(&tm0_);
+        cudaEventCreate(&tm1_);
+    }
+    if (op == 0) {
+        cudaEventRecord(tm0_, st_);
+        return 0;
+    }
+    cudaEventRecord(tm1_, st_);
+    cudaError_t e = cudaEventSynchronize(tm1_);
+    float f = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&f, tm0_, tm1_);
+    if (e != cudaSuccess) return set_cuda_error(e, "timer");
+    if (ms) *ms = f;
+    return 0;
+}
+
+}  // namespace sle_gb300

@@ -1,0 +1,169 @@
+// Engine: one network model resident on one GPU, solved by the level-scheduled
+// multifrontal Gauss-Newton pipeline.  Mirrors the reference SLEEngine solve
+// path (sle_engine.cu:450-682) and WLSSolver (wls_solver.cu:221-537).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../kernels/kernels.cuh"
+#include "../model/model.h"
+#include "../symbolic/symbolic.h"
+
+namespace sle_gb300 {
+
+// Reference EngineConfig defaults (sle_engine.h:84-122, sle_engine.config).
+struct EngineConfig {
+    int32_t device_id = 0;
+    size_t max_buses = 200000, max_branches = 400000, max_measurements = 2000000, max_switching_devices = 100000;
+    int32_t enable_robust = 0;
+    double huber_gamma = 1.5;
+    double convergence_tolerance = 1e-6;  // SLE_CONVERGENCE_TOL of the FP64 build (sle_types.cuh:63)
+    int32_t max_realtime_iterations = 5;
+    int32_t max_precision_iterations = 100;
+    double realtime_time_limit_ms = 20.0;
+    int32_t use_flat_start_default = 0;
+    int32_t enable_profiling = 0;
+    int32_t use_cuda_graphs = 1;
+    int32_t block_size_standard = 256;
+    int32_t block_size_reduction = 512;
+    int32_t use_double_precision = 1;
+    double voltage_min_pu = 0.5;
+    double voltage_max_pu = 1.5;
+    double bad_data_threshold = 3.0;
+    int32_t auto_bad_data_rejection = 0;
+    // Extensions (sle_ExSetOption).
+    int32_t exact_jacobian = 1;  // 0: the reference's Jacobian formulas
+    int32_t gain_policy = 0;     // 0: refactor every iteration; 1: reuse the factor until invalidated
+    int32_t ordering = 0;        // symbolic ordering (see SymbolicParams)
+};
+
+enum class Mode : int32_t { REALTIME = 0, PRECISION = 1 };
+
+struct SolveRequest {
+    Mode mode = Mode::REALTIME;
+    int32_t max_iterations = 5;
+    double tolerance = 1e-6;
+    double huber_gamma = 1.5;
+    int32_t robust = 0;
+    int32_t flat_start = 0;
+    double time_limit_ms = 0.0;
+};
+
+// ConvergenceStatus values (sle_types.cuh:142-149).
+enum ConvStatus : int32_t { CONV_OK = 0, CONV_MAXIT = 1, CONV_DIVERGED = 2, CONV_SINGULAR = 3, CONV_NOTOBS = 4, CONV_RUNNING = 5 };
+
+struct SolveResult {
+    int32_t status = CONV_RUNNING;
+    int32_t iterations = 0;
+    double max_mismatch = 0.0;
+    double objective = 0.0;
+    double time_ms = 0.0;
+    double largest_residual = 0.0;
+    int32_t largest_idx = -1;
+    int32_t bad_count = 0;
+};
+
+// Per-stage statistics (launch counts always; CUDA-event times when
+// cfg.enable_profiling is set).
+enum Stage : int32_t { ST_EVALUATE = 0, ST_FACTOR = 1, ST_RHS = 2, ST_SOLVE = 3, ST_UPDATE = 4, ST_OTHER = 5, ST_COUNT = 6 };
+struct StageStats {
+    int64_t launches[ST_COUNT] = {0, 0, 0, 0, 0, 0};
+    double ms[ST_COUNT] = {0, 0, 0, 0, 0, 0};
+    int64_t calls[ST_COUNT] = {0, 0, 0, 0, 0, 0};
+    int64_t iterations = 0, solves = 0;
+};
+
+class Engine {
+public:
+    explicit Engine(const EngineConfig& c) : cfg(c) {}
+    ~Engine();
+    Engine(const Engine&) = delete;
+    Engine& operator=(const Engine&) = delete;
+
+    EngineConfig cfg;
+    Model model;
+    std::string config_path;
+    std::string last_error;
+
+    int32_t initialize();
+    int32_t analyze();  // host-only symbolic analysis of the current model
+    int32_t upload();
+    int32_t update_telemetry(const double* z, int32_t count);
+    int32_t sync_measurements();
+    int32_t solve(const SolveRequest& rq, SolveResult& out);
+    int32_t flat_start();
+    // Refresh the host model from the device; `what` is a mask of
+    // DL_STATE (V, theta), DL_MEAS (h(x), residuals), DL_FLOWS (injections,
+    // branch flows).  Only arrays changed since the last solve are copied.
+    enum : int32_t { DL_STATE = 1, DL_MEAS = 2, DL_FLOWS = 4, DL_ALL = 7 };
+    int32_t download_results(int32_t what = DL_ALL);
+
+    // Stage-level access for parity tests.
+    int32_t evaluate_at(const double* v, const double* th, int32_t exact);
+    int32_t export_gain(std::vector<int32_t>& rows, std::vector<int32_t>& cols, std::vector<double>& vals);
+    int32_t factor_and_solve(const double* rhs_orig, double* x_orig);
+    int32_t export_ybus(std::vector<double>& g, std::vector<double>& b);
+    int32_t export_eval(double* hval, double* hx, double* rhs_orig);
+
+    // Measurement hooks.
+    int32_t stage_telemetry(const double* z, int32_t count, int32_t slot);  // host -> device slot
+    int32_t use_telemetry(int32_t slot);                                    // device slot -> z (on stream)
+    int32_t flush_l2(size_t bytes);                                         // overwrite a scratch buffer
+    int32_t timer(int32_t op, double* ms);                                  // 0 start, 1 stop (+ elapsed)
+    StageStats stats;
+
+    bool initialized() const { return init_; }
+    bool analyzed() const { return analyzed_; }
+    bool uploaded() const { return uploaded_; }
+    const Plan& plan() const { return plan_; }
+    size_t device_bytes() const { return arena_bytes_; }
+    double last_solve_ms() const { return last_.time_ms; }
+    const SolveResult& last_result() const { return last_; }
+    std::string device_info();
+
+    // Device copies of per-element results (downloaded lazily).
+    std::vector<double> p_inj, q_inj, pf, qf, pt, qt;
+
+private:
+    bool init_ = false, analyzed_ = false, uploaded_ = false, factor_valid_ = false;
+    int32_t stale_ = 0;  // DL_* mask of host copies older than the device
+    cudaStream_t st_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    void* arena_ = nullptr;
+    size_t arena_bytes_ = 0;
+    DevStatus* h_status_ = nullptr;
+    double* h_stage_ = nullptr;  // pinned staging for telemetry
+    size_t h_stage_n_ = 0;
+    Plan plan_;
+    DevNet net_{};
+    DevFactor fac_{};
+    DevWork work_{};
+    LevelSchedule sched_{};
+    std::vector<int32_t> sch_small_ptr_, sch_small_, sch_big_ptr_, sch_big_, sch_all_ptr_, sch_all_, sch_maxf_;
+    std::vector<int64_t> big_off_;
+    int32_t* d_small_ = nullptr;
+    int32_t* d_all_ = nullptr;
+    SolveResult last_{};
+    double* d_slots_ = nullptr;
+    int32_t n_slots_ = 0;
+    void* d_scratch_ = nullptr;
+    size_t scratch_bytes_ = 0;
+    cudaEvent_t tm0_ = nullptr, tm1_ = nullptr;
+    std::vector<cudaEvent_t> ev_pool_;
+    std::vector<std::pair<int32_t, int32_t>> ev_marks_;  // (stage, pool index of the start event)
+    size_t ev_used_ = 0;
+    int32_t stage_begin(int32_t stage);
+    void stage_end(int32_t stage, int32_t mark, int64_t launches_before);
+    void collect_stage_times();
+
+    void release_device();
+    int32_t set_cuda_error(cudaError_t e, const char* where);
+    SolveParams params(const SolveRequest& rq) const;
+    int32_t run_iteration(const SolveParams& sp, bool refactor);
+};
+
+}  // namespace sle_gb300

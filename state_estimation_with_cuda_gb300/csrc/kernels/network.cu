@@ -1,0 +1,464 @@
+// Network-side kernels: branch admittances, Ybus assembly, the fused
+// measurement evaluation (h(x), residual, weights, Jacobian values), the
+// gain right-hand side, state update / convergence and the result pass.
+#include "kernels.cuh"
+
+#include <cfloat>
+
+namespace sle_gb300 {
+namespace {
+
+constexpr double kEps = 1e-12;   // SLE_REAL_EPSILON of the FP64 build (sle_types.cuh:62)
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Deterministic block sum (fixed tree), result valid in thread 0.
+__device__ double block_sum(double v, double* sh) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    v = (threadIdx.x < (blockDim.x >> 5)) ? sh[lane] : 0.0;
+    if (wid == 0) v = warp_sum(v);
+    __syncthreads();
+    return v;
+}
+__device__ double block_max(double v, double* sh) {
+    v = warp_max(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    v = (threadIdx.x < (blockDim.x >> 5)) ? sh[lane] : 0.0;
+    if (wid == 0) v = warp_max(v);
+    __syncthreads();
+    return v;
+}
+
+// a1: per-branch series admittance and charging split
+// (network_model.cu:595-612 / sparse_matrix.cu:321-355).
+__global__ void k_admittance(DevNet net) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= net.n_branch) return;
+    const double r = net.br_r[k], x = net.br_x[k], bt = net.br_bch[k], a = net.br_tap[k];
+    double den = r * r + x * x;
+    if (den < kEps) den = kEps;
+    net.br_g[k] = r / den;
+    net.br_b[k] = -x / den;
+    net.br_bsf[k] = bt / (2.0 * a * a);
+    net.br_bst[k] = bt / 2.0;
+}
+
+// a2: Ybus values on the canonical pattern, one thread per bus row; the
+// diagonal accumulates the row's branch contributions in entry order
+// (sparse_matrix.cu:410-492 without floating-point atomics).
+__global__ void k_ybus(DevNet net) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= net.n_bus) return;
+    const int e0 = net.y_ptr[i], e1 = net.y_ptr[i + 1];
+    double dg = 0.0, db = 0.0;
+    for (int e = e0 + 1; e < e1; ++e) {
+        const int src = net.y_src[e];
+        const int k = src >> 1, end = src & 1;
+        const double g = net.br_g[k], b = net.br_b[k];
+        const double a = fmax(net.br_tap[k], kEps);
+        const double phi = net.br_shift[k];
+        double sph, cph;
+        sincos(phi, &sph, &cph);
+        const double inv_a = 1.0 / a;
+        if (end == 0) {  // row = from bus: Y_ij = -(g+jb) e^{-j phi} / a
+            net.y_g[e] = -(g * cph + b * sph) * inv_a;
+            net.y_b[e] = -(-g * sph + b * cph) * inv_a;
+            dg += g / (a * a);
+            db += b / (a * a) + net.br_bsf[k];
+        } else {         // row = to bus: Y_ji = -(g+jb) e^{+j phi} / a
+            net.y_g[e] = -(g * cph - b * sph) * inv_a;
+            net.y_b[e] = -(g * sph + b * cph) * inv_a;
+            dg += g;
+            db += b + net.br_bst[k];
+        }
+    }
+    net.y_g[e0] = dg;
+    net.y_b[e0] = db;
+}
+
+struct FlowTerms {
+    double val;
+    double d[4];  // theta_i, V_i, theta_j, V_j
+};
+
+// a4 + a8 flow rows: value of P/Q at one end and its derivatives.
+__device__ FlowTerms flow_terms(const DevNet& net, const double* v, const double* th, int k, bool is_q,
+                                bool to_end, bool exact) {
+    const int i = net.br_from[k], j = net.br_to[k];
+    const double Vi = v[i], Vj = v[j];
+    const double t = th[i] - th[j] - net.br_shift[k];
+    double s, c;
+    sincos(t, &s, &c);
+    const double g = net.br_g[k], b = net.br_b[k];
+    const double A = fmax(net.br_tap[k], kEps);
+    const double inv = 1.0 / A, a2 = A * A;
+    const double on = net.br_closed[k] ? 1.0 : 0.0;
+    const double vv = Vi * Vj * inv;
+    FlowTerms f;
+    if (!is_q && !to_end) {
+        f.val = Vi * Vi / a2 * g - vv * (g * c + b * s);
+        f.d[0] = vv * (g * s - b * c);
+        f.d[1] = 2.0 * Vi / a2 * g - Vj * inv * (g * c + b * s);
+        f.d[2] = -f.d[0];
+        f.d[3] = -Vi * inv * (g * c + b * s);
+    } else if (is_q && !to_end) {
+        const double bsf = net.br_bsf[k];
+        f.val = -(Vi * Vi / a2) * (b + bsf) - vv * (g * s - b * c);
+        f.d[0] = -vv * (g * c + b * s);
+        f.d[1] = (exact ? -2.0 * Vi * (b + bsf) / a2 : -2.0 * Vi * b / a2) - Vj * inv * (g * s - b * c);
+        f.d[2] = -f.d[0];
+        f.d[3] = -Vi * inv * (g * s - b * c);
+    } else if (!is_q && to_end) {
+        f.val = Vj * Vj * g - vv * (g * c - b * s);
+        // exact: dP_t/dtheta_i = (ViVj/a)(g s + b c); the reference flips the sign.
+        f.d[0] = exact ? vv * (g * s + b * c) : vv * (-g * s - b * c);
+        f.d[1] = -Vj * inv * (g * c - b * s);
+        f.d[2] = -f.d[0];
+        f.d[3] = 2.0 * Vj * g - Vi * inv * (g * c - b * s);
+    } else {
+        const double bst = net.br_bst[k];
+        f.val = -Vj * Vj * (b + bst) + vv * (g * s + b * c);
+        f.d[0] = vv * (g * c - b * s);
+        f.d[1] = Vj * inv * (g * s + b * c);
+        f.d[2] = -f.d[0];
+        f.d[3] = (exact ? -2.0 * Vj * (b + bst) : -2.0 * Vj * b) + Vi * inv * (g * s + b * c);
+    }
+    f.val *= on;
+    if (exact) {
+        for (int x = 0; x < 4; ++x) f.d[x] *= on;
+    }
+    return f;
+}
+
+__device__ __forceinline__ void put_flow(double* hrow, int fpos, const double d[4]) {
+    for (int x = 0; x < 4; ++x) {
+        const int p = (fpos >> (8 * x)) & 0xFF;
+        if (p != 0xFF) hrow[p] += d[x];
+    }
+}
+
+// a3/a6/a7/a8/a9 fused: one thread per measurement row.
+__global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, SolveParams sp) {
+    __shared__ double sh[32];
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    double obj = 0.0;
+    if (q < net.n_meas) {
+        const int kind = net.m_kind[q];
+        const int ty = net.m_type[q];
+        const int loc = net.m_loc[q];
+        const bool exact = sp.exact_jacobian != 0;
+        const int base = net.h_ptr[q];
+        const int nh = net.h_ptr[q + 1] - base;
+        double* hrow = w.hval + base;
+        for (int x = 0; x < nh; ++x) hrow[x] = 0.0;
+        double hv = 0.0;
+        if (kind == 0) {  // V_MAG
+            hv = w.v[loc];
+            hrow[0] = 1.0;
+        } else if (kind == 1) {  // V_ANGLE
+            hv = w.th[loc];
+            if (nh > 0) hrow[0] = 1.0;
+        } else if (kind == 2) {  // P/Q injection or pseudo
+            const bool isq = (ty == 3 || ty == 8);
+            const double Vi = w.v[loc], ti = w.th[loc];
+            double dVi = 0.0, dTi = 0.0;
+            const int e0 = net.y_ptr[loc], e1 = net.y_ptr[loc + 1];
+            for (int e = e0; e < e1; ++e) {
+                const int j = net.y_col[e];
+                const double G = net.y_g[e], B = net.y_b[e];
+                if (j == loc) {
+                    if (!isq) {
+                        hv += Vi * Vi * G;
+                        dVi += 2.0 * Vi * G;
+                        if (!exact) dTi += Vi * Vi * B;
+                    } else {
+                        hv -= Vi * Vi * B;
+                        dVi -= 2.0 * Vi * B;
+                        if (!exact) dTi += Vi * Vi * G;
+                    }
+                } else {
+                    const double Vj = w.v[j];
+                    double s, c;
+                    sincos(ti - w.th[j], &s, &c);
+                    const double gcbs = G * c + B * s, gsbc = G * s - B * c;
+                    double dTj, dVj;
+                    if (!isq) {
+                        hv += Vi * Vj * gcbs;
+                        dVi += Vj * gcbs;
+                        dTi -= Vi * Vj * gsbc;
+                        dTj = Vi * Vj * gsbc;
+                        dVj = Vi * gcbs;
+                    } else {
+                        hv += Vi * Vj * gsbc;
+                        dVi += Vj * gsbc;
+                        dTi += Vi * Vj * gcbs;
+                        dTj = -Vi * Vj * gcbs;
+                        dVj = Vi * gsbc;
+                    }
+                    const int pt = net.y_hpos_t[e];
+                    if (pt >= 0) hrow[pt] += dTj;
+                    hrow[net.y_hpos_v[e]] += dVj;
+                }
+            }
+            const int pt = net.y_hpos_t[e0];
+            if (pt >= 0) hrow[pt] += dTi;
+            hrow[net.y_hpos_v[e0]] += dVi;
+        } else if (kind == 3) {  // P/Q flow
+            const bool to_end = net.m_end[q] != 0;
+            const FlowTerms f = flow_terms(net, w.v, w.th, loc, ty == 5, to_end, exact);
+            hv = f.val;
+            put_flow(hrow, net.m_fpos[q], f.d);
+        } else if (kind == 4) {  // current magnitude
+            const bool to_end = net.m_end[q] != 0;
+            const FlowTerms fp = flow_terms(net, w.v, w.th, loc, false, to_end, exact);
+            const int ib = to_end ? net.br_to[loc] : net.br_from[loc];
+            const double ve = w.v[ib];
+            const double vs = fmax(ve, kEps);
+            const double on = net.br_closed[loc] ? 1.0 : 0.0;
+            double d[4];
+            if (!exact) {  // the reference reuses the P-flow derivatives
+                hv = 0.0;
+                const FlowTerms fq = flow_terms(net, w.v, w.th, loc, true, to_end, exact);
+                hv = sqrt(fp.val * fp.val + fq.val * fq.val) / vs * on;
+                for (int x = 0; x < 4; ++x) d[x] = fp.d[x];
+            } else {
+                const FlowTerms fq = flow_terms(net, w.v, w.th, loc, true, to_end, exact);
+                const double S = sqrt(fp.val * fp.val + fq.val * fq.val);
+                hv = S / vs * on;
+                for (int x = 0; x < 4; ++x)
+                    d[x] = (S > 0.0) ? (fp.val * fp.d[x] + fq.val * fq.d[x]) / (S * vs) * on : 0.0;
+                if (ve > kEps) d[to_end ? 3 : 1] -= S / (vs * vs) * on;
+            }
+            put_flow(hrow, net.m_fpos[q], d);
+        }
+        double rr = 0.0, we = 0.0;
+        if (kind != 5) {
+            rr = w.z[q] - hv;
+            const double wb = net.m_w[q];
+            we = wb;
+            if (sp.robust) {  // kernels.cu:634-671
+                const double sg = net.m_sigma[q];
+                const double rn = fabs(rr / sg);
+                if (!(rn <= sp.huber_gamma)) we = sp.huber_gamma / (sg * fabs(rr) + kEps);
+            }
+            obj = wb * rr * rr;
+        } else {
+            hv = 0.0;
+        }
+        w.h[q] = hv;
+        w.r[q] = rr;
+        w.w_eff[q] = we;
+        w.wr[q] = we * rr;
+    }
+    const double s = block_sum(obj, sh);
+    if (threadIdx.x == 0) w.part[blockIdx.x] = s;
+}
+
+// a11: b = H^T (w r) in permuted state order, one thread per state (gather).
+__global__ void k_rhs(DevNet net, DevFactor f, DevWork w) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= f.n_state) return;
+    double acc = 0.0;
+    for (int x = f.rhs_ptr[t]; x < f.rhs_ptr[t + 1]; ++x) {
+        const int hidx = f.rhs_h[x];
+        acc += w.hval[hidx] * w.wr[net.h_row[hidx]];
+    }
+    w.rhs[t] = acc;
+}
+
+// Objective, largest |r| (lowest index on ties) and the bad-data count
+// (active rows with sigma > 0 and |r| / sigma > threshold,
+// sle_engine.cu:959-977): single block, fixed order.
+__global__ void k_objective(DevNet net, DevWork w, int nblk, double bad_threshold) {
+    __shared__ double sh[32];
+    __shared__ double sb[1024];
+    __shared__ int si[1024];
+    __shared__ int sc[1024];
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) acc += w.part[b];
+    const double tot = block_sum(acc, sh);
+    double best = -1.0;
+    int bidx = 0x7fffffff, cnt = 0;
+    for (int q = threadIdx.x; q < net.n_meas; q += blockDim.x) {
+        if (net.m_kind[q] == 5) continue;
+        const double a = fabs(w.r[q]);
+        if (a > best) { best = a; bidx = q; }
+        const double sg = net.m_sigma[q];
+        if (sg > 0.0 && a / sg > bad_threshold) ++cnt;
+    }
+    sb[threadIdx.x] = best;
+    si[threadIdx.x] = bidx;
+    sc[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            const double b2 = sb[threadIdx.x + o];
+            const int i2 = si[threadIdx.x + o];
+            if (b2 > sb[threadIdx.x] || (b2 == sb[threadIdx.x] && i2 < si[threadIdx.x])) {
+                sb[threadIdx.x] = b2;
+                si[threadIdx.x] = i2;
+            }
+            sc[threadIdx.x] += sc[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        w.status->objective = tot;
+        w.status->largest_residual = sb[0] < 0.0 ? 0.0 : sb[0];
+        w.status->largest_idx = si[0] == 0x7fffffff ? -1 : si[0];
+        w.status->bad_count = sc[0];
+    }
+}
+
+// a13: x += dx (slack angle fixed), V clamped, block maxima of |dx|.
+__global__ void __launch_bounds__(kBlock) k_update(DevNet net, DevFactor f, DevWork w, SolveParams sp) {
+    __shared__ double sh[32];
+    __shared__ int bad;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double mx = 0.0;
+    if (i < net.n_bus) {
+        const int pt = f.bus_ps_theta[i];
+        const double dv = w.sol[f.bus_ps_v[i]];
+        double dt = 0.0;
+        if (pt >= 0) {
+            dt = w.sol[pt];
+            w.th[i] += dt;
+        }
+        double vn = w.v[i] + dv;
+        vn = fmax(vn, sp.vmin);
+        vn = fmin(vn, sp.vmax);
+        w.v[i] = vn;
+        if (!isfinite(dt) || !isfinite(dv)) bad = 1;
+        mx = fmax(fabs(dt), fabs(dv));
+        if (mx != mx) mx = 0.0;
+    }
+    const double m = block_max(mx, sh);
+    if (threadIdx.x == 0) {
+        w.part[blockIdx.x] = m;
+        if (bad) atomicOr(&w.status->flags, FLAG_NONFINITE);
+    }
+}
+
+__global__ void k_update_finalize(DevWork w, int nblk, double tol) {
+    __shared__ double sh[32];
+    double m = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) m = fmax(m, w.part[b]);
+    m = block_max(m, sh);
+    if (threadIdx.x == 0) {
+        w.status->max_mismatch = m;
+        if (m < tol) atomicOr(&w.status->flags, FLAG_CONVERGED);
+    }
+}
+
+// kernels.cu:799-817
+__global__ void k_flat_start(DevNet net, DevWork w) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= net.n_bus) return;
+    const int t = net.bus_type[i];
+    w.v[i] = (t == 1 || t == 2) ? net.v_setpoint[i] : 1.0;
+    w.th[i] = 0.0;
+}
+
+__global__ void k_injections(DevNet net, DevWork w) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= net.n_bus) return;
+    const double Vi = w.v[i], ti = w.th[i];
+    double P = 0.0, Q = 0.0;
+    for (int e = net.y_ptr[i]; e < net.y_ptr[i + 1]; ++e) {
+        const int j = net.y_col[e];
+        const double G = net.y_g[e], B = net.y_b[e];
+        double s = 0.0, c = 1.0;
+        if (j != i) sincos(ti - w.th[j], &s, &c);
+        const double vv = Vi * w.v[j];
+        P += vv * (G * c + B * s);
+        Q += vv * (G * s - B * c);
+    }
+    w.p_inj[i] = P;
+    w.q_inj[i] = Q;
+}
+
+__global__ void k_flows(DevNet net, DevWork w) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= net.n_branch) return;
+    w.pf[k] = flow_terms(net, w.v, w.th, k, false, false, true).val;
+    w.qf[k] = flow_terms(net, w.v, w.th, k, true, false, true).val;
+    w.pt[k] = flow_terms(net, w.v, w.th, k, false, true, true).val;
+    w.qt[k] = flow_terms(net, w.v, w.th, k, true, true, true).val;
+}
+
+inline int nblocks(int n) { return (n + kBlock - 1) / kBlock; }
+
+}  // namespace
+
+std::atomic<int64_t> g_kernel_launches{0};
+
+cudaError_t launch_admittance_and_ybus(const DevNet& net, cudaStream_t st) {
+    if (net.n_branch > 0) {
+        k_admittance<<<nblocks(net.n_branch), kBlock, 0, st>>>(net);
+        ++g_kernel_launches;
+    }
+    k_ybus<<<nblocks(net.n_bus), kBlock, 0, st>>>(net);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_evaluate(const DevNet& net, const DevWork& w, const SolveParams& sp, cudaStream_t st) {
+    if (net.n_meas <= 0) return cudaSuccess;
+    k_evaluate<<<nblocks(net.n_meas), kBlock, 0, st>>>(net, w, sp);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_objective(const DevNet& net, const DevWork& w, double bad_threshold, cudaStream_t st) {
+    k_objective<<<1, 1024, 0, st>>>(net, w, net.n_meas > 0 ? nblocks(net.n_meas) : 0, bad_threshold);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rhs(const DevNet& net, const DevFactor& f, const DevWork& w, cudaStream_t st) {
+    k_rhs<<<nblocks(f.n_state), kBlock, 0, st>>>(net, f, w);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_update(const DevNet& net, const DevFactor& f, const DevWork& w, const SolveParams& sp,
+                          cudaStream_t st) {
+    const int nb = nblocks(net.n_bus);
+    k_update<<<nb, kBlock, 0, st>>>(net, f, w, sp);
+    k_update_finalize<<<1, 1024, 0, st>>>(w, nb, sp.tol);
+    g_kernel_launches += 2;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flat_start(const DevNet& net, const DevWork& w, cudaStream_t st) {
+    k_flat_start<<<nblocks(net.n_bus), kBlock, 0, st>>>(net, w);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_results(const DevNet& net, const DevWork& w, cudaStream_t st) {
+    k_injections<<<nblocks(net.n_bus), kBlock, 0, st>>>(net, w);
+    ++g_kernel_launches;
+    if (net.n_branch > 0) {
+        k_flows<<<nblocks(net.n_branch), kBlock, 0, st>>>(net, w);
+        ++g_kernel_launches;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace sle_gb300

@@ -1,0 +1,743 @@
+// Symbolic analysis for the GPU WLS pipeline (definitions in symbolic.h).
+#include "symbolic.h"
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <functional>
+
+namespace sle_gb300 {
+
+std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const std::vector<int32_t>& adj);
+
+namespace {
+
+inline bool is_bus_type(int32_t t) { return t == 0 || t == 1 || t == 2 || t == 3 || t == 7 || t == 8; }
+inline bool is_inj_type(int32_t t) { return t == 2 || t == 3 || t == 7 || t == 8; }
+
+// ---------------------------------------------------------------------------
+// Nested dissection on the bus graph.
+// ---------------------------------------------------------------------------
+class NestedDissection {
+public:
+    NestedDissection(int32_t n, const std::vector<int32_t>& ptr, const std::vector<int32_t>& adj, int32_t leaf)
+        : n_(n), ptr_(ptr), adj_(adj), leaf_(std::max(leaf, 4)), stamp_(n, -1), level_(n, -1) {}
+
+    std::vector<int32_t> run() {
+        order_.clear();
+        order_.reserve(n_);
+        std::vector<int32_t> all(n_);
+        std::iota(all.begin(), all.end(), 0);
+        dissect(all, 0);
+        return order_;
+    }
+
+private:
+    int32_t n_;
+    const std::vector<int32_t>& ptr_;
+    const std::vector<int32_t>& adj_;
+    int32_t leaf_;
+    std::vector<int32_t> stamp_, level_;
+    int32_t next_stamp_ = 0;
+    std::vector<int32_t> order_;
+
+    int32_t new_stamp(const std::vector<int32_t>& nodes) {
+        const int32_t s = next_stamp_++;
+        for (int32_t v : nodes) stamp_[v] = s;
+        return s;
+    }
+
+    // BFS inside the stamped subset; returns visit order, fills level_.
+    std::vector<int32_t> bfs(int32_t root, int32_t s) {
+        std::vector<int32_t> q{root};
+        level_[root] = 0;
+        std::vector<int32_t> seen{root};
+        const int32_t mark = -2 - s;  // temporary visited marker in level_ is not used; use a local set
+        (void)mark;
+        std::vector<int32_t> visited_flag;
+        size_t head = 0;
+        while (head < q.size()) {
+            const int32_t u = q[head++];
+            for (int32_t e = ptr_[u]; e < ptr_[u + 1]; ++e) {
+                const int32_t v = adj_[e];
+                if (stamp_[v] != s || level_[v] >= 0) continue;
+                level_[v] = level_[u] + 1;
+                q.push_back(v);
+            }
+        }
+        return q;
+    }
+
+    void clear_levels(const std::vector<int32_t>& nodes) {
+        for (int32_t v : nodes) level_[v] = -1;
+    }
+
+    int32_t degree_in(int32_t v, int32_t s) const {
+        int32_t d = 0;
+        for (int32_t e = ptr_[v]; e < ptr_[v + 1]; ++e) d += (stamp_[adj_[e]] == s);
+        return d;
+    }
+
+    void leaf_order(const std::vector<int32_t>& nodes) {
+        // Minimum degree on the induced subgraph (exact degrees, ties -> lowest bus).
+        const int32_t k = static_cast<int32_t>(nodes.size());
+        if (k == 0) return;
+        std::vector<int32_t> sorted = nodes;
+        std::sort(sorted.begin(), sorted.end());
+        std::vector<int32_t> local(k);
+        // map bus -> local through a temporary use of level_
+        for (int32_t i = 0; i < k; ++i) level_[sorted[i]] = i;
+        std::vector<std::vector<char>> a(k, std::vector<char>(k, 0));
+        for (int32_t i = 0; i < k; ++i) {
+            const int32_t u = sorted[i];
+            for (int32_t e = ptr_[u]; e < ptr_[u + 1]; ++e) {
+                const int32_t v = adj_[e];
+                if (level_[v] >= 0 && level_[v] < k && v != u && sorted[level_[v]] == v) a[i][level_[v]] = 1;
+            }
+        }
+        for (int32_t i = 0; i < k; ++i) level_[sorted[i]] = -1;
+        std::vector<char> alive(k, 1);
+        std::vector<int32_t> deg(k, 0);
+        for (int32_t i = 0; i < k; ++i)
+            for (int32_t j = 0; j < k; ++j) deg[i] += a[i][j];
+        for (int32_t step = 0; step < k; ++step) {
+            int32_t best = -1;
+            for (int32_t i = 0; i < k; ++i)
+                if (alive[i] && (best < 0 || deg[i] < deg[best])) best = i;
+            order_.push_back(sorted[best]);
+            alive[best] = 0;
+            std::vector<int32_t> nb;
+            for (int32_t j = 0; j < k; ++j)
+                if (alive[j] && a[best][j]) nb.push_back(j);
+            for (int32_t j : nb) {
+                a[j][best] = 0;
+                --deg[j];
+            }
+            for (size_t x = 0; x < nb.size(); ++x)
+                for (size_t y = x + 1; y < nb.size(); ++y) {
+                    const int32_t p = nb[x], q = nb[y];
+                    if (!a[p][q]) {
+                        a[p][q] = a[q][p] = 1;
+                        ++deg[p];
+                        ++deg[q];
+                    }
+                }
+        }
+    }
+
+    void dissect(std::vector<int32_t> nodes, int depth) {
+        if (static_cast<int32_t>(nodes.size()) <= leaf_ || depth > 200) {
+            leaf_order(nodes);
+            return;
+        }
+        const int32_t s = new_stamp(nodes);
+        // Connected components inside the subset.
+        std::vector<int32_t> sorted = nodes;
+        std::sort(sorted.begin(), sorted.end());
+        std::vector<std::vector<int32_t>> comps;
+        for (int32_t v : sorted) {
+            if (level_[v] >= 0) continue;
+            comps.push_back(bfs(v, s));
+        }
+        clear_levels(nodes);
+        if (comps.size() > 1) {
+            for (auto& c : comps) dissect(c, depth + 1);
+            return;
+        }
+        // Pseudo-peripheral root: start at the min-degree vertex.
+        int32_t root = sorted[0];
+        int32_t best_deg = degree_in(root, s);
+        for (int32_t v : sorted) {
+            const int32_t d = degree_in(v, s);
+            if (d < best_deg) { best_deg = d; root = v; }
+        }
+        std::vector<int32_t> q;
+        int32_t ecc = -1;
+        for (int it = 0; it < 6; ++it) {
+            q = bfs(root, s);
+            const int32_t e = level_[q.back()];
+            if (e <= ecc) { break; }
+            ecc = e;
+            // min-degree vertex in the last level
+            int32_t cand = q.back();
+            int32_t cd = degree_in(cand, s);
+            for (auto itq = q.rbegin(); itq != q.rend() && level_[*itq] == e; ++itq) {
+                const int32_t d = degree_in(*itq, s);
+                if (d < cd || (d == cd && *itq < cand)) { cd = d; cand = *itq; }
+            }
+            clear_levels(q);
+            root = cand;
+        }
+        clear_levels(q);
+        q = bfs(root, s);
+        const int32_t depth_levels = level_[q.back()];
+        if (depth_levels < 2) {
+            clear_levels(q);
+            leaf_order(nodes);
+            return;
+        }
+        std::vector<int32_t> cnt(depth_levels + 1, 0);
+        for (int32_t v : q) ++cnt[level_[v]];
+        const int32_t total = static_cast<int32_t>(q.size());
+        // Choose the smallest level among those keeping 40..60 % balance;
+        // fall back to the median level.
+        int32_t cum = 0, median = 1;
+        std::vector<int32_t> below(depth_levels + 1, 0);
+        for (int32_t l = 0; l <= depth_levels; ++l) {
+            below[l] = cum;
+            cum += cnt[l];
+        }
+        for (int32_t l = 1; l < depth_levels; ++l) {
+            if (below[l] + cnt[l] >= total / 2) { median = l; break; }
+            median = l;
+        }
+        int32_t sep = median;
+        for (int32_t l = 1; l < depth_levels; ++l) {
+            const double lo = static_cast<double>(below[l]) / total;
+            const double hi = static_cast<double>(total - below[l] - cnt[l]) / total;
+            if (lo >= 0.35 && hi >= 0.35 && cnt[l] < cnt[sep]) sep = l;
+        }
+        // Parts: 0 = A (levels < sep), 1 = separator, 2 = B.
+        std::vector<int32_t> A, S, B;
+        for (int32_t v : q) {
+            const int32_t l = level_[v];
+            if (l < sep) A.push_back(v);
+            else if (l == sep) S.push_back(v);
+            else B.push_back(v);
+        }
+        // Thin the separator: a separator vertex with no neighbour in B joins A,
+        // then one with no neighbour in A joins B.
+        auto part_of = [&](int32_t v) { return level_[v] < sep ? 0 : (level_[v] == sep ? 1 : 2); };
+        std::vector<int32_t> S2;
+        for (int32_t v : S) {
+            bool touches_b = false;
+            for (int32_t e = ptr_[v]; e < ptr_[v + 1] && !touches_b; ++e) {
+                const int32_t u = adj_[e];
+                if (stamp_[u] == s && part_of(u) == 2) touches_b = true;
+            }
+            if (!touches_b) {
+                A.push_back(v);
+                level_[v] = sep - 1;  // now part of A
+            } else {
+                S2.push_back(v);
+            }
+        }
+        std::vector<int32_t> S3;
+        for (int32_t v : S2) {
+            bool touches_a = false;
+            for (int32_t e = ptr_[v]; e < ptr_[v + 1] && !touches_a; ++e) {
+                const int32_t u = adj_[e];
+                if (stamp_[u] == s && part_of(u) == 0) touches_a = true;
+            }
+            if (!touches_a) {
+                B.push_back(v);
+                level_[v] = sep + 1;
+            } else {
+                S3.push_back(v);
+            }
+        }
+        clear_levels(q);
+        if (A.empty() || B.empty()) {
+            leaf_order(nodes);
+            return;
+        }
+        dissect(std::move(A), depth + 1);
+        dissect(std::move(B), depth + 1);
+        // Separator last, ordered by minimum degree among itself.
+        leaf_order_small_or_natural(S3);
+    }
+
+    void leaf_order_small_or_natural(std::vector<int32_t>& S) {
+        if (static_cast<int32_t>(S.size()) <= 4 * leaf_) {
+            leaf_order(S);
+        } else {
+            std::sort(S.begin(), S.end());
+            for (int32_t v : S) order_.push_back(v);
+        }
+    }
+};
+
+int64_t trapezoid(int64_t nc, int64_t f) { return nc * f - nc * (nc - 1) / 2; }
+
+}  // namespace
+
+void bus_graph(const Topology& t, const std::vector<int32_t>& y_ptr, const std::vector<int32_t>& y_col,
+               std::vector<int32_t>& adj_ptr, std::vector<int32_t>& adj) {
+    std::vector<std::pair<int32_t, int32_t>> edges;
+    std::vector<int32_t> buses;
+    for (int32_t q = 0; q < t.n_meas; ++q) {
+        if (t.m_active && !t.m_active[q]) continue;
+        const int32_t ty = t.m_type[q], loc = t.m_loc[q];
+        buses.clear();
+        if (is_inj_type(ty)) {
+            buses.push_back(loc);
+            for (int32_t e = y_ptr[loc]; e < y_ptr[loc + 1]; ++e) buses.push_back(y_col[e]);
+        } else if (ty == 4 || ty == 5 || ty == 6) {
+            buses.push_back(t.br_from[loc]);
+            buses.push_back(t.br_to[loc]);
+        } else {
+            continue;
+        }
+        std::sort(buses.begin(), buses.end());
+        buses.erase(std::unique(buses.begin(), buses.end()), buses.end());
+        for (size_t a = 0; a < buses.size(); ++a)
+            for (size_t b = a + 1; b < buses.size(); ++b) {
+                edges.emplace_back(buses[a], buses[b]);
+                edges.emplace_back(buses[b], buses[a]);
+            }
+    }
+    std::sort(edges.begin(), edges.end());
+    edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
+    adj_ptr.assign(t.n_bus + 1, 0);
+    for (auto& e : edges) ++adj_ptr[e.first + 1];
+    for (int32_t i = 0; i < t.n_bus; ++i) adj_ptr[i + 1] += adj_ptr[i];
+    adj.resize(edges.size());
+    for (size_t k = 0; k < edges.size(); ++k) adj[k] = edges[k].second;
+}
+
+bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::string& err) {
+    const int32_t n = t.n_bus, nbr = t.n_branch, m = t.n_meas, s = t.slack;
+    if (n < 1 || s < 0 || s >= n) { err = "invalid bus count or slack index"; return false; }
+    P = Plan();
+    P.n_bus = n;
+    P.n_state = 2 * n - 1;
+    P.n_meas = m;
+    P.slack = s;
+    for (int32_t k = 0; k < nbr; ++k) {
+        if (t.br_from[k] < 0 || t.br_from[k] >= n || t.br_to[k] < 0 || t.br_to[k] >= n) {
+            err = "branch references an unknown bus";
+            return false;
+        }
+    }
+    for (int32_t q = 0; q < m; ++q) {
+        const int32_t ty = t.m_type[q], loc = t.m_loc[q];
+        if (ty < 0 || ty > 8) { err = "unknown measurement type"; return false; }
+        const int32_t lim = is_bus_type(ty) ? n : nbr;
+        if (loc < 0 || loc >= lim) { err = "measurement location out of range"; return false; }
+    }
+    auto col_t = [&](int32_t i) { return i == s ? -1 : (i < s ? i : i - 1); };
+    auto col_v = [&](int32_t i) { return n - 1 + i; };
+
+    // --- Ybus pattern -----------------------------------------------------------
+    {
+        std::vector<std::vector<std::pair<int32_t, int32_t>>> rows(n);  // (col, src)
+        for (int32_t k = 0; k < nbr; ++k) {
+            if (!t.br_closed[k]) continue;
+            rows[t.br_from[k]].emplace_back(t.br_to[k], (k << 1) | 0);
+            rows[t.br_to[k]].emplace_back(t.br_from[k], (k << 1) | 1);
+        }
+        P.y_ptr.assign(n + 1, 0);
+        for (int32_t i = 0; i < n; ++i) {
+            auto& r = rows[i];
+            std::sort(r.begin(), r.end());
+            P.y_col.push_back(i);
+            P.y_src.push_back(-1);
+            for (auto& e : r) {
+                P.y_col.push_back(e.first);
+                P.y_src.push_back(e.second);
+            }
+            P.y_ptr[i + 1] = static_cast<int32_t>(P.y_col.size());
+        }
+    }
+
+    // --- H pattern ------------------------------------------------------------------
+    {
+        // Injection-row column lists per bus (computed once per bus).
+        std::vector<int32_t> inj_cols_ptr(n + 1, 0), inj_cols;
+        P.y_hpos_t.assign(P.y_col.size(), -1);
+        P.y_hpos_v.assign(P.y_col.size(), -1);
+        std::vector<int32_t> cols;
+        for (int32_t i = 0; i < n; ++i) {
+            cols.clear();
+            for (int32_t e = P.y_ptr[i]; e < P.y_ptr[i + 1]; ++e) {
+                const int32_t j = P.y_col[e];
+                if (col_t(j) >= 0) cols.push_back(col_t(j));
+                cols.push_back(col_v(j));
+            }
+            std::sort(cols.begin(), cols.end());
+            cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+            for (int32_t e = P.y_ptr[i]; e < P.y_ptr[i + 1]; ++e) {
+                const int32_t j = P.y_col[e];
+                if (col_t(j) >= 0)
+                    P.y_hpos_t[e] = static_cast<int32_t>(std::lower_bound(cols.begin(), cols.end(), col_t(j)) - cols.begin());
+                P.y_hpos_v[e] = static_cast<int32_t>(std::lower_bound(cols.begin(), cols.end(), col_v(j)) - cols.begin());
+            }
+            inj_cols.insert(inj_cols.end(), cols.begin(), cols.end());
+            inj_cols_ptr[i + 1] = static_cast<int32_t>(inj_cols.size());
+        }
+        P.h_ptr.assign(m + 1, 0);
+        P.m_kind.assign(m, ROW_NONE);
+        P.m_fpos.assign(m, -1);
+        for (int32_t q = 0; q < m; ++q) {
+            const int32_t ty = t.m_type[q], loc = t.m_loc[q];
+            const bool active = !t.m_active || t.m_active[q];
+            if (active) {
+                if (ty == 0) {
+                    P.m_kind[q] = ROW_VMAG;
+                    P.h_col.push_back(col_v(loc));
+                } else if (ty == 1) {
+                    P.m_kind[q] = ROW_VANG;
+                    if (col_t(loc) >= 0) P.h_col.push_back(col_t(loc));
+                } else if (is_inj_type(ty)) {
+                    P.m_kind[q] = ROW_INJ;
+                    P.h_col.insert(P.h_col.end(), inj_cols.begin() + inj_cols_ptr[loc],
+                                   inj_cols.begin() + inj_cols_ptr[loc + 1]);
+                } else {
+                    P.m_kind[q] = (ty == 6) ? ROW_IMAG : ROW_FLOW;
+                    const int32_t i = t.br_from[loc], j = t.br_to[loc];
+                    const int32_t c4[4] = {col_t(i), col_v(i), col_t(j), col_v(j)};
+                    cols.clear();
+                    for (int32_t c : c4)
+                        if (c >= 0) cols.push_back(c);
+                    std::sort(cols.begin(), cols.end());
+                    cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+                    uint32_t packed = 0;
+                    for (int x = 0; x < 4; ++x) {
+                        uint32_t pos = 0xFF;
+                        if (c4[x] >= 0)
+                            pos = static_cast<uint32_t>(std::lower_bound(cols.begin(), cols.end(), c4[x]) - cols.begin());
+                        packed |= pos << (8 * x);
+                    }
+                    P.m_fpos[q] = static_cast<int32_t>(packed);
+                    P.h_col.insert(P.h_col.end(), cols.begin(), cols.end());
+                }
+            }
+            P.h_ptr[q + 1] = static_cast<int32_t>(P.h_col.size());
+        }
+        P.h_row.resize(P.h_col.size());
+        for (int32_t q = 0; q < m; ++q)
+            for (int32_t h = P.h_ptr[q]; h < P.h_ptr[q + 1]; ++h) P.h_row[h] = q;
+    }
+
+    // --- ordering on the bus graph -----------------------------------------------------
+    std::vector<int32_t> gptr, gadj;
+    bus_graph(t, P.y_ptr, P.y_col, gptr, gadj);
+    std::vector<int32_t> order;
+    if (prm.ordering == 1) {
+        order.resize(n);
+        std::iota(order.begin(), order.end(), 0);
+    } else if (prm.ordering == 2) {
+        NestedDissection nd(n, gptr, gadj, prm.leaf_size);
+        order = nd.run();
+    } else {
+        order = amd_order(n, gptr, gadj);
+    }
+    if (static_cast<int32_t>(order.size()) != n) { err = "ordering failed"; return false; }
+    std::vector<int32_t> pos(n, -1);
+    for (int32_t k = 0; k < n; ++k) pos[order[k]] = k;
+
+    // --- elimination tree (Liu) and postorder ---------------------------------------------
+    auto etree_of = [&](const std::vector<int32_t>& ord, const std::vector<int32_t>& ps, std::vector<int32_t>& parent) {
+        parent.assign(n, -1);
+        std::vector<int32_t> anc(n, -1);
+        for (int32_t j = 0; j < n; ++j) {
+            const int32_t b = ord[j];
+            for (int32_t e = gptr[b]; e < gptr[b + 1]; ++e) {
+                int32_t i = ps[gadj[e]];
+                if (i >= j) continue;
+                while (anc[i] != -1 && anc[i] != j) {
+                    const int32_t nx = anc[i];
+                    anc[i] = j;
+                    i = nx;
+                }
+                if (anc[i] == -1) {
+                    anc[i] = j;
+                    parent[i] = j;
+                }
+            }
+        }
+    };
+    std::vector<int32_t> parent;
+    etree_of(order, pos, parent);
+    {
+        std::vector<int32_t> head(n, -1), next(n, -1);
+        for (int32_t j = n - 1; j >= 0; --j) {
+            if (parent[j] >= 0) {
+                next[j] = head[parent[j]];
+                head[parent[j]] = j;
+            }
+        }
+        std::vector<int32_t> post;
+        post.reserve(n);
+        std::vector<int32_t> stack;
+        for (int32_t r = 0; r < n; ++r) {
+            if (parent[r] != -1) continue;
+            stack.push_back(r);
+            while (!stack.empty()) {
+                const int32_t v = stack.back();
+                if (head[v] != -1) {
+                    const int32_t c = head[v];
+                    head[v] = next[c];
+                    stack.push_back(c);
+                } else {
+                    stack.pop_back();
+                    post.push_back(v);
+                }
+            }
+        }
+        std::vector<int32_t> order2(n);
+        for (int32_t k = 0; k < n; ++k) order2[k] = order[post[k]];
+        order.swap(order2);
+        for (int32_t k = 0; k < n; ++k) pos[order[k]] = k;
+        etree_of(order, pos, parent);
+    }
+
+    // --- column structures (bus level, strictly below the diagonal) ----------------------
+    std::vector<std::vector<int32_t>> cstruct(n);
+    {
+        std::vector<std::vector<int32_t>> kids(n);
+        for (int32_t j = 0; j < n; ++j)
+            if (parent[j] >= 0) kids[parent[j]].push_back(j);
+        std::vector<int32_t> tmp, merged;
+        for (int32_t j = 0; j < n; ++j) {
+            tmp.clear();
+            const int32_t b = order[j];
+            for (int32_t e = gptr[b]; e < gptr[b + 1]; ++e) {
+                const int32_t i = pos[gadj[e]];
+                if (i > j) tmp.push_back(i);
+            }
+            std::sort(tmp.begin(), tmp.end());
+            for (int32_t c : kids[j]) {
+                merged.clear();
+                const auto& cs = cstruct[c];
+                auto it = std::upper_bound(cs.begin(), cs.end(), j);
+                std::set_union(tmp.begin(), tmp.end(), it, cs.end(), std::back_inserter(merged));
+                tmp.swap(merged);
+            }
+            cstruct[j] = tmp;
+        }
+    }
+
+    // --- fundamental supernodes + relaxed amalgamation (bus level) ------------------------
+    std::vector<int32_t> nkids(n, 0);
+    for (int32_t j = 0; j < n; ++j)
+        if (parent[j] >= 0) ++nkids[parent[j]];
+    std::vector<int32_t> fs_start;  // fundamental supernode starts
+    for (int32_t j = 0; j < n; ++j) {
+        const bool joins_prev = j > 0 && parent[j - 1] == j && nkids[j] == 1 &&
+                                cstruct[j - 1].size() == cstruct[j].size() + 1;
+        if (!joins_prev) fs_start.push_back(j);
+    }
+    const int32_t nfs = static_cast<int32_t>(fs_start.size());
+    fs_start.push_back(n);
+    std::vector<int32_t> fs_of(n);
+    for (int32_t f = 0; f < nfs; ++f)
+        for (int32_t j = fs_start[f]; j < fs_start[f + 1]; ++j) fs_of[j] = f;
+    std::vector<int32_t> g_start(nfs), g_nc(nfs), g_f(nfs);
+    std::vector<int64_t> g_true(nfs);
+    std::vector<char> merged_up(nfs, 0);
+    for (int32_t f = 0; f < nfs; ++f) {
+        const int32_t last = fs_start[f + 1] - 1;
+        g_start[f] = fs_start[f];
+        g_nc[f] = fs_start[f + 1] - fs_start[f];
+        g_f[f] = g_nc[f] + static_cast<int32_t>(cstruct[last].size());
+        g_true[f] = trapezoid(g_nc[f], g_f[f]);
+    }
+    for (int32_t f = 0; f < nfs; ++f) {
+        const int32_t last = fs_start[f + 1] - 1;
+        const int32_t pj = parent[last];
+        if (pj < 0) continue;
+        const int32_t p = fs_of[pj];
+        if (fs_start[f + 1] != g_start[p]) continue;  // not immediately before the parent
+        const int64_t nc = g_nc[f] + g_nc[p];
+        const int64_t ff = g_nc[f] + g_f[p];
+        const int64_t ent = trapezoid(nc, ff);
+        const double z = static_cast<double>(ent - g_true[f] - g_true[p]) / static_cast<double>(ent);
+        bool merge = false;
+        if (nc <= prm.nrelax[0]) merge = true;
+        else if (nc <= prm.nrelax[1]) merge = z < prm.zrelax[0];
+        else if (nc <= prm.nrelax[2]) merge = z < prm.zrelax[1];
+        else merge = z < prm.zrelax[2];
+        if (!merge) continue;
+        merged_up[f] = 1;
+        g_start[p] = g_start[f];
+        g_nc[p] = static_cast<int32_t>(nc);
+        g_f[p] = static_cast<int32_t>(ff);
+        g_true[p] += g_true[f];
+    }
+    // Final supernodes: surviving groups, ordered by start column (= index order).
+    std::vector<int32_t> sn_b0, sn_b1, sn_top;  // bus position ranges, top fundamental
+    for (int32_t f = 0; f < nfs; ++f) {
+        if (merged_up[f]) continue;
+        sn_b0.push_back(g_start[f]);
+        sn_b1.push_back(fs_start[f + 1]);
+        sn_top.push_back(f);
+    }
+    const int32_t ns = static_cast<int32_t>(sn_b0.size());
+    std::vector<int32_t> sn_of_pos(n);
+    for (int32_t k = 0; k < ns; ++k)
+        for (int32_t j = sn_b0[k]; j < sn_b1[k]; ++j) sn_of_pos[j] = k;
+
+    // --- expansion to states --------------------------------------------------------------
+    std::vector<int32_t> ps0(n + 1, 0);
+    for (int32_t k = 0; k < n; ++k) ps0[k + 1] = ps0[k] + (order[k] == s ? 1 : 2);
+    P.bus_perm = order;
+    P.bus_ps_theta.assign(n, -1);
+    P.bus_ps_v.assign(n, -1);
+    P.state_of_ps.assign(P.n_state, -1);
+    for (int32_t k = 0; k < n; ++k) {
+        const int32_t b = order[k];
+        if (b == s) {
+            P.bus_ps_v[b] = ps0[k];
+        } else {
+            P.bus_ps_theta[b] = ps0[k];
+            P.bus_ps_v[b] = ps0[k] + 1;
+            P.state_of_ps[ps0[k]] = col_t(b);
+        }
+        P.state_of_ps[P.bus_ps_v[b]] = col_v(b);
+    }
+    std::vector<int32_t> ps_of_state(P.n_state);
+    for (int32_t p = 0; p < P.n_state; ++p) ps_of_state[P.state_of_ps[p]] = p;
+
+    P.n_super = ns;
+    P.sn_c0.assign(ns + 1, 0);
+    P.sn_f.assign(ns, 0);
+    P.sn_parent.assign(ns, -1);
+    P.sn_rows_off.assign(ns + 1, 0);
+    P.sn_lx_off.assign(ns + 1, 0);
+    P.sn_u_off.assign(ns + 1, 0);
+    P.sn_su_off.assign(ns + 1, 0);
+    std::vector<int32_t> sn_of_ps(P.n_state);
+    for (int32_t k = 0; k < ns; ++k) {
+        P.sn_c0[k] = ps0[sn_b0[k]];
+        const int32_t lastpos = sn_b1[k] - 1;
+        // rows: own columns then structure of the last column
+        for (int32_t j = sn_b0[k]; j < sn_b1[k]; ++j)
+            for (int32_t x = ps0[j]; x < ps0[j + 1]; ++x) P.sn_rows.push_back(x);
+        for (int32_t r : cstruct[lastpos])
+            for (int32_t x = ps0[r]; x < ps0[r + 1]; ++x) P.sn_rows.push_back(x);
+        P.sn_rows_off[k + 1] = static_cast<int64_t>(P.sn_rows.size());
+        const int64_t f = P.sn_rows_off[k + 1] - P.sn_rows_off[k];
+        P.sn_f[k] = static_cast<int32_t>(f);
+        const int32_t pj = parent[lastpos];
+        P.sn_parent[k] = pj >= 0 ? sn_of_pos[pj] : -1;
+        for (int32_t x = ps0[sn_b0[k]]; x < ps0[sn_b1[k]]; ++x) sn_of_ps[x] = k;
+    }
+    P.sn_c0[ns] = P.n_state;
+    int64_t lx = 0, uu = 0, su = 0;
+    P.nnz_l = 0;
+    P.flops = 0.0;
+    P.max_front = 0;
+    for (int32_t k = 0; k < ns; ++k) {
+        const int64_t nc = P.sn_c0[k + 1] - P.sn_c0[k];
+        const int64_t f = P.sn_f[k];
+        P.sn_lx_off[k] = lx;
+        P.sn_u_off[k] = uu;
+        P.sn_su_off[k] = su;
+        lx += f * nc;
+        uu += (f - nc) * (f - nc);
+        su += f - nc;
+        P.nnz_l += trapezoid(nc, f);
+        for (int64_t c = 0; c < nc; ++c) {
+            const double below = static_cast<double>(f - c - 1);
+            P.flops += below * (below + 1.0) + below + 1.0;
+        }
+        P.max_front = std::max<int32_t>(P.max_front, static_cast<int32_t>(f));
+    }
+    P.sn_lx_off[ns] = lx;
+    P.sn_u_off[ns] = uu;
+    P.sn_su_off[ns] = su;
+    P.lx_size = lx;
+    P.u_size = uu;
+    P.su_size = su;
+
+    // children, relative maps, levels
+    P.sn_child_ptr.assign(ns + 1, 0);
+    for (int32_t k = 0; k < ns; ++k)
+        if (P.sn_parent[k] >= 0) ++P.sn_child_ptr[P.sn_parent[k] + 1];
+    for (int32_t k = 0; k < ns; ++k) P.sn_child_ptr[k + 1] += P.sn_child_ptr[k];
+    P.sn_child.assign(P.sn_child_ptr[ns], 0);
+    {
+        std::vector<int32_t> fill(P.sn_child_ptr.begin(), P.sn_child_ptr.end() - 1);
+        for (int32_t k = 0; k < ns; ++k)
+            if (P.sn_parent[k] >= 0) P.sn_child[fill[P.sn_parent[k]]++] = k;
+    }
+    P.sn_relmap.assign(su, 0);
+    for (int32_t k = 0; k < ns; ++k) {
+        const int32_t p = P.sn_parent[k];
+        const int64_t nc = P.sn_c0[k + 1] - P.sn_c0[k];
+        const int64_t f = P.sn_f[k];
+        if (f > nc && p < 0) { err = "front has below rows but no parent"; return false; }
+        if (p < 0) continue;
+        const int32_t* pr = P.sn_rows.data() + P.sn_rows_off[p];
+        const int32_t pf = P.sn_f[p];
+        for (int64_t r = nc; r < f; ++r) {
+            const int32_t row = P.sn_rows[P.sn_rows_off[k] + r];
+            const int32_t* it = std::lower_bound(pr, pr + pf, row);
+            if (it == pr + pf || *it != row) { err = "child row missing from parent front"; return false; }
+            P.sn_relmap[P.sn_su_off[k] + (r - nc)] = static_cast<int32_t>(it - pr);
+        }
+    }
+    {
+        std::vector<int32_t> lvl(ns, 0);
+        int32_t maxl = 0;
+        for (int32_t k = 0; k < ns; ++k) {  // children precede parents
+            for (int32_t c = P.sn_child_ptr[k]; c < P.sn_child_ptr[k + 1]; ++c)
+                lvl[k] = std::max(lvl[k], lvl[P.sn_child[c]] + 1);
+            maxl = std::max(maxl, lvl[k]);
+        }
+        P.n_levels = ns ? maxl + 1 : 0;
+        P.lvl_ptr.assign(P.n_levels + 1, 0);
+        for (int32_t k = 0; k < ns; ++k) ++P.lvl_ptr[lvl[k] + 1];
+        for (int32_t l = 0; l < P.n_levels; ++l) P.lvl_ptr[l + 1] += P.lvl_ptr[l];
+        P.lvl_sn.assign(ns, 0);
+        std::vector<int32_t> fill(P.lvl_ptr.begin(), P.lvl_ptr.end() - 1);
+        for (int32_t k = 0; k < ns; ++k) P.lvl_sn[fill[lvl[k]]++] = k;
+    }
+
+    // --- gain assembly targets --------------------------------------------------------
+    {
+        struct PairRec { int32_t local; int32_t a; int32_t b; };
+        std::vector<std::vector<PairRec>> per_sn(ns);
+        for (int32_t q = 0; q < m; ++q) {
+            for (int32_t x = P.h_ptr[q]; x < P.h_ptr[q + 1]; ++x) {
+                const int32_t px = ps_of_state[P.h_col[x]];
+                for (int32_t y = x; y < P.h_ptr[q + 1]; ++y) {
+                    const int32_t py = ps_of_state[P.h_col[y]];
+                    const int32_t lo = std::min(px, py), hi = std::max(px, py);
+                    const int32_t k = sn_of_ps[lo];
+                    const int32_t* rows = P.sn_rows.data() + P.sn_rows_off[k];
+                    const int32_t f = P.sn_f[k];
+                    const int32_t* it = std::lower_bound(rows, rows + f, hi);
+                    if (it == rows + f || *it != hi) { err = "gain entry outside the front structure"; return false; }
+                    const int32_t lr = static_cast<int32_t>(it - rows);
+                    const int32_t lc = lo - P.sn_c0[k];
+                    per_sn[k].push_back({lr + lc * f, x, y});
+                }
+            }
+        }
+        P.sn_tgt_ptr.assign(ns + 1, 0);
+        P.tgt_pair_ptr.assign(1, 0);
+        for (int32_t k = 0; k < ns; ++k) {
+            auto& v = per_sn[k];
+            std::stable_sort(v.begin(), v.end(), [](const PairRec& u, const PairRec& w) { return u.local < w.local; });
+            for (size_t i = 0; i < v.size();) {
+                size_t j = i;
+                while (j < v.size() && v[j].local == v[i].local) {
+                    P.pair_a.push_back(v[j].a);
+                    P.pair_b.push_back(v[j].b);
+                    ++j;
+                }
+                P.tgt_local.push_back(v[i].local);
+                P.tgt_pair_ptr.push_back(static_cast<int64_t>(P.pair_a.size()));
+                i = j;
+            }
+            P.sn_tgt_ptr[k + 1] = static_cast<int32_t>(P.tgt_local.size());
+            std::vector<PairRec>().swap(v);
+        }
+    }
+
+    // --- RHS gather ------------------------------------------------------------------------
+    {
+        const int64_t nnz = static_cast<int64_t>(P.h_col.size());
+        P.rhs_ptr.assign(P.n_state + 1, 0);
+        for (int64_t h = 0; h < nnz; ++h) ++P.rhs_ptr[ps_of_state[P.h_col[h]] + 1];
+        for (int32_t p = 0; p < P.n_state; ++p) P.rhs_ptr[p + 1] += P.rhs_ptr[p];
+        P.rhs_h.assign(nnz, 0);
+        std::vector<int32_t> fill(P.rhs_ptr.begin(), P.rhs_ptr.end() - 1);
+        for (int64_t h = 0; h < nnz; ++h) P.rhs_h[fill[ps_of_state[P.h_col[h]]]++] = static_cast<int32_t>(h);
+    }
+    return true;
+}
+
+}  // namespace sle_gb300
