@@ -158,8 +158,9 @@ def profile_traffic(kernel):
     return None
 
 
-def stage_bytes(info, g):
-    """Algorithmic DRAM bytes per call of each stage (FP64 values, int32 indices)."""
+def stage_bytes(info, g, vb=8):
+    """Algorithmic DRAM bytes per call of each stage (vb-byte factor values,
+    FP64 vectors, int32 indices)."""
     m, n, ns = info.n_meas, info.n_bus, info.n_state
     nnz_h = info.nnz_h
     n_inj = int(np.isin(g.m_type, (2, 3, 7, 8)).sum())
@@ -169,29 +170,28 @@ def stage_bytes(info, g):
         # row metadata + z, w, sigma in; h, r, w_eff, w*r and H values out; state and Ybus gathers
         "evaluate": 72.0 * m + 8.0 * nnz_h + 16.0 * n + 28.0 * n_inj * avg_y + 48.0 * n_flow,
         # gain pairs + targets + H / weights in; L panels out; update matrices written and read once
-        "factor": 8.0 * info.n_gain_pairs + 12.0 * info.n_gain_targets + 8.0 * nnz_h + 8.0 * m
-                  + 8.0 * info.lx_size + 16.0 * info.u_size,
+        "factor": 8.0 * info.n_gain_pairs + 12.0 * info.n_gain_targets + vb * nnz_h + 8.0 * m
+                  + vb * info.lx_size + 2.0 * vb * info.u_size,
         # column gather lists + H + w*r in, b out
         "rhs": 16.0 * nnz_h + 8.0 * m + 8.0 * ns,
         # L read by the forward and the backward sweep; vectors
-        "solve": 16.0 * info.lx_size + 32.0 * ns,
+        "solve": 2.0 * vb * info.lx_size + 32.0 * ns,
         "update": 48.0 * n,
     }
 
 
-def run_gb300(args, world, rank, local):
-    from state_estimation_with_cuda_gb300 import Estimator, native, workloads
+def run_leg(args, g, snaps, local, mixed, world):
+    """One precision form: device-resident leg, end-to-end leg, profiled pass."""
+    from state_estimation_with_cuda_gb300 import Estimator, native
     from state_estimation_with_cuda_gb300.api import MODE_PRECISION
 
-    g = workloads.make(WORKLOAD)
-    snaps = [g.renoise(u).copy() for u in range(args.warmup + args.steps)]
     cfg = native.SLE_Config()
     est0 = Estimator()
     lib = est0.lib
     lib.sle_GetConfig(est0.h, ctypes.byref(cfg))
     est0.close()
     cfg.device_id = local
-    cfg.use_double_precision = 1
+    cfg.use_double_precision = 0 if mixed else 1
     est = Estimator(cfg)
     est.load_network(g, z=g.z)
     est.upload_model()
@@ -218,7 +218,6 @@ def run_gb300(args, world, rank, local):
     for i in range(args.warmup):
         device_step(i)
     clocks = ClockSampler(local)
-    lib.sle_ExResetStats(est.h)
     st0 = native.SLE_ExStats()
     lib.sle_ExGetStats(est.h, ctypes.byref(st0))
     barrier(world)
@@ -234,11 +233,15 @@ def run_gb300(args, world, rank, local):
     barrier(world)
     total_ms = allreduce_max(sum(times), world)
     launches = st1.total_launches - st0.total_launches
+    v_dev = np.empty(g.n_bus)
+    t_dev = np.empty(g.n_bus)
+    dp = ctypes.POINTER(ctypes.c_double)
+    est._check(lib.sle_GetVoltageMagnitudes(est.h, v_dev.ctypes.data_as(dp), g.n_bus))
+    est._check(lib.sle_GetVoltageAngles(est.h, t_dev.ctypes.data_as(dp), g.n_bus))
 
     # ---- end-to-end leg through the C ABI with host buffers ---------------------------
     vbuf = np.empty(g.n_bus)
     tbuf = np.empty(g.n_bus)
-    dp = ctypes.POINTER(ctypes.c_double)
     e2e_times = []
     for k in range(args.warmup + args.steps):
         z = snaps[k]
@@ -264,52 +267,82 @@ def run_gb300(args, world, rank, local):
         device_step(args.warmup + k)
     prof = native.SLE_ExStats()
     lib.sle_ExGetStats(est.h, ctypes.byref(prof))
+    est.close()
     names = ["evaluate", "factor", "rhs", "solve", "update", "final"]
-    stage_ms = {names[i]: prof.ms[i] for i in range(6)}
-    stage_launch = {names[i]: prof.launches[i] for i in range(6)}
-    stage_calls = {names[i]: prof.calls[i] for i in range(6)}
-    dom = max(("evaluate", "factor", "rhs", "solve", "update"), key=lambda s: stage_ms[s])
-    sb = stage_bytes(info, g)
-    peak, peak_kind = load_peaks()
-    per_call_ms = stage_ms[dom] / max(stage_calls[dom], 1)
-    achieved = sb[dom] / (per_call_ms * 1e-3) / 1e9 if per_call_ms > 0 else 0.0
-    kernel_name = {"evaluate": "k_evaluate", "factor": "front_factorisation", "rhs": "k_rhs",
-                   "solve": "front_solves", "update": "k_update"}[dom]
-    traffic = profile_traffic(kernel_name)
+    return dict(
+        times=times, iters=iters, total_ms=total_ms, launches=launches, clk=clk, e2e_times=e2e_times,
+        e2e_total=e2e_total, info=info, v=v_dev, th=t_dev,
+        stage_ms={names[i]: prof.ms[i] for i in range(6)},
+        stage_launch={names[i]: prof.launches[i] for i in range(6)},
+        stage_calls={names[i]: prof.calls[i] for i in range(6)})
 
+
+def roofline(leg, g, mixed):
+    info = leg["info"]
+    dom = max(("evaluate", "factor", "rhs", "solve", "update"), key=lambda s: leg["stage_ms"][s])
+    sb = stage_bytes(info, g, 4 if mixed else 8)
+    peak, peak_kind = load_peaks()
+    per_call_ms = leg["stage_ms"][dom] / max(leg["stage_calls"][dom], 1)
+    achieved = sb[dom] / (per_call_ms * 1e-3) / 1e9 if per_call_ms > 0 else 0.0
+    kernel = {"evaluate": "k_evaluate", "factor": "front_factorisation", "rhs": "k_rhs", "solve": "front_solves",
+              "update": "k_update"}[dom]
+    return {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 2), "peak": peak, "peak_kind": peak_kind,
+            "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": profile_traffic(kernel),
+            "algorithmic_bytes_per_call": int(sb[dom])}
+
+
+def run_gb300(args, world, rank, local):
+    from state_estimation_with_cuda_gb300 import workloads
+
+    g = workloads.make(WORKLOAD)
+    snaps = [g.renoise(u).copy() for u in range(args.warmup + args.steps)]
+    mixed = run_leg(args, g, snaps, local, True, world)
+    fp64 = run_leg(args, g, snaps, local, False, world)
     out = None
     if rank == 0:
-        value = world * args.steps / (total_ms * 1e-3)
-        e2e_value = world * args.steps / (e2e_total * 1e-3)
-        lat = np.array(times)
+        def summary(leg):
+            lat = np.array(leg["times"])
+            return {"value": round(world * args.steps / (leg["total_ms"] * 1e-3), 3),
+                    "ms_per_step": round(leg["total_ms"] / args.steps, 5),
+                    "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 4),
+                                   "p99": round(float(np.percentile(lat, 99)), 4)},
+                    "e2e": {"value": round(world * args.steps / (leg["e2e_total"] * 1e-3), 3), "unit": UNIT,
+                            "h2d_bytes_per_step": 8 * g.n_meas, "d2h_bytes_per_step": 16 * g.n_bus,
+                            "latency_ms": {"p50": round(float(np.percentile(leg["e2e_times"], 50)), 4),
+                                           "p99": round(float(np.percentile(leg["e2e_times"], 99)), 4)}},
+                    "iterations_per_solve": round(float(np.mean(leg["iters"])), 3),
+                    "gpu_launches": int(leg["launches"]),
+                    "stages_ms_per_solve": {k: round(v / max(args.steps, 1), 5) for k, v in leg["stage_ms"].items()},
+                    "stage_launches_per_solve": {k: round(v / max(args.steps, 1), 2)
+                                                 for k, v in leg["stage_launch"].items()}}
+        sm, sf = summary(mixed), summary(fp64)
+        err = float(max(np.abs(mixed["v"] - fp64["v"]).max(), np.abs(mixed["th"] - fp64["th"]).max()))
+        info = mixed["info"]
         out = {
-            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 5), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+            "metric": METRIC, "value": sm["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sm["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 gain/factor + f64 residual/refinement/state",
+            "data": "synthetic (seeded generator)",
             "config": {
                 "workload": "grid10k hot-start solves: %d buses, %d branches, %d rows, %d states; 1%% of rows "
-                            "re-noised per step; FP64, tol 1e-6, gain refactorised every iteration"
-                            % (g.n_bus, g.n_branch, g.n_meas, 2 * g.n_bus - 1),
+                            "re-noised per step; tol 1e-6, gain refactorised every iteration; mixed precision "
+                            "(value) and plain FP64 (fp64)" % (g.n_bus, g.n_branch, g.n_meas, 2 * g.n_bus - 1),
                 "l2": "flushed before every timed step (256 MiB write)",
                 "parallelism": "replicas" if world > 1 else "single",
-                "iterations_per_solve": round(float(np.mean(iters)), 3),
+                "iterations_per_solve": sm["iterations_per_solve"],
             },
-            "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 4), "p99": round(float(np.percentile(lat, 99)), 4)},
-            "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": 8 * g.n_meas,
-                    "d2h_bytes_per_step": 16 * g.n_bus,
-                    "latency_ms": {"p50": round(float(np.percentile(e2e_times, 50)), 4),
-                                   "p99": round(float(np.percentile(e2e_times, 99)), 4)}},
-            "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": round(achieved, 2), "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 5),
-                         "traffic": traffic, "algorithmic_bytes_per_call": int(sb[dom])},
-            "stages_ms_per_solve": {k: round(v / max(args.steps, 1), 5) for k, v in stage_ms.items()},
-            "stage_launches_per_solve": {k: round(v / max(args.steps, 1), 2) for k, v in stage_launch.items()},
-            "clocks": clk,
+            "latency_ms": sm["latency_ms"],
+            "e2e": sm["e2e"],
+            "gpu_launches": sm["gpu_launches"],
+            "roofline": roofline(mixed, g, True),
+            "stages_ms_per_solve": sm["stages_ms_per_solve"],
+            "stage_launches_per_solve": sm["stage_launches_per_solve"],
+            "fp64": dict(sf, roofline=roofline(fp64, g, False)),
+            "mixed_vs_fp64_max_state_err": err,
+            "clocks": mixed["clk"],
             "plan": {"nnz_l": info.nnz_l, "n_super": info.n_super, "levels": info.n_levels,
                      "max_front": info.max_front, "factor_flops": info.factor_flops},
         }
-    est.close()
     return out, g
 
 

@@ -42,7 +42,11 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
  *                              wls_solver.cu:416-419)
  *   "ordering"              0 approximate minimum degree, 1 natural,
  *                           2 nested dissection (takes effect at upload)
- *   "use_double_precision"  as SLE_Config.use_double_precision */
+ *   "use_double_precision"  as SLE_Config.use_double_precision (re-uploads)
+ *   "refine_steps"          mixed precision: refinement steps per Gauss-Newton
+ *                           step (default 1)
+ *   "big_front_flops"       FP64: fronts with more factor flops than this use
+ *                           the tiled multi-CTA kernels (re-uploads) */
 SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* key, double value);
 
 typedef struct SLE_ExPlanInfo {

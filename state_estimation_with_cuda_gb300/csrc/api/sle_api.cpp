@@ -314,6 +314,7 @@ SLE_API SLE_StatusCode SLE_CALL sle_SetConfig(SLE_Handle handle, const SLE_Confi
     EngineConfig c = E(handle)->cfg;
     cfg_from_c(config, c);
     c.device_id = E(handle)->cfg.device_id;  // device is fixed after creation
+    if (c.use_double_precision != E(handle)->cfg.use_double_precision) E(handle)->model.structure_dirty = true;
     E(handle)->cfg = c;
     return SLE_OK;
 }
@@ -946,7 +947,11 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* k
     if (k == "exact_jacobian") c.exact_jacobian = value != 0.0;
     else if (k == "gain_policy") c.gain_policy = static_cast<int32_t>(value);
     else if (k == "ordering") { c.ordering = static_cast<int32_t>(value); E(handle)->model.structure_dirty = true; }
-    else if (k == "use_double_precision") c.use_double_precision = value != 0.0;
+    else if (k == "use_double_precision") {
+        c.use_double_precision = value != 0.0;
+        E(handle)->model.structure_dirty = true;
+    } else if (k == "refine_steps") c.refine_steps = static_cast<int32_t>(value);
+    else if (k == "big_front_flops") { c.big_front_flops = value; E(handle)->model.structure_dirty = true; }
     else return fail(SLE_ERROR_INVALID_ARGUMENT, "unknown option");
     return SLE_OK;
 }

@@ -49,6 +49,7 @@ Engine::~Engine() {
 }
 
 void Engine::release_device() {
+    drop_graphs();
     if (d_slots_) cudaFree(d_slots_);
     d_slots_ = nullptr;
     n_slots_ = 0;
@@ -123,6 +124,110 @@ int32_t Engine::analyze() {
     return 0;
 }
 
+// Splits every level into single-CTA fronts and big fronts (more factor
+// flops than cfg.big_front_flops, or too large for shared memory), lays out
+// the factor storage (big fronts in place in an f x f region) and builds the
+// tile work lists of the big-front kernels.
+void Engine::build_schedule() {
+    const Plan& P = plan_;
+    const int32_t ns = P.n_super, nl = P.n_levels;
+    sch_small_ptr_.assign(nl + 1, 0);
+    sch_small_maxf_.assign(nl, 0);
+    sch_asm_ptr_.assign(nl + 1, 0);
+    sch_panels_.assign(nl, 0);
+    sch_step_ptr_.assign(nl + 1, 0);
+    sch_all_ptr_.assign(nl + 1, 0);
+    sch_maxf_.assign(nl, 0);
+    sch_maxpanel_.assign(nl, 0);
+    sch_small_.clear();
+    sch_all_.clear();
+    sch_asm_.clear();
+    sch_pot_.clear();
+    sch_pan_.clear();
+    sch_upd_.clear();
+    sch_pot_ptr_.assign(1, 0);
+    sch_pan_ptr_.assign(1, 0);
+    sch_upd_ptr_.assign(1, 0);
+    lay_lx_off_.assign(ns + 1, 0);
+    lay_u_off_.assign(ns + 1, 0);
+    lay_u_ld_.assign(ns, 0);
+    lay_u_big_.assign(ns, 0);
+    std::vector<char> big(ns, 0);
+    for (int32_t s = 0; s < ns; ++s) {
+        const int64_t f = P.sn_f[s], nc = P.sn_c0[s + 1] - P.sn_c0[s];
+        double fl = 0.0;
+        for (int64_t c = 0; c < nc; ++c) fl += static_cast<double>(f - c - 1) * (f - c);
+        // FP64 work per front is costly on this GPU, so the FP64 pipeline moves
+        // fronts with many flops to the tiled path; in FP32 only size decides
+        big[s] = (f > kSmallFrontMax || (!mixed_ && fl > cfg.big_front_flops)) ? 1 : 0;
+    }
+    int64_t lx = 0, uu = 0;
+    for (int32_t s = 0; s < ns; ++s) {
+        const int64_t f = P.sn_f[s], nc = P.sn_c0[s + 1] - P.sn_c0[s];
+        lay_lx_off_[s] = lx;
+        if (big[s]) {
+            lay_u_off_[s] = lx + nc + nc * f;
+            lay_u_ld_[s] = static_cast<int32_t>(f);
+            lay_u_big_[s] = 1;
+            lx += f * f;
+        } else {
+            lay_u_off_[s] = uu;
+            lay_u_ld_[s] = static_cast<int32_t>(f - nc);
+            lx += f * nc;
+            uu += (f - nc) * (f - nc);
+        }
+    }
+    lay_lx_off_[ns] = lx;
+    lay_u_off_[ns] = uu;
+    lay_lx_size_ = lx;
+    lay_u_size_ = uu;
+    for (int32_t l = 0; l < nl; ++l) {
+        std::vector<int32_t> bigs;
+        for (int32_t x = P.lvl_ptr[l]; x < P.lvl_ptr[l + 1]; ++x) {
+            const int32_t s = P.lvl_sn[x];
+            sch_all_.push_back(s);
+            sch_maxf_[l] = std::max(sch_maxf_[l], P.sn_f[s]);
+            sch_maxpanel_[l] = std::max<int64_t>(sch_maxpanel_[l],
+                                                 static_cast<int64_t>(P.sn_f[s]) * (P.sn_c0[s + 1] - P.sn_c0[s]));
+            if (big[s]) {
+                bigs.push_back(s);
+            } else {
+                sch_small_.push_back(s);
+                sch_small_maxf_[l] = std::max(sch_small_maxf_[l], P.sn_f[s]);
+            }
+        }
+        int32_t panels = 0;
+        for (int32_t s : bigs) {
+            const int32_t f = P.sn_f[s], nc = P.sn_c0[s + 1] - P.sn_c0[s];
+            const int32_t tiles = (f + kTile - 1) / kTile;
+            for (int32_t tj = 0; tj < tiles; ++tj) sch_asm_.push_back(make_int4(s, tj, 0, 0));
+            panels = std::max(panels, (nc + kTile - 1) / kTile);
+        }
+        sch_panels_[l] = panels;
+        sch_step_ptr_[l + 1] = sch_step_ptr_[l] + panels;
+        for (int32_t p = 0; p < panels; ++p) {
+            for (int32_t s : bigs) {
+                const int32_t f = P.sn_f[s], nc = P.sn_c0[s + 1] - P.sn_c0[s];
+                if (nc <= p * kTile) continue;
+                const int32_t tiles = (f + kTile - 1) / kTile;
+                const int32_t pb = std::min(kTile, nc - p * kTile);
+                const int32_t q0 = p * kTile + pb;
+                sch_pot_.push_back(make_int4(s, p, 0, 0));
+                for (int32_t ti = p + 1; ti < tiles; ++ti) sch_pan_.push_back(make_int4(s, ti, 0, 0));
+                if (q0 < f)
+                    for (int32_t tj = q0 / kTile; tj < tiles; ++tj)
+                        for (int32_t ti = tj; ti < tiles; ++ti) sch_upd_.push_back(make_int4(s, ti, tj, 0));
+            }
+            sch_pot_ptr_.push_back(static_cast<int32_t>(sch_pot_.size()));
+            sch_pan_ptr_.push_back(static_cast<int32_t>(sch_pan_.size()));
+            sch_upd_ptr_.push_back(static_cast<int32_t>(sch_upd_.size()));
+        }
+        sch_small_ptr_[l + 1] = static_cast<int32_t>(sch_small_.size());
+        sch_asm_ptr_[l + 1] = static_cast<int32_t>(sch_asm_.size());
+        sch_all_ptr_[l + 1] = static_cast<int32_t>(sch_all_.size());
+    }
+}
+
 int32_t Engine::upload() {
     int32_t rc = initialize();
     if (rc) return rc;
@@ -133,35 +238,13 @@ int32_t Engine::upload() {
     if (rc) return rc;
     const int32_t n = model.n_bus(), nbr = model.n_branch(), m = model.n_meas();
     const Plan& P = plan_;
-    // level schedule
-    sch_small_ptr_.assign(P.n_levels + 1, 0);
-    sch_big_ptr_.assign(P.n_levels + 1, 0);
-    sch_all_ptr_.assign(P.n_levels + 1, 0);
-    sch_small_.clear();
-    sch_big_.clear();
-    sch_all_.clear();
-    sch_maxf_.assign(P.n_levels, 0);
-    big_off_.assign(P.n_super + 1, -1);
-    int64_t big_total = 0;
-    int32_t max_small = 1;
-    for (int32_t l = 0; l < P.n_levels; ++l) {
-        for (int32_t x = P.lvl_ptr[l]; x < P.lvl_ptr[l + 1]; ++x) {
-            const int32_t s = P.lvl_sn[x];
-            const int32_t f = P.sn_f[s];
-            sch_all_.push_back(s);
-            sch_maxf_[l] = std::max(sch_maxf_[l], f);
-            if (f <= kSmallFrontMax) {
-                sch_small_.push_back(s);
-                max_small = std::max(max_small, f);
-            } else {
-                sch_big_.push_back(s);
-                big_off_[s] = big_total;
-                big_total += static_cast<int64_t>(f) * f;
-            }
-        }
-        sch_small_ptr_[l + 1] = static_cast<int32_t>(sch_small_.size());
-        sch_big_ptr_[l + 1] = static_cast<int32_t>(sch_big_.size());
-        sch_all_ptr_[l + 1] = static_cast<int32_t>(sch_all_.size());
+    mixed_ = cfg.use_double_precision == 0;
+    build_schedule();
+    {
+        std::vector<int32_t> ps_of_state(P.n_state);
+        for (int32_t p = 0; p < P.n_state; ++p) ps_of_state[P.state_of_ps[p]] = p;
+        h_pcol_.resize(P.h_col.size());
+        for (size_t h = 0; h < P.h_col.size(); ++h) h_pcol_[h] = ps_of_state[P.h_col[h]];
     }
     const int64_t nnz_h = static_cast<int64_t>(P.h_col.size());
     const int64_t nnz_y = static_cast<int64_t>(P.y_col.size());
@@ -201,6 +284,7 @@ int32_t Engine::upload() {
         net_.m_w = c.take<double>(m);
         net_.h_ptr = c.take<int32_t>(m + 1);
         net_.h_row = c.take<int32_t>(nnz_h);
+        net_.h_pcol = c.take<int32_t>(nnz_h);
         // factor plan
         fac_.sn_c0 = c.take<int32_t>(ns + 1);
         fac_.sn_f = c.take<int32_t>(ns);
@@ -221,9 +305,14 @@ int32_t Engine::upload() {
         fac_.rhs_h = c.take<int32_t>(P.rhs_h.size());
         fac_.bus_ps_theta = c.take<int32_t>(n);
         fac_.bus_ps_v = c.take<int32_t>(n);
-        fac_.sn_big_off = c.take<int64_t>(ns + 1);
+        fac_.sn_u_ld = c.take<int32_t>(ns);
+        fac_.sn_u_big = c.take<uint8_t>(ns);
         d_small_ = c.take<int32_t>(sch_small_.size());
         d_all_ = c.take<int32_t>(sch_all_.size());
+        d_asm_ = c.take<int4>(sch_asm_.size());
+        d_pot_ = c.take<int4>(sch_pot_.size());
+        d_pan_ = c.take<int4>(sch_pan_.size());
+        d_upd_ = c.take<int4>(sch_upd_.size());
         // work
         work_.v = c.take<double>(n);
         work_.th = c.take<double>(n);
@@ -235,10 +324,20 @@ int32_t Engine::upload() {
         work_.hval = c.take<double>(nnz_h);
         work_.rhs = c.take<double>(P.n_state);
         work_.sol = c.take<double>(P.n_state);
-        work_.lx = c.take<double>(P.lx_size);
-        work_.u = c.take<double>(P.u_size);
+        work_.hval32 = mixed_ ? c.take<float>(nnz_h) : nullptr;
+        work_.b0 = c.take<double>(P.n_state);
+        work_.dx = c.take<double>(P.n_state);
+        work_.hdx = c.take<double>(m);
+        work_.lx = mixed_ ? nullptr : c.take<double>(lay_lx_size_);
+        work_.u = mixed_ ? nullptr : c.take<double>(lay_u_size_);
+        work_.lx32 = mixed_ ? c.take<float>(lay_lx_size_) : nullptr;
+        work_.u32 = mixed_ ? c.take<float>(lay_u_size_) : nullptr;
         work_.su = c.take<double>(P.su_size);
-        work_.big = c.take<double>(big_total);
+        work_.gvals = c.take<double>(P.tgt_local.size());
+        work_.rdiag = c.take<double>(P.n_state);
+        work_.rhs32 = mixed_ ? c.take<float>(P.n_state) : nullptr;
+        work_.sol32 = mixed_ ? c.take<float>(P.n_state) : nullptr;
+        work_.su32 = mixed_ ? c.take<float>(P.su_size) : nullptr;
         work_.p_inj = c.take<double>(n);
         work_.q_inj = c.take<double>(n);
         work_.pf = c.take<double>(nbr);
@@ -299,12 +398,13 @@ int32_t Engine::upload() {
     chk(put(const_cast<double*>(net_.m_w), model.m_w, st_));
     chk(put(const_cast<int32_t*>(net_.h_ptr), P.h_ptr, st_));
     chk(put(const_cast<int32_t*>(net_.h_row), P.h_row, st_));
+    chk(put(const_cast<int32_t*>(net_.h_pcol), h_pcol_, st_));
     chk(put(const_cast<int32_t*>(fac_.sn_c0), P.sn_c0, st_));
     chk(put(const_cast<int32_t*>(fac_.sn_f), P.sn_f, st_));
     chk(put(const_cast<int64_t*>(fac_.sn_rows_off), P.sn_rows_off, st_));
     chk(put(const_cast<int32_t*>(fac_.sn_rows), P.sn_rows, st_));
-    chk(put(const_cast<int64_t*>(fac_.sn_lx_off), P.sn_lx_off, st_));
-    chk(put(const_cast<int64_t*>(fac_.sn_u_off), P.sn_u_off, st_));
+    chk(put(const_cast<int64_t*>(fac_.sn_lx_off), lay_lx_off_, st_));
+    chk(put(const_cast<int64_t*>(fac_.sn_u_off), lay_u_off_, st_));
     chk(put(const_cast<int64_t*>(fac_.sn_su_off), P.sn_su_off, st_));
     chk(put(const_cast<int32_t*>(fac_.sn_child_ptr), P.sn_child_ptr, st_));
     chk(put(const_cast<int32_t*>(fac_.sn_child), P.sn_child, st_));
@@ -318,32 +418,42 @@ int32_t Engine::upload() {
     chk(put(const_cast<int32_t*>(fac_.rhs_h), P.rhs_h, st_));
     chk(put(const_cast<int32_t*>(fac_.bus_ps_theta), P.bus_ps_theta, st_));
     chk(put(const_cast<int32_t*>(fac_.bus_ps_v), P.bus_ps_v, st_));
-    chk(put(const_cast<int64_t*>(fac_.sn_big_off), big_off_, st_));
+    chk(put(const_cast<int32_t*>(fac_.sn_u_ld), lay_u_ld_, st_));
+    chk(put(const_cast<uint8_t*>(fac_.sn_u_big), lay_u_big_, st_));
     chk(put(d_small_, sch_small_, st_));
     chk(put(d_all_, sch_all_, st_));
+    chk(put(d_asm_, sch_asm_, st_));
+    chk(put(d_pot_, sch_pot_, st_));
+    chk(put(d_pan_, sch_pan_, st_));
+    chk(put(d_upd_, sch_upd_, st_));
     chk(put(work_.v, model.bus_v, st_));
     chk(put(work_.th, model.bus_th, st_));
     chk(put(work_.z, model.m_value, st_));
     chk(cudaMemsetAsync(work_.status, 0, sizeof(DevStatus), st_));
     chk(launch_admittance_and_ybus(net_, st_));
+    chk(prepare_factor_kernels());
     chk(cudaStreamSynchronize(st_));
     if (e != cudaSuccess) return set_cuda_error(e, "upload");
 
     sched_.n_levels = P.n_levels;
+    sched_.n_tgt = static_cast<int32_t>(P.tgt_local.size());
     sched_.h_small_ptr = sch_small_ptr_.data();
     sched_.d_small = d_small_;
-    sched_.h_big_ptr = sch_big_ptr_.data();
-    sched_.h_big = sch_big_.data();
+    sched_.h_small_maxf = sch_small_maxf_.data();
+    sched_.h_asm_ptr = sch_asm_ptr_.data();
+    sched_.d_asm = d_asm_;
+    sched_.h_lvl_panels = sch_panels_.data();
+    sched_.h_step_ptr = sch_step_ptr_.data();
+    sched_.h_pot_ptr = sch_pot_ptr_.data();
+    sched_.d_pot = d_pot_;
+    sched_.h_pan_ptr = sch_pan_ptr_.data();
+    sched_.d_pan = d_pan_;
+    sched_.h_upd_ptr = sch_upd_ptr_.data();
+    sched_.d_upd = d_upd_;
     sched_.h_all_ptr = sch_all_ptr_.data();
     sched_.d_all = d_all_;
     sched_.h_lvl_maxf = sch_maxf_.data();
-    sched_.h_sn_f = plan_.sn_f.data();
-    sched_.h_sn_c0 = plan_.sn_c0.data();
-    sched_.h_big_off = big_off_.data();
-    sched_.h_tgt_ptr = plan_.sn_tgt_ptr.data();
-    sched_.h_child_ptr = plan_.sn_child_ptr.data();
-    sched_.h_child = plan_.sn_child.data();
-    sched_.max_small_f = max_small;
+    sched_.h_lvl_maxpanel = sch_maxpanel_.data();
 
     if (h_stage_n_ < static_cast<size_t>(m)) {
         if (h_stage_) cudaFreeHost(h_stage_);
@@ -412,6 +522,7 @@ int32_t Engine::flat_start() {
 SolveParams Engine::params(const SolveRequest& rq) const {
     SolveParams sp{};
     sp.exact_jacobian = cfg.exact_jacobian;
+    sp.mixed = mixed_ ? 1 : 0;
     sp.robust = rq.robust;
     sp.huber_gamma = rq.huber_gamma;
     sp.tol = rq.tolerance;
@@ -450,32 +561,96 @@ void Engine::collect_stage_times() {
     ev_used_ = 0;
 }
 
-int32_t Engine::run_iteration(const SolveParams& sp, bool refactor) {
+int32_t Engine::enqueue_iteration(const SolveParams& sp, bool refactor, int64_t* per_stage) {
     cudaError_t e = cudaMemsetAsync(&work_.status->flags, 0, sizeof(uint32_t), st_);
-    int64_t l0 = g_kernel_launches.load();
-    int32_t mk = stage_begin(ST_EVALUATE);
-    if (e == cudaSuccess) e = launch_evaluate(net_, work_, sp, st_);
-    stage_end(ST_EVALUATE, mk, l0);
-    if (e == cudaSuccess && refactor) {
-        l0 = g_kernel_launches.load();
-        mk = stage_begin(ST_FACTOR);
-        e = launch_factor(net_, fac_, work_, sched_, st_);
-        stage_end(ST_FACTOR, mk, l0);
+    auto stage = [&](int32_t st, auto&& fn) {
+        if (e != cudaSuccess) return;
+        const int64_t l0 = g_kernel_launches.load();
+        const int32_t mk = stage_begin(st);
+        e = fn();
+        if (per_stage) per_stage[st] += g_kernel_launches.load() - l0;
+        if (mk >= 0) cudaEventRecord(ev_pool_[mk + 1], st_);
+    };
+    stage(ST_EVALUATE, [&] { return launch_evaluate(net_, work_, sp, st_); });
+    if (!mixed_) {
+        if (refactor) stage(ST_FACTOR, [&] { return launch_factor(net_, fac_, work_, sched_, st_); });
+        stage(ST_RHS, [&] { return launch_rhs(net_, fac_, work_, st_); });
+        stage(ST_SOLVE, [&] { return launch_solve(fac_, work_, sched_, st_); });
+        stage(ST_UPDATE, [&] { return launch_update(net_, fac_, work_, sp, work_.sol, st_); });
+    } else {
+        if (refactor) stage(ST_FACTOR, [&] { return launch_factor32(net_, fac_, work_, sched_, st_); });
+        stage(ST_RHS, [&] { return launch_rhs(net_, fac_, work_, st_); });
+        stage(ST_SOLVE, [&] {
+            cudaError_t ee = launch_to_fp32(fac_, work_, st_);
+            if (ee == cudaSuccess) ee = launch_solve32(fac_, work_, sched_, st_);
+            if (ee == cudaSuccess) ee = launch_refine_begin(fac_, work_, st_);
+            for (int32_t k = 0; k < cfg.refine_steps && ee == cudaSuccess; ++k) {
+                ee = launch_refine_residual(net_, fac_, work_, st_);
+                if (ee == cudaSuccess) ee = launch_solve32(fac_, work_, sched_, st_);
+                if (ee == cudaSuccess) ee = launch_refine_accumulate(fac_, work_, st_);
+            }
+            return ee;
+        });
+        stage(ST_UPDATE, [&] { return launch_update(net_, fac_, work_, sp, work_.dx, st_); });
     }
-    l0 = g_kernel_launches.load();
-    mk = stage_begin(ST_RHS);
-    if (e == cudaSuccess) e = launch_rhs(net_, fac_, work_, st_);
-    stage_end(ST_RHS, mk, l0);
-    l0 = g_kernel_launches.load();
-    mk = stage_begin(ST_SOLVE);
-    if (e == cudaSuccess) e = launch_solve(fac_, work_, sched_, st_);
-    stage_end(ST_SOLVE, mk, l0);
-    l0 = g_kernel_launches.load();
-    mk = stage_begin(ST_UPDATE);
-    if (e == cudaSuccess) e = launch_update(net_, fac_, work_, sp, st_);
-    stage_end(ST_UPDATE, mk, l0);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_status_, work_.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st_);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) {
+        set_cuda_error(e, "iteration");
+        return -3;
+    }
+    return 0;
+}
+
+void Engine::drop_graphs() {
+    for (auto& g : graphs_) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = IterGraph();
+    }
+}
+
+int32_t Engine::run_iteration(const SolveParams& sp, bool refactor) {
+    int64_t per_stage[ST_COUNT] = {0, 0, 0, 0, 0, 0};
+    const bool use_graph = cfg.use_cuda_graphs && !cfg.enable_profiling;
+    if (!use_graph) {
+        const int32_t rc = enqueue_iteration(sp, refactor, per_stage);
+        if (rc) return rc;
+    } else {
+        IterGraph& g = graphs_[refactor ? 1 : 0];
+        if (!g.exec || std::memcmp(&g.sp, &sp, sizeof(sp)) != 0) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            g = IterGraph();
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return set_cuda_error(e, "graph capture");
+            const int64_t before = g_kernel_launches.load();
+            const int32_t rc = enqueue_iteration(sp, refactor, g.launches);
+            e = cudaStreamEndCapture(st_, &graph);
+            g.total = g_kernel_launches.load() - before;
+            g_kernel_launches -= g.total;  // counted when the graph runs
+            if (rc) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&g.exec, graph, 0);
+            if (graph) cudaGraphDestroy(graph);
+            if (e != cudaSuccess) {
+                g.exec = nullptr;
+                return set_cuda_error(e, "graph instantiate");
+            }
+            g.sp = sp;
+        }
+        cudaError_t e = cudaGraphLaunch(g.exec, st_);
+        if (e != cudaSuccess) return set_cuda_error(e, "graph launch");
+        g_kernel_launches += g.total;
+        for (int i = 0; i < ST_COUNT; ++i) per_stage[i] = g.launches[i];
+    }
+    for (int i = 0; i < ST_COUNT; ++i) {
+        if (i == ST_FACTOR && !refactor) continue;
+        if (i == ST_OTHER) continue;
+        stats.launches[i] += per_stage[i];
+        stats.calls[i] += 1;
+    }
+    cudaError_t e = cudaStreamSynchronize(st_);
     ++stats.iterations;
     if (e != cudaSuccess) {
         set_cuda_error(e, "iteration");
@@ -624,6 +799,7 @@ int32_t Engine::evaluate_at(const double* v, const double* th, int32_t exact) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(work_.th, th, sizeof(double) * n, cudaMemcpyHostToDevice, st_);
     SolveParams sp{};
     sp.exact_jacobian = exact;
+    sp.mixed = mixed_ ? 1 : 0;
     sp.robust = 0;
     sp.huber_gamma = cfg.huber_gamma;
     sp.tol = cfg.convergence_tolerance;
@@ -641,6 +817,10 @@ int32_t Engine::evaluate_at(const double* v, const double* th, int32_t exact) {
 
 int32_t Engine::export_gain(std::vector<int32_t>& rows, std::vector<int32_t>& cols, std::vector<double>& vals) {
     const Plan& P = plan_;
+    if (mixed_) {
+        last_error = "stage access needs the FP64 pipeline (use_double_precision = 1)";
+        return -4;
+    }
     const int32_t nt = static_cast<int32_t>(P.tgt_local.size());
     double* d = nullptr;
     cudaError_t e = cudaMalloc(&d, sizeof(double) * std::max(nt, 1));
@@ -666,6 +846,10 @@ int32_t Engine::export_gain(std::vector<int32_t>& rows, std::vector<int32_t>& co
 
 int32_t Engine::factor_and_solve(const double* rhs_orig, double* x_orig) {
     const Plan& P = plan_;
+    if (mixed_) {
+        last_error = "stage access needs the FP64 pipeline (use_double_precision = 1)";
+        return -4;
+    }
     std::vector<double> b(P.n_state);
     for (int32_t p = 0; p < P.n_state; ++p) b[p] = rhs_orig[P.state_of_ps[p]];
     cudaError_t e = cudaMemsetAsync(&work_.status->flags, 0, sizeof(uint32_t), st_);

@@ -39,6 +39,8 @@ struct EngineConfig {
     int32_t exact_jacobian = 1;  // 0: the reference's Jacobian formulas
     int32_t gain_policy = 0;     // 0: refactor every iteration; 1: reuse the factor until invalidated
     int32_t ordering = 0;        // symbolic ordering (see SymbolicParams)
+    double big_front_flops = 2.0e5;  // FP64: fronts above this many factor flops use the tiled multi-CTA path
+    int32_t refine_steps = 1;        // mixed precision: refinement steps per Gauss-Newton step
 };
 
 enum class Mode : int32_t { REALTIME = 0, PRECISION = 1 };
@@ -130,6 +132,7 @@ public:
 
 private:
     bool init_ = false, analyzed_ = false, uploaded_ = false, factor_valid_ = false;
+    bool mixed_ = false;  // pipeline of the current upload: FP32 gain/factor + FP64 refinement
     int32_t stale_ = 0;  // DL_* mask of host copies older than the device
     cudaStream_t st_ = nullptr;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
@@ -143,10 +146,33 @@ private:
     DevFactor fac_{};
     DevWork work_{};
     LevelSchedule sched_{};
-    std::vector<int32_t> sch_small_ptr_, sch_small_, sch_big_ptr_, sch_big_, sch_all_ptr_, sch_all_, sch_maxf_;
-    std::vector<int64_t> big_off_;
+    // level schedule (host copies) and in-place storage layout
+    std::vector<int32_t> sch_small_ptr_, sch_small_, sch_small_maxf_, sch_asm_ptr_, sch_panels_, sch_step_ptr_,
+        sch_pot_ptr_, sch_pan_ptr_, sch_upd_ptr_, sch_all_ptr_, sch_all_, sch_maxf_;
+    std::vector<int4> sch_asm_, sch_pot_, sch_pan_, sch_upd_;
+    std::vector<int64_t> sch_maxpanel_;
+    std::vector<int64_t> lay_lx_off_, lay_u_off_;
+    std::vector<int32_t> lay_u_ld_, h_pcol_;
+    std::vector<uint8_t> lay_u_big_;
+    int64_t lay_lx_size_ = 0, lay_u_size_ = 0;
     int32_t* d_small_ = nullptr;
     int32_t* d_all_ = nullptr;
+    int4* d_asm_ = nullptr;
+    int4* d_pot_ = nullptr;
+    int4* d_pan_ = nullptr;
+    int4* d_upd_ = nullptr;
+    void build_schedule();
+    // CUDA graphs of one Gauss-Newton iteration, [0] without and [1] with
+    // the refactorisation; re-captured when the solve parameters change.
+    struct IterGraph {
+        cudaGraphExec_t exec = nullptr;
+        SolveParams sp{};
+        int64_t launches[ST_COUNT] = {0, 0, 0, 0, 0, 0};
+        int64_t total = 0;
+    };
+    IterGraph graphs_[2];
+    void drop_graphs();
+    int32_t enqueue_iteration(const SolveParams& sp, bool refactor, int64_t* per_stage);
     SolveResult last_{};
     double* d_slots_ = nullptr;
     int32_t n_slots_ = 0;

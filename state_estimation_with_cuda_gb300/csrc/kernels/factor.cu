@@ -1,88 +1,154 @@
 // Level-scheduled multifrontal Cholesky of the gain matrix G = H^T W H and the
 // forward / backward solves (replaces the reference's per-call
-// cusolverSp csrlsvchol, sparse_matrix.cu:793-895, and its quadratic RHS).
+// cusolverSp csrlsvchol, sparse_matrix.cu:793-895, and its quadratic RHS
+// kernel, kernels.cu:823-862).
 //
-// Front s (rows R_s, nc_s pivot columns) is assembled from
+// Front s (rows R_s, nc_s pivot columns, order f_s) is assembled from
 //   - its gain entries, each a fixed-order sum of w_m H[m,a] H[m,b] over the
 //     measurement rows m that couple the two states (gathered, no atomics), and
 //   - its children's update matrices, extend-added through relative maps,
 // then partially factorised: L11 = chol(F11), L21 = F21 L11^-T,
-// U_s = F22 - L21 L21^T.  Fronts with f <= kSmallFrontMax live in shared memory
-// (one CTA per front); larger fronts are factorised in a global workspace by a
-// blocked right-looking loop whose panel, triangular-solve and trailing-update
-// steps are spread over many CTAs.
+// U_s = F22 - L21 L21^T.
+//
+// Small fronts (little work) are one CTA each with the whole front in shared
+// memory.  Big fronts live in place in an f x f region (L panel = first nc
+// columns, update matrix = trailing block, both column-major with ld = f) and
+// are processed for a whole level at once by tile work lists: an assembly
+// kernel (one CTA per 32-column tile column, so every entry has one writer), a
+// panel kernel (each CTA factors the 32 x 32 diagonal tile and solves one row
+// tile against it) and a trailing-update kernel (one CTA per 32 x 32 tile).
+// The factor type T is double for the FP64 pipeline and float for the
+// mixed-precision one; sums of the gain entries are always formed in double.
 #include "kernels.cuh"
+
+#include <algorithm>
 
 namespace sle_gb300 {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kNB = 32;  // panel width of the blocked big-front path
 
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
 }
 
-__device__ __forceinline__ double gain_entry(const DevNet& net, const DevFactor& F, const DevWork& W, int tg) {
+template <typename HV>
+__device__ __forceinline__ double gain_entry(const DevNet& net, const DevFactor& F, const DevWork& W, const HV* hval,
+                                             int tg) {
     double acc = 0.0;
     const int64_t p1 = F.tgt_pair_ptr[tg + 1];
     for (int64_t p = F.tgt_pair_ptr[tg]; p < p1; ++p) {
         const int a = F.pair_a[p], b = F.pair_b[p];
-        acc += W.w_eff[net.h_row[a]] * W.hval[a] * W.hval[b];
+        acc += W.w_eff[net.h_row[a]] * static_cast<double>(hval[a]) * static_cast<double>(hval[b]);
     }
     return acc;
 }
 
-__device__ __forceinline__ double safe_pivot(double d, uint32_t* flags) {
+// All gain entries of the factorisation at once: fully parallel, so the
+// dependent gathers are hidden by occupancy instead of sitting on the
+// elimination tree's critical path.
+template <typename T, typename HV>
+__global__ void k_gain_values(DevNet net, DevFactor F, DevWork W, const HV* hval, T* gv, int n_tgt) {
+    for (int tg = blockIdx.x * blockDim.x + threadIdx.x; tg < n_tgt; tg += gridDim.x * blockDim.x)
+        gv[tg] = static_cast<T>(gain_entry(net, F, W, hval, tg));
+}
+
+// Pivot: L_kk = sqrt(d) and its reciprocal.  Non-positive or non-finite d
+// flags the gain matrix as not positive definite and continues with 1.
+// FP64: a reciprocal square root seeded in FP32 and refined by two
+// Newton-Raphson steps y <- y (3 - d y^2) / 2 (each step doubles the correct
+// bits: ~24 -> 48 -> 96), which keeps serial FP64 work short on a GPU with
+// few FP64 units; the library routines are used outside the FP32 range.
+__device__ __forceinline__ void pivot(float d, float* sq, float* inv, uint32_t* flags) {
+    if (!(d > 0.f) || !isfinite(d)) {
+        atomicOr(flags, FLAG_SINGULAR);
+        d = 1.f;
+    }
+    *sq = sqrtf(d);
+    *inv = 1.f / *sq;
+}
+__device__ __forceinline__ void pivot(double d, double* sq, double* inv, uint32_t* flags) {
     if (!(d > 0.0) || !isfinite(d)) {
         atomicOr(flags, FLAG_SINGULAR);
-        return 1.0;
+        d = 1.0;
     }
-    return sqrt(d);
+    if (d > 1e-30 && d < 1e30) {
+        double y = static_cast<double>(rsqrtf(static_cast<float>(d)));
+        y = y * (1.5 - 0.5 * d * y * y);
+        y = y * (1.5 - 0.5 * d * y * y);
+        *sq = d * y;
+        *inv = y;
+    } else {
+        *sq = sqrt(d);
+        *inv = 1.0 / *sq;
+    }
+}
+
+// Extend-add child c's update matrix (lower triangle) into a front buffer.
+template <typename T>
+__device__ __forceinline__ const T* update_of(const DevFactor& F, const T* lx, const T* ub, int c) {
+    return (F.sn_u_big[c] ? lx : ub) + F.sn_u_off[c];
+}
+
+template <typename T>
+__device__ __forceinline__ void extend_add_child(const DevFactor& F, const T* lx, const T* ubase, int c, T* dst,
+                                                 int ldd, int tid, int nth) {
+    const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
+    const T* U = update_of<T>(F, lx, ubase, c);
+    const int uld = F.sn_u_ld[c];
+    const int* rel = F.sn_relmap + F.sn_su_off[c];
+    for (int x = tid; x < m * m; x += nth) {
+        const int i = x % m, j = x / m;
+        if (i >= j) dst[rel[i] + rel[j] * ldd] += U[i + (int64_t)j * uld];
+    }
 }
 
 // ---------------------------------------------------------------------------
 // Small fronts: one CTA per front, front held in shared memory.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_front_small(DevNet net, DevFactor F, DevWork W, const int* fronts) {
-    extern __shared__ double Fm[];
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_front_small(DevFactor F, DevWork W, const T* gv, T* lx, T* ub,
+                                                          const int* fronts) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* Fm = reinterpret_cast<T*>(smem_raw);
     const int s = fronts[blockIdx.x];
     const int f = F.sn_f[s];
     const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
     const int tid = threadIdx.x, nth = blockDim.x;
-    for (int x = tid; x < f * f; x += nth) Fm[x] = 0.0;
+    for (int x = tid; x < f * f; x += nth) Fm[x] = T(0);
     __syncthreads();
-    for (int tg = F.sn_tgt_ptr[s] + tid; tg < F.sn_tgt_ptr[s + 1]; tg += nth) Fm[F.tgt_local[tg]] = gain_entry(net, F, W, tg);
+    for (int tg = F.sn_tgt_ptr[s] + tid; tg < F.sn_tgt_ptr[s + 1]; tg += nth) Fm[F.tgt_local[tg]] = gv[tg];
     __syncthreads();
     for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) {
-        const int c = F.sn_child[ci];
-        const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
-        const double* U = W.u + F.sn_u_off[c];
-        const int* rel = F.sn_relmap + F.sn_su_off[c];
-        for (int x = tid; x < m * m; x += nth) {
-            const int i = x % m, j = x / m;
-            if (i >= j) Fm[rel[i] + rel[j] * f] += U[x];
-        }
+        extend_add_child<T>(F, lx, ub, F.sn_child[ci], Fm, f, tid, nth);
         __syncthreads();
     }
     const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
+    __shared__ T rpiv;
+    T* rdg = reinterpret_cast<T*>(W.rdiag) + F.sn_c0[s];
     for (int k = 0; k < nc; ++k) {
-        if (tid == 0) Fm[k + k * f] = safe_pivot(Fm[k + k * f], &W.status->flags);
+        if (tid == 0) {
+            T sq, inv;
+            pivot(Fm[k + k * f], &sq, &inv, &W.status->flags);
+            Fm[k + k * f] = sq;
+            rpiv = inv;
+            rdg[k] = inv;
+        }
         __syncthreads();
-        const double piv = Fm[k + k * f];
-        for (int i = k + 1 + tid; i < f; i += nth) Fm[i + k * f] /= piv;
+        const T inv = rpiv;
+        for (int i = k + 1 + tid; i < f; i += nth) Fm[i + k * f] *= inv;
         __syncthreads();
         for (int j = k + 1 + warp; j < f; j += nwarp) {
-            const double ljk = Fm[j + k * f];
+            const T ljk = Fm[j + k * f];
             for (int i = j + lane; i < f; i += 32) Fm[i + j * f] -= Fm[i + k * f] * ljk;
         }
         __syncthreads();
     }
-    double* L = W.lx + F.sn_lx_off[s];
+    T* L = lx + F.sn_lx_off[s];
     for (int x = tid; x < f * nc; x += nth) L[x] = Fm[x];
     const int m = f - nc;
-    double* U = W.u + F.sn_u_off[s];
+    T* U = ub + F.sn_u_off[s];
     for (int x = tid; x < m * m; x += nth) {
         const int i = x % m, j = x / m;
         U[x] = Fm[(nc + i) + (nc + j) * f];
@@ -90,190 +156,311 @@ __global__ void __launch_bounds__(kThreads) k_front_small(DevNet net, DevFactor 
 }
 
 // ---------------------------------------------------------------------------
-// Big fronts: global workspace, blocked right-looking partial factorisation.
+// Big fronts, in place (L panel and update matrix share the f x f region at
+// sn_lx_off with ld = f).  Work lists hold int4 (front, a, b, 0).
 // ---------------------------------------------------------------------------
-__global__ void k_big_zero(double* B, int64_t n) {
-    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) B[x] = 0.0;
-}
-
-__global__ void k_big_targets(DevNet net, DevFactor F, DevWork W, int s) {
-    double* B = W.big + F.sn_big_off[s];
-    const int t0 = F.sn_tgt_ptr[s], t1 = F.sn_tgt_ptr[s + 1];
-    for (int tg = t0 + blockIdx.x * blockDim.x + threadIdx.x; tg < t1; tg += gridDim.x * blockDim.x)
-        B[F.tgt_local[tg]] = gain_entry(net, F, W, tg);
-}
-
-__global__ void k_big_extend_add(DevFactor F, DevWork W, int s, int c) {
-    double* B = W.big + F.sn_big_off[s];
-    const int f = F.sn_f[s];
-    const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
-    const double* U = W.u + F.sn_u_off[c];
-    const int* rel = F.sn_relmap + F.sn_su_off[c];
-    const int64_t mm = (int64_t)m * m;
-    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < mm; x += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(x % m), j = (int)(x / m);
-        if (i >= j) B[rel[i] + (int64_t)rel[j] * f] += U[x];
+__device__ __forceinline__ int lower_bound_i32(const int* a, int lo, int hi, int key) {
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
     }
+    return lo;
 }
 
-// Factor the pb x pb diagonal block at column p0 (one CTA).
-__global__ void k_big_potrf(DevFactor F, DevWork W, int s, int p0, int pb) {
-    __shared__ double D[kNB * kNB];
-    double* B = W.big + F.sn_big_off[s];
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_big_assemble(DevFactor F, const T* gv, T* lx, T* ub, const int4* work) {
+    const int4 wk = work[blockIdx.x];
+    const int s = wk.x, tj = wk.y;
     const int f = F.sn_f[s];
-    for (int x = threadIdx.x; x < pb * pb; x += blockDim.x) {
-        const int i = x % pb, j = x / pb;
-        D[x] = B[(p0 + i) + (int64_t)(p0 + j) * f];
+    T* B = lx + F.sn_lx_off[s];
+    const int c0 = tj * kTile, c1 = min(c0 + kTile, f);
+    const int tid = threadIdx.x, nth = blockDim.x;
+    for (int x = tid; x < (c1 - c0) * f; x += nth) {
+        const int c = c0 + x / f, r = x % f;
+        if (r >= c) B[r + (int64_t)c * f] = T(0);
     }
     __syncthreads();
-    for (int k = 0; k < pb; ++k) {
-        if (threadIdx.x == 0) D[k + k * pb] = safe_pivot(D[k + k * pb], &W.status->flags);
-        __syncthreads();
-        const double piv = D[k + k * pb];
-        for (int i = k + 1 + threadIdx.x; i < pb; i += blockDim.x) D[i + k * pb] /= piv;
-        __syncthreads();
-        for (int x = threadIdx.x; x < pb * pb; x += blockDim.x) {
-            const int i = x % pb, j = x / pb;
-            if (j > k && i >= j) D[i + j * pb] -= D[i + k * pb] * D[j + k * pb];
+    // tgt_local = row + col * f is sorted, so a tile column is a contiguous range
+    const int lo = lower_bound_i32(F.tgt_local, F.sn_tgt_ptr[s], F.sn_tgt_ptr[s + 1], c0 * f);
+    const int hi = lower_bound_i32(F.tgt_local, lo, F.sn_tgt_ptr[s + 1], c1 * f);
+    for (int tg = lo + tid; tg < hi; tg += nth) B[F.tgt_local[tg]] = gv[tg];
+    __syncthreads();
+    for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) {
+        const int c = F.sn_child[ci];
+        const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
+        const int* rel = F.sn_relmap + F.sn_su_off[c];
+        const int j0 = lower_bound_i32(rel, 0, m, c0);  // rel is increasing
+        const int j1 = lower_bound_i32(rel, j0, m, c1);
+        const T* U = update_of<T>(F, lx, ub, c);
+        const int uld = F.sn_u_ld[c];
+        const int nj = j1 - j0;
+        for (int x = tid; x < nj * m; x += nth) {
+            const int j = j0 + x / m, i = x % m;
+            if (i >= j) B[rel[i] + (int64_t)rel[j] * f] += U[i + (int64_t)j * uld];
         }
         __syncthreads();
     }
+}
+
+// Panel step p, part 1 (one CTA per front): factor the diagonal tile in
+// place and solve the rows of tile p below the panel's last column.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, T* lx, const int4* work, int p) {
+    constexpr int ld = kTile + 1;
+    __shared__ T D[kTile * ld];
+    __shared__ T rdiag[kTile];
+    const int s = work[blockIdx.x].x;
+    const int f = F.sn_f[s];
+    const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
+    T* B = lx + F.sn_lx_off[s];
+    const int p0 = p * kTile;
+    const int pb = min(kTile, nc - p0);
     for (int x = threadIdx.x; x < pb * pb; x += blockDim.x) {
         const int i = x % pb, j = x / pb;
-        if (i >= j) B[(p0 + i) + (int64_t)(p0 + j) * f] = D[x];
+        D[i + j * ld] = (i >= j) ? B[(p0 + i) + (int64_t)(p0 + j) * f] : T(0);
+    }
+    __syncthreads();
+    // one warp factors the tile: lane i owns row i
+    if (threadIdx.x < 32) {
+        const int i = threadIdx.x;
+        for (int k = 0; k < pb; ++k) {
+            if (i == k) {
+                T sq, inv;
+                pivot(D[k + k * ld], &sq, &inv, &W.status->flags);
+                D[k + k * ld] = sq;
+                rdiag[k] = inv;
+                reinterpret_cast<T*>(W.rdiag)[F.sn_c0[s] + p0 + k] = inv;
+            }
+            __syncwarp();
+            const T inv = rdiag[k];
+            if (i > k && i < pb) D[i + k * ld] *= inv;
+            __syncwarp();
+            if (i > k && i < pb) {
+                const T lik = D[i + k * ld];
+                for (int j = k + 1; j <= i; ++j) D[i + j * ld] -= lik * D[j + k * ld];
+            }
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    for (int x = threadIdx.x; x < pb * pb; x += blockDim.x) {
+        const int i = x % pb, j = x / pb;
+        if (i >= j) B[(p0 + i) + (int64_t)(p0 + j) * f] = D[i + j * ld];
+    }
+    const int r = p0 + pb + threadIdx.x;
+    if (threadIdx.x < kTile && r < min(p0 + kTile, f)) {
+        T x[kTile];
+        for (int c = 0; c < pb; ++c) {
+            T a = B[r + (int64_t)(p0 + c) * f];
+            for (int k = 0; k < c; ++k) a -= x[k] * D[c + k * ld];
+            x[c] = a * rdiag[c];
+        }
+        for (int c = 0; c < pb; ++c) B[r + (int64_t)(p0 + c) * f] = x[c];
     }
 }
 
-// Rows below the diagonal block: X = A L_dd^-T, 64 rows per CTA.
-__global__ void k_big_trsm(DevFactor F, DevWork W, int s, int p0, int pb) {
-    __shared__ double D[kNB * kNB];
-    double* B = W.big + F.sn_big_off[s];
+// Panel step p, part 2 (one CTA per row tile ti > p): X = A L_dd^-T with the
+// diagonal tile factored by part 1.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_big_trsm(DevFactor F, T* lx, const void* Wrdiag, const int4* work, int p) {
+    constexpr int ld = kTile + 1;
+    __shared__ T D[kTile * ld];
+    __shared__ T A[kTile * ld];
+    __shared__ T rdiag[kTile];
+    const int4 wk = work[blockIdx.x];
+    const int s = wk.x, ti = wk.y;
     const int f = F.sn_f[s];
+    const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
+    T* B = lx + F.sn_lx_off[s];
+    const int p0 = p * kTile;
+    const int pb = min(kTile, nc - p0);
+    const int r0 = ti * kTile, nr = min(kTile, f - r0);
+    const int c0s = F.sn_c0[s];
     for (int x = threadIdx.x; x < pb * pb; x += blockDim.x) {
         const int i = x % pb, j = x / pb;
-        D[x] = B[(p0 + i) + (int64_t)(p0 + j) * f];
+        D[i + j * ld] = (i >= j) ? B[(p0 + i) + (int64_t)(p0 + j) * f] : T(0);
+    }
+    for (int x = threadIdx.x; x < nr * pb; x += blockDim.x) {
+        const int i = x % nr, j = x / nr;
+        A[i + j * ld] = B[(r0 + i) + (int64_t)(p0 + j) * f];
     }
     __syncthreads();
-    const int r = p0 + pb + blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= f) return;
-    double x[kNB];
+    if (threadIdx.x < pb) rdiag[threadIdx.x] = reinterpret_cast<const T*>(Wrdiag)[c0s + p0 + threadIdx.x];
+    __syncthreads();
+    // column sweep: all rows of the tile advance together, one column per step
     for (int c = 0; c < pb; ++c) {
-        double a = B[r + (int64_t)(p0 + c) * f];
-        for (int k = 0; k < c; ++k) a -= x[k] * D[c + k * pb];
-        x[c] = a / D[c + c * pb];
+        if (threadIdx.x < nr) A[threadIdx.x + c * ld] *= rdiag[c];
+        __syncthreads();
+        for (int x = threadIdx.x; x < nr * (pb - c - 1); x += blockDim.x) {
+            const int i = x % nr, j = c + 1 + x / nr;
+            A[i + j * ld] -= A[i + c * ld] * D[j + c * ld];
+        }
+        __syncthreads();
     }
-    for (int c = 0; c < pb; ++c) B[r + (int64_t)(p0 + c) * f] = x[c];
+    for (int x = threadIdx.x; x < nr * pb; x += blockDim.x) {
+        const int i = x % nr, j = x / nr;
+        B[(r0 + i) + (int64_t)(p0 + j) * f] = A[i + j * ld];
+    }
 }
 
-// Trailing lower update C -= A A^T over rows/cols >= q0 = p0 + pb with the
-// panel columns [p0, p0 + pb); 32 x 32 tiles, lower tiles only.
-__global__ void __launch_bounds__(256) k_big_syrk(DevFactor F, DevWork W, int s, int p0, int pb) {
-    __shared__ double Ai[32][kNB + 1];
-    __shared__ double Aj[32][kNB + 1];
-    double* B = W.big + F.sn_big_off[s];
+// Trailing update of step p: tile (ti, tj) -= A_i A_j^T over the panel's
+// columns, restricted to rows >= cols >= p0 + pb.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, T* lx, const int4* work, int p) {
+    __shared__ T Ai[kTile][kTile + 1];
+    __shared__ T Aj[kTile][kTile + 1];
+    const int4 wk = work[blockIdx.x];
+    const int s = wk.x, ti = wk.y, tj = wk.z;
     const int f = F.sn_f[s];
+    const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
+    T* B = lx + F.sn_lx_off[s];
+    const int p0 = p * kTile;
+    const int pb = min(kTile, nc - p0);
     const int q0 = p0 + pb;
-    // map blockIdx.x -> (ti, tj), tj <= ti
-    int t = blockIdx.x, ti = 0;
-    while (t > ti) { t -= ti + 1; ++ti; }
-    const int tj = t;
-    const int r0 = q0 + ti * 32, c0 = q0 + tj * 32;
-    for (int x = threadIdx.x; x < 32 * pb; x += blockDim.x) {
-        const int rr = x % 32, kk = x / 32;
-        Ai[rr][kk] = (r0 + rr < f) ? B[(r0 + rr) + (int64_t)(p0 + kk) * f] : 0.0;
-        Aj[rr][kk] = (c0 + rr < f) ? B[(c0 + rr) + (int64_t)(p0 + kk) * f] : 0.0;
+    const int R0 = ti * kTile, C0 = tj * kTile;
+    for (int x = threadIdx.x; x < kTile * pb; x += blockDim.x) {
+        const int rr = x % kTile, kk = x / kTile;
+        Ai[rr][kk] = (R0 + rr < f) ? B[(R0 + rr) + (int64_t)(p0 + kk) * f] : T(0);
+        Aj[rr][kk] = (C0 + rr < f) ? B[(C0 + rr) + (int64_t)(p0 + kk) * f] : T(0);
     }
     __syncthreads();
-    // each thread: 4 outputs, rows (threadIdx.x % 32), cols (threadIdx.x / 32) + 8 * q
-    const int rr = threadIdx.x % 32;
-    for (int qq = 0; qq < 4; ++qq) {
-        const int cc = threadIdx.x / 32 + 8 * qq;
-        const int gr = r0 + rr, gc = c0 + cc;
-        if (gr >= f || gc >= f || gr < gc) continue;
-        double acc = 0.0;
-        for (int k = 0; k < pb; ++k) acc += Ai[rr][k] * Aj[cc][k];
+    const int rr = threadIdx.x % kTile;
+    for (int cq = threadIdx.x / kTile; cq < kTile; cq += blockDim.x / kTile) {
+        const int gr = R0 + rr, gc = C0 + cq;
+        if (gr >= f || gc >= f || gr < gc || gc < q0) continue;
+        T acc = T(0);
+        for (int k = 0; k < pb; ++k) acc += Ai[rr][k] * Aj[cq][k];
         B[gr + (int64_t)gc * f] -= acc;
     }
 }
 
-__global__ void k_big_writeout(DevFactor F, DevWork W, int s) {
-    const double* Bm = W.big + F.sn_big_off[s];
-    const int f = F.sn_f[s];
-    const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
-    const int m = f - nc;
-    double* L = W.lx + F.sn_lx_off[s];
-    const int64_t nl = (int64_t)f * nc;
-    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < nl; x += (int64_t)gridDim.x * blockDim.x) L[x] = Bm[x];
-    double* U = W.u + F.sn_u_off[s];
-    const int64_t nu = (int64_t)m * m;
-    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < nu; x += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(x % m), j = (int)(x / m);
-        U[x] = Bm[(nc + i) + (int64_t)(nc + j) * f];
-    }
-}
-
 // ---------------------------------------------------------------------------
-// Solves.  Forward (bottom-up): v = [rhs of own columns; 0] + children's
-// update vectors; y = L11^-1 v1; update vector = v2 - L21 y.
+// Solves.  Forward (bottom-up): v = [b of own columns; 0] + children's update
+// vectors; y = L11^-1 v1; update vector = v2 - L21 y.
 // Backward (top-down): x1 = L11^-T (y - L21^T x_rows).
+// Blocked by kTile columns: the diagonal tile is staged in shared memory and
+// swept by one warp; the rectangular update below (forward) or the dot
+// products against the solved rows (backward) use every thread with
+// coalesced reads of the column-major panel.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_fwd(DevFactor F, DevWork W, const int* fronts) {
-    extern __shared__ double v[];
+struct SolveVecs {
+    const void* rhs;  // [n_state] right-hand side, permuted (V)
+    void* sol;        // [n_state] solution, permuted (V)
+    void* su;         // solve update vectors (V)
+};
+
+template <typename T, typename V>
+__global__ void __launch_bounds__(kThreads) k_fwd(DevFactor F, const T* lx, const T* rdiag, SolveVecs sv,
+                                                  const int* fronts) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    V* v = reinterpret_cast<V*>(smem_raw);
+    __shared__ T D[kTile * (kTile + 1)];
+    const V* rhs = reinterpret_cast<const V*>(sv.rhs);
+    V* sol = reinterpret_cast<V*>(sv.sol);
+    V* sub = reinterpret_cast<V*>(sv.su);
     const int s = fronts[blockIdx.x];
     const int f = F.sn_f[s];
     const int c0 = F.sn_c0[s];
     const int nc = F.sn_c0[s + 1] - c0;
     const int tid = threadIdx.x, nth = blockDim.x;
-    for (int i = tid; i < f; i += nth) v[i] = (i < nc) ? W.rhs[c0 + i] : 0.0;
+    const T* L = lx + F.sn_lx_off[s];
+    for (int i = tid; i < f; i += nth) v[i] = (i < nc) ? rhs[c0 + i] : V(0);
     __syncthreads();
     for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) {
         const int c = F.sn_child[ci];
         const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
-        const double* su = W.su + F.sn_su_off[c];
+        const V* su = sub + F.sn_su_off[c];
         const int* rel = F.sn_relmap + F.sn_su_off[c];
         for (int i = tid; i < m; i += nth) v[rel[i]] += su[i];
         __syncthreads();
     }
-    const double* L = W.lx + F.sn_lx_off[s];
-    for (int k = 0; k < nc; ++k) {
-        const double yk = v[k] / L[k + (int64_t)k * f];
-        for (int i = k + 1 + tid; i < f; i += nth) v[i] -= L[i + (int64_t)k * f] * yk;
+    constexpr int ld = kTile + 1;
+    for (int k0 = 0; k0 < nc; k0 += kTile) {
+        const int kb = min(kTile, nc - k0);
+        for (int x = tid; x < kb * kb; x += nth) {
+            const int i = x % kb, j = x / kb;
+            D[i + j * ld] = (i == j) ? rdiag[c0 + k0 + i] : L[(k0 + i) + (int64_t)(k0 + j) * f];
+        }
+        __syncthreads();
+        if (tid < 32) {
+            for (int k = 0; k < kb; ++k) {
+                const V yk = v[k0 + k] * static_cast<V>(D[k + k * ld]);
+                __syncwarp();
+                const int i = k + 1 + tid;
+                if (i < kb) v[k0 + i] -= static_cast<V>(D[i + k * ld]) * yk;
+                if (tid == 0) v[k0 + k] = yk;
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        for (int i = k0 + kb + tid; i < f; i += nth) {
+            V acc = v[i];
+            for (int k = 0; k < kb; ++k) acc -= static_cast<V>(L[i + (int64_t)(k0 + k) * f]) * v[k0 + k];
+            v[i] = acc;
+        }
         __syncthreads();
     }
-    for (int k = tid; k < nc; k += nth) W.sol[c0 + k] = v[k] / L[k + (int64_t)k * f];
-    double* su = W.su + F.sn_su_off[s];
+    for (int k = tid; k < nc; k += nth) sol[c0 + k] = v[k];
+    V* su = sub + F.sn_su_off[s];
     for (int i = tid; i < f - nc; i += nth) su[i] = v[nc + i];
 }
 
-__global__ void __launch_bounds__(kThreads) k_bwd(DevFactor F, DevWork W, const int* fronts) {
-    extern __shared__ double t[];
+template <typename V>
+__device__ __forceinline__ V warp_sum_v(V v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename T, typename V>
+__global__ void __launch_bounds__(kThreads) k_bwd(DevFactor F, const T* lx, const T* rdiag, SolveVecs sv,
+                                                  const int* fronts) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    V* x = reinterpret_cast<V*>(smem_raw);  // [f]: solution of the front's rows
+    __shared__ T D[kTile * (kTile + 1)];
+    V* sol = reinterpret_cast<V*>(sv.sol);
     const int s = fronts[blockIdx.x];
     const int f = F.sn_f[s];
     const int c0 = F.sn_c0[s];
     const int nc = F.sn_c0[s + 1] - c0;
     const int* rows = F.sn_rows + F.sn_rows_off[s];
-    const double* L = W.lx + F.sn_lx_off[s];
+    const T* L = lx + F.sn_lx_off[s];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    for (int k = warp; k < nc; k += nwarp) {
-        double acc = 0.0;
-        for (int r = nc + lane; r < f; r += 32) acc += L[r + (int64_t)k * f] * W.sol[rows[r]];
-        acc = warp_sum(acc);
-        if (lane == 0) t[k] = W.sol[c0 + k] - acc;
-    }
+    for (int r = threadIdx.x; r < f; r += blockDim.x) x[r] = (r < nc) ? sol[c0 + r] : sol[rows[r]];
     __syncthreads();
-    for (int k = nc - 1; k >= 0; --k) {
-        const double xk = t[k] / L[k + (int64_t)k * f];
+    constexpr int ld = kTile + 1;
+    const int nblk = (nc + kTile - 1) / kTile;
+    for (int b = nblk - 1; b >= 0; --b) {
+        const int k0 = b * kTile, kb = min(kTile, nc - k0);
+        for (int k = k0 + warp; k < k0 + kb; k += nwarp) {
+            V acc = V(0);
+            for (int r = k0 + kb + lane; r < f; r += 32) acc += static_cast<V>(L[r + (int64_t)k * f]) * x[r];
+            acc = warp_sum_v(acc);
+            if (lane == 0) x[k] -= acc;
+        }
+        for (int q = threadIdx.x; q < kb * kb; q += blockDim.x) {
+            const int i = q % kb, j = q / kb;
+            D[i + j * ld] = (i == j) ? rdiag[c0 + k0 + i] : L[(k0 + i) + (int64_t)(k0 + j) * f];
+        }
         __syncthreads();
-        for (int i = threadIdx.x; i < k; i += blockDim.x) t[i] -= L[k + (int64_t)i * f] * xk;
-        if (threadIdx.x == 0) t[k] = xk;
+        if (threadIdx.x < 32) {
+            for (int k = kb - 1; k >= 0; --k) {
+                const V xk = x[k0 + k] * static_cast<V>(D[k + k * ld]);
+                __syncwarp();
+                const int i = threadIdx.x;
+                if (i < k) x[k0 + i] -= static_cast<V>(D[k + i * ld]) * xk;
+                if (threadIdx.x == 0) x[k0 + k] = xk;
+                __syncwarp();
+            }
+        }
         __syncthreads();
     }
-    for (int k = threadIdx.x; k < nc; k += blockDim.x) W.sol[c0 + k] = t[k];
+    for (int k = threadIdx.x; k < nc; k += blockDim.x) sol[c0 + k] = x[k];
 }
 
-__global__ void k_gain_export(DevNet net, DevFactor F, DevWork W, int n_tgt, double* out) {
+template <typename HV>
+__global__ void k_gain_export(DevNet net, DevFactor F, DevWork W, const HV* hval, int n_tgt, double* out) {
     for (int tg = blockIdx.x * blockDim.x + threadIdx.x; tg < n_tgt; tg += gridDim.x * blockDim.x)
-        out[tg] = gain_entry(net, F, W, tg);
+        out[tg] = gain_entry(net, F, W, hval, tg);
 }
 
 inline int grid_for(int64_t n, int threads) {
@@ -282,87 +469,119 @@ inline int grid_for(int64_t n, int threads) {
     return (int)(g < 1 ? 1 : g);
 }
 
-}  // namespace
+template <typename V>
+size_t solve_smem(int maxf) {
+    return (size_t)(maxf + 2) * sizeof(V);
+}
 
-cudaError_t launch_factor(const DevNet& net, const DevFactor& F, const DevWork& W, const LevelSchedule& ls,
-                          cudaStream_t st) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_front_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             kSmallFrontMax * kSmallFrontMax * (int)sizeof(double));
-        if (e != cudaSuccess) return e;
-        attr_set = true;
+template <typename T, typename HV>
+cudaError_t prepare_impl() {
+    cudaError_t e = cudaFuncSetAttribute(k_front_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kSmallFrontMax * kSmallFrontMax * (int)sizeof(double));
+    const int mx = (int)solve_smem<double>(16384);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fwd<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bwd<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    return e;
+}
+
+template <typename T, typename HV>
+cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W, const LevelSchedule& ls, const HV* hval,
+                        T* lx, T* ub, cudaStream_t st) {
+    T* gv = reinterpret_cast<T*>(W.gvals);
+    if (ls.n_tgt > 0) {
+        k_gain_values<T, HV><<<grid_for(ls.n_tgt, 256), 256, 0, st>>>(net, F, W, hval, gv, ls.n_tgt);
+        ++g_kernel_launches;
     }
     for (int l = 0; l < ls.n_levels; ++l) {
         const int ns = ls.h_small_ptr[l + 1] - ls.h_small_ptr[l];
         if (ns > 0) {
-            const int mf = ls.max_small_f;
-            const size_t smem = (size_t)mf * mf * sizeof(double);
-            k_front_small<<<ns, kThreads, smem, st>>>(net, F, W, ls.d_small + ls.h_small_ptr[l]);
+            const int mf = ls.h_small_maxf[l];
+            k_front_small<T><<<ns, kThreads, (size_t)mf * mf * sizeof(T), st>>>(F, W, gv, lx, ub,
+                                                                                  ls.d_small + ls.h_small_ptr[l]);
             ++g_kernel_launches;
         }
-        for (int b = ls.h_big_ptr[l]; b < ls.h_big_ptr[l + 1]; ++b) {
-            const int s = ls.h_big[b];
-            const int f = ls.h_sn_f[s];
-            const int nc = ls.h_sn_c0[s + 1] - ls.h_sn_c0[s];
-            double* B = W.big + ls.h_big_off[s];
-            k_big_zero<<<grid_for((int64_t)f * f, 256), 256, 0, st>>>(B, (int64_t)f * f);
+        const int na = ls.h_asm_ptr[l + 1] - ls.h_asm_ptr[l];
+        if (na > 0) {
+            k_big_assemble<T><<<na, kThreads, 0, st>>>(F, gv, lx, ub, ls.d_asm + ls.h_asm_ptr[l]);
             ++g_kernel_launches;
-            const int nt = ls.h_tgt_ptr[s + 1] - ls.h_tgt_ptr[s];
-            if (nt > 0) {
-                k_big_targets<<<grid_for(nt, 256), 256, 0, st>>>(net, F, W, s);
-                ++g_kernel_launches;
-            }
-            for (int ci = ls.h_child_ptr[s]; ci < ls.h_child_ptr[s + 1]; ++ci) {
-                const int c = ls.h_child[ci];
-                const int64_t m = ls.h_sn_f[c] - (ls.h_sn_c0[c + 1] - ls.h_sn_c0[c]);
-                if (m > 0) {
-                    k_big_extend_add<<<grid_for(m * m, 256), 256, 0, st>>>(F, W, s, c);
+            for (int p = 0; p < ls.h_lvl_panels[l]; ++p) {
+                const int slot = ls.h_step_ptr[l] + p;
+                const int npot = ls.h_pot_ptr[slot + 1] - ls.h_pot_ptr[slot];
+                const int npan = ls.h_pan_ptr[slot + 1] - ls.h_pan_ptr[slot];
+                const int nupd = ls.h_upd_ptr[slot + 1] - ls.h_upd_ptr[slot];
+                if (npot > 0) {
+                    k_big_potrf<T><<<npot, kThreads, 0, st>>>(F, W, lx, ls.d_pot + ls.h_pot_ptr[slot], p);
+                    ++g_kernel_launches;
+                }
+                if (npan > 0) {
+                    k_big_trsm<T><<<npan, kThreads, 0, st>>>(F, lx, W.rdiag, ls.d_pan + ls.h_pan_ptr[slot], p);
+                    ++g_kernel_launches;
+                }
+                if (nupd > 0) {
+                    k_big_update<T><<<nupd, kThreads, 0, st>>>(F, lx, ls.d_upd + ls.h_upd_ptr[slot], p);
                     ++g_kernel_launches;
                 }
             }
-            for (int p0 = 0; p0 < nc; p0 += kNB) {
-                const int pb = (nc - p0) < kNB ? (nc - p0) : kNB;
-                k_big_potrf<<<1, 256, 0, st>>>(F, W, s, p0, pb);
-                ++g_kernel_launches;
-                const int rows = f - p0 - pb;
-                if (rows > 0) {
-                    k_big_trsm<<<(rows + 63) / 64, 64, 0, st>>>(F, W, s, p0, pb);
-                    const int T = (rows + 31) / 32;
-                    k_big_syrk<<<T * (T + 1) / 2, 256, 0, st>>>(F, W, s, p0, pb);
-                    g_kernel_launches += 2;
-                }
-            }
-            k_big_writeout<<<grid_for((int64_t)f * f, 256), 256, 0, st>>>(F, W, s);
-            ++g_kernel_launches;
         }
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_gain_export(const DevNet& net, const DevFactor& F, const DevWork& W, int32_t n_tgt, double* out,
-                               cudaStream_t st) {
-    if (n_tgt > 0) {
-        k_gain_export<<<grid_for(n_tgt, 256), 256, 0, st>>>(net, F, W, n_tgt, out);
-        ++g_kernel_launches;
-    }
-    return cudaGetLastError();
-}
-
-cudaError_t launch_solve(const DevFactor& F, const DevWork& W, const LevelSchedule& ls, cudaStream_t st) {
+template <typename T>
+cudaError_t solve_impl(const DevFactor& F, const LevelSchedule& ls, const T* lx, const T* rdiag, SolveVecs sv,
+                       cudaStream_t st) {
     for (int l = 0; l < ls.n_levels; ++l) {
         const int n = ls.h_all_ptr[l + 1] - ls.h_all_ptr[l];
         if (n > 0) {
-            k_fwd<<<n, kThreads, (size_t)ls.h_lvl_maxf[l] * sizeof(double), st>>>(F, W, ls.d_all + ls.h_all_ptr[l]);
+            k_fwd<T, T><<<n, kThreads, solve_smem<T>(ls.h_lvl_maxf[l]), st>>>(F, lx, rdiag, sv,
+                                                                               ls.d_all + ls.h_all_ptr[l]);
             ++g_kernel_launches;
         }
     }
     for (int l = ls.n_levels - 1; l >= 0; --l) {
         const int n = ls.h_all_ptr[l + 1] - ls.h_all_ptr[l];
         if (n > 0) {
-            k_bwd<<<n, kThreads, (size_t)ls.h_lvl_maxf[l] * sizeof(double), st>>>(F, W, ls.d_all + ls.h_all_ptr[l]);
+            k_bwd<T, T><<<n, kThreads, solve_smem<T>(ls.h_lvl_maxf[l]), st>>>(F, lx, rdiag, sv,
+                                                                               ls.d_all + ls.h_all_ptr[l]);
             ++g_kernel_launches;
         }
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t prepare_factor_kernels() {
+    cudaError_t e = prepare_impl<double, double>();
+    if (e == cudaSuccess) e = prepare_impl<float, float>();
+    return e;
+}
+
+cudaError_t launch_factor32(const DevNet& net, const DevFactor& F, const DevWork& W, const LevelSchedule& ls,
+                            cudaStream_t st) {
+    return factor_impl<float, float>(net, F, W, ls, W.hval32, W.lx32, W.u32, st);
+}
+
+cudaError_t launch_solve32(const DevFactor& F, const DevWork& W, const LevelSchedule& ls, cudaStream_t st) {
+    return solve_impl<float>(F, ls, W.lx32, reinterpret_cast<const float*>(W.rdiag),
+                             SolveVecs{W.rhs32, W.sol32, W.su32}, st);
+}
+
+cudaError_t launch_factor(const DevNet& net, const DevFactor& F, const DevWork& W, const LevelSchedule& ls,
+                          cudaStream_t st) {
+    return factor_impl<double, double>(net, F, W, ls, W.hval, W.lx, W.u, st);
+}
+
+cudaError_t launch_solve(const DevFactor& F, const DevWork& W, const LevelSchedule& ls, cudaStream_t st) {
+    return solve_impl<double>(F, ls, W.lx, reinterpret_cast<const double*>(W.rdiag), SolveVecs{W.rhs, W.sol, W.su},
+                              st);
+}
+
+cudaError_t launch_gain_export(const DevNet& net, const DevFactor& F, const DevWork& W, int32_t n_tgt, double* out,
+                               cudaStream_t st) {
+    if (n_tgt > 0) {
+        k_gain_export<double><<<grid_for(n_tgt, 256), 256, 0, st>>>(net, F, W, W.hval, n_tgt, out);
+        ++g_kernel_launches;
     }
     return cudaGetLastError();
 }

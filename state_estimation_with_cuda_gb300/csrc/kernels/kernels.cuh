@@ -66,6 +66,7 @@ struct DevNet {
     // H pattern
     const int32_t* h_ptr;
     const int32_t* h_row;
+    const int32_t* h_pcol;   // column of each H entry in the permuted state order
 };
 
 // Factorisation plan (device).
@@ -90,8 +91,11 @@ struct DevFactor {
     const int32_t* rhs_h;
     const int32_t* bus_ps_theta;
     const int32_t* bus_ps_v;
-    // big-front workspace offsets (-1 for fronts handled in shared memory)
-    const int64_t* sn_big_off;
+    // update-matrix leading dimension and location: small fronts keep a
+    // compact (f-nc)^2 block in the update array; big fronts keep it in place
+    // inside their f x f region of the factor array (sn_u_big = 1, ld = f)
+    const int32_t* sn_u_ld;
+    const uint8_t* sn_u_big;
 };
 
 // Mutable per-iteration state (device).
@@ -104,12 +108,22 @@ struct DevWork {
     double* w_eff;    // [n_meas] weights used for G and the RHS (Huber or base)
     double* wr;       // [n_meas] w_eff * r
     double* hval;     // [nnz_H]
+    float* hval32;    // [nnz_H] FP32 copy (mixed-precision pipeline)
     double* rhs;      // [n_state] permuted
     double* sol;      // [n_state] permuted (y after forward, x after backward)
-    double* lx;       // L panels
-    double* u;        // update matrices
+    double* b0;       // [n_state] permuted gradient H^T W r of the iteration (mixed)
+    double* dx;       // [n_state] permuted refined step (mixed)
+    double* hdx;      // [n_meas] w * (H dx) (mixed refinement)
+    double* lx;       // L panels (FP64 pipeline)
+    double* u;        // update matrices (FP64 pipeline)
+    float* lx32;      // L panels (mixed pipeline)
+    float* u32;       // update matrices (mixed pipeline)
     double* su;       // solve update vectors
-    double* big;      // big-front workspace
+    void* gvals;      // [n_tgt] gain entries of the current factorisation (factor type)
+    void* rdiag;      // [n_state] reciprocals of L's diagonal (factor type)
+    float* rhs32;     // [n_state] FP32 right-hand side (mixed solves)
+    float* sol32;     // [n_state] FP32 solution (mixed solves)
+    float* su32;      // FP32 solve update vectors (mixed solves)
     double* p_inj;    // [n_bus]
     double* q_inj;
     double* pf;       // [n_branch] flows (filled by the result pass)
@@ -122,6 +136,7 @@ struct DevWork {
 
 struct SolveParams {
     int32_t exact_jacobian;  // 1: analytic derivatives of h(x); 0: the reference's formulas
+    int32_t mixed;           // 1: also store H in FP32 for the mixed-precision pipeline
     int32_t robust;          // Huber weights
     double huber_gamma;
     double tol;
@@ -135,9 +150,19 @@ cudaError_t launch_admittance_and_ybus(const DevNet& net, cudaStream_t st);
 cudaError_t launch_evaluate(const DevNet& net, const DevWork& w, const SolveParams& sp, cudaStream_t st);
 // RHS b = H^T (w r), permuted.
 cudaError_t launch_rhs(const DevNet& net, const DevFactor& f, const DevWork& w, cudaStream_t st);
-// State update + convergence / validity, then status finalisation.
+// State update x += step (permuted step vector) + convergence / validity,
+// then status finalisation.
 cudaError_t launch_update(const DevNet& net, const DevFactor& f, const DevWork& w, const SolveParams& sp,
-                          cudaStream_t st);
+                          const double* step, cudaStream_t st);
+// Mixed-precision refinement pieces (the solves run in FP32):
+//   rhs32 = (float) rhs
+cudaError_t launch_to_fp32(const DevFactor& f, const DevWork& w, cudaStream_t st);
+//   b0 = rhs (kept), dx = sol32
+cudaError_t launch_refine_begin(const DevFactor& f, const DevWork& w, cudaStream_t st);
+//   rhs32 = b0 - H^T W H dx  (FP64 accumulation over the FP32 H)
+cudaError_t launch_refine_residual(const DevNet& net, const DevFactor& f, const DevWork& w, cudaStream_t st);
+//   dx += sol32
+cudaError_t launch_refine_accumulate(const DevFactor& f, const DevWork& w, cudaStream_t st);
 // Objective, largest residual and bad-data count after an evaluation pass.
 cudaError_t launch_objective(const DevNet& net, const DevWork& w, double bad_threshold, cudaStream_t st);
 // Flat start: V = setpoint for PV/slack, else 1; theta = 0.
@@ -146,28 +171,43 @@ cudaError_t launch_flat_start(const DevNet& net, const DevWork& w, cudaStream_t 
 cudaError_t launch_results(const DevNet& net, const DevWork& w, cudaStream_t st);
 
 // Level-scheduled multifrontal factorisation and solves.  Host-side copies
-// of the plan arrays size the launches; device copies are read by kernels.
+// of the schedule size the launches; device copies are read by kernels.
+// Work-list entries are int4 (front, a, b, 0).
 struct LevelSchedule {
     int32_t n_levels = 0;
-    const int32_t* h_small_ptr = nullptr;  // [n_levels+1] offsets into d_small
-    const int32_t* d_small = nullptr;      // fronts with f <= kSmallFrontMax, per level
-    const int32_t* h_big_ptr = nullptr;    // [n_levels+1] offsets into h_big
-    const int32_t* h_big = nullptr;        // fronts with f > kSmallFrontMax, per level
-    const int32_t* h_all_ptr = nullptr;    // [n_levels+1] offsets into d_all
-    const int32_t* d_all = nullptr;        // every front, per level (solves)
-    const int32_t* h_lvl_maxf = nullptr;   // [n_levels] largest front per level
-    const int32_t* h_sn_f = nullptr;
-    const int32_t* h_sn_c0 = nullptr;
-    const int64_t* h_big_off = nullptr;    // workspace offsets (host copy)
-    const int32_t* h_tgt_ptr = nullptr;
-    const int32_t* h_child_ptr = nullptr;
-    const int32_t* h_child = nullptr;
-    int32_t max_small_f = 0;
+    int32_t n_tgt = 0;                      // gain entries (targets)
+    const int32_t* h_small_ptr = nullptr;   // [n_levels+1] offsets into d_small
+    const int32_t* d_small = nullptr;       // single-CTA fronts, per level
+    const int32_t* h_small_maxf = nullptr;  // [n_levels] largest single-CTA front
+    const int32_t* h_asm_ptr = nullptr;     // [n_levels+1] offsets into d_asm
+    const int4* d_asm = nullptr;            // (big front, tile column)
+    const int32_t* h_lvl_panels = nullptr;  // [n_levels] panel steps of the level
+    const int32_t* h_step_ptr = nullptr;    // [n_levels+1] first step slot of a level
+    const int32_t* h_pot_ptr = nullptr;     // [n_slots+1] offsets into d_pot
+    const int4* d_pot = nullptr;            // (big front) diagonal-tile factorisations
+    const int32_t* h_pan_ptr = nullptr;     // [n_slots+1] offsets into d_pan
+    const int4* d_pan = nullptr;            // (big front, row tile below the panel)
+    const int32_t* h_upd_ptr = nullptr;     // [n_slots+1] offsets into d_upd
+    const int4* d_upd = nullptr;            // (big front, row tile, column tile)
+    const int32_t* h_all_ptr = nullptr;     // [n_levels+1] offsets into d_all
+    const int32_t* d_all = nullptr;         // every front, per level (solves)
+    const int32_t* h_lvl_maxf = nullptr;    // [n_levels] largest front per level
+    const int64_t* h_lvl_maxpanel = nullptr;  // [n_levels] largest f * nc per level
 };
 
+// Tile edge of the big-front kernels.
+constexpr int kTile = 32;
+
+// Sets the kernel attributes (dynamic shared memory limits) on the current
+// device; call before launching or capturing the factorisation.
+cudaError_t prepare_factor_kernels();
 cudaError_t launch_factor(const DevNet& net, const DevFactor& f, const DevWork& w, const LevelSchedule& ls,
                           cudaStream_t st);
 cudaError_t launch_solve(const DevFactor& f, const DevWork& w, const LevelSchedule& ls, cudaStream_t st);
+// FP32 gain / factor and mixed solves (FP32 L, FP64 vectors).
+cudaError_t launch_factor32(const DevNet& net, const DevFactor& f, const DevWork& w, const LevelSchedule& ls,
+                            cudaStream_t st);
+cudaError_t launch_solve32(const DevFactor& f, const DevWork& w, const LevelSchedule& ls, cudaStream_t st);
 
 // Kernels launched by this library since load (all engines of the process).
 extern std::atomic<int64_t> g_kernel_launches;

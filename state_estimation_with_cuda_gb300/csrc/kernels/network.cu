@@ -244,6 +244,8 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
             }
             put_flow(hrow, net.m_fpos[q], d);
         }
+        if (sp.mixed)
+            for (int x = 0; x < nh; ++x) w.hval32[base + x] = static_cast<float>(hrow[x]);
         double rr = 0.0, we = 0.0;
         if (kind != 5) {
             rr = w.z[q] - hv;
@@ -277,6 +279,47 @@ __global__ void k_rhs(DevNet net, DevFactor f, DevWork w) {
         acc += w.hval[hidx] * w.wr[net.h_row[hidx]];
     }
     w.rhs[t] = acc;
+}
+
+// Mixed-precision refinement of one Gauss-Newton step (FP32 factor M ~ G):
+//   dx0 = M^-1 b;  repeat: rho = b - H^T W (H dx) in FP64, dx += M^-1 rho.
+__global__ void k_to_fp32(DevFactor f, DevWork w) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= f.n_state) return;
+    w.rhs32[t] = static_cast<float>(w.rhs[t]);
+}
+
+__global__ void k_refine_begin(DevFactor f, DevWork w) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= f.n_state) return;
+    w.b0[t] = w.rhs[t];
+    w.dx[t] = static_cast<double>(w.sol32[t]);
+}
+
+__global__ void k_refine_spmv(DevNet net, DevWork w) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= net.n_meas) return;
+    double acc = 0.0;
+    for (int h = net.h_ptr[q]; h < net.h_ptr[q + 1]; ++h)
+        acc += static_cast<double>(w.hval32[h]) * w.dx[net.h_pcol[h]];
+    w.hdx[q] = w.w_eff[q] * acc;
+}
+
+__global__ void k_refine_rhs(DevNet net, DevFactor f, DevWork w) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= f.n_state) return;
+    double acc = 0.0;
+    for (int x = f.rhs_ptr[t]; x < f.rhs_ptr[t + 1]; ++x) {
+        const int hidx = f.rhs_h[x];
+        acc += static_cast<double>(w.hval32[hidx]) * w.hdx[net.h_row[hidx]];
+    }
+    w.rhs32[t] = static_cast<float>(w.b0[t] - acc);
+}
+
+__global__ void k_refine_accumulate(DevFactor f, DevWork w) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= f.n_state) return;
+    w.dx[t] += static_cast<double>(w.sol32[t]);
 }
 
 // Objective, largest |r| (lowest index on ties) and the bad-data count
@@ -324,7 +367,8 @@ __global__ void k_objective(DevNet net, DevWork w, int nblk, double bad_threshol
 }
 
 // a13: x += dx (slack angle fixed), V clamped, block maxima of |dx|.
-__global__ void __launch_bounds__(kBlock) k_update(DevNet net, DevFactor f, DevWork w, SolveParams sp) {
+__global__ void __launch_bounds__(kBlock) k_update(DevNet net, DevFactor f, DevWork w, SolveParams sp,
+                                                   const double* step) {
     __shared__ double sh[32];
     __shared__ int bad;
     if (threadIdx.x == 0) bad = 0;
@@ -333,10 +377,10 @@ __global__ void __launch_bounds__(kBlock) k_update(DevNet net, DevFactor f, DevW
     double mx = 0.0;
     if (i < net.n_bus) {
         const int pt = f.bus_ps_theta[i];
-        const double dv = w.sol[f.bus_ps_v[i]];
+        const double dv = step[f.bus_ps_v[i]];
         double dt = 0.0;
         if (pt >= 0) {
-            dt = w.sol[pt];
+            dt = step[pt];
             w.th[i] += dt;
         }
         double vn = w.v[i] + dv;
@@ -437,11 +481,39 @@ cudaError_t launch_rhs(const DevNet& net, const DevFactor& f, const DevWork& w, 
 }
 
 cudaError_t launch_update(const DevNet& net, const DevFactor& f, const DevWork& w, const SolveParams& sp,
-                          cudaStream_t st) {
+                          const double* step, cudaStream_t st) {
     const int nb = nblocks(net.n_bus);
-    k_update<<<nb, kBlock, 0, st>>>(net, f, w, sp);
+    k_update<<<nb, kBlock, 0, st>>>(net, f, w, sp, step);
     k_update_finalize<<<1, 1024, 0, st>>>(w, nb, sp.tol);
     g_kernel_launches += 2;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_fp32(const DevFactor& f, const DevWork& w, cudaStream_t st) {
+    k_to_fp32<<<nblocks(f.n_state), kBlock, 0, st>>>(f, w);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refine_begin(const DevFactor& f, const DevWork& w, cudaStream_t st) {
+    k_refine_begin<<<nblocks(f.n_state), kBlock, 0, st>>>(f, w);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refine_residual(const DevNet& net, const DevFactor& f, const DevWork& w, cudaStream_t st) {
+    if (net.n_meas > 0) {
+        k_refine_spmv<<<nblocks(net.n_meas), kBlock, 0, st>>>(net, w);
+        ++g_kernel_launches;
+    }
+    k_refine_rhs<<<nblocks(f.n_state), kBlock, 0, st>>>(net, f, w);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refine_accumulate(const DevFactor& f, const DevWork& w, cudaStream_t st) {
+    k_refine_accumulate<<<nblocks(f.n_state), kBlock, 0, st>>>(f, w);
+    ++g_kernel_launches;
     return cudaGetLastError();
 }
 
