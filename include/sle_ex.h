@@ -44,7 +44,9 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
  *                           2 nested dissection (takes effect at upload)
  *   "use_double_precision"  as SLE_Config.use_double_precision (re-uploads)
  *   "refine_steps"          mixed precision: refinement steps per Gauss-Newton
- *                           step (default 1)
+ *                           step, each b - H^T W H dx in FP64 and an FP32 solve
+ *                           (default 0: the Gauss-Newton loop itself re-forms
+ *                           the FP64 residual and gradient every step)
  *   "big_front_flops"       FP64: fronts with more factor flops than this use
  *                           the tiled multi-CTA kernels (re-uploads) */
 SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* key, double value);

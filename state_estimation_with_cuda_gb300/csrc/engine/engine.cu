@@ -148,6 +148,10 @@ void Engine::build_schedule() {
     sch_pot_ptr_.assign(1, 0);
     sch_pan_ptr_.assign(1, 0);
     sch_upd_ptr_.assign(1, 0);
+    sch_flow_a_.clear();
+    sch_flow_b_.clear();
+    sch_down_.clear();
+    flow_a_maxf_ = flow_b_maxf_ = 0;
     lay_lx_off_.assign(ns + 1, 0);
     lay_u_off_.assign(ns + 1, 0);
     lay_u_ld_.assign(ns, 0);
@@ -159,8 +163,28 @@ void Engine::build_schedule() {
         for (int64_t c = 0; c < nc; ++c) fl += static_cast<double>(f - c - 1) * (f - c);
         // FP64 work per front is costly on this GPU, so the FP64 pipeline moves
         // fronts with many flops to the tiled path; in FP32 only size decides
-        big[s] = (f > kSmallFrontMax || (!mixed_ && fl > cfg.big_front_flops)) ? 1 : 0;
+        const int64_t fmax = mixed_ ? kSmallFrontMax32 : kSmallFrontMax;
+        big[s] = (f > fmax || (!mixed_ && fl > cfg.big_front_flops)) ? 1 : 0;
     }
+    // Dataflow phases: a front whose subtree holds no big front is factorised
+    // by the persistent kernels (phase A if no front of its subtree is wider
+    // than kFlowSmallF, phase B otherwise); the rest stays level-synchronous.
+    std::vector<char> sub_big(ns, 0);
+    std::vector<int32_t> sub_maxf(ns, 0);
+    for (int32_t l = 0; l < nl; ++l)
+        for (int32_t x = P.lvl_ptr[l]; x < P.lvl_ptr[l + 1]; ++x) {
+            const int32_t s = P.lvl_sn[x];
+            sub_big[s] = static_cast<char>(sub_big[s] | big[s]);
+            sub_maxf[s] = std::max(sub_maxf[s], P.sn_f[s]);
+            const int32_t p = P.sn_parent[s];
+            if (p >= 0) {
+                sub_big[p] = static_cast<char>(sub_big[p] | sub_big[s]);
+                sub_maxf[p] = std::max(sub_maxf[p], sub_maxf[s]);
+            }
+        }
+    flow_phase_.assign(ns, 0);
+    for (int32_t s = 0; s < ns; ++s)
+        if (cfg.dataflow && !sub_big[s]) flow_phase_[s] = sub_maxf[s] <= kFlowSmallF ? 1 : 2;
     int64_t lx = 0, uu = 0;
     for (int32_t s = 0; s < ns; ++s) {
         const int64_t f = P.sn_f[s], nc = P.sn_c0[s + 1] - P.sn_c0[s];
@@ -191,6 +215,12 @@ void Engine::build_schedule() {
                                                  static_cast<int64_t>(P.sn_f[s]) * (P.sn_c0[s + 1] - P.sn_c0[s]));
             if (big[s]) {
                 bigs.push_back(s);
+            } else if (flow_phase_[s] == 1) {
+                sch_flow_a_.push_back(s);
+                flow_a_maxf_ = std::max(flow_a_maxf_, P.sn_f[s]);
+            } else if (flow_phase_[s] == 2) {
+                sch_flow_b_.push_back(s);
+                flow_b_maxf_ = std::max(flow_b_maxf_, P.sn_f[s]);
             } else {
                 sch_small_.push_back(s);
                 sch_small_maxf_[l] = std::max(sch_small_maxf_[l], P.sn_f[s]);
@@ -226,6 +256,8 @@ void Engine::build_schedule() {
         sch_asm_ptr_[l + 1] = static_cast<int32_t>(sch_asm_.size());
         sch_all_ptr_[l + 1] = static_cast<int32_t>(sch_all_.size());
     }
+    // every front, top-down, for the backward dataflow sweep
+    sch_down_.assign(sch_all_.rbegin(), sch_all_.rend());
 }
 
 int32_t Engine::upload() {
@@ -288,6 +320,7 @@ int32_t Engine::upload() {
         // factor plan
         fac_.sn_c0 = c.take<int32_t>(ns + 1);
         fac_.sn_f = c.take<int32_t>(ns);
+        fac_.sn_parent = c.take<int32_t>(ns);
         fac_.sn_rows_off = c.take<int64_t>(ns + 1);
         fac_.sn_rows = c.take<int32_t>(P.sn_rows.size());
         fac_.sn_lx_off = c.take<int64_t>(ns + 1);
@@ -313,6 +346,9 @@ int32_t Engine::upload() {
         d_pot_ = c.take<int4>(sch_pot_.size());
         d_pan_ = c.take<int4>(sch_pan_.size());
         d_upd_ = c.take<int4>(sch_upd_.size());
+        d_flow_a_ = c.take<int32_t>(sch_flow_a_.size());
+        d_flow_b_ = c.take<int32_t>(sch_flow_b_.size());
+        d_down_ = c.take<int32_t>(sch_down_.size());
         // work
         work_.v = c.take<double>(n);
         work_.th = c.take<double>(n);
@@ -334,6 +370,7 @@ int32_t Engine::upload() {
         work_.u32 = mixed_ ? c.take<float>(lay_u_size_) : nullptr;
         work_.su = c.take<double>(P.su_size);
         work_.gvals = c.take<double>(P.tgt_local.size());
+        work_.flow = c.take<int32_t>(3 * static_cast<int64_t>(ns) + 16);
         work_.rdiag = c.take<double>(P.n_state);
         work_.rhs32 = mixed_ ? c.take<float>(P.n_state) : nullptr;
         work_.sol32 = mixed_ ? c.take<float>(P.n_state) : nullptr;
@@ -401,6 +438,7 @@ int32_t Engine::upload() {
     chk(put(const_cast<int32_t*>(net_.h_pcol), h_pcol_, st_));
     chk(put(const_cast<int32_t*>(fac_.sn_c0), P.sn_c0, st_));
     chk(put(const_cast<int32_t*>(fac_.sn_f), P.sn_f, st_));
+    chk(put(const_cast<int32_t*>(fac_.sn_parent), P.sn_parent, st_));
     chk(put(const_cast<int64_t*>(fac_.sn_rows_off), P.sn_rows_off, st_));
     chk(put(const_cast<int32_t*>(fac_.sn_rows), P.sn_rows, st_));
     chk(put(const_cast<int64_t*>(fac_.sn_lx_off), lay_lx_off_, st_));
@@ -426,6 +464,9 @@ int32_t Engine::upload() {
     chk(put(d_pot_, sch_pot_, st_));
     chk(put(d_pan_, sch_pan_, st_));
     chk(put(d_upd_, sch_upd_, st_));
+    chk(put(d_flow_a_, sch_flow_a_, st_));
+    chk(put(d_flow_b_, sch_flow_b_, st_));
+    chk(put(d_down_, sch_down_, st_));
     chk(put(work_.v, model.bus_v, st_));
     chk(put(work_.th, model.bus_th, st_));
     chk(put(work_.z, model.m_value, st_));
@@ -454,6 +495,23 @@ int32_t Engine::upload() {
     sched_.d_all = d_all_;
     sched_.h_lvl_maxf = sch_maxf_.data();
     sched_.h_lvl_maxpanel = sch_maxpanel_.data();
+    {
+        const int32_t ms = max_solve_front();
+        FlowGrids g = flow_grids(mixed_, flow_a_maxf_, flow_b_maxf_, ms);
+        sched_.d_flow_a = d_flow_a_;
+        sched_.flow_a_n = static_cast<int32_t>(sch_flow_a_.size());
+        sched_.flow_a_maxf = flow_a_maxf_;
+        sched_.flow_a_grid = std::max(1, std::min(g.a, sched_.flow_a_n));
+        sched_.d_flow_b = d_flow_b_;
+        sched_.flow_b_n = static_cast<int32_t>(sch_flow_b_.size());
+        sched_.flow_b_maxf = flow_b_maxf_;
+        sched_.flow_b_grid = std::max(1, std::min(g.b, sched_.flow_b_n));
+        sched_.solve_flow = (cfg.dataflow && g.solve > 0) ? 1 : 0;
+        sched_.d_up = d_all_;
+        sched_.d_down = d_down_;
+        sched_.solve_maxf = ms;
+        sched_.solve_grid = std::max(1, std::min(g.solve, ns));
+    }
 
     if (h_stage_n_ < static_cast<size_t>(m)) {
         if (h_stage_) cudaFreeHost(h_stage_);
@@ -695,6 +753,10 @@ int32_t Engine::solve(const SolveRequest& rq, SolveResult& out) {
                 break;
             }
             const uint32_t fl = h_status_->flags;
+            if (fl & FLAG_TIMEOUT) {
+                last_error = "factorisation dataflow wait timed out";
+                return -3;
+            }
             if (fl & FLAG_SINGULAR) {
                 out.status = CONV_SINGULAR;
                 factor_valid_ = false;
@@ -863,7 +925,17 @@ int32_t Engine::factor_and_solve(const double* rhs_orig, double* x_orig) {
     if (e != cudaSuccess) return set_cuda_error(e, "factor/solve");
     for (int32_t p = 0; p < P.n_state; ++p) x_orig[P.state_of_ps[p]] = x[p];
     factor_valid_ = false;
+    if (h_status_->flags & FLAG_TIMEOUT) {
+        last_error = "factorisation dataflow wait timed out";
+        return -3;
+    }
     return (h_status_->flags & FLAG_SINGULAR) ? -7 : 0;
+}
+
+int32_t Engine::max_solve_front() const {
+    int32_t m = 0;
+    for (int32_t f : plan_.sn_f) m = std::max(m, f);
+    return m;
 }
 
 int32_t Engine::export_ybus(std::vector<double>& g, std::vector<double>& b) {

@@ -40,7 +40,8 @@ struct EngineConfig {
     int32_t gain_policy = 0;     // 0: refactor every iteration; 1: reuse the factor until invalidated
     int32_t ordering = 0;        // symbolic ordering (see SymbolicParams)
     double big_front_flops = 2.0e5;  // FP64: fronts above this many factor flops use the tiled multi-CTA path
-    int32_t refine_steps = 1;        // mixed precision: refinement steps per Gauss-Newton step
+    int32_t refine_steps = 0;        // mixed precision: extra refinement steps per Gauss-Newton step
+    int32_t dataflow = 1;            // persistent dataflow kernels below the big fronts and for the solves
 };
 
 enum class Mode : int32_t { REALTIME = 0, PRECISION = 1 };
@@ -151,6 +152,13 @@ private:
         sch_pot_ptr_, sch_pan_ptr_, sch_upd_ptr_, sch_all_ptr_, sch_all_, sch_maxf_;
     std::vector<int4> sch_asm_, sch_pot_, sch_pan_, sch_upd_;
     std::vector<int64_t> sch_maxpanel_;
+    std::vector<int32_t> sch_flow_a_, sch_flow_b_, sch_down_;
+    std::vector<char> flow_phase_;
+    int32_t flow_a_maxf_ = 0, flow_b_maxf_ = 0;
+    int32_t* d_flow_a_ = nullptr;
+    int32_t* d_flow_b_ = nullptr;
+    int32_t* d_down_ = nullptr;
+    int32_t max_solve_front() const;
     std::vector<int64_t> lay_lx_off_, lay_u_off_;
     std::vector<int32_t> lay_u_ld_, h_pcol_;
     std::vector<uint8_t> lay_u_big_;

@@ -91,57 +91,124 @@ __device__ __forceinline__ const T* update_of(const DevFactor& F, const T* lx, c
     return (F.sn_u_big[c] ? lx : ub) + F.sn_u_off[c];
 }
 
+// Each child's relative map is staged in shared memory (relbuf, >= m ints)
+// and the update entries are loaded four per lane before they are scattered,
+// so several global loads are in flight per lane.
 template <typename T>
 __device__ __forceinline__ void extend_add_child(const DevFactor& F, const T* lx, const T* ubase, int c, T* dst,
-                                                 int ldd, int tid, int nth) {
+                                                 int ldd, int tid, int nth, int* relbuf) {
     const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
     const T* U = update_of<T>(F, lx, ubase, c);
     const int uld = F.sn_u_ld[c];
     const int* rel = F.sn_relmap + F.sn_su_off[c];
-    for (int x = tid; x < m * m; x += nth) {
-        const int i = x % m, j = x / m;
-        if (i >= j) dst[rel[i] + rel[j] * ldd] += U[i + (int64_t)j * uld];
+    for (int i = tid; i < m; i += nth) relbuf[i] = rel[i];
+    __syncthreads();
+    const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
+    for (int j = warp; j < m; j += nwarp) {
+        const int pj = relbuf[j] * ldd;
+        const T* Uj = U + (int64_t)j * uld;
+        for (int i0 = j + lane; i0 < m; i0 += 128) {
+            T u[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int i = i0 + 32 * t;
+                u[t] = (i < m) ? __ldcg(Uj + i) : T(0);
+            }
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int i = i0 + 32 * t;
+                if (i < m) dst[relbuf[i] + pj] += u[t];
+            }
+        }
     }
 }
 
 // ---------------------------------------------------------------------------
 // Small fronts: one CTA per front, front held in shared memory.
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_front_small(DevFactor F, DevWork W, const T* gv, T* lx, T* ub,
-                                                          const int* fronts) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* Fm = reinterpret_cast<T*>(smem_raw);
-    const int s = fronts[blockIdx.x];
+constexpr int kPanel = 8;  // panel width of the in-shared-memory factorisation
+
+// Assembles and partially factorises front s in shared memory (Fm holds
+// f x f values; relbuf >= kSmallFrontMax32 ints; rpan >= kPanel values).
+// kRowsPerLane = rows a lane keeps in registers: ceil(largest f / 32).
+template <typename T, int kRowsPerLane>
+__device__ void front_factor(const DevFactor& F, const DevWork& W, const T* gv, T* lx, T* ub, int s, T* Fm,
+                             int* relbuf, T* rpan) {
     const int f = F.sn_f[s];
     const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
     const int tid = threadIdx.x, nth = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
     for (int x = tid; x < f * f; x += nth) Fm[x] = T(0);
     __syncthreads();
     for (int tg = F.sn_tgt_ptr[s] + tid; tg < F.sn_tgt_ptr[s + 1]; tg += nth) Fm[F.tgt_local[tg]] = gv[tg];
     __syncthreads();
     for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) {
-        extend_add_child<T>(F, lx, ub, F.sn_child[ci], Fm, f, tid, nth);
+        extend_add_child<T>(F, lx, ub, F.sn_child[ci], Fm, f, tid, nth, relbuf);
         __syncthreads();
     }
-    const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
-    __shared__ T rpiv;
     T* rdg = reinterpret_cast<T*>(W.rdiag) + F.sn_c0[s];
-    for (int k = 0; k < nc; ++k) {
-        if (tid == 0) {
-            T sq, inv;
-            pivot(Fm[k + k * f], &sq, &inv, &W.status->flags);
-            Fm[k + k * f] = sq;
-            rpiv = inv;
-            rdg[k] = inv;
+    for (int k0 = 0; k0 < nc; k0 += kPanel) {
+        const int kb = min(kPanel, nc - k0);
+        // (1) one warp factors the kb x kb diagonal block
+        if (warp == 0) {
+            for (int k = 0; k < kb; ++k) {
+                const int kk = k0 + k;
+                if (lane == 0) {
+                    T sq, inv;
+                    pivot(Fm[kk + kk * f], &sq, &inv, &W.status->flags);
+                    Fm[kk + kk * f] = sq;
+                    rpan[k] = inv;
+                    rdg[kk] = inv;
+                }
+                __syncwarp();
+                const int i = kk + 1 + lane;
+                if (i < k0 + kb) Fm[i + kk * f] *= rpan[k];
+                __syncwarp();
+                if (i < k0 + kb) {
+                    const T lik = Fm[i + kk * f];
+                    for (int j = kk + 1; j <= i; ++j) Fm[i + j * f] -= lik * Fm[j + kk * f];
+                }
+                __syncwarp();
+            }
         }
         __syncthreads();
-        const T inv = rpiv;
-        for (int i = k + 1 + tid; i < f; i += nth) Fm[i + k * f] *= inv;
+        // (2) rows below the block: L[i, panel] = A[i, panel] L_dd^-T, one row per thread
+        for (int i = k0 + kb + tid; i < f; i += nth) {
+            T x[kPanel];
+            for (int c = 0; c < kb; ++c) {
+                T a = Fm[i + (k0 + c) * f];
+                for (int k = 0; k < c; ++k) a -= x[k] * Fm[(k0 + c) + (k0 + k) * f];
+                x[c] = a * rpan[c];
+            }
+            for (int c = 0; c < kb; ++c) Fm[i + (k0 + c) * f] = x[c];
+        }
         __syncthreads();
-        for (int j = k + 1 + warp; j < f; j += nwarp) {
-            const T ljk = Fm[j + k * f];
-            for (int i = j + lane; i < f; i += 32) Fm[i + j * f] -= Fm[i + k * f] * ljk;
+        // (3) trailing update of the lower triangle right of the panel; each
+        // lane keeps its rows' panel values in registers
+        const int q0 = k0 + kb;
+        if (q0 < f) {
+            T P[kRowsPerLane][kPanel];
+#pragma unroll
+            for (int t = 0; t < kRowsPerLane; ++t) {
+                const int i = lane + 32 * t;
+#pragma unroll
+                for (int c = 0; c < kPanel; ++c) P[t][c] = (i < f && c < kb) ? Fm[i + (k0 + c) * f] : T(0);
+            }
+            for (int j = q0 + warp; j < f; j += nwarp) {
+                T pj[kPanel];
+#pragma unroll
+                for (int c = 0; c < kPanel; ++c) pj[c] = (c < kb) ? Fm[j + (k0 + c) * f] : T(0);
+#pragma unroll
+                for (int t = 0; t < kRowsPerLane; ++t) {
+                    const int i = lane + 32 * t;
+                    if (i >= j && i < f) {
+                        T acc = T(0);
+#pragma unroll
+                        for (int c = 0; c < kPanel; ++c) acc += P[t][c] * pj[c];
+                        Fm[i + j * f] -= acc;
+                    }
+                }
+            }
         }
         __syncthreads();
     }
@@ -149,9 +216,74 @@ __global__ void __launch_bounds__(kThreads) k_front_small(DevFactor F, DevWork W
     for (int x = tid; x < f * nc; x += nth) L[x] = Fm[x];
     const int m = f - nc;
     T* U = ub + F.sn_u_off[s];
-    for (int x = tid; x < m * m; x += nth) {
-        const int i = x % m, j = x / m;
-        U[x] = Fm[(nc + i) + (nc + j) * f];
+    for (int j = warp; j < m; j += nwarp)
+        for (int i = lane; i < m; i += 32) U[i + (int64_t)j * m] = Fm[(nc + i) + (nc + j) * f];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_front_small(DevFactor F, DevWork W, const T* gv, T* lx, T* ub,
+                                                          const int* fronts) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ T rpan[kPanel];
+    __shared__ int relbuf[kSmallFrontMax32];
+    front_factor<T, (small_front_max<T>() + 31) / 32>(F, W, gv, lx, ub, fronts[blockIdx.x],
+                                                       reinterpret_cast<T*>(smem_raw), relbuf, rpan);
+}
+
+// ---------------------------------------------------------------------------
+// Dataflow scheduling: a persistent grid claims work items in order from an
+// atomic counter; an item waits (bounded) until the items it depends on have
+// published their completion flag.  Items are ordered so that every
+// dependency is claimed earlier, and a CTA only waits on items already
+// claimed by running CTAs, so progress never depends on CTAs that have not
+// started.  Data produced inside the pass is read with L1-bypassing loads.
+// ---------------------------------------------------------------------------
+constexpr long long kSpinLimit = 1LL << 22;
+constexpr int kFlowRowsA = (kFlowSmallF + 31) / 32;  // phase A: every front has f <= kFlowSmallF
+template <typename T>
+constexpr int kFlowRowsB = (small_front_max<T>() + 31) / 32;
+
+__device__ __forceinline__ void wait_done(const int* flag, uint32_t* status) {
+    long long spins = 0;
+    while (atomicAdd(const_cast<int*>(flag), 0) == 0) {
+        if (++spins > kSpinLimit) {
+            atomicOr(status, FLAG_TIMEOUT);
+            return;
+        }
+        __nanosleep(64);
+    }
+    __threadfence();
+}
+
+__device__ __forceinline__ void publish_done(int* flag) {
+    __threadfence();
+    atomicExch(flag, 1);
+}
+
+__device__ __forceinline__ int claim(int* counter, int* slot) {
+    __syncthreads();
+    if (threadIdx.x == 0) *slot = atomicAdd(counter, 1);
+    __syncthreads();
+    return *slot;
+}
+
+template <typename T, int kRowsPerLane>
+__global__ void __launch_bounds__(kThreads) k_front_flow(DevFactor F, DevWork W, const T* gv, T* lx, T* ub,
+                                                         const int* order, int n_items, int* counter, int* done) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ T rpan[kPanel];
+    __shared__ int relbuf[kSmallFrontMax32];
+    __shared__ int slot;
+    for (;;) {
+        const int item = claim(counter, &slot);
+        if (item >= n_items) break;
+        const int s = order[item];
+        if (threadIdx.x == 0)
+            for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) wait_done(done + F.sn_child[ci], &W.status->flags);
+        __syncthreads();
+        front_factor<T, kRowsPerLane>(F, W, gv, lx, ub, s, reinterpret_cast<T*>(smem_raw), relbuf, rpan);
+        __syncthreads();
+        if (threadIdx.x == 0) publish_done(done + s);
     }
 }
 
@@ -193,10 +325,23 @@ __global__ void __launch_bounds__(kThreads) k_big_assemble(DevFactor F, const T*
         const int j1 = lower_bound_i32(rel, j0, m, c1);
         const T* U = update_of<T>(F, lx, ub, c);
         const int uld = F.sn_u_ld[c];
-        const int nj = j1 - j0;
-        for (int x = tid; x < nj * m; x += nth) {
-            const int j = j0 + x / m, i = x % m;
-            if (i >= j) B[rel[i] + (int64_t)rel[j] * f] += U[i + (int64_t)j * uld];
+        const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
+        for (int j = j0 + warp; j < j1; j += nwarp) {
+            const int64_t pj = (int64_t)rel[j] * f;
+            const T* Uj = U + (int64_t)j * uld;
+            for (int i0 = j + lane; i0 < m; i0 += 128) {
+                T u[4];
+                int r[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int i = i0 + 32 * t;
+                    u[t] = (i < m) ? Uj[i] : T(0);
+                    r[t] = (i < m) ? rel[i] : 0;
+                }
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    if (i0 + 32 * t < m) B[r[t] + pj] += u[t];
+            }
         }
         __syncthreads();
     }
@@ -350,15 +495,10 @@ struct SolveVecs {
 };
 
 template <typename T, typename V>
-__global__ void __launch_bounds__(kThreads) k_fwd(DevFactor F, const T* lx, const T* rdiag, SolveVecs sv,
-                                                  const int* fronts) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    V* v = reinterpret_cast<V*>(smem_raw);
-    __shared__ T D[kTile * (kTile + 1)];
+__device__ void front_fwd(const DevFactor& F, const T* lx, const T* rdiag, const SolveVecs& sv, int s, V* v, T* D) {
     const V* rhs = reinterpret_cast<const V*>(sv.rhs);
     V* sol = reinterpret_cast<V*>(sv.sol);
     V* sub = reinterpret_cast<V*>(sv.su);
-    const int s = fronts[blockIdx.x];
     const int f = F.sn_f[s];
     const int c0 = F.sn_c0[s];
     const int nc = F.sn_c0[s + 1] - c0;
@@ -371,7 +511,11 @@ __global__ void __launch_bounds__(kThreads) k_fwd(DevFactor F, const T* lx, cons
         const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
         const V* su = sub + F.sn_su_off[c];
         const int* rel = F.sn_relmap + F.sn_su_off[c];
-        for (int i = tid; i < m; i += nth) v[rel[i]] += su[i];
+        for (int i = tid; i < m; i += nth) {
+            const V val = __ldcg(su + i);
+            const int r = rel[i];
+            v[r] += val;
+        }
         __syncthreads();
     }
     constexpr int ld = kTile + 1;
@@ -412,20 +556,15 @@ __device__ __forceinline__ V warp_sum_v(V v) {
 }
 
 template <typename T, typename V>
-__global__ void __launch_bounds__(kThreads) k_bwd(DevFactor F, const T* lx, const T* rdiag, SolveVecs sv,
-                                                  const int* fronts) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    V* x = reinterpret_cast<V*>(smem_raw);  // [f]: solution of the front's rows
-    __shared__ T D[kTile * (kTile + 1)];
+__device__ void front_bwd(const DevFactor& F, const T* lx, const T* rdiag, const SolveVecs& sv, int s, V* x, T* D) {
     V* sol = reinterpret_cast<V*>(sv.sol);
-    const int s = fronts[blockIdx.x];
     const int f = F.sn_f[s];
     const int c0 = F.sn_c0[s];
     const int nc = F.sn_c0[s + 1] - c0;
     const int* rows = F.sn_rows + F.sn_rows_off[s];
     const T* L = lx + F.sn_lx_off[s];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    for (int r = threadIdx.x; r < f; r += blockDim.x) x[r] = (r < nc) ? sol[c0 + r] : sol[rows[r]];
+    for (int r = threadIdx.x; r < f; r += blockDim.x) x[r] = (r < nc) ? __ldcg(sol + c0 + r) : __ldcg(sol + rows[r]);
     __syncthreads();
     constexpr int ld = kTile + 1;
     const int nblk = (nc + kTile - 1) / kTile;
@@ -457,6 +596,63 @@ __global__ void __launch_bounds__(kThreads) k_bwd(DevFactor F, const T* lx, cons
     for (int k = threadIdx.x; k < nc; k += blockDim.x) sol[c0 + k] = x[k];
 }
 
+template <typename T, typename V>
+__global__ void __launch_bounds__(kThreads) k_fwd(DevFactor F, const T* lx, const T* rdiag, SolveVecs sv,
+                                                  const int* fronts) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ T D[kTile * (kTile + 1)];
+    front_fwd<T, V>(F, lx, rdiag, sv, fronts[blockIdx.x], reinterpret_cast<V*>(smem_raw), D);
+}
+
+template <typename T, typename V>
+__global__ void __launch_bounds__(kThreads) k_bwd(DevFactor F, const T* lx, const T* rdiag, SolveVecs sv,
+                                                  const int* fronts) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ T D[kTile * (kTile + 1)];
+    front_bwd<T, V>(F, lx, rdiag, sv, fronts[blockIdx.x], reinterpret_cast<V*>(smem_raw), D);
+}
+
+// Forward sweep as dataflow: order = fronts bottom-up, waits on children.
+template <typename T, typename V>
+__global__ void __launch_bounds__(kThreads) k_fwd_flow(DevFactor F, DevWork W, const T* lx, const T* rdiag,
+                                                       SolveVecs sv, const int* order, int n_items, int* counter,
+                                                       int* done) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ T D[kTile * (kTile + 1)];
+    __shared__ int slot;
+    for (;;) {
+        const int item = claim(counter, &slot);
+        if (item >= n_items) break;
+        const int s = order[item];
+        if (threadIdx.x == 0)
+            for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) wait_done(done + F.sn_child[ci], &W.status->flags);
+        __syncthreads();
+        front_fwd<T, V>(F, lx, rdiag, sv, s, reinterpret_cast<V*>(smem_raw), D);
+        __syncthreads();
+        if (threadIdx.x == 0) publish_done(done + s);
+    }
+}
+
+// Backward sweep as dataflow: order = fronts top-down, waits on the parent.
+template <typename T, typename V>
+__global__ void __launch_bounds__(kThreads) k_bwd_flow(DevFactor F, DevWork W, const T* lx, const T* rdiag,
+                                                       SolveVecs sv, const int* order, int n_items, int* counter,
+                                                       int* done) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ T D[kTile * (kTile + 1)];
+    __shared__ int slot;
+    for (;;) {
+        const int item = claim(counter, &slot);
+        if (item >= n_items) break;
+        const int s = order[item];
+        if (threadIdx.x == 0 && F.sn_parent[s] >= 0) wait_done(done + F.sn_parent[s], &W.status->flags);
+        __syncthreads();
+        front_bwd<T, V>(F, lx, rdiag, sv, s, reinterpret_cast<V*>(smem_raw), D);
+        __syncthreads();
+        if (threadIdx.x == 0) publish_done(done + s);
+    }
+}
+
 template <typename HV>
 __global__ void k_gain_export(DevNet net, DevFactor F, DevWork W, const HV* hval, int n_tgt, double* out) {
     for (int tg = blockIdx.x * blockDim.x + threadIdx.x; tg < n_tgt; tg += gridDim.x * blockDim.x)
@@ -477,10 +673,15 @@ size_t solve_smem(int maxf) {
 template <typename T, typename HV>
 cudaError_t prepare_impl() {
     cudaError_t e = cudaFuncSetAttribute(k_front_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         kSmallFrontMax * kSmallFrontMax * (int)sizeof(double));
+                                         small_front_max<T>() * small_front_max<T>() * (int)sizeof(T));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_front_flow<T, kFlowRowsB<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 small_front_max<T>() * small_front_max<T>() * (int)sizeof(T));
     const int mx = (int)solve_smem<double>(16384);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fwd<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bwd<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fwd_flow<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bwd_flow<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     return e;
 }
 
@@ -491,6 +692,23 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
     if (ls.n_tgt > 0) {
         k_gain_values<T, HV><<<grid_for(ls.n_tgt, 256), 256, 0, st>>>(net, F, W, hval, gv, ls.n_tgt);
         ++g_kernel_launches;
+    }
+    if (ls.flow_a_n + ls.flow_b_n > 0) {
+        cudaError_t e = cudaMemsetAsync(W.flow, 0, sizeof(int) * (size_t)(F.n_super + 8), st);
+        if (e != cudaSuccess) return e;
+        int* counters = W.flow + F.n_super;
+        if (ls.flow_a_n > 0) {
+            const int mf = ls.flow_a_maxf;
+            k_front_flow<T, kFlowRowsA><<<ls.flow_a_grid, kThreads, (size_t)mf * mf * sizeof(T), st>>>(
+                F, W, gv, lx, ub, ls.d_flow_a, ls.flow_a_n, counters + 0, W.flow);
+            ++g_kernel_launches;
+        }
+        if (ls.flow_b_n > 0) {
+            const int mf = ls.flow_b_maxf;
+            k_front_flow<T, kFlowRowsB<T>><<<ls.flow_b_grid, kThreads, (size_t)mf * mf * sizeof(T), st>>>(
+                F, W, gv, lx, ub, ls.d_flow_b, ls.flow_b_n, counters + 1, W.flow);
+            ++g_kernel_launches;
+        }
     }
     for (int l = 0; l < ls.n_levels; ++l) {
         const int ns = ls.h_small_ptr[l + 1] - ls.h_small_ptr[l];
@@ -528,8 +746,24 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
 }
 
 template <typename T>
-cudaError_t solve_impl(const DevFactor& F, const LevelSchedule& ls, const T* lx, const T* rdiag, SolveVecs sv,
-                       cudaStream_t st) {
+cudaError_t solve_impl(const DevFactor& F, const DevWork& W, const LevelSchedule& ls, const T* lx, const T* rdiag,
+                       SolveVecs sv, cudaStream_t st) {
+    if (ls.solve_flow) {
+        // flags: [0, n_super) forward, [n_super, 2 n_super) backward, then counters
+        const int ns = F.n_super;
+        int* fwd_done = W.flow + ns + 8;
+        int* bwd_done = fwd_done + ns;
+        int* counters = bwd_done + ns;
+        cudaError_t e = cudaMemsetAsync(fwd_done, 0, sizeof(int) * (size_t)(2 * ns + 8), st);
+        if (e != cudaSuccess) return e;
+        const size_t smem = solve_smem<T>(ls.solve_maxf);
+        k_fwd_flow<T, T><<<ls.solve_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_up, ns, counters + 0,
+                                                                fwd_done);
+        k_bwd_flow<T, T><<<ls.solve_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_down, ns, counters + 1,
+                                                                bwd_done);
+        g_kernel_launches += 2;
+        return cudaGetLastError();
+    }
     for (int l = 0; l < ls.n_levels; ++l) {
         const int n = ls.h_all_ptr[l + 1] - ls.h_all_ptr[l];
         if (n > 0) {
@@ -549,7 +783,30 @@ cudaError_t solve_impl(const DevFactor& F, const LevelSchedule& ls, const T* lx,
     return cudaGetLastError();
 }
 
+template <typename T>
+FlowGrids flow_grids_impl(int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf) {
+    FlowGrids g{0, 0, 0};
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return g;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return g;
+    auto resident = [&](const void* fn, size_t smem) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem) != cudaSuccess) return 0;
+        return per_sm * sms;
+    };
+    g.a = resident((const void*)k_front_flow<T, kFlowRowsA>, (size_t)maxf_a * maxf_a * sizeof(T));
+    g.b = resident((const void*)k_front_flow<T, kFlowRowsB<T>>, (size_t)maxf_b * maxf_b * sizeof(T));
+    if (solve_maxf <= 16384) g.solve = resident((const void*)k_fwd_flow<T, T>, solve_smem<T>(solve_maxf));
+    cudaGetLastError();
+    return g;
+}
+
 }  // namespace
+
+FlowGrids flow_grids(bool mixed, int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf) {
+    return mixed ? flow_grids_impl<float>(maxf_a, maxf_b, solve_maxf)
+                 : flow_grids_impl<double>(maxf_a, maxf_b, solve_maxf);
+}
 
 cudaError_t prepare_factor_kernels() {
     cudaError_t e = prepare_impl<double, double>();
@@ -563,7 +820,7 @@ cudaError_t launch_factor32(const DevNet& net, const DevFactor& F, const DevWork
 }
 
 cudaError_t launch_solve32(const DevFactor& F, const DevWork& W, const LevelSchedule& ls, cudaStream_t st) {
-    return solve_impl<float>(F, ls, W.lx32, reinterpret_cast<const float*>(W.rdiag),
+    return solve_impl<float>(F, W, ls, W.lx32, reinterpret_cast<const float*>(W.rdiag),
                              SolveVecs{W.rhs32, W.sol32, W.su32}, st);
 }
 
@@ -573,8 +830,8 @@ cudaError_t launch_factor(const DevNet& net, const DevFactor& F, const DevWork& 
 }
 
 cudaError_t launch_solve(const DevFactor& F, const DevWork& W, const LevelSchedule& ls, cudaStream_t st) {
-    return solve_impl<double>(F, ls, W.lx, reinterpret_cast<const double*>(W.rdiag), SolveVecs{W.rhs, W.sol, W.su},
-                              st);
+    return solve_impl<double>(F, W, ls, W.lx, reinterpret_cast<const double*>(W.rdiag),
+                              SolveVecs{W.rhs, W.sol, W.su}, st);
 }
 
 cudaError_t launch_gain_export(const DevNet& net, const DevFactor& F, const DevWork& W, int32_t n_tgt, double* out,

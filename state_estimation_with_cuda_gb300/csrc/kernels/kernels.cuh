@@ -12,6 +12,7 @@ enum StatusFlag : uint32_t {
     FLAG_SINGULAR = 1u,   // non-positive / non-finite pivot in the factorisation
     FLAG_NONFINITE = 2u,  // NaN/Inf in the state step
     FLAG_CONVERGED = 4u,  // max |dx| < tolerance
+    FLAG_TIMEOUT = 8u,    // a dataflow wait gave up (bounded spin)
 };
 
 // Per-solve scalars kept on the device; read back once per iteration.
@@ -74,6 +75,7 @@ struct DevFactor {
     int32_t n_super, n_state;
     const int32_t* sn_c0;
     const int32_t* sn_f;
+    const int32_t* sn_parent;
     const int64_t* sn_rows_off;
     const int32_t* sn_rows;
     const int64_t* sn_lx_off;
@@ -120,6 +122,7 @@ struct DevWork {
     float* u32;       // update matrices (mixed pipeline)
     double* su;       // solve update vectors
     void* gvals;      // [n_tgt] gain entries of the current factorisation (factor type)
+    int* flow;        // dataflow flags and counters: [n_super + 8] factor, [2 n_super + 8] solves
     void* rdiag;      // [n_state] reciprocals of L's diagonal (factor type)
     float* rhs32;     // [n_state] FP32 right-hand side (mixed solves)
     float* sol32;     // [n_state] FP32 solution (mixed solves)
@@ -193,7 +196,27 @@ struct LevelSchedule {
     const int32_t* d_all = nullptr;         // every front, per level (solves)
     const int32_t* h_lvl_maxf = nullptr;    // [n_levels] largest front per level
     const int64_t* h_lvl_maxpanel = nullptr;  // [n_levels] largest f * nc per level
+    // dataflow phases of the factorisation (fronts below every big front):
+    // A = fronts whose whole subtree has f <= kFlowSmallF, B = the rest
+    const int32_t* d_flow_a = nullptr;
+    int32_t flow_a_n = 0, flow_a_maxf = 0, flow_a_grid = 0;
+    const int32_t* d_flow_b = nullptr;
+    int32_t flow_b_n = 0, flow_b_maxf = 0, flow_b_grid = 0;
+    // dataflow solves over every front: d_up = bottom-up order, d_down = top-down
+    int32_t solve_flow = 0;
+    const int32_t* d_up = nullptr;
+    const int32_t* d_down = nullptr;
+    int32_t solve_maxf = 0, solve_grid = 0;
 };
+
+// Largest front of the high-occupancy dataflow phase.
+constexpr int32_t kFlowSmallF = 64;
+
+// Resident-CTA grid sizes of the persistent dataflow kernels (0 = cannot run).
+struct FlowGrids {
+    int32_t a, b, solve;
+};
+FlowGrids flow_grids(bool mixed, int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf);
 
 // Tile edge of the big-front kernels.
 constexpr int kTile = 32;
@@ -212,7 +235,11 @@ cudaError_t launch_solve32(const DevFactor& f, const DevWork& w, const LevelSche
 // Kernels launched by this library since load (all engines of the process).
 extern std::atomic<int64_t> g_kernel_launches;
 
-// Largest front (rows) handled by the single-CTA shared-memory kernel.
+// Largest front (rows) handled by the single-CTA shared-memory kernel:
+// 160 x 160 doubles or 224 x 224 floats (<= 200 KiB of shared memory).
 constexpr int32_t kSmallFrontMax = 160;
+constexpr int32_t kSmallFrontMax32 = 224;
+template <typename T>
+__host__ __device__ constexpr int32_t small_front_max() { return sizeof(T) == 4 ? kSmallFrontMax32 : kSmallFrontMax; }
 
 }  // namespace sle_gb300

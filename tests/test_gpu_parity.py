@@ -172,9 +172,10 @@ def test_solve_is_deterministic():
     assert np.array_equal(out[0], out[1])
 
 
-def mixed_engine(g):
+def mixed_engine(g, refine=0):
     e = Estimator()
     e.set_option("use_double_precision", 0)
+    e.set_option("refine_steps", refine)
     e.load_network(g)
     e.upload_model()
     return e
@@ -192,9 +193,10 @@ def test_mixed_precision_flat_start_within_1e6(name):
     assert max(np.abs(v - ov).max(), np.abs(th - oth).max()) < 1e-6
 
 
-def test_mixed_precision_hot_start_sequence_grid10k():
+@pytest.mark.parametrize("refine", [0, 1])
+def test_mixed_precision_hot_start_sequence_grid10k(refine):
     g = grid("grid10k")
-    e, o = mixed_engine(g), Oracle(g)
+    e, o = mixed_engine(g, refine), Oracle(g)
     e.solve_with(max_iterations=20, tolerance=1e-6, flat_start=True)
     ov, oth, _, _ = o.wls(g.z, g.v_setpoint, np.zeros(g.n_bus), max_iterations=20, tolerance=1e-6)
     for u in range(4):
