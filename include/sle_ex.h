@@ -83,6 +83,20 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExGetGain(SLE_Handle handle, int32_t* rows, 
 /* Factorise G from the last evaluation and solve G x = rhs (state order). */
 SLE_API SLE_StatusCode SLE_CALL sle_ExFactorSolve(SLE_Handle handle, const SLE_Real* rhs, SLE_Real* x);
 
+/* Allocation-free variant of sle_ExFactorSolve (no counterpart in the
+ * reference SLE Engine): same inputs and result, but the call allocates no
+ * host or device memory.  Its scratch (right-hand side and solution staging,
+ * dataflow flags, solve update vectors, update matrices of the small fronts)
+ * lives in one static device array of 16 MiB in the library.
+ *   - The first call on a device looks the array up with that device current
+ *     (one-time set-up); make that first call before any stream capture.
+ *   - Every call on a device shares the array: calls that overlap in time
+ *     (two threads, two handles) race and must be serialised by the caller.
+ *   - A model whose scratch exceeds 16 MiB is rejected with
+ *     SLE_ERROR_INVALID_ARGUMENT and a message giving the bytes it needs.
+ * FP64 pipeline only (use_double_precision = 1), after sle_ExEvaluateAt. */
+SLE_API SLE_StatusCode SLE_CALL sle_ExFactorSolveNoAlloc(SLE_Handle handle, const SLE_Real* rhs, SLE_Real* x);
+
 /* Symbolic analysis: bus_perm[n_bus] (position -> bus), state_of_ps[n_state]
  * (permuted -> state index), sn_c0[n_super+1], sn_parent[n_super],
  * sn_rows_off[n_super+1], sn_rows[sn_rows_off[n_super]].  Any may be NULL. */

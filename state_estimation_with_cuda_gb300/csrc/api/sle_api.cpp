@@ -1046,6 +1046,16 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExFactorSolve(SLE_Handle handle, const SLE_R
     return SLE_OK;
 }
 
+SLE_API SLE_StatusCode SLE_CALL sle_ExFactorSolveNoAlloc(SLE_Handle handle, const SLE_Real* rhs, SLE_Real* x) {
+    if (!handle) return SLE_ERROR_INVALID_HANDLE;
+    if (!rhs || !x) return SLE_ERROR_INVALID_ARGUMENT;
+    const int32_t rc = E(handle)->factor_and_solve_noalloc(rhs, x);
+    if (rc == -7) return fail(SLE_ERROR_SINGULAR_MATRIX, "gain matrix is not positive definite");
+    if (rc == -11) return fail(SLE_ERROR_INVALID_ARGUMENT, E(handle)->last_error);
+    if (rc) return fail(SLE_ERROR_CUDA_FAILURE, E(handle)->last_error);
+    return SLE_OK;
+}
+
 SLE_API SLE_StatusCode SLE_CALL sle_ExGetSymbolic(SLE_Handle handle, int32_t* bus_perm, int32_t* state_of_ps,
                                                   int32_t* sn_c0, int32_t* sn_parent, int64_t* sn_rows_off,
                                                   int32_t* sn_rows) {

@@ -932,6 +932,35 @@ int32_t Engine::factor_and_solve(const double* rhs_orig, double* x_orig) {
     return (h_status_->flags & FLAG_SINGULAR) ? -7 : 0;
 }
 
+int32_t Engine::factor_and_solve_noalloc(const double* rhs_orig, double* x_orig) {
+    if (!uploaded_) {
+        last_error = "no model on the device (upload and evaluate first)";
+        return -4;
+    }
+    if (mixed_) {
+        last_error = "stage access needs the FP64 pipeline (use_double_precision = 1)";
+        return -4;
+    }
+    const NoAllocShape sh{lay_u_size_, plan_.su_size, plan_.n_state, plan_.n_super};
+    const size_t need = noalloc_scratch_need(sh);
+    if (need > kNoAllocScratchBytes) {
+        last_error = "allocation-free factor/solve needs " + std::to_string(need) + " bytes of scratch; the static limit is " +
+                     std::to_string(kNoAllocScratchBytes) + " bytes";
+        return -11;
+    }
+    cudaError_t e = cudaMemsetAsync(&work_.status->flags, 0, sizeof(uint32_t), st_);
+    if (e == cudaSuccess) e = launch_factor_solve_noalloc(net_, fac_, work_, sched_, sh, rhs_orig, x_orig, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_status_, work_.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "allocation-free factor/solve");
+    factor_valid_ = false;
+    if (h_status_->flags & FLAG_TIMEOUT) {
+        last_error = "factorisation dataflow wait timed out";
+        return -3;
+    }
+    return (h_status_->flags & FLAG_SINGULAR) ? -7 : 0;
+}
+
 int32_t Engine::max_solve_front() const {
     int32_t m = 0;
     for (int32_t f : plan_.sn_f) m = std::max(m, f);

@@ -109,6 +109,10 @@ public:
     int32_t evaluate_at(const double* v, const double* th, int32_t exact);
     int32_t export_gain(std::vector<int32_t>& rows, std::vector<int32_t>& cols, std::vector<double>& vals);
     int32_t factor_and_solve(const double* rhs_orig, double* x_orig);
+    // Same result as factor_and_solve, with every per-call scratch buffer in
+    // a static device array (no host or device allocation); -11 when the
+    // model needs more scratch than kNoAllocScratchBytes.
+    int32_t factor_and_solve_noalloc(const double* rhs_orig, double* x_orig);
     int32_t export_ybus(std::vector<double>& g, std::vector<double>& b);
     int32_t export_eval(double* hval, double* hx, double* rhs_orig);
 

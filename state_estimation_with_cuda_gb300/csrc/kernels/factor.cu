@@ -22,6 +22,7 @@
 #include "kernels.cuh"
 
 #include <algorithm>
+#include <mutex>
 
 namespace sle_gb300 {
 namespace {
@@ -841,6 +842,117 @@ cudaError_t launch_gain_export(const DevNet& net, const DevFactor& F, const DevW
         ++g_kernel_launches;
     }
     return cudaGetLastError();
+}
+
+
+// ---------------------------------------------------------------------------
+// Allocation-free factor/solve.  One call's scratch -- right-hand side and
+// solution staging in state order, the dataflow flags, the solve update
+// vectors and the small fronts' update matrices -- lives in one file-scope
+// device array of kNoAllocScratchBytes.  The address is looked up once per
+// device (cudaGetSymbolAddress, with that device current); every call on a
+// device shares the array, so calls that overlap in time race.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+struct NoAllocLayout {
+    size_t rhs, x, flow, su, u, total;  // byte offsets into the scratch array
+};
+
+NoAllocLayout noalloc_layout(const NoAllocShape& sh) {
+    NoAllocLayout l{};
+    size_t off = 0;
+    l.rhs = off;
+    off = align256(off + sizeof(double) * (size_t)sh.n_state);
+    l.x = off;
+    off = align256(off + sizeof(double) * (size_t)sh.n_state);
+    l.flow = off;
+    off = align256(off + sizeof(int) * (3 * (size_t)sh.n_super + 16));
+    l.su = off;
+    off = align256(off + sizeof(double) * (size_t)sh.su_elems);
+    l.u = off;
+    off = align256(off + sizeof(double) * (size_t)sh.u_elems);
+    l.total = off;
+    return l;
+}
+
+// state index -> permuted position (theta of every bus but the slack, then |V|)
+__device__ __forceinline__ int ps_of_state(const DevNet& net, const DevFactor& F, int st) {
+    const int nth = net.n_bus - 1;
+    if (st < nth) return F.bus_ps_theta[st < net.slack ? st : st + 1];
+    return F.bus_ps_v[st - nth];
+}
+
+__global__ void k_state_to_ps(DevNet net, DevFactor F, const double* in, double* out) {
+    const int st = blockIdx.x * blockDim.x + threadIdx.x;
+    if (st < F.n_state) out[ps_of_state(net, F, st)] = in[st];
+}
+
+__global__ void k_ps_to_state(DevNet net, DevFactor F, const double* in, double* out) {
+    const int st = blockIdx.x * blockDim.x + threadIdx.x;
+    if (st < F.n_state) out[st] = in[ps_of_state(net, F, st)];
+}
+}  // namespace
+
+size_t noalloc_scratch_need(const NoAllocShape& sh) { return noalloc_layout(sh).total; }
+
+cudaError_t noalloc_scratch_setup(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return cudaSuccess;
+}
+
+cudaError_t launch_factor_solve_noalloc(const DevNet& net, const DevFactor& F, const DevWork& W,
+                                        const LevelSchedule& ls, const NoAllocShape& sh, const double* rhs_host,
+                                        double* x_host, cudaStream_t st) {
+    const NoAllocLayout l = noalloc_layout(sh);
+    if (l.total > kNoAllocScratchBytes) return cudaErrorInvalidValue;  // callers check the size first
+    void* base = nullptr;
+    cudaError_t e = noalloc_scratch_setup(&base);
+    if (e != cudaSuccess) return e;
+    unsigned char* b = static_cast<unsigned char*>(base);
+    double* d_rhs = reinterpret_cast<double*>(b + l.rhs);
+    double* d_x = reinterpret_cast<double*>(b + l.x);
+    DevWork W2 = W;
+    W2.flow = reinterpret_cast<int*>(b + l.flow);  // cleared at the start of each pass
+    W2.su = reinterpret_cast<double*>(b + l.su);
+    W2.u = reinterpret_cast<double*>(b + l.u);
+    const int n = F.n_state;
+    e = cudaMemcpyAsync(d_rhs, rhs_host, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    if (n > 0) {
+        k_state_to_ps<<<grid_for(n, 256), 256, 0, st>>>(net, F, d_rhs, W2.rhs);
+        ++g_kernel_launches;
+    }
+    e = factor_impl<double, double>(net, F, W2, ls, W2.hval, W2.lx, W2.u, st);
+    if (e == cudaSuccess)
+        e = solve_impl<double>(F, W2, ls, W2.lx, reinterpret_cast<const double*>(W2.rdiag),
+                               SolveVecs{W2.rhs, W2.sol, W2.su}, st);
+    if (e != cudaSuccess) return e;
+    if (n > 0) {
+        k_ps_to_state<<<grid_for(n, 256), 256, 0, st>>>(net, F, W2.sol, d_x);
+        ++g_kernel_launches;
+    }
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(x_host, d_x, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, st);
+    return e;
 }
 
 }  // namespace sle_gb300

@@ -218,6 +218,21 @@ struct FlowGrids {
 };
 FlowGrids flow_grids(bool mixed, int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf);
 
+// Allocation-free FP64 factor/solve (scratch in a static device array).
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
+struct NoAllocShape {
+    int64_t u_elems;   // update-matrix entries of the small fronts (layout size)
+    int64_t su_elems;  // solve update-vector entries
+    int32_t n_state, n_super;
+};
+size_t noalloc_scratch_need(const NoAllocShape& sh);
+// Looks the array up for the current device on first use.
+cudaError_t noalloc_scratch_setup(void** out);
+// rhs_host / x_host in state order; status flags land in W.status.
+cudaError_t launch_factor_solve_noalloc(const DevNet& net, const DevFactor& F, const DevWork& W,
+                                        const LevelSchedule& ls, const NoAllocShape& sh, const double* rhs_host,
+                                        double* x_host, cudaStream_t st);
+
 // Tile edge of the big-front kernels.
 constexpr int kTile = 32;
 

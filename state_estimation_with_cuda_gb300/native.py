@@ -210,6 +210,7 @@ SLE_SIGNATURES = {
     "sle_ExGetJacobian": (I, [H, P(I), P(I), P(D), P(D), P(D)]),
     "sle_ExGetGain": (I, [H, P(I), P(I), P(D)]),
     "sle_ExFactorSolve": (I, [H, P(D), P(D)]),
+    "sle_ExFactorSolveNoAlloc": (I, [H, P(D), P(D)]),
     "sle_ExGetSymbolic": (I, [H, P(I), P(I), P(I), P(I), P(ctypes.c_int64), P(I)]),
     "sle_ExStageTelemetry": (I, [H, P(D), I, I]),
     "sle_ExUseTelemetry": (I, [H, I]),
