@@ -29,11 +29,6 @@ namespace {
 
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ double warp_sum(double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-
 template <typename HV>
 __device__ __forceinline__ double gain_entry(const DevNet& net, const DevFactor& F, const DevWork& W, const HV* hval,
                                              int tg) {
@@ -86,6 +81,25 @@ __device__ __forceinline__ void pivot(double d, double* sq, double* inv, uint32_
     }
 }
 
+// L_kk = sqrt(d) and 1 / L_kk for a positive finite d (the caller checks).
+__device__ __forceinline__ void pivot_value(float d, float* sq, float* inv) {
+    const float y = __frsqrt_rn(d);
+    *sq = d * y;
+    *inv = y;
+}
+__device__ __forceinline__ void pivot_value(double d, double* sq, double* inv) {
+    if (d > 1e-30 && d < 1e30) {
+        double y = static_cast<double>(rsqrtf(static_cast<float>(d)));
+        y = y * (1.5 - 0.5 * d * y * y);
+        y = y * (1.5 - 0.5 * d * y * y);
+        *sq = d * y;
+        *inv = y;
+    } else {
+        *sq = sqrt(d);
+        *inv = 1.0 / *sq;
+    }
+}
+
 // Extend-add child c's update matrix (lower triangle) into a front buffer.
 template <typename T>
 __device__ __forceinline__ const T* update_of(const DevFactor& F, const T* lx, const T* ub, int c) {
@@ -126,109 +140,226 @@ __device__ __forceinline__ void extend_add_child(const DevFactor& F, const T* lx
 
 // ---------------------------------------------------------------------------
 // Small fronts: one CTA per front, front held in shared memory.
+//
+// Layout: column-major with a leading dimension padded to 16 bytes
+// (front_ld), so four consecutive rows of a column are one or two aligned
+// vector loads.  The partial factorisation runs over 32-column panels:
+//   (1) warp 0 factors the diagonal block in registers (lane i holds row i,
+//       columns broadcast by shuffles) and leaves L11^T and 1/diag in shared
+//       memory;
+//   (2) every thread solves one row of the panel below the block,
+//       x = a L11^-T, by forward substitution in registers;
+//   (3) the trailing lower triangle is updated by 4x4 register tiles,
+//       A22 -= X X^T, two vector loads and sixteen FMAs per panel column.
 // ---------------------------------------------------------------------------
-constexpr int kPanel = 8;  // panel width of the in-shared-memory factorisation
+constexpr int kPanel = 32;  // widest panel of the in-shared-memory factorisation
+static_assert(kThreads >= kSmallFrontMax32, "one thread per front row");
+
+template <typename T>
+__device__ __forceinline__ void load4(const T* p, T (&v)[4]);
+template <>
+__device__ __forceinline__ void load4<float>(const float* p, float (&v)[4]) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+}
+template <>
+__device__ __forceinline__ void load4<double>(const double* p, double (&v)[4]) {
+    const double2 q0 = reinterpret_cast<const double2*>(p)[0];
+    const double2 q1 = reinterpret_cast<const double2*>(p)[1];
+    v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
+}
+template <typename T>
+__device__ __forceinline__ void store4(T* p, const T (&v)[4]);
+template <>
+__device__ __forceinline__ void store4<float>(float* p, const float (&v)[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+template <>
+__device__ __forceinline__ void store4<double>(double* p, const double (&v)[4]) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+    reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+}
+
+// Shared-memory scratch of one front besides the front itself.
+template <typename T>
+struct FrontSmem {
+    T lt[kPanel][kPanel + 1];  // lt[c][r] = L11[r][c] of the current panel
+    T rinv[kPanel];            // 1 / L11[c][c]
+    int relbuf[kSmallFrontMax32];
+};
 
 // Assembles and partially factorises front s in shared memory (Fm holds
-// f x f values; relbuf >= kSmallFrontMax32 ints; rpan >= kPanel values).
-// kRowsPerLane = rows a lane keeps in registers: ceil(largest f / 32).
-template <typename T, int kRowsPerLane>
+// front_ld(f) x f values) with panels of KP <= kPanel columns.
+template <typename T, int KP>
 __device__ void front_factor(const DevFactor& F, const DevWork& W, const T* gv, T* lx, T* ub, int s, T* Fm,
-                             int* relbuf, T* rpan) {
+                             FrontSmem<T>& sm) {
+    static_assert(KP <= kPanel && KP <= 32, "panel wider than a warp");
     const int f = F.sn_f[s];
+    const int ldf = front_ld<T>(f);
     const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
     const int tid = threadIdx.x, nth = blockDim.x;
-    const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
-    for (int x = tid; x < f * f; x += nth) Fm[x] = T(0);
+    const int lane = tid & 31, warp = tid >> 5;
+    for (int x = tid; x < ldf * f; x += nth) Fm[x] = T(0);
     __syncthreads();
-    for (int tg = F.sn_tgt_ptr[s] + tid; tg < F.sn_tgt_ptr[s + 1]; tg += nth) Fm[F.tgt_local[tg]] = gv[tg];
+    if (ldf == f) {
+        for (int tg = F.sn_tgt_ptr[s] + tid; tg < F.sn_tgt_ptr[s + 1]; tg += nth) Fm[F.tgt_local[tg]] = gv[tg];
+    } else {
+        for (int tg = F.sn_tgt_ptr[s] + tid; tg < F.sn_tgt_ptr[s + 1]; tg += nth) {
+            const int l = F.tgt_local[tg];  // row + col * f
+            const int c = l / f;
+            Fm[(l - c * f) + c * ldf] = gv[tg];
+        }
+    }
     __syncthreads();
     for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) {
-        extend_add_child<T>(F, lx, ub, F.sn_child[ci], Fm, f, tid, nth, relbuf);
+        extend_add_child<T>(F, lx, ub, F.sn_child[ci], Fm, ldf, tid, nth, sm.relbuf);
         __syncthreads();
     }
     T* rdg = reinterpret_cast<T*>(W.rdiag) + F.sn_c0[s];
-    for (int k0 = 0; k0 < nc; k0 += kPanel) {
-        const int kb = min(kPanel, nc - k0);
-        // (1) one warp factors the kb x kb diagonal block
+#pragma unroll 1
+    for (int k0 = 0; k0 < nc; k0 += KP) {
+        const int kb = min(KP, nc - k0);
+        // (1) diagonal block, one warp, in registers.  The loop over the
+        // block's columns stays rolled (compact code for a single warp); the
+        // current column is picked out of the row registers by selects.
         if (warp == 0) {
-            for (int k = 0; k < kb; ++k) {
-                const int kk = k0 + k;
-                if (lane == 0) {
+            T a[KP];
+            const int i = k0 + lane;
+#pragma unroll
+            for (int j = 0; j < KP; ++j) a[j] = (lane < kb && j <= lane) ? Fm[i + (k0 + j) * ldf] : T(0);
+            bool bad = false;
+            T my_inv = T(0);  // 1 / L_kk of this lane's row
+            // Fully unrolled and branch-free: the chain from one pivot to the
+            // next is a shuffle, a reciprocal square root and two FMAs; the
+            // other shuffles and updates of a step overlap with it.
+#pragma unroll
+            for (int k = 0; k < KP; ++k) {
+                if (k < kb) {
+                    T d = __shfl_sync(0xffffffffu, a[k], k);
+                    bad |= !(d > T(0)) || !isfinite(d);
+                    d = (d > T(0) && isfinite(d)) ? d : T(1);
                     T sq, inv;
-                    pivot(Fm[kk + kk * f], &sq, &inv, &W.status->flags);
-                    Fm[kk + kk * f] = sq;
-                    rpan[k] = inv;
-                    rdg[kk] = inv;
-                }
-                __syncwarp();
-                const int i = kk + 1 + lane;
-                if (i < k0 + kb) Fm[i + kk * f] *= rpan[k];
-                __syncwarp();
-                if (i < k0 + kb) {
-                    const T lik = Fm[i + kk * f];
-                    for (int j = kk + 1; j <= i; ++j) Fm[i + j * f] -= lik * Fm[j + kk * f];
-                }
-                __syncwarp();
-            }
-        }
-        __syncthreads();
-        // (2) rows below the block: L[i, panel] = A[i, panel] L_dd^-T, one row per thread
-        for (int i = k0 + kb + tid; i < f; i += nth) {
-            T x[kPanel];
-            for (int c = 0; c < kb; ++c) {
-                T a = Fm[i + (k0 + c) * f];
-                for (int k = 0; k < c; ++k) a -= x[k] * Fm[(k0 + c) + (k0 + k) * f];
-                x[c] = a * rpan[c];
-            }
-            for (int c = 0; c < kb; ++c) Fm[i + (k0 + c) * f] = x[c];
-        }
-        __syncthreads();
-        // (3) trailing update of the lower triangle right of the panel; each
-        // lane keeps its rows' panel values in registers
-        const int q0 = k0 + kb;
-        if (q0 < f) {
-            T P[kRowsPerLane][kPanel];
+                    pivot_value(d, &sq, &inv);
+                    const T lk = (lane == k) ? sq : (lane > k ? a[k] * inv : a[k]);
+                    a[k] = lk;
+                    my_inv = (lane == k) ? inv : my_inv;
 #pragma unroll
-            for (int t = 0; t < kRowsPerLane; ++t) {
-                const int i = lane + 32 * t;
-#pragma unroll
-                for (int c = 0; c < kPanel; ++c) P[t][c] = (i < f && c < kb) ? Fm[i + (k0 + c) * f] : T(0);
-            }
-            for (int j = q0 + warp; j < f; j += nwarp) {
-                T pj[kPanel];
-#pragma unroll
-                for (int c = 0; c < kPanel; ++c) pj[c] = (c < kb) ? Fm[j + (k0 + c) * f] : T(0);
-#pragma unroll
-                for (int t = 0; t < kRowsPerLane; ++t) {
-                    const int i = lane + 32 * t;
-                    if (i >= j && i < f) {
-                        T acc = T(0);
-#pragma unroll
-                        for (int c = 0; c < kPanel; ++c) acc += P[t][c] * pj[c];
-                        Fm[i + j * f] -= acc;
+                    for (int j = k + 1; j < KP; ++j) {
+                        const T ljk = __shfl_sync(0xffffffffu, lk, j);
+                        a[j] = (lane >= j) ? a[j] - lk * ljk : a[j];
                     }
+                    __syncwarp();
+                }
+            }
+            if (lane < kb) {
+                sm.rinv[lane] = my_inv;
+                rdg[k0 + lane] = my_inv;
+            }
+            if (bad && lane == 0) atomicOr(&W.status->flags, FLAG_SINGULAR);
+#pragma unroll
+            for (int j = 0; j < KP; ++j)
+                if (lane < kb && j <= lane) {
+                    Fm[i + (k0 + j) * ldf] = a[j];
+                    sm.lt[j][lane] = a[j];
+                }
+        }
+        __syncthreads();
+        // (2) rows below the block: x = a L11^-T, one row per thread (f <= kThreads)
+        const int q0 = k0 + kb;
+        {
+            const int r = q0 + tid;
+            if (r < f) {
+                T x[KP];
+#pragma unroll
+                for (int c = 0; c < KP; ++c) x[c] = (c < kb) ? Fm[r + (k0 + c) * ldf] : T(0);
+#pragma unroll
+                for (int c = 0; c < KP; ++c) {
+                    if (c < kb) {
+                        x[c] *= sm.rinv[c];
+#pragma unroll
+                        for (int c2 = c + 1; c2 < KP; ++c2) x[c2] -= x[c] * sm.lt[c][c2];
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < KP; ++c)
+                    if (c < kb) Fm[r + (k0 + c) * ldf] = x[c];
+            }
+        }
+        __syncthreads();
+        // (3) trailing update of the lower triangle, 4x4 tiles on 4-aligned
+        // rows; tiles are numbered down each tile column so that neighbouring
+        // threads touch neighbouring rows (conflict-free vector accesses)
+        if (q0 < f) {
+            const int R0 = q0 & ~3;
+            const int nt = (f - R0 + 3) >> 2;
+            const int ntiles = nt * (nt + 1) / 2;
+            const float b2 = 2.f * nt + 1.f;
+#pragma unroll 1
+            for (int t = tid; t < ntiles; t += nth) {
+                // column bj holds tiles bi = bj..nt-1 and starts at bj*nt - bj*(bj-1)/2
+                int bj = static_cast<int>((b2 - sqrtf(b2 * b2 - 8.f * t)) * 0.5f);
+                bj = max(0, min(bj, nt - 1));
+                while (bj > 0 && bj * nt - bj * (bj - 1) / 2 > t) --bj;
+                while (bj + 1 < nt && (bj + 1) * nt - (bj + 1) * bj / 2 <= t) ++bj;
+                const int bi = bj + (t - (bj * nt - bj * (bj - 1) / 2));
+                const int i0 = R0 + 4 * bi, j0 = R0 + 4 * bj;
+                T acc[4][4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) acc[u][v] = T(0);
+#pragma unroll 2
+                for (int c = 0; c < kb; ++c) {
+                    const T* col = Fm + (k0 + c) * ldf;
+                    T av[4], bv[4];
+                    load4<T>(col + i0, av);
+                    load4<T>(col + j0, bv);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+#pragma unroll
+                        for (int v = 0; v < 4; ++v) acc[u][v] += av[u] * bv[v];
+                }
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    const int j = j0 + v;
+                    if (j < q0 || j >= f) continue;
+                    T* dst = Fm + i0 + j * ldf;
+                    T cur[4];
+                    load4<T>(dst, cur);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (i0 + u >= j && i0 + u < f) cur[u] -= acc[u][v];
+                    store4<T>(dst, cur);
                 }
             }
         }
         __syncthreads();
     }
     T* L = lx + F.sn_lx_off[s];
-    for (int x = tid; x < f * nc; x += nth) L[x] = Fm[x];
+    for (int x = tid; x < f * nc; x += nth) {
+        const int c = x / f;
+        L[x] = Fm[(x - c * f) + c * ldf];
+    }
     const int m = f - nc;
     T* U = ub + F.sn_u_off[s];
+    const int nwarp = nth >> 5;
     for (int j = warp; j < m; j += nwarp)
-        for (int i = lane; i < m; i += 32) U[i + (int64_t)j * m] = Fm[(nc + i) + (nc + j) * f];
+        for (int i = lane; i < m; i += 32) U[i + (int64_t)j * m] = Fm[(nc + i) + (nc + j) * ldf];
 }
 
+// Panel widths: fronts of the high-occupancy dataflow phase (f <= 64) use
+// 16-column panels and a register budget for several CTAs per SM; the rest
+// use 32-column panels and the full register file (one CTA per SM anyway).
+constexpr int kPanelSmall = 16;
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_front_small(DevFactor F, DevWork W, const T* gv, T* lx, T* ub,
-                                                          const int* fronts) {
+constexpr int kMinBlocksA = sizeof(T) == 4 ? 3 : 2;
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 1) k_front_small(DevFactor F, DevWork W, const T* gv, T* lx, T* ub,
+                                                             const int* fronts) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ T rpan[kPanel];
-    __shared__ int relbuf[kSmallFrontMax32];
-    front_factor<T, (small_front_max<T>() + 31) / 32>(F, W, gv, lx, ub, fronts[blockIdx.x],
-                                                       reinterpret_cast<T*>(smem_raw), relbuf, rpan);
+    __shared__ FrontSmem<T> sm;
+    front_factor<T, kPanel>(F, W, gv, lx, ub, fronts[blockIdx.x], reinterpret_cast<T*>(smem_raw), sm);
 }
 
 // ---------------------------------------------------------------------------
@@ -240,9 +371,6 @@ __global__ void __launch_bounds__(kThreads) k_front_small(DevFactor F, DevWork W
 // started.  Data produced inside the pass is read with L1-bypassing loads.
 // ---------------------------------------------------------------------------
 constexpr long long kSpinLimit = 1LL << 22;
-constexpr int kFlowRowsA = (kFlowSmallF + 31) / 32;  // phase A: every front has f <= kFlowSmallF
-template <typename T>
-constexpr int kFlowRowsB = (small_front_max<T>() + 31) / 32;
 
 __device__ __forceinline__ void wait_done(const int* flag, uint32_t* status) {
     long long spins = 0;
@@ -261,19 +389,23 @@ __device__ __forceinline__ void publish_done(int* flag) {
     atomicExch(flag, 1);
 }
 
+// Thread 0 alone claims, waits and publishes; each such step is followed by
+// __syncwarp() so that warp 0 is converged again before the block barrier
+// (the single-warp phases of a front rely on a converged warp 0).
 __device__ __forceinline__ int claim(int* counter, int* slot) {
     __syncthreads();
     if (threadIdx.x == 0) *slot = atomicAdd(counter, 1);
+    __syncwarp();
     __syncthreads();
     return *slot;
 }
 
-template <typename T, int kRowsPerLane>
-__global__ void __launch_bounds__(kThreads) k_front_flow(DevFactor F, DevWork W, const T* gv, T* lx, T* ub,
-                                                         const int* order, int n_items, int* counter, int* done) {
+template <typename T, int KP, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_front_flow(DevFactor F, DevWork W, const T* gv, T* lx,
+                                                                     T* ub, const int* order, int n_items,
+                                                                     int* counter, int* done) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ T rpan[kPanel];
-    __shared__ int relbuf[kSmallFrontMax32];
+    __shared__ FrontSmem<T> sm;
     __shared__ int slot;
     for (;;) {
         const int item = claim(counter, &slot);
@@ -281,8 +413,9 @@ __global__ void __launch_bounds__(kThreads) k_front_flow(DevFactor F, DevWork W,
         const int s = order[item];
         if (threadIdx.x == 0)
             for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) wait_done(done + F.sn_child[ci], &W.status->flags);
+        __syncwarp();
         __syncthreads();
-        front_factor<T, kRowsPerLane>(F, W, gv, lx, ub, s, reinterpret_cast<T*>(smem_raw), relbuf, rpan);
+        front_factor<T, KP>(F, W, gv, lx, ub, s, reinterpret_cast<T*>(smem_raw), sm);
         __syncthreads();
         if (threadIdx.x == 0) publish_done(done + s);
     }
@@ -627,6 +760,7 @@ __global__ void __launch_bounds__(kThreads) k_fwd_flow(DevFactor F, DevWork W, c
         const int s = order[item];
         if (threadIdx.x == 0)
             for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) wait_done(done + F.sn_child[ci], &W.status->flags);
+        __syncwarp();
         __syncthreads();
         front_fwd<T, V>(F, lx, rdiag, sv, s, reinterpret_cast<V*>(smem_raw), D);
         __syncthreads();
@@ -647,6 +781,7 @@ __global__ void __launch_bounds__(kThreads) k_bwd_flow(DevFactor F, DevWork W, c
         if (item >= n_items) break;
         const int s = order[item];
         if (threadIdx.x == 0 && F.sn_parent[s] >= 0) wait_done(done + F.sn_parent[s], &W.status->flags);
+        __syncwarp();
         __syncthreads();
         front_bwd<T, V>(F, lx, rdiag, sv, s, reinterpret_cast<V*>(smem_raw), D);
         __syncthreads();
@@ -674,10 +809,10 @@ size_t solve_smem(int maxf) {
 template <typename T, typename HV>
 cudaError_t prepare_impl() {
     cudaError_t e = cudaFuncSetAttribute(k_front_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         small_front_max<T>() * small_front_max<T>() * (int)sizeof(T));
+                                         (int)front_smem<T>(small_front_max<T>()));
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_front_flow<T, kFlowRowsB<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 small_front_max<T>() * small_front_max<T>() * (int)sizeof(T));
+        e = cudaFuncSetAttribute(k_front_flow<T, kPanel, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)front_smem<T>(small_front_max<T>()));
     const int mx = (int)solve_smem<double>(16384);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fwd<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bwd<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -700,13 +835,13 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
         int* counters = W.flow + F.n_super;
         if (ls.flow_a_n > 0) {
             const int mf = ls.flow_a_maxf;
-            k_front_flow<T, kFlowRowsA><<<ls.flow_a_grid, kThreads, (size_t)mf * mf * sizeof(T), st>>>(
+            k_front_flow<T, kPanelSmall, kMinBlocksA<T>><<<ls.flow_a_grid, kThreads, front_smem<T>(mf), st>>>(
                 F, W, gv, lx, ub, ls.d_flow_a, ls.flow_a_n, counters + 0, W.flow);
             ++g_kernel_launches;
         }
         if (ls.flow_b_n > 0) {
             const int mf = ls.flow_b_maxf;
-            k_front_flow<T, kFlowRowsB<T>><<<ls.flow_b_grid, kThreads, (size_t)mf * mf * sizeof(T), st>>>(
+            k_front_flow<T, kPanel, 1><<<ls.flow_b_grid, kThreads, front_smem<T>(mf), st>>>(
                 F, W, gv, lx, ub, ls.d_flow_b, ls.flow_b_n, counters + 1, W.flow);
             ++g_kernel_launches;
         }
@@ -715,7 +850,7 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
         const int ns = ls.h_small_ptr[l + 1] - ls.h_small_ptr[l];
         if (ns > 0) {
             const int mf = ls.h_small_maxf[l];
-            k_front_small<T><<<ns, kThreads, (size_t)mf * mf * sizeof(T), st>>>(F, W, gv, lx, ub,
+            k_front_small<T><<<ns, kThreads, front_smem<T>(mf), st>>>(F, W, gv, lx, ub,
                                                                                   ls.d_small + ls.h_small_ptr[l]);
             ++g_kernel_launches;
         }
@@ -795,8 +930,8 @@ FlowGrids flow_grids_impl(int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf) {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem) != cudaSuccess) return 0;
         return per_sm * sms;
     };
-    g.a = resident((const void*)k_front_flow<T, kFlowRowsA>, (size_t)maxf_a * maxf_a * sizeof(T));
-    g.b = resident((const void*)k_front_flow<T, kFlowRowsB<T>>, (size_t)maxf_b * maxf_b * sizeof(T));
+    g.a = resident((const void*)k_front_flow<T, kPanelSmall, kMinBlocksA<T>>, front_smem<T>(maxf_a));
+    g.b = resident((const void*)k_front_flow<T, kPanel, 1>, front_smem<T>(maxf_b));
     if (solve_maxf <= 16384) g.solve = resident((const void*)k_fwd_flow<T, T>, solve_smem<T>(solve_maxf));
     cudaGetLastError();
     return g;

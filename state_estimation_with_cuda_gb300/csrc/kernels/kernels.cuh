@@ -256,5 +256,16 @@ constexpr int32_t kSmallFrontMax = 160;
 constexpr int32_t kSmallFrontMax32 = 224;
 template <typename T>
 __host__ __device__ constexpr int32_t small_front_max() { return sizeof(T) == 4 ? kSmallFrontMax32 : kSmallFrontMax; }
+// Leading dimension of a front held in shared memory: f rounded up to a
+// multiple of 4 elements (16-byte aligned columns; 4-row tiles stay inside
+// their column).
+template <typename T>
+__host__ __device__ constexpr int32_t front_ld(int32_t f) {
+    return (f + 3) / 4 * 4;
+}
+template <typename T>
+__host__ __device__ constexpr size_t front_smem(int32_t f) {
+    return static_cast<size_t>(front_ld<T>(f)) * static_cast<size_t>(f) * sizeof(T);
+}
 
 }  // namespace sle_gb300
