@@ -388,6 +388,7 @@ SEGrid* segen_create(const SEGenParams* p) {
         add(4, k, 1, p->sigma_flow);
         add(5, k, 1, p->sigma_flow);
     }
+    const int32_t m_tele = static_cast<int32_t>(g->mtype.size());  // telemetry rows (before pseudo rows)
     // Observability restoration (topological observability: a spanning tree
     // whose branches each carry a distinct measurement).  Flow-measured
     // branches join their ends; each injection-measured bus then joins one
@@ -440,10 +441,15 @@ SEGrid* segen_create(const SEGenParams* p) {
     g->z.resize(g->m);
     for (int32_t q = 0; q < g->m; ++q) g->z[q] = g->htrue[q] + g->sigma[q] * rng_noise.normal();
     g->gross.assign(g->m, 0);
+    // Gross errors model telemetry failures: they hit a seeded fraction of the
+    // telemetry rows only, never the pseudo-measurements that restore
+    // observability (a +-30 sigma error on a pseudo flow, sigma 0.05, is a
+    // 1.5 pu error on the only row covering a leaf and drives |V| into the
+    // clamp, so the iteration cannot converge).
     if (p->gross_frac > 0.0) {
         Rng rng_gross(mix_seed(p->seed, 6));
-        const int32_t ng = static_cast<int32_t>(std::lround(p->gross_frac * g->m));
-        for (int32_t q : sample_sorted(rng_gross, g->m, ng)) {
+        const int32_t ng = static_cast<int32_t>(std::lround(p->gross_frac * m_tele));
+        for (int32_t q : sample_sorted(rng_gross, m_tele, ng)) {
             const double mag = 10.0 + 20.0 * rng_gross.uniform();
             const double sgn = (rng_gross.next() >> 63) ? -1.0 : 1.0;
             g->z[q] += sgn * mag * g->sigma[q];
