@@ -1,30 +1,39 @@
 #!/usr/bin/env python3
-"""Benchmark: WLS state-estimation hot-start solves on one GB300 per rank.
+"""Benchmark: WLS state-estimation solves on one GB300 per rank.
 
-Workload (the configuration the headline metric is quoted on): the seeded
-10,000-bus / 14,000-branch synthetic grid (|V| at 30 % of buses, P+Q
-injection at 60 %, both-end P+Q flows on 70 % of branches, plus the pseudo
-flows that restore observability), plain FP64.  A flat-start solve brings the
-state to the operating point; each step is then one telemetry update that
-re-noises 1 % of the rows followed by a hot-start Gauss-Newton solve to
-max|dx| < 1e-6 (sle_SolveWithConfig, PRECISION mode, refactorised gain).
+Headline workload (the serving form): a resident fleet of 200 seeded
+synthetic grids with Zipf(1.2) sizes over 30..200,000 buses (1.4 branches per
+bus; |V| at 30 % of buses, P+Q injection at 60 %, both-end P+Q flows on 70 %
+of branches, plus the pseudo flows that restore observability).  Requests
+arrive as a Poisson stream at 2,000 requests/s, each a fresh FP64
+measurement snapshot for a uniformly chosen grid (0.5 % also open or close a
+non-bridge branch), hot-started from the grid's last estimate, max|dx| < 1e-6.
 
-  value   solves/s with the telemetry snapshots already resident in device
-          memory (device-to-device copy into the engine, then the solve),
-          timed with CUDA events on the engine's stream;
-  e2e     the same metric through the reference-facing C ABI with host
-          buffers: sle_UpdateTelemetry (host -> device) + sle_SolveWithConfig
-          + sle_GetVoltageMagnitudes / sle_GetVoltageAngles (device -> host),
-          wall-clock per step;
-L2 is flushed (256 MiB write on the engine's stream) before every timed step
-in both legs.  With torchrun (N > 1) every rank solves its own replica (the
-path does not shard; there is no collective); value = all ranks' solves / the
+One step = one request.  W warm-up requests are served and drained, then
+exactly K requests are timed, from the first submission to the last
+completion, through the C ABI with host buffers (sle_ExServerSubmit copies
+the snapshot host -> device, sle_ExServerWait returns the result):
+
+  value            requests completed per second, mixed-precision server
+                   (FP32 gain / factor / solves, FP64 residual, gradient and
+                   state), with latency_ms p50 / p99 from submit to result;
+  served_fp64      the same stream through a plain-FP64 server;
+  per_grid_fp64    the plain FP64 per-grid path on the same K requests: one
+                   engine per grid (sle_UpdateTelemetry + sle_SolveWithConfig),
+                   one request at a time;
+  batch512 / grid200k / grid10k   the other configurations (batched form,
+                   200k-bus flat start, 10k-bus hot starts with the device-
+                   resident leg, e2e leg and per-stage roofline).
+
+With torchrun (N > 1) every rank serves its own replica of the fleet (grids
+do not shard across GPUs; no collective); value = all ranks' requests / the
 slowest rank's time.
 
 --impl reference times the reference's algorithm on the host cores instead:
 the reference has no CPU implementation and its GPU path cannot run, so this
 arm runs the CPU FP64 oracle (the restatement of the reference's
-Gauss-Newton WLS) on the same workload.
+Gauss-Newton WLS) on requests of the same stream, in arrival order, within a
+time budget.
 """
 import argparse
 import ctypes
@@ -46,14 +55,22 @@ WORKLOAD = "grid10k"
 FLUSH_BYTES = 256 << 20
 
 
+LAMBDA = 2000.0
+FLEET = 200
+SNAPS_PER_GRID = 4
+BREAKER_FRAC = 0.005
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3000, help="timed requests")
+    ap.add_argument("--warmup", type=int, default=200, help="warm-up requests")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bounded CPU-baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=60.0, help="bounded CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid10k-steps", type=int, default=40)
+    ap.add_argument("--skip-extra", action="store_true", help="headline legs only")
     return ap.parse_args()
 
 
@@ -181,7 +198,8 @@ def stage_bytes(info, g, vb=8):
 
 
 def run_leg(args, g, snaps, local, mixed, world):
-    """One precision form: device-resident leg, end-to-end leg, profiled pass."""
+    """grid10k, one precision form: device-resident leg, end-to-end leg,
+    profiled pass (args.steps / args.warmup here are the grid10k counts)."""
     from state_estimation_with_cuda_gb300 import Estimator, native
     from state_estimation_with_cuda_gb300.api import MODE_PRECISION
 
@@ -291,116 +309,361 @@ def roofline(leg, g, mixed):
             "algorithmic_bytes_per_call": int(sb[dom])}
 
 
-def run_gb300(args, world, rank, local):
-    from state_estimation_with_cuda_gb300 import workloads
+class Stream:
+    """The serving workload: fleet, per-grid snapshots, seeded request stream."""
 
-    g = workloads.make(WORKLOAD)
-    snaps = [g.renoise(u).copy() for u in range(args.warmup + args.steps)]
-    mixed = run_leg(args, g, snaps, local, True, world)
-    fp64 = run_leg(args, g, snaps, local, False, world)
-    out = None
-    if rank == 0:
-        def summary(leg):
-            lat = np.array(leg["times"])
-            return {"value": round(world * args.steps / (leg["total_ms"] * 1e-3), 3),
-                    "ms_per_step": round(leg["total_ms"] / args.steps, 5),
-                    "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 4),
-                                   "p99": round(float(np.percentile(lat, 99)), 4)},
-                    "e2e": {"value": round(world * args.steps / (leg["e2e_total"] * 1e-3), 3), "unit": UNIT,
-                            "h2d_bytes_per_step": 8 * g.n_meas, "d2h_bytes_per_step": 16 * g.n_bus,
-                            "latency_ms": {"p50": round(float(np.percentile(leg["e2e_times"], 50)), 4),
-                                           "p99": round(float(np.percentile(leg["e2e_times"], 99)), 4)}},
-                    "iterations_per_solve": round(float(np.mean(leg["iters"])), 3),
-                    "gpu_launches": int(leg["launches"]),
-                    "stages_ms_per_solve": {k: round(v / max(args.steps, 1), 5) for k, v in leg["stage_ms"].items()},
-                    "stage_launches_per_solve": {k: round(v / max(args.steps, 1), 2)
-                                                 for k, v in leg["stage_launch"].items()}}
-        sm, sf = summary(mixed), summary(fp64)
-        err = float(max(np.abs(mixed["v"] - fp64["v"]).max(), np.abs(mixed["th"] - fp64["th"]).max()))
-        info = mixed["info"]
-        out = {
-            "metric": METRIC, "value": sm["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": sm["ms_per_step"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 gain/factor + f64 residual/refinement/state",
-            "data": "synthetic (seeded generator)",
-            "config": {
-                "workload": "grid10k hot-start solves: %d buses, %d branches, %d rows, %d states; 1%% of rows "
-                            "re-noised per step; tol 1e-6, gain refactorised every iteration; mixed precision "
-                            "(value) and plain FP64 (fp64)" % (g.n_bus, g.n_branch, g.n_meas, 2 * g.n_bus - 1),
-                "l2": "flushed before every timed step (256 MiB write)",
-                "parallelism": "replicas" if world > 1 else "single",
-                "iterations_per_solve": sm["iterations_per_solve"],
-            },
-            "latency_ms": sm["latency_ms"],
-            "e2e": sm["e2e"],
-            "gpu_launches": sm["gpu_launches"],
-            "roofline": roofline(mixed, g, True),
-            "stages_ms_per_solve": sm["stages_ms_per_solve"],
-            "stage_launches_per_solve": sm["stage_launches_per_solve"],
-            "fp64": dict(sf, roofline=roofline(fp64, g, False)),
-            "mixed_vs_fp64_max_state_err": err,
-            "clocks": mixed["clk"],
-            "plan": {"nnz_l": info.nnz_l, "n_super": info.n_super, "levels": info.n_levels,
-                     "max_front": info.max_front, "factor_flops": info.factor_flops},
-        }
-    return out, g
+    def __init__(self, n_req):
+        from state_estimation_with_cuda_gb300 import workloads
+
+        self.grids = workloads.fleet_grids(FLEET)
+        self.snaps = [[g.renoise(u).copy() for u in range(SNAPS_PER_GRID)] for g in self.grids]
+        rng = np.random.default_rng(0x5E04 + 1)
+        self.arrival = np.cumsum(rng.exponential(1.0 / LAMBDA, n_req))
+        self.target = rng.integers(0, FLEET, n_req)
+        self.breaker = rng.random(n_req) < BREAKER_FRAC
+        # snapshot index per request: a grid's k-th request uses its snapshot k mod SNAPS_PER_GRID
+        seen = np.zeros(FLEET, np.int64)
+        self.snap = np.empty(n_req, np.int64)
+        for i, g in enumerate(self.target):
+            self.snap[i] = seen[g] % SNAPS_PER_GRID
+            seen[g] += 1
+        # breaker edits: open a non-bridge branch, close it again at the grid's next edit
+        self.branch = np.full(n_req, -1, np.int64)
+        self.closed = np.ones(n_req, np.int64)
+        opened = {}
+        for i in np.nonzero(self.breaker)[0]:
+            g = int(self.target[i])
+            if g in opened:
+                self.branch[i], self.closed[i] = opened.pop(g), 1
+            else:
+                k = self.grids[g]._lib.segen_pick_nonbridge(self.grids[g]._h, int(i))
+                if k >= 0:
+                    self.branch[i], self.closed[i] = k, 0
+                    opened[g] = k
+        self.n_req = n_req
+
+    def z(self, i):
+        return self.snaps[int(self.target[i])][int(self.snap[i])]
+
+    def describe(self):
+        n = [g.n_bus for g in self.grids]
+        return {"grids": FLEET, "buses_min": int(min(n)), "buses_max": int(max(n)), "buses_total": int(sum(n)),
+                "rows_total": int(sum(g.n_meas for g in self.grids)), "lambda_per_s": LAMBDA,
+                "breaker_fraction": BREAKER_FRAC}
 
 
-def cpu_hot_start(g, seconds, min_solves=3, max_solves=None):
-    """Oracle hot-start solves of the same workload for about `seconds`."""
+def run_served(args, stream, mixed, local, lo, hi, clocks=None):
+    """Requests [lo, hi) of the stream paced at their arrival offsets through a
+    Server; warm-up requests [0, lo) are served and drained first."""
+    import threading
+
+    from state_estimation_with_cuda_gb300 import Server, native
+
+    t0 = time.perf_counter()
+    srv = Server(mixed=mixed, device_id=local)
+    lib = srv.lib
+    for g in stream.grids:
+        srv.add_grid(g)
+    srv.start()
+    t_start = time.perf_counter() - t0
+
+    def serve(a, b):
+        tickets = [None] * (b - a)
+
+        def submitter():
+            base = time.perf_counter()
+            off = stream.arrival[a]
+            for i in range(a, b):
+                dt = (stream.arrival[i] - off) - (time.perf_counter() - base)
+                if dt > 0:
+                    time.sleep(dt)
+                tickets[i - a] = srv.submit(int(stream.target[i]), stream.z(i), int(stream.branch[i]),
+                                            int(stream.closed[i]))
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        out = []
+        for k in range(b - a):
+            while tickets[k] is None:
+                time.sleep(0.0002)
+            out.append(srv.wait(tickets[k], 3.6e6))
+        th.join()
+        return out
+
+    serve(0, lo)
+    stats = native.SLE_ExStats()
+    est = None
+    from state_estimation_with_cuda_gb300 import Estimator
+
+    est = Estimator()
+    lib.sle_ExGetStats(est.h, ctypes.byref(stats))
+    l0 = stats.total_launches
+    if clocks:
+        clocks.start()
+    res = serve(lo, hi)
+    clk = clocks.stop() if clocks else None
+    lib.sle_ExGetStats(est.h, ctypes.byref(stats))
+    launches = stats.total_launches - l0
+    est.close()
+    st = srv.stats()
+    srv.close()
+    lat = np.array([(r.t_done_ns - r.t_submit_ns) / 1e6 for r in res])
+    t_first = min(r.t_submit_ns for r in res)
+    t_last = max(r.t_done_ns for r in res)
+    big = np.array([stream.grids[int(stream.target[i])].n_bus >= 20000 for i in range(lo, hi)])
+    return {
+        "elapsed_s": (t_last - t_first) / 1e9, "lat": lat, "ok": int(sum(r.status == 0 for r in res)),
+        "iters": float(np.mean([r.iterations for r in res])), "batch": float(np.mean([r.batch_size for r in res])),
+        "units": st.units, "device_bytes": int(st.device_bytes), "start_s": t_start, "launches": int(launches),
+        "clk": clk, "lat_small": lat[~big], "lat_big": lat[big],
+        "h2d": float(np.mean([8 * stream.grids[int(stream.target[i])].n_meas for i in range(lo, hi)])),
+    }
+
+
+def run_per_grid_fp64(stream, local, lo, hi):
+    """Plain FP64 per-grid path: one engine per grid, requests one at a time
+    (breaker requests are served as plain snapshots here: no re-analysis)."""
+    from state_estimation_with_cuda_gb300 import Estimator
+
+    engines = {}
+    for i in range(lo, hi):
+        g = int(stream.target[i])
+        if g not in engines:
+            e = Estimator()
+            e.load_network(stream.grids[g])
+            e.upload_model()
+            e.solve_with(max_iterations=20, tolerance=1e-6, flat_start=True)
+            engines[g] = e
+    lat = []
+    t0 = time.perf_counter()
+    for i in range(lo, hi):
+        e = engines[int(stream.target[i])]
+        ts = time.perf_counter()
+        e.update_telemetry(stream.z(i))
+        rc, r = e.solve_with(max_iterations=20, tolerance=1e-6)
+        lat.append((time.perf_counter() - ts) * 1e3)
+    dt = time.perf_counter() - t0
+    for e in engines.values():
+        e.close()
+    return {"value": round((hi - lo) / dt, 3), "service_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
+                                                              "p99": round(float(np.percentile(lat, 99)), 3)},
+            "note": "one engine per grid, one request at a time; breaker requests served as plain snapshots"}
+
+
+def run_batch512():
+    from state_estimation_with_cuda_gb300 import BatchEstimator, workloads
+
+    grids = workloads.batch_grids(512)
+    snaps = [[g.renoise(u).copy() for g in grids] for u in range(3)]
+    out = {}
+    for mixed in (True, False):
+        b = BatchEstimator(mixed=mixed)
+        for g in grids:
+            b.add_grid(g)
+        b.upload_model()
+        b.solve(flat_start=True)
+        times, its = [], []
+        for u in range(3):
+            t0 = time.perf_counter()
+            for i in range(len(grids)):
+                b.set_telemetry(i, snaps[u][i])
+            res = b.solve(flat_start=False)
+            times.append(time.perf_counter() - t0)
+            its += [r.iterations for r in res]
+            assert all(r.status == 0 for r in res)
+        b.close()
+        out["mixed" if mixed else "fp64"] = {"value": round(3 * len(grids) / sum(times), 1),
+                                             "ms_per_batch": round(1e3 * float(np.mean(times)), 2),
+                                             "iterations_mean": round(float(np.mean(its)), 3),
+                                             "iterations_max": int(max(its))}
+    out["config"] = ("512 grids, log-uniform 30..5000 buses (%d buses, %d rows); hot start after a 1%% re-noise; "
+                     "all grids in one batch (one pass of each kernel per Gauss-Newton step)"
+                     % (sum(g.n_bus for g in grids), sum(g.n_meas for g in grids)))
+    out["unit"] = "solves/s"
+    return out
+
+
+def run_grid200k():
+    from state_estimation_with_cuda_gb300 import Estimator, workloads
+
+    g = workloads.make("grid200k")
+    out, states = {}, {}
+    for mixed in (True, False):
+        e = Estimator()
+        e.set_option("use_double_precision", 0 if mixed else 1)
+        e.load_network(g)
+        e.upload_model()
+        e.solve_with(max_iterations=2, tolerance=1e-6, flat_start=True)  # graphs captured
+        t0 = time.perf_counter()
+        rc, r = e.solve_with(max_iterations=30, tolerance=1e-6, flat_start=True)
+        dt = time.perf_counter() - t0
+        states[mixed] = e.voltages()
+        rc, rh = e.solve_with(max_iterations=100, tolerance=1e-6, flat_start=True, robust=True, huber_gamma=1.5)
+        e.close()
+        out["mixed" if mixed else "fp64"] = {
+            "flat_start_ms": round(dt * 1e3, 2), "iterations": r.iterations, "status": r.status,
+            "huber": {"status": rh.status, "iterations": rh.iterations, "max_mismatch": rh.max_mismatch}}
+    out["mixed_vs_fp64_max_state_err"] = float(max(np.abs(states[True][0] - states[False][0]).max(),
+                                                   np.abs(states[True][1] - states[False][1]).max()))
+    out["config"] = ("%d buses, %d branches, %d rows, 2%% gross errors on telemetry rows; plain WLS flat start "
+                     "(wall clock of sle_SolveWithConfig); Huber IRLS (gamma 1.5, the reference's weights) capped "
+                     "at 100 iterations" % (g.n_bus, g.n_branch, g.n_meas))
+    return out
+
+
+def oracle_served(stream, lo, budget_s, max_req=None):
+    """The CPU FP64 oracle on requests [lo, ...) of the stream in arrival order,
+    each hot-started from the grid's true state, until the time budget."""
     from oracle.binding import Oracle, threads
 
-    o = Oracle(g)
-    v, th, res, _ = o.wls(g.z, g.v_setpoint, np.zeros(g.n_bus), max_iterations=30, tolerance=1e-6)
-    assert res.status == 0
+    cache = {}
     times = []
-    u = 0
-    t_start = time.perf_counter()
-    while True:
-        z = g.renoise(10000 + u)
+    i = lo
+    spent = 0.0
+    while i < stream.n_req and (max_req is None or len(times) < max_req):
+        g = int(stream.target[i])
+        grid = stream.grids[g]
+        if g not in cache:
+            cache[g] = Oracle(grid)
         t0 = time.perf_counter()
-        v, th, res, _ = o.wls(z, v, th, max_iterations=20, tolerance=1e-6, flat_start=False)
-        times.append(time.perf_counter() - t0)
-        u += 1
-        if max_solves is not None and u >= max_solves:
+        cache[g].wls(stream.z(i), grid.v_true, grid.theta_true, max_iterations=20, tolerance=1e-6, flat_start=False)
+        dt = time.perf_counter() - t0
+        times.append(dt)
+        spent += dt
+        i += 1
+        if spent > budget_s and len(times) >= 5:
             break
-        if u >= min_solves and time.perf_counter() - t_start > seconds:
-            break
-    o.close()
+    for o in cache.values():
+        o.close()
     return len(times) / sum(times), times, threads()
+
+
+def run_gb300(args, world, rank, local):
+    lo, hi = args.warmup, args.warmup + args.steps
+    stream = Stream(hi)
+    clocks = ClockSampler(local)
+    barrier(world)
+    sm = run_served(args, stream, True, local, lo, hi, clocks)
+    barrier(world)
+    sf = run_served(args, stream, False, local, lo, hi)
+    elapsed = allreduce_max(sm["elapsed_s"], world)
+    out = None
+    extra = {}
+    if rank == 0:
+        extra["per_grid_fp64"] = run_per_grid_fp64(stream, local, lo, hi)
+        if not args.skip_extra:
+            extra["batch512"] = run_batch512()
+            extra["grid200k"] = run_grid200k()
+    g10 = None
+    if not args.skip_extra:
+        from state_estimation_with_cuda_gb300 import workloads
+
+        a10 = argparse.Namespace(**vars(args))
+        a10.steps, a10.warmup = args.grid10k_steps, 3
+        g10 = workloads.make("grid10k")
+        snaps10 = [g10.renoise(u).copy() for u in range(a10.warmup + a10.steps)]
+        m10 = run_leg(a10, g10, snaps10, local, True, world)
+        f10 = run_leg(a10, g10, snaps10, local, False, world)
+    if rank == 0:
+        def pct(a, q):
+            return round(float(np.percentile(a, q)), 3) if len(a) else None
+
+        value = round(world * args.steps / elapsed, 3)
+        served_fp64 = round(args.steps / sf["elapsed_s"], 3)
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * elapsed / args.steps, 5), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 gain/factor/solves + f64 residual/gradient/state",
+            "data": "synthetic (seeded generator)",
+            "config": dict(stream.describe(), workload=(
+                "serving form: resident fleet of 200 grids, Zipf(1.2) sizes over 30..200000 buses, Poisson "
+                "requests at 2000/s (uniform grid, fresh snapshot, 0.5%% breaker edits), hot start, max|dx| < 1e-6; "
+                "one step = one request; %d warm-up requests then %d timed" % (args.warmup, args.steps)),
+                parallelism="replicas" if world > 1 else "single",
+                l2="working set of the fleet (%.1f GB) exceeds L2" % (sm["device_bytes"] / 1e9)),
+            "latency_ms": {"p50": pct(sm["lat"], 50), "p99": pct(sm["lat"], 99),
+                           "p50_small_grids": pct(sm["lat_small"], 50), "p99_small_grids": pct(sm["lat_small"], 99),
+                           "p50_grids_20k_plus": pct(sm["lat_big"], 50), "p99_grids_20k_plus": pct(sm["lat_big"], 99)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": int(sm["h2d"]), "d2h_bytes_per_step": 56,
+                    "note": "the served leg is end to end: host snapshot in (sle_ExServerSubmit), result out "
+                            "(sle_ExServerWait)"},
+            "gpu_launches": sm["launches"],
+            "served": {"ok": sm["ok"], "iterations_mean": round(sm["iters"], 3), "mean_batch": round(sm["batch"], 2),
+                       "units": sm["units"], "device_bytes": sm["device_bytes"], "start_s": round(sm["start_s"], 2)},
+            "served_fp64": {"value": served_fp64, "latency_ms": {"p50": pct(sf["lat"], 50), "p99": pct(sf["lat"], 99)},
+                            "ok": sf["ok"], "iterations_mean": round(sf["iters"], 3)},
+            "clocks": sm["clk"],
+        }
+        out.update(extra)
+        pg = extra["per_grid_fp64"]["value"]
+        out["served_mixed_vs_per_grid_fp64"] = round(value / pg, 3) if pg else None
+        if g10 is not None:
+            out["grid10k"] = summarize_leg(m10, f10, g10, a10, world)
+    return out, stream
+
+
+def summarize_leg(mixed, fp64, g, a, world):
+    def summary(leg):
+        lat = np.array(leg["times"])
+        return {"value": round(world * a.steps / (leg["total_ms"] * 1e-3), 3),
+                "ms_per_step": round(leg["total_ms"] / a.steps, 5),
+                "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 4),
+                               "p99": round(float(np.percentile(lat, 99)), 4)},
+                "e2e": {"value": round(world * a.steps / (leg["e2e_total"] * 1e-3), 3), "unit": UNIT,
+                        "h2d_bytes_per_step": 8 * g.n_meas, "d2h_bytes_per_step": 16 * g.n_bus},
+                "iterations_per_solve": round(float(np.mean(leg["iters"])), 3),
+                "gpu_launches": int(leg["launches"]),
+                "stages_ms_per_solve": {k: round(v / max(a.steps, 1), 5) for k, v in leg["stage_ms"].items()}}
+    sm, sf = summary(mixed), summary(fp64)
+    err = float(max(np.abs(mixed["v"] - fp64["v"]).max(), np.abs(mixed["th"] - fp64["th"]).max()))
+    info = mixed["info"]
+    return {
+        "config": "grid10k hot-start solves: %d buses, %d branches, %d rows, %d states; 1%% of rows re-noised per "
+                  "step; device-resident telemetry, L2 flushed (256 MiB write) before every step"
+                  % (g.n_bus, g.n_branch, g.n_meas, 2 * g.n_bus - 1),
+        "mixed": dict(sm, roofline=roofline(mixed, g, True)),
+        "fp64": dict(sf, roofline=roofline(fp64, g, False)),
+        "mixed_vs_fp64_max_state_err": err,
+        "plan": {"nnz_l": info.nnz_l, "n_super": info.n_super, "levels": info.n_levels,
+                 "max_front": info.max_front, "factor_flops": info.factor_flops},
+    }
 
 
 def main():
     args = parse()
     world, rank, local = dist_setup()
+    lo, hi = args.warmup, args.warmup + args.steps
     if args.impl == "reference":
         if rank != 0:
             return
-        from state_estimation_with_cuda_gb300 import workloads
-
-        g = workloads.make(WORKLOAD)
-        # warm-up solves (untimed), then exactly `steps` timed hot-start solves
-        _, _, _ = cpu_hot_start(g, 0.0, min_solves=max(args.warmup, 1), max_solves=max(args.warmup, 1))
-        value, times, cores = cpu_hot_start(g, 0.0, min_solves=args.steps, max_solves=args.steps)
+        stream = Stream(hi)
+        oracle_served(stream, 0, 0.0, max_req=min(3, args.warmup))  # warm-up (untimed)
+        value, times, cores = oracle_served(stream, lo, args.cpu_seconds * 2, max_req=args.steps)
         line = {
-            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": len(times),
             "warmup": args.warmup, "ms_per_step": round(1e3 * float(np.mean(times)), 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
-            "config": {"workload": "grid10k hot-start solves (as the gb300 arm)", "l2": "n/a (host)"},
+            "config": dict(stream.describe(), workload="serving form (as the gb300 arm): the CPU FP64 oracle serves "
+                           "the same request stream in arrival order, one request at a time, each hot-started "
+                           "from the grid's true state, within a time budget"),
             "impl": "reference",
-            "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "%d hot-start solves of grid10k (1%% re-noise each)" % len(times)},
-            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "the first %d timed requests of the stream (%.1f s of CPU solves)"
+                                       % (len(times), sum(times))},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(line))
         return
-    out, g = run_gb300(args, world, rank, local)
+    out, stream = run_gb300(args, world, rank, local)
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:
-            value, times, cores = cpu_hot_start(g, args.cpu_seconds)
-            out["cpu_baseline"] = {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": "port",
-                                   "sample": "%d hot-start solves of grid10k (1%% re-noise each), %.1f s"
-                                             % (len(times), sum(times))}
+            value, times, cores = oracle_served(stream, lo, args.cpu_seconds)
+            out["cpu_baseline"] = {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                                   "sample": "the first %d timed requests of the stream, in arrival order "
+                                             "(%.1f s of CPU solves)" % (len(times), sum(times))}
+        out["roofline"] = out.get("grid10k", {}).get("mixed", {}).get("roofline")
+        if out["roofline"]:
+            out["roofline"] = dict(out["roofline"], workload="grid10k hot start (the factorisation stage)")
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

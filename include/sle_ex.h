@@ -131,6 +131,116 @@ typedef struct SLE_ExStats {
 SLE_API SLE_StatusCode SLE_CALL sle_ExGetStats(SLE_Handle handle, SLE_ExStats* stats);
 SLE_API SLE_StatusCode SLE_CALL sle_ExResetStats(SLE_Handle handle);
 
+/* ---- Batch of independent grids (no counterpart in the reference) --------
+ * One handle holds many grids, solved together: the union of the grids'
+ * symbolic plans is factorised by the same kernels in one pass, and every
+ * grid stops on its own convergence test, so each grid's result and
+ * iteration count are those of solving it alone.  The pattern keeps every
+ * branch, so sle_ExBatchSetBranchStatus changes values only (no new
+ * symbolic analysis).  Grids are added before the first solve; adding a grid
+ * later re-analyses the batch.  Per-grid retries from a flat start (single
+ * grid: wls_solver.cu:326-332) are not performed: a grid that diverges or
+ * meets a non-positive pivot reports that status. */
+typedef struct SLE_ExGridResult {
+    int32_t status;     /* SLE_ConvergenceStatus */
+    int32_t iterations; /* Gauss-Newton steps taken */
+    double max_mismatch;
+    double objective;   /* sum w r^2 at the returned state */
+} SLE_ExGridResult;
+
+/* Append a grid (arrays and index rules of sle_ExLoadNetwork, indices local
+ * to the grid); *grid_id receives its index in the batch. */
+SLE_API SLE_StatusCode SLE_CALL sle_ExBatchAddGrid(SLE_Handle handle, int32_t n_bus, const int32_t* bus_type,
+                                                   const SLE_Real* v_setpoint, int32_t n_branch, const int32_t* from,
+                                                   const int32_t* to, const SLE_Real* r, const SLE_Real* x,
+                                                   const SLE_Real* b, const SLE_Real* tap, const SLE_Real* shift,
+                                                   const int32_t* status, int32_t n_meas, const int32_t* mtype,
+                                                   const int32_t* mloc, const int32_t* mend, const SLE_Real* sigma,
+                                                   const SLE_Real* z, int32_t* grid_id);
+SLE_API int32_t SLE_CALL sle_ExBatchGridCount(SLE_Handle handle);
+/* New telemetry of one grid (count = its measurement count). */
+SLE_API SLE_StatusCode SLE_CALL sle_ExBatchUpdateTelemetry(SLE_Handle handle, int32_t grid, const SLE_Real* values,
+                                                           int32_t count);
+/* Solve grids[0..n) together (the others keep their state); flat_start may
+ * be NULL (hot start from each grid's last state).  results may be NULL. */
+SLE_API SLE_StatusCode SLE_CALL sle_ExBatchSolve(SLE_Handle handle, int32_t n, const int32_t* grids,
+                                                 const uint8_t* flat_start, int32_t max_iterations, double tolerance,
+                                                 int32_t robust, double huber_gamma, SLE_ExGridResult* results);
+/* |V| and theta of one grid (its n_bus values each; either may be NULL). */
+SLE_API SLE_StatusCode SLE_CALL sle_ExBatchGetState(SLE_Handle handle, int32_t grid, SLE_Real* v, SLE_Real* theta);
+/* Breaker edit: open (0) or close (1) branch `branch` of grid `grid`. */
+SLE_API SLE_StatusCode SLE_CALL sle_ExBatchSetBranchStatus(SLE_Handle handle, int32_t grid, int32_t branch,
+                                                           int32_t closed);
+
+/* ---- Serving runtime (no counterpart in the reference) --------------------
+ * A resident fleet of grids answering measurement snapshots and breaker
+ * edits as they arrive.  Small grids share batch units (the sle_ExBatch
+ * machinery), grids of at least own_unit_bus buses get a unit of their own;
+ * each unit has its own stream and worker thread, and solves every grid
+ * with a pending request in one pass, hot-started from the grid's last state
+ * (continuous batching: requests arriving during a pass join the next one).
+ * Units are admitted in order while their device arenas fit the memory
+ * budget; requests for grids of units left out complete at once with
+ * admitted = 0.  Thread-safe: submit / wait may be called from any thread. */
+typedef struct SLE_ExServer SLE_ExServer;
+
+typedef struct SLE_ExServerConfig {
+    int32_t use_double_precision; /* 0: mixed form (default), 1: FP64 */
+    int32_t max_iterations;       /* per request (default 20) */
+    double tolerance;             /* max |dx| (default 1e-6) */
+    int32_t robust;               /* Huber weights */
+    double huber_gamma;
+    int32_t bucket_bus[4];        /* upper bus bounds of the shared units, ascending, 0 = unused */
+    int32_t own_unit_bus;         /* grids at least this large get their own unit */
+    int32_t device_id;
+    size_t memory_budget;         /* bytes; 0 = 90 % of the free device memory at start */
+} SLE_ExServerConfig;
+
+typedef struct SLE_ExServeResult {
+    int32_t status;      /* SLE_ConvergenceStatus */
+    int32_t iterations;
+    double max_mismatch;
+    double objective;
+    int32_t admitted;    /* 0: the grid's unit is outside the memory budget */
+    int32_t batch_size;  /* grids solved in the same pass */
+    int64_t t_submit_ns, t_start_ns, t_done_ns; /* steady clock */
+} SLE_ExServeResult;
+
+typedef struct SLE_ExServerStats {
+    int64_t submitted, completed, rejected, passes, grid_solves;
+    int32_t units, admitted_units, grids, pad;
+    size_t device_bytes, budget_bytes;
+} SLE_ExServerStats;
+
+/* Defaults of SLE_ExServerConfig. */
+SLE_API void SLE_CALL sle_ExServerDefaultConfig(SLE_ExServerConfig* config);
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerCreate(SLE_ExServer** server, const SLE_ExServerConfig* config);
+SLE_API void SLE_CALL sle_ExServerDestroy(SLE_ExServer* server);
+/* Arrays and index rules of sle_ExLoadNetwork; *grid_id is the fleet index. */
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerAddGrid(SLE_ExServer* server, int32_t n_bus, const int32_t* bus_type,
+                                                    const SLE_Real* v_setpoint, int32_t n_branch, const int32_t* from,
+                                                    const int32_t* to, const SLE_Real* r, const SLE_Real* x,
+                                                    const SLE_Real* b, const SLE_Real* tap, const SLE_Real* shift,
+                                                    const int32_t* status, int32_t n_meas, const int32_t* mtype,
+                                                    const int32_t* mloc, const int32_t* mend, const SLE_Real* sigma,
+                                                    const SLE_Real* z, int32_t* grid_id);
+/* Partition, admit, upload, estimate every resident grid once from a flat
+ * start, start the workers. */
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerStart(SLE_ExServer* server);
+/* Queue a snapshot (count = the grid's measurement count, copied before
+ * return); branch >= 0 opens (closed = 0) or closes that branch first. */
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerSubmit(SLE_ExServer* server, int32_t grid, const SLE_Real* values,
+                                                   int32_t count, int32_t branch, int32_t closed, int64_t* ticket);
+/* Wait for a ticket: returns 1 when done (result filled), 0 on timeout
+ * (timeout_ms < 0 waits forever), negative on error.  A ticket is read once. */
+SLE_API int32_t SLE_CALL sle_ExServerWait(SLE_ExServer* server, int64_t ticket, double timeout_ms,
+                                          SLE_ExServeResult* result);
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerGetState(SLE_ExServer* server, int32_t grid, SLE_Real* v,
+                                                     SLE_Real* theta);
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerGetStats(SLE_ExServer* server, SLE_ExServerStats* stats);
+/* Last error of this server (valid until its next call). */
+SLE_API const char* SLE_CALL sle_ExServerLastError(SLE_ExServer* server);
+
 #ifdef __cplusplus
 }
 #endif

@@ -6,7 +6,7 @@ kernels, exported from the in-tree library lib/libsle_gb300.so.  This package
 holds the ctypes bindings (native.py), a Python mirror of the C interface
 (api.py) and the seeded synthetic workloads (workloads.py).
 """
-from .api import Estimator, SLEError  # noqa: F401
+from .api import BatchEstimator, Estimator, Server, SLEError  # noqa: F401
 from .native import NativeLibraryMissing, sle_lib, segen_lib  # noqa: F401
 from .workloads import SyntheticGrid, make  # noqa: F401
 

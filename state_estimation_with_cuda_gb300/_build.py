@@ -29,7 +29,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", "-Wall", "-Wno-unused-function"]
 
 CORE_CU = ["kernels/network.cu", "kernels/factor.cu", "engine/engine.cu"]
-CORE_CPP = ["model/model.cpp", "symbolic/symbolic.cpp", "symbolic/amd.cpp", "api/sle_api.cpp"]
+CORE_CPP = ["model/model.cpp", "symbolic/symbolic.cpp", "symbolic/amd.cpp", "serve/server.cpp", "api/sle_api.cpp"]
 
 
 def _newest(paths):

@@ -261,3 +261,147 @@ class Estimator:
         rows = np.empty(int(off[-1]), np.int32)
         self._check(self.lib.sle_ExGetSymbolic(self.h, None, None, None, None, None, _ip(rows)))
         return dict(bus_perm=bus_perm, state_of_ps=sop, sn_c0=c0, sn_parent=par, sn_rows_off=off, sn_rows=rows)
+
+
+class BatchEstimator(Estimator):
+    """Many independent grids on one handle, solved together
+    (sle_ExBatch*; no reference counterpart).  Grid i's result and iteration
+    count equal those of solving grid i alone."""
+
+    def __init__(self, config=None, mixed=True):
+        super().__init__(config)
+        if mixed:
+            self.set_option("use_double_precision", 0)
+        self._grid_arrays = []
+        self.sizes = []
+
+    def add_grid(self, grid, z=None):
+        a = [np.ascontiguousarray(x) for x in (
+            grid.bus_type.astype(np.int32), grid.v_setpoint.astype(np.float64), grid.br_from.astype(np.int32),
+            grid.br_to.astype(np.int32), grid.br_r, grid.br_x, grid.br_b, grid.br_tap, grid.br_shift,
+            grid.br_status.astype(np.int32), grid.m_type.astype(np.int32), grid.m_loc.astype(np.int32),
+            grid.m_end.astype(np.int32), grid.m_sigma, np.asarray(grid.z if z is None else z, np.float64))]
+        gid = ctypes.c_int32()
+        self._check(self.lib.sle_ExBatchAddGrid(self.h, grid.n_bus, _ip(a[0]), _dp(a[1]), grid.n_branch, _ip(a[2]),
+                                                _ip(a[3]), _dp(a[4]), _dp(a[5]), _dp(a[6]), _dp(a[7]), _dp(a[8]),
+                                                _ip(a[9]), grid.n_meas, _ip(a[10]), _ip(a[11]), _ip(a[12]),
+                                                _dp(a[13]), _dp(a[14]), ctypes.byref(gid)))
+        self.sizes.append((grid.n_bus, grid.n_meas))
+        return gid.value
+
+    def grid_count(self):
+        return self.lib.sle_ExBatchGridCount(self.h)
+
+    def set_telemetry(self, gid, z):
+        z = np.ascontiguousarray(z, np.float64)
+        self._check(self.lib.sle_ExBatchUpdateTelemetry(self.h, int(gid), _dp(z), len(z)))
+
+    def solve(self, grids=None, flat_start=False, max_iterations=20, tolerance=1e-6, robust=False, huber_gamma=1.5):
+        """Solve the listed grids (default: all); returns SLE_ExGridResult[n]."""
+        ids = np.arange(self.grid_count(), dtype=np.int32) if grids is None else np.ascontiguousarray(grids, np.int32)
+        flat = np.full(len(ids), 1 if flat_start is True else 0, np.uint8) if isinstance(flat_start, bool) \
+            else np.ascontiguousarray(flat_start, np.uint8)
+        res = (N.SLE_ExGridResult * max(len(ids), 1))()
+        self._check(self.lib.sle_ExBatchSolve(self.h, len(ids), _ip(ids),
+                                              flat.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                              int(max_iterations), float(tolerance), int(bool(robust)),
+                                              float(huber_gamma), res))
+        return list(res)[:len(ids)]
+
+    def state(self, gid):
+        n = self.sizes[gid][0]
+        v = np.empty(n, np.float64)
+        t = np.empty(n, np.float64)
+        self._check(self.lib.sle_ExBatchGetState(self.h, int(gid), _dp(v), _dp(t)))
+        return v, t
+
+    def set_branch_status(self, gid, branch, closed):
+        self._check(self.lib.sle_ExBatchSetBranchStatus(self.h, int(gid), int(branch), int(bool(closed))))
+
+
+def _grid_arrays(grid, z=None):
+    return [np.ascontiguousarray(x) for x in (
+        grid.bus_type.astype(np.int32), grid.v_setpoint.astype(np.float64), grid.br_from.astype(np.int32),
+        grid.br_to.astype(np.int32), grid.br_r, grid.br_x, grid.br_b, grid.br_tap, grid.br_shift,
+        grid.br_status.astype(np.int32), grid.m_type.astype(np.int32), grid.m_loc.astype(np.int32),
+        grid.m_end.astype(np.int32), grid.m_sigma, np.asarray(grid.z if z is None else z, np.float64))]
+
+
+class Server:
+    """Serving runtime (sle_ExServer*; no reference counterpart): a resident
+    fleet answering snapshots as they arrive, with continuous batching."""
+
+    def __init__(self, mixed=True, max_iterations=20, tolerance=1e-6, bucket_bus=(300, 2000, 20000, 0),
+                 own_unit_bus=1 << 30, memory_budget=0, robust=False, huber_gamma=1.5, device_id=0):
+        self.lib = N.sle_lib()
+        c = N.SLE_ExServerConfig()
+        self.lib.sle_ExServerDefaultConfig(ctypes.byref(c))
+        c.use_double_precision = 0 if mixed else 1
+        c.max_iterations = int(max_iterations)
+        c.tolerance = float(tolerance)
+        c.robust = int(bool(robust))
+        c.huber_gamma = float(huber_gamma)
+        for i in range(4):
+            c.bucket_bus[i] = int(bucket_bus[i]) if i < len(bucket_bus) else 0
+        c.own_unit_bus = int(own_unit_bus)
+        c.memory_budget = int(memory_budget)
+        c.device_id = int(device_id)
+        self.s = ctypes.c_void_p()
+        self._check(self.lib.sle_ExServerCreate(ctypes.byref(self.s), ctypes.byref(c)))
+        self.sizes = []
+
+    def _check(self, rc):
+        if rc != OK:
+            err = self.lib.sle_ExServerLastError(self.s) if self.s else None
+            raise SLEError(rc, err.decode() if err else "error")
+        return rc
+
+    def add_grid(self, grid, z=None):
+        a = _grid_arrays(grid, z)
+        gid = ctypes.c_int32()
+        self._check(self.lib.sle_ExServerAddGrid(self.s, grid.n_bus, _ip(a[0]), _dp(a[1]), grid.n_branch, _ip(a[2]),
+                                                 _ip(a[3]), _dp(a[4]), _dp(a[5]), _dp(a[6]), _dp(a[7]), _dp(a[8]),
+                                                 _ip(a[9]), grid.n_meas, _ip(a[10]), _ip(a[11]), _ip(a[12]),
+                                                 _dp(a[13]), _dp(a[14]), ctypes.byref(gid)))
+        self.sizes.append((grid.n_bus, grid.n_meas))
+        return gid.value
+
+    def start(self):
+        self._check(self.lib.sle_ExServerStart(self.s))
+
+    def submit(self, gid, z, branch=-1, closed=1):
+        z = np.ascontiguousarray(z, np.float64)
+        t = ctypes.c_int64()
+        self._check(self.lib.sle_ExServerSubmit(self.s, int(gid), _dp(z), len(z), int(branch), int(closed),
+                                                ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket, timeout_ms=-1.0):
+        r = N.SLE_ExServeResult()
+        rc = self.lib.sle_ExServerWait(self.s, int(ticket), float(timeout_ms), ctypes.byref(r))
+        if rc < 0:
+            self._check(rc)
+        return r if rc == 1 else None
+
+    def state(self, gid):
+        n = self.sizes[gid][0]
+        v = np.empty(n, np.float64)
+        t = np.empty(n, np.float64)
+        self._check(self.lib.sle_ExServerGetState(self.s, int(gid), _dp(v), _dp(t)))
+        return v, t
+
+    def stats(self):
+        st = N.SLE_ExServerStats()
+        self._check(self.lib.sle_ExServerGetStats(self.s, ctypes.byref(st)))
+        return st
+
+    def close(self):
+        if self.s:
+            self.lib.sle_ExServerDestroy(self.s)
+            self.s = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -15,6 +15,7 @@
 #include <string>
 
 #include "../engine/engine.h"
+#include "../serve/server.h"
 
 using sle_gb300::Engine;
 using sle_gb300::EngineConfig;
@@ -938,6 +939,196 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
     E(handle)->model.load_soa(n_bus, bus_type, v_setpoint, n_branch, from, to, r, x, b, tap, shift, status, n_meas,
                               mtype, mloc, mend, sigma, z);
     return SLE_OK;
+}
+
+// ---- serving runtime ----------------------------------------------------------
+struct SLE_ExServer {
+    sle_gb300::Server srv;
+    std::string err;
+    explicit SLE_ExServer(const sle_gb300::ServeConfig& c) : srv(c) {}
+};
+
+static SLE_StatusCode server_rc(SLE_ExServer* s, int32_t rc) {
+    if (rc == 0) return SLE_OK;
+    s->err = s->srv.last_error;
+    if (rc == -4) return fail(SLE_ERROR_INVALID_ARGUMENT, s->err);
+    if (rc == -11) return fail(SLE_ERROR_ELEMENT_NOT_FOUND, s->err);
+    if (rc == -5) return fail(SLE_ERROR_MODEL_INCOMPLETE, s->err);
+    if (rc == -10) return fail(SLE_ERROR_OUT_OF_MEMORY, s->err);
+    return fail(SLE_ERROR_CUDA_FAILURE, s->err);
+}
+
+SLE_API void SLE_CALL sle_ExServerDefaultConfig(SLE_ExServerConfig* c) {
+    if (!c) return;
+    const sle_gb300::ServeConfig d;
+    c->use_double_precision = d.use_double_precision;
+    c->max_iterations = d.max_iterations;
+    c->tolerance = d.tolerance;
+    c->robust = d.robust;
+    c->huber_gamma = d.huber_gamma;
+    for (int i = 0; i < 4; ++i) c->bucket_bus[i] = d.bucket_bus[i];
+    c->own_unit_bus = d.own_unit_bus;
+    c->device_id = d.device_id;
+    c->memory_budget = d.memory_budget;
+}
+
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerCreate(SLE_ExServer** out, const SLE_ExServerConfig* c) {
+    if (!out) return SLE_ERROR_INVALID_ARGUMENT;
+    sle_gb300::ServeConfig sc;
+    if (c) {
+        sc.use_double_precision = c->use_double_precision;
+        sc.max_iterations = c->max_iterations > 0 ? c->max_iterations : sc.max_iterations;
+        sc.tolerance = c->tolerance > 0.0 ? c->tolerance : sc.tolerance;
+        sc.robust = c->robust;
+        sc.huber_gamma = c->huber_gamma > 0.0 ? c->huber_gamma : sc.huber_gamma;
+        for (int i = 0; i < 4; ++i) sc.bucket_bus[i] = c->bucket_bus[i];
+        sc.own_unit_bus = c->own_unit_bus > 0 ? c->own_unit_bus : sc.own_unit_bus;
+        sc.device_id = c->device_id;
+        sc.memory_budget = c->memory_budget;
+    }
+    *out = new SLE_ExServer(sc);
+    return SLE_OK;
+}
+
+SLE_API void SLE_CALL sle_ExServerDestroy(SLE_ExServer* s) { delete s; }
+
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerAddGrid(SLE_ExServer* s, int32_t n_bus, const int32_t* bus_type,
+                                                    const SLE_Real* v_setpoint, int32_t n_branch, const int32_t* from,
+                                                    const int32_t* to, const SLE_Real* r, const SLE_Real* x,
+                                                    const SLE_Real* b, const SLE_Real* tap, const SLE_Real* shift,
+                                                    const int32_t* status, int32_t n_meas, const int32_t* mtype,
+                                                    const int32_t* mloc, const int32_t* mend, const SLE_Real* sigma,
+                                                    const SLE_Real* z, int32_t* grid_id) {
+    if (!s) return SLE_ERROR_INVALID_HANDLE;
+    return server_rc(s, s->srv.add_grid(n_bus, bus_type, v_setpoint, n_branch, from, to, r, x, b, tap, shift, status,
+                                        n_meas, mtype, mloc, mend, sigma, z, grid_id));
+}
+
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerStart(SLE_ExServer* s) {
+    if (!s) return SLE_ERROR_INVALID_HANDLE;
+    return server_rc(s, s->srv.start());
+}
+
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerSubmit(SLE_ExServer* s, int32_t grid, const SLE_Real* values, int32_t count,
+                                                   int32_t branch, int32_t closed, int64_t* ticket) {
+    if (!s) return SLE_ERROR_INVALID_HANDLE;
+    return server_rc(s, s->srv.submit(grid, values, count, branch, closed, ticket));
+}
+
+SLE_API int32_t SLE_CALL sle_ExServerWait(SLE_ExServer* s, int64_t ticket, double timeout_ms, SLE_ExServeResult* res) {
+    if (!s) return SLE_ERROR_INVALID_HANDLE;
+    sle_gb300::ServeResult r;
+    const int32_t done = s->srv.wait(ticket, timeout_ms, &r);
+    if (done == 1 && res) {
+        res->status = r.status;
+        res->iterations = r.iterations;
+        res->max_mismatch = r.max_mismatch;
+        res->objective = r.objective;
+        res->admitted = r.admitted;
+        res->batch_size = r.batch_size;
+        res->t_submit_ns = r.t_submit_ns;
+        res->t_start_ns = r.t_start_ns;
+        res->t_done_ns = r.t_done_ns;
+    }
+    return done;
+}
+
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerGetState(SLE_ExServer* s, int32_t grid, SLE_Real* v, SLE_Real* theta) {
+    if (!s) return SLE_ERROR_INVALID_HANDLE;
+    return server_rc(s, s->srv.get_state(grid, v, theta));
+}
+
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerGetStats(SLE_ExServer* s, SLE_ExServerStats* out) {
+    if (!s || !out) return SLE_ERROR_INVALID_ARGUMENT;
+    const sle_gb300::ServeStats st = s->srv.stats();
+    out->submitted = st.submitted;
+    out->completed = st.completed;
+    out->rejected = st.rejected;
+    out->passes = st.passes;
+    out->grid_solves = st.grid_solves;
+    out->units = st.units;
+    out->admitted_units = st.admitted_units;
+    out->grids = st.grids;
+    out->pad = 0;
+    out->device_bytes = st.device_bytes;
+    out->budget_bytes = st.budget_bytes;
+    return SLE_OK;
+}
+
+SLE_API const char* SLE_CALL sle_ExServerLastError(SLE_ExServer* s) {
+    if (!s) return "invalid server";
+    s->err = s->srv.last_error;
+    return s->err.c_str();
+}
+
+static SLE_StatusCode batch_rc(SLE_Handle handle, int32_t rc) {
+    if (rc == 0) return SLE_OK;
+    const std::string& msg = E(handle)->last_error;
+    if (rc == -4) return fail(SLE_ERROR_INVALID_ARGUMENT, msg);
+    if (rc == -11) return fail(SLE_ERROR_ELEMENT_NOT_FOUND, msg);
+    if (rc == -5) return fail(SLE_ERROR_MODEL_INCOMPLETE, msg);
+    return fail(SLE_ERROR_CUDA_FAILURE, msg);
+}
+
+SLE_API SLE_StatusCode SLE_CALL sle_ExBatchAddGrid(SLE_Handle handle, int32_t n_bus, const int32_t* bus_type,
+                                                   const SLE_Real* v_setpoint, int32_t n_branch, const int32_t* from,
+                                                   const int32_t* to, const SLE_Real* r, const SLE_Real* x,
+                                                   const SLE_Real* b, const SLE_Real* tap, const SLE_Real* shift,
+                                                   const int32_t* status, int32_t n_meas, const int32_t* mtype,
+                                                   const int32_t* mloc, const int32_t* mend, const SLE_Real* sigma,
+                                                   const SLE_Real* z, int32_t* grid_id) {
+    if (!handle) return SLE_ERROR_INVALID_HANDLE;
+    if (bus_type)
+        for (int32_t i = 0; i < n_bus; ++i)
+            if (bus_type[i] < 0 || bus_type[i] > 2) return fail(SLE_ERROR_INVALID_ARGUMENT, "invalid bus type");
+    return batch_rc(handle, E(handle)->batch_add_grid(n_bus, bus_type, v_setpoint, n_branch, from, to, r, x, b, tap,
+                                                      shift, status, n_meas, mtype, mloc, mend, sigma, z, grid_id));
+}
+
+SLE_API int32_t SLE_CALL sle_ExBatchGridCount(SLE_Handle handle) {
+    return handle ? static_cast<int32_t>(E(handle)->grids().size()) : 0;
+}
+
+SLE_API SLE_StatusCode SLE_CALL sle_ExBatchUpdateTelemetry(SLE_Handle handle, int32_t grid, const SLE_Real* values,
+                                                           int32_t count) {
+    if (!handle) return SLE_ERROR_INVALID_HANDLE;
+    return batch_rc(handle, E(handle)->batch_set_telemetry(grid, values, count));
+}
+
+SLE_API SLE_StatusCode SLE_CALL sle_ExBatchSolve(SLE_Handle handle, int32_t n, const int32_t* grids,
+                                                 const uint8_t* flat_start, int32_t max_iterations, double tolerance,
+                                                 int32_t robust, double huber_gamma, SLE_ExGridResult* results) {
+    if (!handle) return SLE_ERROR_INVALID_HANDLE;
+    if (n < 0 || (n > 0 && !grids) || max_iterations < 1 || !(tolerance > 0.0))
+        return fail(SLE_ERROR_INVALID_ARGUMENT, "invalid batch solve arguments");
+    sle_gb300::SolveRequest rq;
+    rq.mode = sle_gb300::Mode::PRECISION;
+    rq.max_iterations = max_iterations;
+    rq.tolerance = tolerance;
+    rq.robust = robust;
+    rq.huber_gamma = huber_gamma;
+    std::vector<sle_gb300::Engine::GridResult> out(static_cast<size_t>(n));
+    const int32_t rc = E(handle)->batch_solve(n, grids, flat_start, rq, out.data());
+    if (rc) return batch_rc(handle, rc);
+    if (results)
+        for (int32_t i = 0; i < n; ++i) {
+            results[i].status = out[i].status;
+            results[i].iterations = out[i].iterations;
+            results[i].max_mismatch = out[i].max_mismatch;
+            results[i].objective = out[i].objective;
+        }
+    return SLE_OK;
+}
+
+SLE_API SLE_StatusCode SLE_CALL sle_ExBatchGetState(SLE_Handle handle, int32_t grid, SLE_Real* v, SLE_Real* theta) {
+    if (!handle) return SLE_ERROR_INVALID_HANDLE;
+    return batch_rc(handle, E(handle)->batch_get_state(grid, v, theta));
+}
+
+SLE_API SLE_StatusCode SLE_CALL sle_ExBatchSetBranchStatus(SLE_Handle handle, int32_t grid, int32_t branch,
+                                                           int32_t closed) {
+    if (!handle) return SLE_ERROR_INVALID_HANDLE;
+    return batch_rc(handle, E(handle)->batch_set_branch_status(grid, branch, closed));
 }
 
 SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* key, double value) {

@@ -1,5 +1,8 @@
 #include "engine.h"
 
+#include <atomic>
+#include <thread>
+
 #include <algorithm>
 #include <cstring>
 
@@ -41,6 +44,8 @@ Engine::~Engine() {
     if (ev1_) cudaEventDestroy(ev1_);
     if (h_status_) cudaFreeHost(h_status_);
     if (h_stage_) cudaFreeHost(h_stage_);
+    if (h_batch_in_) cudaFreeHost(h_batch_in_);
+    if (h_batch_out_) cudaFreeHost(h_batch_out_);
     if (d_slots_) cudaFree(d_slots_);
     if (d_scratch_) cudaFree(d_scratch_);
     if (tm0_) cudaEventDestroy(tm0_);
@@ -96,6 +101,7 @@ int32_t Engine::initialize() {
 }
 
 int32_t Engine::analyze() {
+    if (batch_mode()) return analyze_batch();
     std::string err;
     if (!model.validate(err)) {
         last_error = err;
@@ -151,6 +157,7 @@ void Engine::build_schedule() {
     sch_flow_a_.clear();
     sch_flow_b_.clear();
     sch_down_.clear();
+    sch_up_.clear();
     flow_a_maxf_ = flow_b_maxf_ = 0;
     lay_lx_off_.assign(ns + 1, 0);
     lay_u_off_.assign(ns + 1, 0);
@@ -216,10 +223,8 @@ void Engine::build_schedule() {
             if (big[s]) {
                 bigs.push_back(s);
             } else if (flow_phase_[s] == 1) {
-                sch_flow_a_.push_back(s);
                 flow_a_maxf_ = std::max(flow_a_maxf_, P.sn_f[s]);
             } else if (flow_phase_[s] == 2) {
-                sch_flow_b_.push_back(s);
                 flow_b_maxf_ = std::max(flow_b_maxf_, P.sn_f[s]);
             } else {
                 sch_small_.push_back(s);
@@ -258,6 +263,29 @@ void Engine::build_schedule() {
     }
     // every front, top-down, for the backward dataflow sweep
     sch_down_.assign(sch_all_.rbegin(), sch_all_.rend());
+    // continuation sweeps: children counts and initially ready fronts, the
+    // ones with the most factor work on their path to the root first
+    phase_nchild_.assign(ns, 0);
+    nchild_.assign(ns, 0);
+    std::vector<double> up_cost(ns, 0.0);
+    for (int32_t s = ns - 1; s >= 0; --s) {  // parents follow their children
+        const int32_t p = P.sn_parent[s];
+        const double f = P.sn_f[s], nc = P.sn_c0[s + 1] - P.sn_c0[s];
+        up_cost[s] = f * f * nc + (p >= 0 ? up_cost[p] : 0.0);
+        if (p >= 0) {
+            ++nchild_[p];
+            if (flow_phase_[p] != 0 && flow_phase_[p] == flow_phase_[s]) ++phase_nchild_[p];
+        }
+    }
+    for (int32_t s = 0; s < ns; ++s) {
+        if (flow_phase_[s] == 1 && phase_nchild_[s] == 0) sch_flow_a_.push_back(s);
+        if (flow_phase_[s] == 2 && phase_nchild_[s] == 0) sch_flow_b_.push_back(s);
+        if (nchild_[s] == 0) sch_up_.push_back(s);
+    }
+    auto by_cost = [&](int32_t a, int32_t b) { return up_cost[a] > up_cost[b] || (up_cost[a] == up_cost[b] && a < b); };
+    std::sort(sch_flow_a_.begin(), sch_flow_a_.end(), by_cost);
+    std::sort(sch_flow_b_.begin(), sch_flow_b_.end(), by_cost);
+    std::sort(sch_up_.begin(), sch_up_.end(), by_cost);
 }
 
 int32_t Engine::upload() {
@@ -266,7 +294,8 @@ int32_t Engine::upload() {
     cudaSetDevice(cfg.device_id);
     // keep the hot-start state across re-uploads
     if (uploaded_) download_results();
-    rc = analyze();
+    if (!(reuse_analysis_once && analyzed_)) rc = analyze();
+    reuse_analysis_once = false;
     if (rc) return rc;
     const int32_t n = model.n_bus(), nbr = model.n_branch(), m = model.n_meas();
     const Plan& P = plan_;
@@ -340,6 +369,26 @@ int32_t Engine::upload() {
         fac_.bus_ps_v = c.take<int32_t>(n);
         fac_.sn_u_ld = c.take<int32_t>(ns);
         fac_.sn_u_big = c.take<uint8_t>(ns);
+        fac_.sn_grid = batch_mode() ? c.take<int32_t>(ns) : nullptr;
+        fac_.tgt_grid = batch_mode() ? c.take<int32_t>(P.tgt_local.size()) : nullptr;
+        fac_.ps_grid = batch_mode() ? c.take<int32_t>(P.n_state) : nullptr;
+        net_.meas_grid = batch_mode() ? c.take<int32_t>(m) : nullptr;
+        if (batch_mode()) {
+            const int32_t G = static_cast<int32_t>(grids_.size());
+            batch_.n_grids = G;
+            batch_.bus_off = c.take<int32_t>(G + 1);
+            batch_.meas_off = c.take<int32_t>(G + 1);
+            batch_.flags = c.take<uint32_t>(G);
+            batch_.iters = c.take<int32_t>(G);
+            batch_.mismatch = c.take<double>(G);
+            batch_.objective = c.take<double>(G);
+            uint8_t* af = c.take<uint8_t>(2 * static_cast<size_t>(G));  // active, then flat
+            batch_.active = af;
+            batch_.flat = af + G;
+            batch_.running = c.take<int32_t>(1);
+        } else {
+            batch_ = DevBatch{};
+        }
         d_small_ = c.take<int32_t>(sch_small_.size());
         d_all_ = c.take<int32_t>(sch_all_.size());
         d_asm_ = c.take<int4>(sch_asm_.size());
@@ -349,6 +398,10 @@ int32_t Engine::upload() {
         d_flow_a_ = c.take<int32_t>(sch_flow_a_.size());
         d_flow_b_ = c.take<int32_t>(sch_flow_b_.size());
         d_down_ = c.take<int32_t>(sch_down_.size());
+        d_up_ = c.take<int32_t>(sch_up_.size());
+        d_phase_ = c.take<int8_t>(ns);
+        d_phase_nchild_ = c.take<int32_t>(ns);
+        d_nchild_ = c.take<int32_t>(ns);
         // work
         work_.v = c.take<double>(n);
         work_.th = c.take<double>(n);
@@ -382,11 +435,20 @@ int32_t Engine::upload() {
         work_.pt = c.take<double>(nbr);
         work_.qt = c.take<double>(nbr);
         work_.part = c.take<double>(nparts);
+        work_.opart = c.take<double>(nparts);
+        work_.oidx = c.take<int32_t>(nparts);
+        work_.ocnt = c.take<int32_t>(nparts);
         work_.status = c.take<DevStatus>(1);
+        work_.grid_flags = batch_mode() ? batch_.flags : nullptr;
     };
     Carver dry(nullptr);
     layout(dry);
     const size_t need = dry.off + 256;
+    if (budget_bytes && need > budget_bytes) {
+        last_error = "device arena of " + std::to_string(need) + " bytes exceeds the admission budget of " +
+                     std::to_string(budget_bytes) + " bytes";
+        return -10;
+    }
     cudaError_t e = cudaStreamSynchronize(st_);
     if (e != cudaSuccess) return set_cuda_error(e, "stream sync");
     release_device();
@@ -458,6 +520,42 @@ int32_t Engine::upload() {
     chk(put(const_cast<int32_t*>(fac_.bus_ps_v), P.bus_ps_v, st_));
     chk(put(const_cast<int32_t*>(fac_.sn_u_ld), lay_u_ld_, st_));
     chk(put(const_cast<uint8_t*>(fac_.sn_u_big), lay_u_big_, st_));
+    if (batch_mode()) {
+        const int32_t G = static_cast<int32_t>(grids_.size());
+        std::vector<int32_t> sg, boff(G + 1, 0), moff(G + 1, 0);
+        sg.reserve(ns);
+        for (int32_t g = 0; g < G; ++g) {
+            sg.insert(sg.end(), grid_plans_[g].n_super, g);
+            boff[g + 1] = grids_[g].bus0 + grids_[g].nbus;
+            moff[g + 1] = grids_[g].m0 + grids_[g].nm;
+        }
+        chk(put(const_cast<int32_t*>(fac_.sn_grid), sg, st_));
+        {
+            std::vector<int32_t> tg(P.tgt_local.size()), pg(P.n_state), mg(m);
+            for (int32_t sn = 0; sn < ns; ++sn)
+                for (int32_t x = P.sn_tgt_ptr[sn]; x < P.sn_tgt_ptr[sn + 1]; ++x) tg[x] = sg[sn];
+            for (int32_t sn = 0; sn < ns; ++sn)
+                for (int32_t p = P.sn_c0[sn]; p < P.sn_c0[sn + 1]; ++p) pg[p] = sg[sn];
+            for (int32_t g = 0; g < G; ++g)
+                for (int32_t q = moff[g]; q < moff[g + 1]; ++q) mg[q] = g;
+            chk(put(const_cast<int32_t*>(fac_.tgt_grid), tg, st_));
+            chk(put(const_cast<int32_t*>(fac_.ps_grid), pg, st_));
+            chk(put(const_cast<int32_t*>(net_.meas_grid), mg, st_));
+        }
+        chk(put(const_cast<int32_t*>(batch_.bus_off), boff, st_));
+        chk(put(const_cast<int32_t*>(batch_.meas_off), moff, st_));
+        const size_t out_bytes = static_cast<size_t>(G) * (4 + 4 + 8 + 8) + 8;
+        if (h_batch_cap_ < static_cast<size_t>(G)) {
+            if (h_batch_in_) cudaFreeHost(h_batch_in_);
+            if (h_batch_out_) cudaFreeHost(h_batch_out_);
+            h_batch_in_ = nullptr;
+            h_batch_out_ = nullptr;
+            h_batch_cap_ = 0;
+            chk(cudaMallocHost(reinterpret_cast<void**>(&h_batch_in_), 2 * static_cast<size_t>(G)));
+            chk(cudaMallocHost(&h_batch_out_, out_bytes));
+            if (e == cudaSuccess) h_batch_cap_ = G;
+        }
+    }
     chk(put(d_small_, sch_small_, st_));
     chk(put(d_all_, sch_all_, st_));
     chk(put(d_asm_, sch_asm_, st_));
@@ -467,6 +565,13 @@ int32_t Engine::upload() {
     chk(put(d_flow_a_, sch_flow_a_, st_));
     chk(put(d_flow_b_, sch_flow_b_, st_));
     chk(put(d_down_, sch_down_, st_));
+    chk(put(d_up_, sch_up_, st_));
+    {
+        std::vector<int8_t> ph(flow_phase_.begin(), flow_phase_.end());
+        chk(put(d_phase_, ph, st_));
+    }
+    chk(put(d_phase_nchild_, phase_nchild_, st_));
+    chk(put(d_nchild_, nchild_, st_));
     chk(put(work_.v, model.bus_v, st_));
     chk(put(work_.th, model.bus_th, st_));
     chk(put(work_.z, model.m_value, st_));
@@ -506,11 +611,16 @@ int32_t Engine::upload() {
         sched_.flow_b_n = static_cast<int32_t>(sch_flow_b_.size());
         sched_.flow_b_maxf = flow_b_maxf_;
         sched_.flow_b_grid = std::max(1, std::min(g.b, sched_.flow_b_n));
+        sched_.d_phase = d_phase_;
+        sched_.d_phase_nchild = d_phase_nchild_;
         sched_.solve_flow = (cfg.dataflow && g.solve > 0) ? 1 : 0;
-        sched_.d_up = d_all_;
+        sched_.d_up = d_up_;
+        sched_.up_n = static_cast<int32_t>(sch_up_.size());
+        sched_.d_nchild = d_nchild_;
         sched_.d_down = d_down_;
         sched_.solve_maxf = ms;
         sched_.solve_grid = std::max(1, std::min(g.solve, ns));
+        sched_.up_grid = std::max(1, std::min(g.solve, sched_.up_n));
     }
 
     if (h_stage_n_ < static_cast<size_t>(m)) {
@@ -586,6 +696,7 @@ SolveParams Engine::params(const SolveRequest& rq) const {
     sp.tol = rq.tolerance;
     sp.vmin = cfg.voltage_min_pu;
     sp.vmax = cfg.voltage_max_pu;
+    sp.skip_flags = FLAG_FROZEN;
     return sp;
 }
 
@@ -621,6 +732,11 @@ void Engine::collect_stage_times() {
 
 int32_t Engine::enqueue_iteration(const SolveParams& sp, bool refactor, int64_t* per_stage) {
     cudaError_t e = cudaMemsetAsync(&work_.status->flags, 0, sizeof(uint32_t), st_);
+    if (e == cudaSuccess && batch_mode()) e = cudaMemsetAsync(batch_.running, 0, sizeof(int32_t), st_);
+    auto update = [&](const double* step) {
+        return batch_mode() ? launch_batch_update(net_, fac_, work_, batch_, sp, step, st_)
+                            : launch_update(net_, fac_, work_, sp, step, st_);
+    };
     auto stage = [&](int32_t st, auto&& fn) {
         if (e != cudaSuccess) return;
         const int64_t l0 = g_kernel_launches.load();
@@ -634,7 +750,7 @@ int32_t Engine::enqueue_iteration(const SolveParams& sp, bool refactor, int64_t*
         if (refactor) stage(ST_FACTOR, [&] { return launch_factor(net_, fac_, work_, sched_, st_); });
         stage(ST_RHS, [&] { return launch_rhs(net_, fac_, work_, st_); });
         stage(ST_SOLVE, [&] { return launch_solve(fac_, work_, sched_, st_); });
-        stage(ST_UPDATE, [&] { return launch_update(net_, fac_, work_, sp, work_.sol, st_); });
+        stage(ST_UPDATE, [&] { return update(work_.sol); });
     } else {
         if (refactor) stage(ST_FACTOR, [&] { return launch_factor32(net_, fac_, work_, sched_, st_); });
         stage(ST_RHS, [&] { return launch_rhs(net_, fac_, work_, st_); });
@@ -649,9 +765,14 @@ int32_t Engine::enqueue_iteration(const SolveParams& sp, bool refactor, int64_t*
             }
             return ee;
         });
-        stage(ST_UPDATE, [&] { return launch_update(net_, fac_, work_, sp, work_.dx, st_); });
+        stage(ST_UPDATE, [&] { return update(work_.dx); });
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_status_, work_.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess && batch_mode()) {
+        const int32_t G = batch_.n_grids;
+        int32_t* h_running = reinterpret_cast<int32_t*>(static_cast<char*>(h_batch_out_) + static_cast<size_t>(G) * 24);
+        e = cudaMemcpyAsync(h_running, batch_.running, sizeof(int32_t), cudaMemcpyDeviceToHost, st_);
+    }
     if (e != cudaSuccess) {
         set_cuda_error(e, "iteration");
         return -3;
@@ -719,6 +840,11 @@ int32_t Engine::run_iteration(const SolveParams& sp, bool refactor) {
 
 int32_t Engine::solve(const SolveRequest& rq, SolveResult& out) {
     out = SolveResult();
+    if (batch_mode()) {
+        last_error = "a batch handle is solved with batch_solve";
+        out.status = CONV_NOTOBS;
+        return -4;
+    }
     if (!init_ || !uploaded_ || model.structure_dirty) {
         const int32_t rc = upload();
         if (rc) {
@@ -933,6 +1059,10 @@ int32_t Engine::factor_and_solve(const double* rhs_orig, double* x_orig) {
 }
 
 int32_t Engine::factor_and_solve_noalloc(const double* rhs_orig, double* x_orig) {
+    if (batch_mode()) {
+        last_error = "not available on a batch handle";
+        return -4;
+    }
     if (!uploaded_) {
         last_error = "no model on the device (upload and evaluate first)";
         return -4;
@@ -1073,6 +1203,262 @@ int32_t Engine::timer(int32_t op, double* ms) {
     if (e == cudaSuccess) e = cudaEventElapsedTime(&f, tm0_, tm1_);
     if (e != cudaSuccess) return set_cuda_error(e, "timer");
     if (ms) *ms = f;
+    return 0;
+}
+
+
+// ---------------------------------------------------------------------------
+// Batch of independent grids
+// ---------------------------------------------------------------------------
+int32_t Engine::batch_add_grid(int32_t nb, const int32_t* btype, const double* vset, int32_t nbr, const int32_t* from,
+                               const int32_t* to, const double* r, const double* x, const double* b,
+                               const double* tap, const double* shift, const int32_t* status, int32_t nm,
+                               const int32_t* mtype, const int32_t* mloc, const int32_t* mend, const double* sigma,
+                               const double* z, int32_t* id) {
+    if (nb <= 0 || nbr < 0 || nm < 0 || !btype || !vset || (nbr > 0 && (!from || !to || !r || !x || !b || !tap || !shift)) ||
+        (nm > 0 && (!mtype || !mloc || !mend || !sigma || !z))) {
+        last_error = "invalid grid arrays";
+        return -4;
+    }
+    if (!batch_mode() && model.n_bus() > 0) {
+        last_error = "the handle already holds a single-grid model";
+        return -4;
+    }
+    int32_t slack = -1;
+    for (int32_t i = 0; i < nb; ++i)
+        if (btype[i] == 2) slack = i;  // the last SLACK, as for one grid
+    if (slack < 0) {
+        last_error = "grid has no slack bus";
+        return -4;
+    }
+    for (int32_t k = 0; k < nbr; ++k)
+        if (from[k] < 0 || from[k] >= nb || to[k] < 0 || to[k] >= nb) {
+            last_error = "branch references an unknown bus";
+            return -11;
+        }
+    for (int32_t q = 0; q < nm; ++q) {
+        const int32_t ty = mtype[q];
+        const bool on_branch = (ty == 4 || ty == 5 || ty == 6);
+        if (ty < 0 || ty > 8 || mloc[q] < 0 || mloc[q] >= (on_branch ? nbr : nb)) {
+            last_error = "measurement references an unknown element";
+            return -11;
+        }
+    }
+    GridSpan sp{model.n_bus(), nb, model.n_branch(), nbr, model.n_meas(), nm, model.n_bus() + slack};
+    model.append_soa(nb, btype, vset, nbr, from, to, r, x, b, tap, shift, status, nm, mtype, mloc, mend, sigma, z);
+    grids_.push_back(sp);
+    analyzed_ = false;
+    if (id) *id = static_cast<int32_t>(grids_.size()) - 1;
+    return 0;
+}
+
+int32_t Engine::analyze_batch() {
+    const int32_t G = static_cast<int32_t>(grids_.size());
+    grid_plans_.assign(G, Plan());
+    std::vector<std::string> errs(G);
+    std::atomic<int32_t> next{0};
+    auto work = [&]() {
+        for (int32_t g = next++; g < G; g = next++) {
+            const GridSpan& S = grids_[g];
+            std::vector<int32_t> from(S.nbr), to(S.nbr), loc(S.nm);
+            for (int32_t k = 0; k < S.nbr; ++k) {
+                from[k] = model.br_from[S.br0 + k] - S.bus0;
+                to[k] = model.br_to[S.br0 + k] - S.bus0;
+            }
+            for (int32_t q = 0; q < S.nm; ++q) {
+                const int32_t ty = model.m_type[S.m0 + q];
+                const bool on_branch = (ty == 4 || ty == 5 || ty == 6);
+                loc[q] = model.m_loc[S.m0 + q] - (on_branch ? S.br0 : S.bus0);
+            }
+            // every branch is in the pattern: opening a breaker changes values only
+            std::vector<uint8_t> all_closed(S.nbr, 1);
+            Topology t;
+            t.n_bus = S.nbus;
+            t.n_branch = S.nbr;
+            t.n_meas = S.nm;
+            t.slack = S.slack - S.bus0;
+            t.br_from = from.data();
+            t.br_to = to.data();
+            t.br_closed = all_closed.data();
+            t.m_type = model.m_type.data() + S.m0;
+            t.m_loc = loc.data();
+            t.m_end = model.m_end.data() + S.m0;
+            t.m_active = model.m_active.data() + S.m0;
+            SymbolicParams prm;
+            prm.ordering = cfg.ordering;
+            if (!build_plan(t, prm, grid_plans_[g], errs[g])) errs[g] = "grid " + std::to_string(g) + ": " + errs[g];
+        }
+    };
+    const int32_t nt = std::max(1, std::min<int32_t>(G, static_cast<int32_t>(std::thread::hardware_concurrency())));
+    std::vector<std::thread> pool;
+    for (int32_t i = 1; i < nt; ++i) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    for (int32_t g = 0; g < G; ++g)
+        if (!errs[g].empty()) {
+            last_error = "symbolic analysis: " + errs[g];
+            analyzed_ = false;
+            return -5;
+        }
+    std::vector<const Plan*> parts(G);
+    std::vector<int32_t> brc(G);
+    for (int32_t g = 0; g < G; ++g) {
+        parts[g] = &grid_plans_[g];
+        brc[g] = grids_[g].nbr;
+    }
+    merge_plans(parts, brc, plan_);
+    analyzed_ = true;
+    return 0;
+}
+
+int32_t Engine::batch_solve(int32_t n, const int32_t* ids, const uint8_t* flat, const SolveRequest& rq,
+                            GridResult* out) {
+    if (!batch_mode()) {
+        last_error = "no batch grids";
+        return -4;
+    }
+    const int32_t G = static_cast<int32_t>(grids_.size());
+    for (int32_t i = 0; i < n; ++i)
+        if (!ids || ids[i] < 0 || ids[i] >= G) {
+            last_error = "grid index out of range";
+            return -4;
+        }
+    if (!init_ || !uploaded_ || model.structure_dirty) {
+        const int32_t rc = upload();
+        if (rc) return rc;
+    }
+    cudaSetDevice(cfg.device_id);
+    if (model.values_dirty) {
+        const int32_t rc = sync_measurements();
+        if (rc) return rc;
+    }
+    const SolveParams sp = params(rq);
+    std::memset(h_batch_in_, 0, 2 * static_cast<size_t>(G));
+    for (int32_t i = 0; i < n; ++i) {
+        h_batch_in_[ids[i]] = 1;
+        h_batch_in_[G + ids[i]] = (flat && flat[i]) ? 1 : 0;
+    }
+    cudaError_t e = cudaMemcpyAsync(const_cast<uint8_t*>(batch_.active), h_batch_in_, 2 * static_cast<size_t>(G),
+                                    cudaMemcpyHostToDevice, st_);  // active and flat are adjacent in the arena
+    if (e != cudaSuccess) return set_cuda_error(e, "batch inputs");
+    cudaEventRecord(ev0_, st_);
+    e = launch_batch_begin(net_, work_, batch_, st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "batch begin");
+    char* ob = static_cast<char*>(h_batch_out_);
+    uint32_t* h_flags = reinterpret_cast<uint32_t*>(ob);
+    int32_t* h_iters = reinterpret_cast<int32_t*>(ob + 4 * static_cast<size_t>(G));
+    double* h_mis = reinterpret_cast<double*>(ob + 8 * static_cast<size_t>(G));
+    double* h_obj = reinterpret_cast<double*>(ob + 16 * static_cast<size_t>(G));
+    int32_t* h_running = reinterpret_cast<int32_t*>(ob + 24 * static_cast<size_t>(G));
+    for (int32_t it = 0; it < rq.max_iterations; ++it) {
+        if (run_iteration(sp, true) != 0) return -3;
+        if (h_status_->flags & FLAG_TIMEOUT) {
+            last_error = "factorisation dataflow wait timed out";
+            return -3;
+        }
+        if (*h_running == 0) break;
+    }
+    SolveParams spf = sp;
+    spf.skip_flags = FLAG_INACTIVE;  // converged grids need their final residuals
+    e = launch_evaluate(net_, work_, spf, st_);
+    if (e == cudaSuccess) e = launch_batch_objective(net_, work_, batch_, st_);
+    cudaEventRecord(ev1_, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_flags, batch_.flags, 4 * static_cast<size_t>(G), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_iters, batch_.iters, 4 * static_cast<size_t>(G), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_mis, batch_.mismatch, 8 * static_cast<size_t>(G), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_obj, batch_.objective, 8 * static_cast<size_t>(G), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "batch solve");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    last_.time_ms = ms;
+    for (int32_t i = 0; i < n; ++i) {
+        const int32_t g = ids[i];
+        const uint32_t fl = h_flags[g];
+        GridResult r;
+        r.status = (fl & FLAG_SINGULAR) ? CONV_SINGULAR
+                   : (fl & FLAG_NONFINITE) ? CONV_DIVERGED
+                   : (fl & FLAG_CONVERGED) ? CONV_OK
+                                           : CONV_MAXIT;
+        r.iterations = h_iters[g];
+        r.max_mismatch = h_mis[g];
+        r.objective = h_obj[g];
+        if (out) out[i] = r;
+    }
+    stale_ = DL_ALL;
+    ++stats.solves;
+    return 0;
+}
+
+int32_t Engine::batch_set_telemetry(int32_t grid, const double* z, int32_t count) {
+    if (grid < 0 || grid >= static_cast<int32_t>(grids_.size()) || !z) {
+        last_error = "grid index out of range";
+        return -4;
+    }
+    const GridSpan& S = grids_[grid];
+    if (count != S.nm) {
+        last_error = "telemetry count does not match the grid's measurement count";
+        return -4;
+    }
+    std::memcpy(model.m_value.data() + S.m0, z, sizeof(double) * count);
+    if (!uploaded_ || model.structure_dirty || count == 0) {
+        model.values_dirty = true;
+        return 0;
+    }
+    cudaError_t e;
+    if (h_stage_ && h_stage_n_ >= static_cast<size_t>(S.m0 + count)) {
+        // this grid's slice of the pinned staging buffer; the copy is ordered
+        // before the next solve on the engine stream
+        e = cudaStreamSynchronize(st_);
+        if (e == cudaSuccess) {
+            std::memcpy(h_stage_ + S.m0, z, sizeof(double) * count);
+            e = cudaMemcpyAsync(work_.z + S.m0, h_stage_ + S.m0, sizeof(double) * count, cudaMemcpyHostToDevice, st_);
+        }
+    } else {
+        e = cudaMemcpy(work_.z + S.m0, z, sizeof(double) * count, cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) return set_cuda_error(e, "telemetry");
+    return 0;
+}
+
+int32_t Engine::batch_get_state(int32_t grid, double* v, double* th) {
+    if (grid < 0 || grid >= static_cast<int32_t>(grids_.size())) {
+        last_error = "grid index out of range";
+        return -4;
+    }
+    const GridSpan& S = grids_[grid];
+    if (!uploaded_) {
+        if (v) std::memcpy(v, model.bus_v.data() + S.bus0, sizeof(double) * S.nbus);
+        if (th) std::memcpy(th, model.bus_th.data() + S.bus0, sizeof(double) * S.nbus);
+        return 0;
+    }
+    cudaError_t e = cudaSuccess;
+    if (v) e = cudaMemcpyAsync(v, work_.v + S.bus0, sizeof(double) * S.nbus, cudaMemcpyDeviceToHost, st_);
+    if (th && e == cudaSuccess) e = cudaMemcpyAsync(th, work_.th + S.bus0, sizeof(double) * S.nbus, cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "batch state");
+    return 0;
+}
+
+int32_t Engine::batch_set_branch_status(int32_t grid, int32_t branch, int32_t closed) {
+    if (grid < 0 || grid >= static_cast<int32_t>(grids_.size())) {
+        last_error = "grid index out of range";
+        return -4;
+    }
+    const GridSpan& S = grids_[grid];
+    if (branch < 0 || branch >= S.nbr) {
+        last_error = "branch index out of range";
+        return -11;
+    }
+    const int32_t k = S.br0 + branch;
+    model.br_closed[k] = closed ? 1 : 0;
+    if (!uploaded_ || model.structure_dirty) return 0;
+    // value-only topology change: every branch is in the batch pattern
+    cudaError_t e = cudaMemcpyAsync(const_cast<uint8_t*>(net_.br_closed) + k, &model.br_closed[k], 1,
+                                    cudaMemcpyHostToDevice, st_);
+    if (e == cudaSuccess) e = launch_admittance_and_ybus(net_, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "breaker edit");
     return 0;
 }
 

@@ -132,6 +132,37 @@ public:
     const SolveResult& last_result() const { return last_; }
     std::string device_info();
 
+    // --- batch of independent grids (block-diagonal system) ---------------------
+    // Grids are appended with batch_add_grid; the model is their union with
+    // shifted indices, the symbolic plan the union of per-grid plans (built
+    // with every branch in the pattern, so breaker edits only change values),
+    // and batch_solve runs the Gauss-Newton loop for a subset of grids at once,
+    // each grid stopping on its own convergence test.
+    struct GridSpan {
+        int32_t bus0, nbus, br0, nbr, m0, nm, slack;
+    };
+    struct GridResult {
+        int32_t status, iterations;
+        double max_mismatch, objective;
+    };
+    int32_t batch_add_grid(int32_t n_bus, const int32_t* bus_type, const double* vset, int32_t n_br,
+                           const int32_t* from, const int32_t* to, const double* r, const double* x, const double* b,
+                           const double* tap, const double* shift, const int32_t* status, int32_t n_meas,
+                           const int32_t* mtype, const int32_t* mloc, const int32_t* mend, const double* sigma,
+                           const double* z, int32_t* id);
+    int32_t batch_solve(int32_t n, const int32_t* ids, const uint8_t* flat, const SolveRequest& rq, GridResult* out);
+    int32_t batch_set_telemetry(int32_t grid, const double* z, int32_t count);
+    int32_t batch_get_state(int32_t grid, double* v, double* th);
+    int32_t batch_set_branch_status(int32_t grid, int32_t branch, int32_t closed);
+    bool batch_mode() const { return !grids_.empty(); }
+    // Admission: when non-zero, upload() refuses (-10, nothing allocated) a
+    // model whose device arena would exceed this many bytes.
+    size_t budget_bytes = 0;
+    // Set by a caller that has just run analyze() on the unchanged model (e.g.
+    // on a worker thread): the next upload() reuses that plan once.
+    bool reuse_analysis_once = false;
+    const std::vector<GridSpan>& grids() const { return grids_; }
+
     // Device copies of per-element results (downloaded lazily).
     std::vector<double> p_inj, q_inj, pf, qf, pt, qt;
 
@@ -156,13 +187,25 @@ private:
         sch_pot_ptr_, sch_pan_ptr_, sch_upd_ptr_, sch_all_ptr_, sch_all_, sch_maxf_;
     std::vector<int4> sch_asm_, sch_pot_, sch_pan_, sch_upd_;
     std::vector<int64_t> sch_maxpanel_;
-    std::vector<int32_t> sch_flow_a_, sch_flow_b_, sch_down_;
+    std::vector<int32_t> sch_flow_a_, sch_flow_b_, sch_down_, sch_up_, phase_nchild_, nchild_;
     std::vector<char> flow_phase_;
     int32_t flow_a_maxf_ = 0, flow_b_maxf_ = 0;
     int32_t* d_flow_a_ = nullptr;
     int32_t* d_flow_b_ = nullptr;
     int32_t* d_down_ = nullptr;
+    int32_t* d_up_ = nullptr;
+    int8_t* d_phase_ = nullptr;
+    int32_t* d_phase_nchild_ = nullptr;
+    int32_t* d_nchild_ = nullptr;
     int32_t max_solve_front() const;
+    // batch state
+    std::vector<GridSpan> grids_;
+    std::vector<Plan> grid_plans_;
+    DevBatch batch_{};
+    uint8_t* h_batch_in_ = nullptr;   // pinned [2 * G]: active, flat
+    void* h_batch_out_ = nullptr;     // pinned: flags, iters, mismatch, objective, running
+    size_t h_batch_cap_ = 0;
+    int32_t analyze_batch();
     std::vector<int64_t> lay_lx_off_, lay_u_off_;
     std::vector<int32_t> lay_u_ld_, h_pcol_;
     std::vector<uint8_t> lay_u_big_;

@@ -46,8 +46,10 @@ __device__ __forceinline__ double gain_entry(const DevNet& net, const DevFactor&
 // elimination tree's critical path.
 template <typename T, typename HV>
 __global__ void k_gain_values(DevNet net, DevFactor F, DevWork W, const HV* hval, T* gv, int n_tgt) {
-    for (int tg = blockIdx.x * blockDim.x + threadIdx.x; tg < n_tgt; tg += gridDim.x * blockDim.x)
+    for (int tg = blockIdx.x * blockDim.x + threadIdx.x; tg < n_tgt; tg += gridDim.x * blockDim.x) {
+        if (F.tgt_grid && (W.grid_flags[F.tgt_grid[tg]] & FLAG_FROZEN)) continue;
         gv[tg] = static_cast<T>(gain_entry(net, F, W, hval, tg));
+    }
 }
 
 // Pivot: L_kk = sqrt(d) and its reciprocal.  Non-positive or non-finite d
@@ -79,6 +81,16 @@ __device__ __forceinline__ void pivot(double d, double* sq, double* inv, uint32_
         *sq = sqrt(d);
         *inv = 1.0 / *sq;
     }
+}
+
+// Where a non-positive pivot of front s is reported: the grid's own flags in
+// a batch, the engine status otherwise.
+__device__ __forceinline__ uint32_t* singular_flags(const DevFactor& F, const DevWork& W, int s) {
+    return W.grid_flags ? W.grid_flags + F.sn_grid[s] : &W.status->flags;
+}
+// Batch: fronts of grids that take no further step are skipped.
+__device__ __forceinline__ bool front_frozen(const DevFactor& F, const DevWork& W, int s) {
+    return W.grid_flags && (W.grid_flags[F.sn_grid[s]] & FLAG_FROZEN);
 }
 
 // L_kk = sqrt(d) and 1 / L_kk for a positive finite d (the caller checks).
@@ -180,6 +192,40 @@ __device__ __forceinline__ void store4<double>(double* p, const double (&v)[4]) 
     reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
 }
 
+// Factors the kb x kb diagonal block held by one warp in registers: lane i
+// owns row i in a[] (entries j <= i, zeros elsewhere and for lanes >= kb).
+// Fully unrolled and branch-free: the chain from one pivot to the next is a
+// shuffle, a reciprocal square root and two FMAs, and the remaining shuffles
+// and updates of a step overlap with it.  On return a[] is row i of L and
+// *inv_out = 1 / L_ii; returns true if a pivot was not positive and finite
+// (then replaced by 1).
+template <typename T, int KP>
+__device__ __forceinline__ bool warp_potrf(T (&a)[KP], int kb, int lane, T* inv_out) {
+    bool bad = false;
+    T my_inv = T(0);
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+        if (k < kb) {
+            T d = __shfl_sync(0xffffffffu, a[k], k);
+            bad |= !(d > T(0)) || !isfinite(d);
+            d = (d > T(0) && isfinite(d)) ? d : T(1);
+            T sq, inv;
+            pivot_value(d, &sq, &inv);
+            const T lk = (lane == k) ? sq : (lane > k ? a[k] * inv : a[k]);
+            a[k] = lk;
+            my_inv = (lane == k) ? inv : my_inv;
+#pragma unroll
+            for (int j = k + 1; j < KP; ++j) {
+                const T ljk = __shfl_sync(0xffffffffu, lk, j);
+                a[j] = (lane >= j) ? a[j] - lk * ljk : a[j];
+            }
+            __syncwarp();
+        }
+    }
+    *inv_out = my_inv;
+    return bad;
+}
+
 // Shared-memory scratch of one front besides the front itself.
 template <typename T>
 struct FrontSmem {
@@ -227,35 +273,13 @@ __device__ void front_factor(const DevFactor& F, const DevWork& W, const T* gv, 
             const int i = k0 + lane;
 #pragma unroll
             for (int j = 0; j < KP; ++j) a[j] = (lane < kb && j <= lane) ? Fm[i + (k0 + j) * ldf] : T(0);
-            bool bad = false;
-            T my_inv = T(0);  // 1 / L_kk of this lane's row
-            // Fully unrolled and branch-free: the chain from one pivot to the
-            // next is a shuffle, a reciprocal square root and two FMAs; the
-            // other shuffles and updates of a step overlap with it.
-#pragma unroll
-            for (int k = 0; k < KP; ++k) {
-                if (k < kb) {
-                    T d = __shfl_sync(0xffffffffu, a[k], k);
-                    bad |= !(d > T(0)) || !isfinite(d);
-                    d = (d > T(0) && isfinite(d)) ? d : T(1);
-                    T sq, inv;
-                    pivot_value(d, &sq, &inv);
-                    const T lk = (lane == k) ? sq : (lane > k ? a[k] * inv : a[k]);
-                    a[k] = lk;
-                    my_inv = (lane == k) ? inv : my_inv;
-#pragma unroll
-                    for (int j = k + 1; j < KP; ++j) {
-                        const T ljk = __shfl_sync(0xffffffffu, lk, j);
-                        a[j] = (lane >= j) ? a[j] - lk * ljk : a[j];
-                    }
-                    __syncwarp();
-                }
-            }
+            T my_inv;
+            const bool bad = warp_potrf<T, KP>(a, kb, lane, &my_inv);
             if (lane < kb) {
                 sm.rinv[lane] = my_inv;
                 rdg[k0 + lane] = my_inv;
             }
-            if (bad && lane == 0) atomicOr(&W.status->flags, FLAG_SINGULAR);
+            if (bad && lane == 0) atomicOr(singular_flags(F, W, s), FLAG_SINGULAR);
 #pragma unroll
             for (int j = 0; j < KP; ++j)
                 if (lane < kb && j <= lane) {
@@ -359,7 +383,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_front_small(DevFactor F, DevWor
                                                              const int* fronts) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ FrontSmem<T> sm;
-    front_factor<T, kPanel>(F, W, gv, lx, ub, fronts[blockIdx.x], reinterpret_cast<T*>(smem_raw), sm);
+    const int s = fronts[blockIdx.x];
+    if (front_frozen(F, W, s)) return;
+    front_factor<T, kPanel>(F, W, gv, lx, ub, s, reinterpret_cast<T*>(smem_raw), sm);
 }
 
 // ---------------------------------------------------------------------------
@@ -400,24 +426,47 @@ __device__ __forceinline__ int claim(int* counter, int* slot) {
     return *slot;
 }
 
+// After front s is complete (all threads past a barrier): thread 0 counts s
+// into its parent's completed children; the CTA that completes the last child
+// of a parent handled by the same sweep (phase[p] == ph, or every front when
+// phase is null) continues with that parent.  Returns the next front or -1.
+__device__ __forceinline__ int continue_up(const DevFactor& F, const int8_t* phase, int ph, const int32_t* nchild,
+                                           int* cnt, int s, int* slot) {
+    if (threadIdx.x == 0) {
+        int nxt = -1;
+        const int p = F.sn_parent[s];
+        if (p >= 0 && (phase == nullptr || phase[p] == ph)) {
+            __threadfence();
+            if (atomicAdd(cnt + p, 1) + 1 == nchild[p]) {
+                __threadfence();
+                nxt = p;
+            }
+        }
+        *slot = nxt;
+    }
+    __syncwarp();
+    __syncthreads();
+    return *slot;
+}
+
 template <typename T, int KP, int kMinBlocks>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) k_front_flow(DevFactor F, DevWork W, const T* gv, T* lx,
-                                                                     T* ub, const int* order, int n_items,
-                                                                     int* counter, int* done) {
+                                                                     T* ub, const int* ready, int n_ready,
+                                                                     const int8_t* phase, int ph,
+                                                                     const int32_t* nchild, int* counter, int* cnt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ FrontSmem<T> sm;
     __shared__ int slot;
     for (;;) {
         const int item = claim(counter, &slot);
-        if (item >= n_items) break;
-        const int s = order[item];
-        if (threadIdx.x == 0)
-            for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) wait_done(done + F.sn_child[ci], &W.status->flags);
-        __syncwarp();
-        __syncthreads();
-        front_factor<T, KP>(F, W, gv, lx, ub, s, reinterpret_cast<T*>(smem_raw), sm);
-        __syncthreads();
-        if (threadIdx.x == 0) publish_done(done + s);
+        if (item >= n_ready) break;
+        int s = ready[item];
+        while (s >= 0) {
+            if (!front_frozen(F, W, s))
+                front_factor<T, KP>(F, W, gv, lx, ub, s, reinterpret_cast<T*>(smem_raw), sm);
+            __syncthreads();
+            s = continue_up(F, phase, ph, nchild, cnt, s, &slot);
+        }
     }
 }
 
@@ -499,26 +548,21 @@ __global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, 
         D[i + j * ld] = (i >= j) ? B[(p0 + i) + (int64_t)(p0 + j) * f] : T(0);
     }
     __syncthreads();
-    // one warp factors the tile: lane i owns row i
+    // one warp factors the tile in registers: lane i owns row i
     if (threadIdx.x < 32) {
         const int i = threadIdx.x;
-        for (int k = 0; k < pb; ++k) {
-            if (i == k) {
-                T sq, inv;
-                pivot(D[k + k * ld], &sq, &inv, &W.status->flags);
-                D[k + k * ld] = sq;
-                rdiag[k] = inv;
-                reinterpret_cast<T*>(W.rdiag)[F.sn_c0[s] + p0 + k] = inv;
-            }
-            __syncwarp();
-            const T inv = rdiag[k];
-            if (i > k && i < pb) D[i + k * ld] *= inv;
-            __syncwarp();
-            if (i > k && i < pb) {
-                const T lik = D[i + k * ld];
-                for (int j = k + 1; j <= i; ++j) D[i + j * ld] -= lik * D[j + k * ld];
-            }
-            __syncwarp();
+        T a[kTile];
+#pragma unroll
+        for (int j = 0; j < kTile; ++j) a[j] = (i < pb && j <= i) ? D[i + j * ld] : T(0);
+        T inv;
+        const bool bad = warp_potrf<T, kTile>(a, pb, i, &inv);
+        if (bad && i == 0) atomicOr(singular_flags(F, W, s), FLAG_SINGULAR);
+#pragma unroll
+        for (int j = 0; j < kTile; ++j)
+            if (i < pb && j <= i) D[i + j * ld] = a[j];
+        if (i < pb) {
+            rdiag[i] = inv;
+            reinterpret_cast<T*>(W.rdiag)[F.sn_c0[s] + p0 + i] = inv;
         }
     }
     __syncthreads();
@@ -746,25 +790,23 @@ __global__ void __launch_bounds__(kThreads) k_bwd(DevFactor F, const T* lx, cons
     front_bwd<T, V>(F, lx, rdiag, sv, fronts[blockIdx.x], reinterpret_cast<V*>(smem_raw), D);
 }
 
-// Forward sweep as dataflow: order = fronts bottom-up, waits on children.
+// Forward sweep by continuation from the leaves (see continue_up).
 template <typename T, typename V>
 __global__ void __launch_bounds__(kThreads) k_fwd_flow(DevFactor F, DevWork W, const T* lx, const T* rdiag,
-                                                       SolveVecs sv, const int* order, int n_items, int* counter,
-                                                       int* done) {
+                                                       SolveVecs sv, const int* ready, int n_ready,
+                                                       const int32_t* nchild, int* counter, int* cnt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ T D[kTile * (kTile + 1)];
     __shared__ int slot;
     for (;;) {
         const int item = claim(counter, &slot);
-        if (item >= n_items) break;
-        const int s = order[item];
-        if (threadIdx.x == 0)
-            for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) wait_done(done + F.sn_child[ci], &W.status->flags);
-        __syncwarp();
-        __syncthreads();
-        front_fwd<T, V>(F, lx, rdiag, sv, s, reinterpret_cast<V*>(smem_raw), D);
-        __syncthreads();
-        if (threadIdx.x == 0) publish_done(done + s);
+        if (item >= n_ready) break;
+        int s = ready[item];
+        while (s >= 0) {
+            if (!front_frozen(F, W, s)) front_fwd<T, V>(F, lx, rdiag, sv, s, reinterpret_cast<V*>(smem_raw), D);
+            __syncthreads();
+            s = continue_up(F, nullptr, 0, nchild, cnt, s, &slot);
+        }
     }
 }
 
@@ -780,6 +822,11 @@ __global__ void __launch_bounds__(kThreads) k_bwd_flow(DevFactor F, DevWork W, c
         const int item = claim(counter, &slot);
         if (item >= n_items) break;
         const int s = order[item];
+        if (front_frozen(F, W, s)) {
+            if (threadIdx.x == 0) publish_done(done + s);
+            __syncwarp();
+            continue;
+        }
         if (threadIdx.x == 0 && F.sn_parent[s] >= 0) wait_done(done + F.sn_parent[s], &W.status->flags);
         __syncwarp();
         __syncthreads();
@@ -836,13 +883,13 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
         if (ls.flow_a_n > 0) {
             const int mf = ls.flow_a_maxf;
             k_front_flow<T, kPanelSmall, kMinBlocksA<T>><<<ls.flow_a_grid, kThreads, front_smem<T>(mf), st>>>(
-                F, W, gv, lx, ub, ls.d_flow_a, ls.flow_a_n, counters + 0, W.flow);
+                F, W, gv, lx, ub, ls.d_flow_a, ls.flow_a_n, ls.d_phase, 1, ls.d_phase_nchild, counters + 0, W.flow);
             ++g_kernel_launches;
         }
         if (ls.flow_b_n > 0) {
             const int mf = ls.flow_b_maxf;
             k_front_flow<T, kPanel, 1><<<ls.flow_b_grid, kThreads, front_smem<T>(mf), st>>>(
-                F, W, gv, lx, ub, ls.d_flow_b, ls.flow_b_n, counters + 1, W.flow);
+                F, W, gv, lx, ub, ls.d_flow_b, ls.flow_b_n, ls.d_phase, 2, ls.d_phase_nchild, counters + 1, W.flow);
             ++g_kernel_launches;
         }
     }
@@ -893,8 +940,8 @@ cudaError_t solve_impl(const DevFactor& F, const DevWork& W, const LevelSchedule
         cudaError_t e = cudaMemsetAsync(fwd_done, 0, sizeof(int) * (size_t)(2 * ns + 8), st);
         if (e != cudaSuccess) return e;
         const size_t smem = solve_smem<T>(ls.solve_maxf);
-        k_fwd_flow<T, T><<<ls.solve_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_up, ns, counters + 0,
-                                                                fwd_done);
+        k_fwd_flow<T, T><<<ls.up_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_up, ls.up_n, ls.d_nchild,
+                                                             counters + 0, fwd_done);
         k_bwd_flow<T, T><<<ls.solve_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_down, ns, counters + 1,
                                                                 bwd_done);
         g_kernel_launches += 2;

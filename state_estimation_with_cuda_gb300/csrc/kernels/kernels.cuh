@@ -13,6 +13,8 @@ enum StatusFlag : uint32_t {
     FLAG_NONFINITE = 2u,  // NaN/Inf in the state step
     FLAG_CONVERGED = 4u,  // max |dx| < tolerance
     FLAG_TIMEOUT = 8u,    // a dataflow wait gave up (bounded spin)
+    FLAG_FROZEN = 16u,    // batch: this grid takes no further steps (inactive or finished)
+    FLAG_INACTIVE = 32u,  // batch: this grid is not part of the current solve
 };
 
 // Per-solve scalars kept on the device; read back once per iteration.
@@ -68,6 +70,7 @@ struct DevNet {
     const int32_t* h_ptr;
     const int32_t* h_row;
     const int32_t* h_pcol;   // column of each H entry in the permuted state order
+    const int32_t* meas_grid;  // batch: grid of each measurement row (nullptr for one grid)
 };
 
 // Factorisation plan (device).
@@ -98,6 +101,9 @@ struct DevFactor {
     // inside their f x f region of the factor array (sn_u_big = 1, ld = f)
     const int32_t* sn_u_ld;
     const uint8_t* sn_u_big;
+    const int32_t* sn_grid;  // batch: grid of each front (nullptr for one grid)
+    const int32_t* tgt_grid; // batch: grid of each gain target
+    const int32_t* ps_grid;  // batch: grid of each permuted state
 };
 
 // Mutable per-iteration state (device).
@@ -134,7 +140,25 @@ struct DevWork {
     double* pt;
     double* qt;
     double* part;     // block partials: [2 * max_blocks]
+    double* opart;    // bad-data pass block partials: largest |r| per block
+    int32_t* oidx;    //   its row
+    int32_t* ocnt;    //   rows over the threshold per block
     DevStatus* status;
+    uint32_t* grid_flags;  // batch: per-grid FLAG_* bits (nullptr for one grid)
+};
+
+// Batch of independent grids solved together (block-diagonal system).
+struct DevBatch {
+    int32_t n_grids;
+    const int32_t* bus_off;   // [n_grids + 1]
+    const int32_t* meas_off;  // [n_grids + 1]
+    uint32_t* flags;          // [n_grids] FLAG_* (also DevWork::grid_flags)
+    int32_t* iters;           // [n_grids] Gauss-Newton steps taken
+    double* mismatch;         // [n_grids] max |dx| of the last step
+    double* objective;        // [n_grids] sum w r^2 at the final state
+    const uint8_t* active;    // [n_grids] 1 = solve this grid
+    const uint8_t* flat;      // [n_grids] 1 = flat start first
+    int32_t* running;         // [1] grids still iterating after this step
 };
 
 struct SolveParams {
@@ -144,6 +168,7 @@ struct SolveParams {
     double huber_gamma;
     double tol;
     double vmin, vmax;
+    uint32_t skip_flags;     // batch: grids whose flags intersect this mask are not evaluated
 };
 
 // Upload-time kernels.
@@ -197,17 +222,32 @@ struct LevelSchedule {
     const int32_t* h_lvl_maxf = nullptr;    // [n_levels] largest front per level
     const int64_t* h_lvl_maxpanel = nullptr;  // [n_levels] largest f * nc per level
     // dataflow phases of the factorisation (fronts below every big front):
-    // A = fronts whose whole subtree has f <= kFlowSmallF, B = the rest
-    const int32_t* d_flow_a = nullptr;
+    // A = fronts whose whole subtree has f <= kFlowSmallF, B = the rest.  A
+    // CTA claims an initially ready front of its phase (no children in the
+    // phase) and, when it completes the last child of a parent in the same
+    // phase, goes on with that parent; CTAs exit when nothing is left.
+    const int32_t* d_flow_a = nullptr;  // initially ready fronts of phase A, claim order
     int32_t flow_a_n = 0, flow_a_maxf = 0, flow_a_grid = 0;
-    const int32_t* d_flow_b = nullptr;
+    const int32_t* d_flow_b = nullptr;  // initially ready fronts of phase B
     int32_t flow_b_n = 0, flow_b_maxf = 0, flow_b_grid = 0;
-    // dataflow solves over every front: d_up = bottom-up order, d_down = top-down
+    const int8_t* d_phase = nullptr;         // [n_super] 1 = A, 2 = B, 0 = level-synchronous
+    const int32_t* d_phase_nchild = nullptr; // [n_super] children in the same phase
+    // dataflow solves over every front: forward by continuation from the
+    // leaves (d_up, up_n), backward in top-down order (d_down) waiting on parents
     int32_t solve_flow = 0;
     const int32_t* d_up = nullptr;
+    int32_t up_n = 0;
+    const int32_t* d_nchild = nullptr;       // [n_super] children
     const int32_t* d_down = nullptr;
-    int32_t solve_maxf = 0, solve_grid = 0;
+    int32_t solve_maxf = 0, solve_grid = 0, up_grid = 0;
 };
+
+// Batch control: begin (flags, flat starts), per-grid update + convergence,
+// per-grid objective at the final state.
+cudaError_t launch_batch_begin(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st);
+cudaError_t launch_batch_update(const DevNet& net, const DevFactor& f, const DevWork& w, const DevBatch& b,
+                                const SolveParams& sp, const double* step, cudaStream_t st);
+cudaError_t launch_batch_objective(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st);
 
 // Largest front of the high-occupancy dataflow phase.
 constexpr int32_t kFlowSmallF = 64;

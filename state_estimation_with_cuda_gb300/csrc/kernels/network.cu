@@ -67,7 +67,10 @@ __global__ void k_ybus(DevNet net) {
     for (int e = e0 + 1; e < e1; ++e) {
         const int src = net.y_src[e];
         const int k = src >> 1, end = src & 1;
-        const double g = net.br_g[k], b = net.br_b[k];
+        // an open branch in the pattern (batch patterns keep every branch)
+        // contributes nothing
+        const double on = net.br_closed[k] ? 1.0 : 0.0;
+        const double g = net.br_g[k] * on, b = net.br_b[k] * on;
         const double a = fmax(net.br_tap[k], kEps);
         const double phi = net.br_shift[k];
         double sph, cph;
@@ -77,12 +80,12 @@ __global__ void k_ybus(DevNet net) {
             net.y_g[e] = -(g * cph + b * sph) * inv_a;
             net.y_b[e] = -(-g * sph + b * cph) * inv_a;
             dg += g / (a * a);
-            db += b / (a * a) + net.br_bsf[k];
+            db += b / (a * a) + net.br_bsf[k] * on;
         } else {         // row = to bus: Y_ji = -(g+jb) e^{+j phi} / a
             net.y_g[e] = -(g * cph - b * sph) * inv_a;
             net.y_b[e] = -(g * sph + b * cph) * inv_a;
             dg += g;
-            db += b + net.br_bst[k];
+            db += b + net.br_bst[k] * on;
         }
     }
     net.y_g[e0] = dg;
@@ -155,7 +158,8 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
     __shared__ double sh[32];
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     double obj = 0.0;
-    if (q < net.n_meas) {
+    const bool skip = q < net.n_meas && net.meas_grid && (w.grid_flags[net.meas_grid[q]] & sp.skip_flags);
+    if (q < net.n_meas && !skip) {
         const int kind = net.m_kind[q];
         const int ty = net.m_type[q];
         const int loc = net.m_loc[q];
@@ -273,6 +277,7 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
 __global__ void k_rhs(DevNet net, DevFactor f, DevWork w) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= f.n_state) return;
+    if (f.ps_grid && (w.grid_flags[f.ps_grid[t]] & FLAG_FROZEN)) return;
     double acc = 0.0;
     for (int x = f.rhs_ptr[t]; x < f.rhs_ptr[t + 1]; ++x) {
         const int hidx = f.rhs_h[x];
@@ -324,8 +329,46 @@ __global__ void k_refine_accumulate(DevFactor f, DevWork w) {
 
 // Objective, largest |r| (lowest index on ties) and the bad-data count
 // (active rows with sigma > 0 and |r| / sigma > threshold,
-// sle_engine.cu:959-977): single block, fixed order.
-__global__ void k_objective(DevNet net, DevWork w, int nblk, double bad_threshold) {
+// sle_engine.cu:959-977).  Two deterministic passes: per-block partials over
+// the rows, then one block over the partials in block order.
+__global__ void __launch_bounds__(kBlock) k_objective_part(DevNet net, DevWork w, double bad_threshold) {
+    __shared__ double sb[kBlock];
+    __shared__ int si[kBlock];
+    __shared__ int sc[kBlock];
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    double best = -1.0;
+    int bidx = 0x7fffffff, cnt = 0;
+    if (q < net.n_meas && net.m_kind[q] != 5) {
+        const double a = fabs(w.r[q]);
+        best = a;
+        bidx = q;
+        const double sg = net.m_sigma[q];
+        if (sg > 0.0 && a / sg > bad_threshold) cnt = 1;
+    }
+    sb[threadIdx.x] = best;
+    si[threadIdx.x] = bidx;
+    sc[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            const double b2 = sb[threadIdx.x + o];
+            const int i2 = si[threadIdx.x + o];
+            if (b2 > sb[threadIdx.x] || (b2 == sb[threadIdx.x] && i2 < si[threadIdx.x])) {
+                sb[threadIdx.x] = b2;
+                si[threadIdx.x] = i2;
+            }
+            sc[threadIdx.x] += sc[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        w.opart[blockIdx.x] = sb[0];
+        w.oidx[blockIdx.x] = si[0];
+        w.ocnt[blockIdx.x] = sc[0];
+    }
+}
+
+__global__ void k_objective(DevNet net, DevWork w, int nblk) {
     __shared__ double sh[32];
     __shared__ double sb[1024];
     __shared__ int si[1024];
@@ -335,12 +378,11 @@ __global__ void k_objective(DevNet net, DevWork w, int nblk, double bad_threshol
     const double tot = block_sum(acc, sh);
     double best = -1.0;
     int bidx = 0x7fffffff, cnt = 0;
-    for (int q = threadIdx.x; q < net.n_meas; q += blockDim.x) {
-        if (net.m_kind[q] == 5) continue;
-        const double a = fabs(w.r[q]);
-        if (a > best) { best = a; bidx = q; }
-        const double sg = net.m_sigma[q];
-        if (sg > 0.0 && a / sg > bad_threshold) ++cnt;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+        const double a = w.opart[b];
+        const int i = w.oidx[b];
+        if (a > best || (a == best && i < bidx)) { best = a; bidx = i; }
+        cnt += w.ocnt[b];
     }
     sb[threadIdx.x] = best;
     si[threadIdx.x] = bidx;
@@ -445,9 +487,113 @@ __global__ void k_flows(DevNet net, DevWork w) {
     w.qt[k] = flow_terms(net, w.v, w.th, k, true, true, true).val;
 }
 
+// Batch: one block per grid.  Clears the grid's flags (FROZEN for grids not
+// in this solve) and applies a flat start where requested.
+__global__ void k_batch_begin(DevNet net, DevWork w, DevBatch b) {
+    const int g = blockIdx.x;
+    const bool act = b.active[g] != 0;
+    if (threadIdx.x == 0) {
+        b.flags[g] = act ? 0u : (FLAG_FROZEN | FLAG_INACTIVE);
+        b.iters[g] = 0;
+        b.mismatch[g] = 0.0;
+    }
+    if (!act || !b.flat[g]) return;
+    for (int i = b.bus_off[g] + threadIdx.x; i < b.bus_off[g + 1]; i += blockDim.x) {
+        const int t = net.bus_type[i];
+        w.v[i] = (t == 1 || t == 2) ? net.v_setpoint[i] : 1.0;
+        w.th[i] = 0.0;
+    }
+}
+
+// Batch a13: one block per grid.  A grid that is frozen takes no step; a grid
+// whose factorisation flagged a non-positive pivot stops as singular without
+// applying the step; otherwise x += dx (slack angle fixed, V clamped) and the
+// grid stops when max |dx| < tol (converged) or dx is not finite (diverged),
+// exactly as the single-grid loop decides after its step.
+__global__ void __launch_bounds__(kBlock) k_batch_update(DevNet net, DevFactor f, DevWork w, DevBatch b,
+                                                         SolveParams sp, const double* step) {
+    __shared__ double sh[32];
+    __shared__ int bad;
+    const int g = blockIdx.x;
+    const uint32_t fl = b.flags[g];
+    if (fl & FLAG_FROZEN) return;
+    if (fl & FLAG_SINGULAR) {
+        if (threadIdx.x == 0) {
+            b.flags[g] = fl | FLAG_FROZEN;
+            b.iters[g] += 1;
+        }
+        return;
+    }
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    double mx = 0.0;
+    for (int i = b.bus_off[g] + threadIdx.x; i < b.bus_off[g + 1]; i += blockDim.x) {
+        const int pt = f.bus_ps_theta[i];
+        const double dv = step[f.bus_ps_v[i]];
+        double dt = 0.0;
+        if (pt >= 0) {
+            dt = step[pt];
+            w.th[i] += dt;
+        }
+        double vn = w.v[i] + dv;
+        vn = fmax(vn, sp.vmin);
+        vn = fmin(vn, sp.vmax);
+        w.v[i] = vn;
+        if (!isfinite(dt) || !isfinite(dv)) bad = 1;
+        double m = fmax(fabs(dt), fabs(dv));
+        if (m != m) m = 0.0;
+        mx = fmax(mx, m);
+    }
+    const double m = block_max(mx, sh);
+    if (threadIdx.x == 0) {
+        b.mismatch[g] = m;
+        b.iters[g] += 1;
+        if (bad) {
+            b.flags[g] = fl | FLAG_NONFINITE | FLAG_FROZEN;
+        } else if (m < sp.tol) {
+            b.flags[g] = fl | FLAG_CONVERGED | FLAG_FROZEN;
+        } else {
+            atomicAdd(b.running, 1);
+        }
+    }
+}
+
+// Batch objective sum w r^2 over each grid's rows in a fixed order.
+__global__ void __launch_bounds__(kBlock) k_batch_objective(DevNet net, DevWork w, DevBatch b) {
+    __shared__ double sh[32];
+    const int g = blockIdx.x;
+    double acc = 0.0;
+    for (int q = b.meas_off[g] + threadIdx.x; q < b.meas_off[g + 1]; q += blockDim.x)
+        if (net.m_kind[q] != 5) acc += net.m_w[q] * w.r[q] * w.r[q];
+    const double tot = block_sum(acc, sh);
+    if (threadIdx.x == 0) b.objective[g] = tot;
+}
+
 inline int nblocks(int n) { return (n + kBlock - 1) / kBlock; }
 
 }  // namespace
+
+cudaError_t launch_batch_begin(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st) {
+    if (b.n_grids <= 0) return cudaSuccess;
+    k_batch_begin<<<b.n_grids, kBlock, 0, st>>>(net, w, b);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_update(const DevNet& net, const DevFactor& f, const DevWork& w, const DevBatch& b,
+                                const SolveParams& sp, const double* step, cudaStream_t st) {
+    if (b.n_grids <= 0) return cudaSuccess;
+    k_batch_update<<<b.n_grids, kBlock, 0, st>>>(net, f, w, b, sp, step);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_objective(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st) {
+    if (b.n_grids <= 0) return cudaSuccess;
+    k_batch_objective<<<b.n_grids, kBlock, 0, st>>>(net, w, b);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+}
 
 std::atomic<int64_t> g_kernel_launches{0};
 
@@ -469,7 +615,12 @@ cudaError_t launch_evaluate(const DevNet& net, const DevWork& w, const SolvePara
 }
 
 cudaError_t launch_objective(const DevNet& net, const DevWork& w, double bad_threshold, cudaStream_t st) {
-    k_objective<<<1, 1024, 0, st>>>(net, w, net.n_meas > 0 ? nblocks(net.n_meas) : 0, bad_threshold);
+    const int nb = net.n_meas > 0 ? nblocks(net.n_meas) : 0;
+    if (nb > 0) {
+        k_objective_part<<<nb, kBlock, 0, st>>>(net, w, bad_threshold);
+        ++g_kernel_launches;
+    }
+    k_objective<<<1, 1024, 0, st>>>(net, w, nb);
     ++g_kernel_launches;
     return cudaGetLastError();
 }

@@ -333,6 +333,58 @@ void Model::load_soa(int32_t nb, const int32_t* btype, const double* vset, int32
     structure_dirty = true;
 }
 
+void Model::append_soa(int32_t nb, const int32_t* btype, const double* vset, int32_t nbr, const int32_t* from,
+                       const int32_t* to, const double* r, const double* x, const double* b, const double* tap,
+                       const double* shift, const int32_t* status, int32_t nm, const int32_t* mtype,
+                       const int32_t* mloc, const int32_t* mend, const double* sigma, const double* z) {
+    const int32_t b0 = n_bus(), k0 = n_branch();
+    for (int32_t i = 0; i < nb; ++i) {
+        bus_type.push_back(btype[i]);
+        bus_vset.push_back(vset[i]);
+        bus_kv.push_back(1.0);
+        bus_p.push_back(0.0);
+        bus_q.push_back(0.0);
+        bus_v.push_back(vset[i]);
+        bus_th.push_back(0.0);
+        bus_id.emplace_back();
+        if (btype[i] == 2 && slack < 0) slack = b0 + i;
+    }
+    for (int32_t k = 0; k < nbr; ++k) {
+        br_from.push_back(from[k] + b0);
+        br_to.push_back(to[k] + b0);
+        br_r.push_back(r[k]);
+        br_x.push_back(x[k]);
+        br_b.push_back(b[k]);
+        br_g.push_back(0.0);
+        br_tap.push_back(tap[k]);
+        br_shift.push_back(shift[k]);
+        br_xfmr.push_back(0);
+        br_closed.push_back(status ? (status[k] ? 1 : 0) : 1);
+        br_id.emplace_back();
+        br_sd.emplace_back();
+    }
+    for (int32_t q = 0; q < nm; ++q) {
+        const int32_t ty = mtype[q];
+        const bool on_branch = (ty == 4 || ty == 5 || ty == 6);
+        m_type.push_back(ty);
+        m_loc.push_back(mloc[q] + (on_branch ? k0 : b0));
+        m_end.push_back(mend[q]);
+        m_pseudo.push_back(0);
+        m_sigma.push_back(sigma[q]);
+        m_pt.push_back(1.0);
+        m_ct.push_back(1.0);
+        m_value.push_back(z[q]);
+        const double s = std::max(sigma[q], kRealEps);
+        m_w.push_back(1.0 / (s * s));
+        m_active.push_back(1);
+        m_est.push_back(0.0);
+        m_res.push_back(0.0);
+        m_id.emplace_back();
+    }
+    names_ready = false;
+    structure_dirty = true;
+}
+
 void Model::clear() { *this = Model(); }
 
 bool Model::validate(std::string& err) const {

@@ -91,6 +91,15 @@ struct Model {
                   const double* shift, const int32_t* status, int32_t n_meas, const int32_t* mtype,
                   const int32_t* mloc, const int32_t* mend, const double* sigma, const double* z);
 
+    // Append one more independent grid (batch mode): bus indices of branches
+    // and bus-located rows are shifted by the current bus count, branch-located
+    // rows (flows, currents) by the current branch count.  The first grid's
+    // slack stays the model's slack.
+    void append_soa(int32_t n_bus, const int32_t* bus_type, const double* vset, int32_t n_br, const int32_t* from,
+                    const int32_t* to, const double* r, const double* x, const double* b, const double* tap,
+                    const double* shift, const int32_t* status, int32_t n_meas, const int32_t* mtype,
+                    const int32_t* mloc, const int32_t* mend, const double* sigma, const double* z);
+
     void clear();
     // Structural validity (reference network_model.cu:576-593).
     bool validate(std::string& err) const;

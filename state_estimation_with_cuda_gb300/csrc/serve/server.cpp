@@ -1,0 +1,359 @@
+#include "server.h"
+
+#include <algorithm>
+#include <chrono>
+#include <numeric>
+
+namespace sle_gb300 {
+
+namespace {
+int64_t now_ns() {
+    return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+}  // namespace
+
+Server::~Server() { stop(); }
+
+int32_t Server::add_grid(int32_t nb, const int32_t* btype, const double* vset, int32_t nbr, const int32_t* from,
+                         const int32_t* to, const double* r, const double* x, const double* b, const double* tap,
+                         const double* shift, const int32_t* status, int32_t nm, const int32_t* mtype,
+                         const int32_t* mloc, const int32_t* mend, const double* sigma, const double* z,
+                         int32_t* id) {
+    if (started_) {
+        last_error = "grids are added before start";
+        return -4;
+    }
+    if (nb <= 0 || nbr < 0 || nm < 0 || !btype || !vset || (nbr > 0 && (!from || !to || !r || !x || !b || !tap || !shift)) ||
+        (nm > 0 && (!mtype || !mloc || !mend || !sigma || !z))) {
+        last_error = "invalid grid arrays";
+        return -4;
+    }
+    GridData g;
+    g.n_bus = nb;
+    g.n_br = nbr;
+    g.n_meas = nm;
+    g.bus_type.assign(btype, btype + nb);
+    g.vset.assign(vset, vset + nb);
+    g.from.assign(from, from + nbr);
+    g.to.assign(to, to + nbr);
+    g.r.assign(r, r + nbr);
+    g.x.assign(x, x + nbr);
+    g.b.assign(b, b + nbr);
+    g.tap.assign(tap, tap + nbr);
+    g.shift.assign(shift, shift + nbr);
+    g.status.assign(nbr, 1);
+    if (status) g.status.assign(status, status + nbr);
+    g.mtype.assign(mtype, mtype + nm);
+    g.mloc.assign(mloc, mloc + nm);
+    g.mend.assign(mend, mend + nm);
+    g.sigma.assign(sigma, sigma + nm);
+    g.z.assign(z, z + nm);
+    fleet_.push_back(std::move(g));
+    if (id) *id = static_cast<int32_t>(fleet_.size()) - 1;
+    return 0;
+}
+
+int32_t Server::start() {
+    if (started_) return 0;
+    const int32_t G = static_cast<int32_t>(fleet_.size());
+    if (G == 0) {
+        last_error = "no grids";
+        return -4;
+    }
+    // partition: shared units by size bound, then one unit per large grid
+    std::vector<int32_t> bounds;
+    for (int32_t v : cfg_.bucket_bus)
+        if (v > 0) bounds.push_back(v);
+    std::sort(bounds.begin(), bounds.end());
+    const int32_t nshared = static_cast<int32_t>(bounds.size()) + 1;  // the last shared unit takes the rest below own_unit_bus
+    std::vector<std::vector<int32_t>> shared(nshared);
+    std::vector<int32_t> own;
+    for (int32_t g = 0; g < G; ++g) {
+        const int32_t n = fleet_[g].n_bus;
+        if (n >= cfg_.own_unit_bus) {
+            own.push_back(g);
+            continue;
+        }
+        int32_t k = 0;
+        while (k < static_cast<int32_t>(bounds.size()) && n > bounds[k]) ++k;
+        shared[k].push_back(g);
+    }
+    std::sort(own.begin(), own.end(), [&](int32_t a, int32_t b) { return fleet_[a].n_bus < fleet_[b].n_bus; });
+    std::vector<std::vector<int32_t>> parts;
+    for (auto& v : shared)
+        if (!v.empty()) parts.push_back(v);
+    for (int32_t g : own) parts.push_back({g});
+    unit_of_.assign(G, -1);
+    local_of_.assign(G, -1);
+    // memory budget
+    size_t budget = cfg_.memory_budget;
+    if (budget == 0) {
+        size_t fr = 0, tot = 0;
+        cudaSetDevice(cfg_.device_id);
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+            last_error = "cudaMemGetInfo failed";
+            return -3;
+        }
+        budget = static_cast<size_t>(0.9 * static_cast<double>(fr));
+    }
+    // build every unit's batch model, then analyse them in parallel (host only)
+    for (auto& members : parts) {
+        auto u = std::make_unique<Unit>();
+        EngineConfig ec;
+        ec.device_id = cfg_.device_id;
+        ec.use_double_precision = cfg_.use_double_precision;
+        u->eng = std::make_unique<Engine>(ec);
+        u->grids = members;
+        u->pending.resize(members.size());
+        const int32_t ui = static_cast<int32_t>(units_.size());
+        for (size_t li = 0; li < members.size(); ++li) {
+            const GridData& d = fleet_[members[li]];
+            int32_t lid = -1;
+            const int32_t rc = u->eng->batch_add_grid(d.n_bus, d.bus_type.data(), d.vset.data(), d.n_br, d.from.data(),
+                                                      d.to.data(), d.r.data(), d.x.data(), d.b.data(), d.tap.data(),
+                                                      d.shift.data(), d.status.data(), d.n_meas, d.mtype.data(),
+                                                      d.mloc.data(), d.mend.data(), d.sigma.data(), d.z.data(), &lid);
+            if (rc) {
+                last_error = u->eng->last_error;
+                return rc;
+            }
+            unit_of_[members[li]] = ui;
+            local_of_[members[li]] = lid;
+        }
+        units_.push_back(std::move(u));
+    }
+    const int32_t U = static_cast<int32_t>(units_.size());
+    auto parallel = [&](auto&& fn) {
+        std::atomic<int32_t> next{0};
+        auto work = [&]() {
+            for (int32_t i = next++; i < U; i = next++) fn(i);
+        };
+        const int32_t nt = std::max(1, std::min<int32_t>(U, static_cast<int32_t>(std::thread::hardware_concurrency())));
+        std::vector<std::thread> pool;
+        for (int32_t t = 1; t < nt; ++t) pool.emplace_back(work);
+        work();
+        for (auto& th : pool) th.join();
+    };
+    std::vector<int32_t> arc(U, 0);
+    parallel([&](int32_t i) {
+        arc[i] = units_[i]->eng->analyze();
+        units_[i]->eng->reuse_analysis_once = (arc[i] == 0);
+    });
+    for (int32_t i = 0; i < U; ++i)
+        if (arc[i]) {
+            last_error = units_[i]->eng->last_error;
+            return arc[i];
+        }
+    // admission in order (shared units first, then own units by size)
+    size_t used = 0;
+    for (auto& u : units_) {
+        u->eng->budget_bytes = budget > used ? budget - used : 1;
+        const int32_t rc = u->eng->upload();
+        if (rc == 0) {
+            u->admitted = true;
+            used += u->eng->device_bytes();
+        } else if (rc != -10) {
+            last_error = u->eng->last_error;
+            return rc;
+        }
+    }
+    // first estimate of every admitted grid from a flat start, units in parallel
+    SolveRequest rq;
+    rq.mode = Mode::PRECISION;
+    rq.max_iterations = cfg_.max_iterations;
+    rq.tolerance = cfg_.tolerance;
+    rq.robust = cfg_.robust;
+    rq.huber_gamma = cfg_.huber_gamma;
+    std::vector<int32_t> src(U, 0);
+    parallel([&](int32_t i) {
+        Unit* u = units_[i].get();
+        if (!u->admitted) return;
+        const int32_t n = static_cast<int32_t>(u->grids.size());
+        std::vector<int32_t> ids(n);
+        std::iota(ids.begin(), ids.end(), 0);
+        std::vector<uint8_t> flat(n, 1);
+        std::vector<Engine::GridResult> res(n);
+        src[i] = u->eng->batch_solve(n, ids.data(), flat.data(), rq, res.data());
+    });
+    for (int32_t i = 0; i < U; ++i)
+        if (src[i]) {
+            last_error = units_[i]->eng->last_error;
+            return src[i];
+        }
+    {
+        std::lock_guard<std::mutex> lk(st_mu_);
+        stats_.units = static_cast<int32_t>(units_.size());
+        stats_.grids = G;
+        stats_.budget_bytes = budget;
+        stats_.device_bytes = used;
+        for (auto& u : units_) stats_.admitted_units += u->admitted ? 1 : 0;
+    }
+    started_ = true;
+    for (auto& u : units_)
+        if (u->admitted) u->worker = std::thread(&Server::run_unit, this, u.get());
+    return 0;
+}
+
+int32_t Server::submit(int32_t grid, const double* z, int32_t count, int32_t branch, int32_t closed, int64_t* ticket) {
+    if (!started_) {
+        last_error = "server not started";
+        return -4;
+    }
+    if (grid < 0 || grid >= static_cast<int32_t>(fleet_.size()) || !z || count != fleet_[grid].n_meas) {
+        last_error = "invalid request";
+        return -4;
+    }
+    if (branch >= fleet_[grid].n_br) {
+        last_error = "branch index out of range";
+        return -11;
+    }
+    int64_t t;
+    {
+        std::lock_guard<std::mutex> lk(res_mu_);
+        t = next_ticket_++;
+    }
+    if (ticket) *ticket = t;
+    {
+        std::lock_guard<std::mutex> lk(st_mu_);
+        ++stats_.submitted;
+    }
+    Unit* u = units_[unit_of_[grid]].get();
+    if (!u->admitted) {
+        ServeResult r;
+        r.admitted = 0;
+        r.status = CONV_NOTOBS;
+        r.t_submit_ns = r.t_start_ns = r.t_done_ns = now_ns();
+        {
+            std::lock_guard<std::mutex> lk(st_mu_);
+            ++stats_.rejected;
+        }
+        finish(t, r);
+        return 0;
+    }
+    Request rq{t, grid, std::vector<double>(z, z + count), branch, closed, now_ns()};
+    {
+        std::lock_guard<std::mutex> lk(u->mu);
+        u->pending[local_of_[grid]].push_back(std::move(rq));
+        ++u->n_pending;
+    }
+    u->cv.notify_one();
+    return 0;
+}
+
+void Server::finish(int64_t ticket, const ServeResult& r) {
+    {
+        std::lock_guard<std::mutex> lk(res_mu_);
+        results_[ticket] = r;
+    }
+    res_cv_.notify_all();
+}
+
+void Server::run_unit(Unit* u) {
+    SolveRequest rq;
+    rq.mode = Mode::PRECISION;
+    rq.max_iterations = cfg_.max_iterations;
+    rq.tolerance = cfg_.tolerance;
+    rq.robust = cfg_.robust;
+    rq.huber_gamma = cfg_.huber_gamma;
+    std::vector<Request> take;
+    std::vector<int32_t> ids;
+    std::vector<Engine::GridResult> res;
+    for (;;) {
+        take.clear();
+        {
+            std::unique_lock<std::mutex> lk(u->mu);
+            u->cv.wait(lk, [&] { return stopping_ || u->n_pending > 0; });
+            if (stopping_ && u->n_pending == 0) return;
+            for (auto& q : u->pending) {
+                if (q.empty()) continue;
+                take.push_back(std::move(q.front()));
+                q.pop_front();
+                --u->n_pending;
+            }
+        }
+        const int64_t t0 = now_ns();
+        ids.resize(take.size());
+        res.assign(take.size(), Engine::GridResult{});
+        int32_t rc = 0;
+        {
+            std::lock_guard<std::mutex> lk(u->eng_mu);
+            for (size_t i = 0; i < take.size() && rc == 0; ++i) {
+                const int32_t lid = local_of_[take[i].grid];
+                ids[i] = lid;
+                if (take[i].branch >= 0) rc = u->eng->batch_set_branch_status(lid, take[i].branch, take[i].closed);
+                if (rc == 0) rc = u->eng->batch_set_telemetry(lid, take[i].z.data(), static_cast<int32_t>(take[i].z.size()));
+            }
+            if (rc == 0) rc = u->eng->batch_solve(static_cast<int32_t>(ids.size()), ids.data(), nullptr, rq, res.data());
+        }
+        const int64_t t1 = now_ns();
+        for (size_t i = 0; i < take.size(); ++i) {
+            ServeResult r;
+            if (rc == 0) {
+                r.status = res[i].status;
+                r.iterations = res[i].iterations;
+                r.max_mismatch = res[i].max_mismatch;
+                r.objective = res[i].objective;
+            } else {
+                r.status = CONV_DIVERGED;
+            }
+            r.batch_size = static_cast<int32_t>(take.size());
+            r.t_submit_ns = take[i].t_submit;
+            r.t_start_ns = t0;
+            r.t_done_ns = t1;
+            finish(take[i].ticket, r);
+        }
+        std::lock_guard<std::mutex> lk(st_mu_);
+        stats_.completed += static_cast<int64_t>(take.size());
+        stats_.grid_solves += static_cast<int64_t>(take.size());
+        ++stats_.passes;
+    }
+}
+
+int32_t Server::wait(int64_t ticket, double timeout_ms, ServeResult* out) {
+    std::unique_lock<std::mutex> lk(res_mu_);
+    auto ready = [&] { return results_.count(ticket) != 0; };
+    if (timeout_ms < 0) {
+        res_cv_.wait(lk, ready);
+    } else if (!res_cv_.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), ready)) {
+        return 0;
+    }
+    if (out) *out = results_[ticket];
+    results_.erase(ticket);
+    return 1;
+}
+
+int32_t Server::get_state(int32_t grid, double* v, double* th) {
+    if (grid < 0 || grid >= static_cast<int32_t>(fleet_.size()) || !started_) {
+        last_error = "invalid grid";
+        return -4;
+    }
+    Unit* u = units_[unit_of_[grid]].get();
+    if (!u->admitted) {
+        last_error = "grid not resident (admission budget)";
+        return -10;
+    }
+    std::lock_guard<std::mutex> lk(u->eng_mu);
+    const int32_t rc = u->eng->batch_get_state(local_of_[grid], v, th);
+    if (rc) last_error = u->eng->last_error;
+    return rc;
+}
+
+ServeStats Server::stats() {
+    std::lock_guard<std::mutex> lk(st_mu_);
+    return stats_;
+}
+
+void Server::stop() {
+    if (!started_) return;
+    stopping_ = true;
+    for (auto& u : units_) {
+        { std::lock_guard<std::mutex> lk(u->mu); }  // a worker between its predicate check and its wait sees the flag
+        u->cv.notify_all();
+    }
+    for (auto& u : units_)
+        if (u->worker.joinable()) u->worker.join();
+    started_ = false;
+}
+
+}  // namespace sle_gb300

@@ -1,0 +1,129 @@
+// Serving runtime: a resident fleet of grids answering measurement snapshots
+// (and breaker edits) as they arrive.
+//
+// Grids are partitioned by size into units.  Small grids share a unit: one
+// batch Engine whose Gauss-Newton loop solves all grids with pending
+// requests together.  A grid at or above `own_unit_bus` gets a unit of its
+// own.  Every unit has its own CUDA stream and worker thread, so the units'
+// work overlaps on the device.  A worker takes, for every grid of its unit, the
+// oldest pending request and solves them as one batch; requests that arrive
+// meanwhile wait for the unit's next pass (continuous batching).  Each grid
+// hot-starts from its last state.  A grid stops on its own convergence
+// test, so its result does not depend on which other requests share the pass.
+//
+// Admission: units are made resident in order (small units first) while the
+// sum of their device arenas stays within the memory budget; requests for
+// grids of units that were not admitted complete at once with
+// `admitted = 0`.
+#pragma once
+
+#include <atomic>
+#include <condition_variable>
+#include <cstdint>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../engine/engine.h"
+
+namespace sle_gb300 {
+
+struct ServeConfig {
+    int32_t use_double_precision = 0;
+    int32_t max_iterations = 20;
+    double tolerance = 1e-6;
+    int32_t robust = 0;
+    double huber_gamma = 1.5;
+    // Upper bus-count bounds of the shared units (ascending; 0 = unused).  A
+    // grid goes to the first unit whose bound is >= its size.
+    int32_t bucket_bus[4] = {300, 2000, 20000, 0};
+    int32_t own_unit_bus = 1 << 30;  // grids at least this large get a unit of their own
+    size_t memory_budget = 0;      // bytes; 0 = 90 % of the free device memory at start
+    int32_t device_id = 0;
+};
+
+struct ServeResult {
+    int32_t status = CONV_RUNNING;
+    int32_t iterations = 0;
+    double max_mismatch = 0.0;
+    double objective = 0.0;
+    int32_t admitted = 1;
+    int32_t batch_size = 0;  // grids solved in the same pass
+    int64_t t_submit_ns = 0, t_start_ns = 0, t_done_ns = 0;  // steady clock
+};
+
+struct ServeStats {
+    int64_t submitted = 0, completed = 0, rejected = 0, passes = 0, grid_solves = 0;
+    int32_t units = 0, admitted_units = 0, grids = 0;
+    size_t device_bytes = 0, budget_bytes = 0;
+};
+
+class Server {
+public:
+    explicit Server(const ServeConfig& c) : cfg_(c) {}
+    ~Server();
+    Server(const Server&) = delete;
+    Server& operator=(const Server&) = delete;
+
+    int32_t add_grid(int32_t n_bus, const int32_t* bus_type, const double* vset, int32_t n_br, const int32_t* from,
+                     const int32_t* to, const double* r, const double* x, const double* b, const double* tap,
+                     const double* shift, const int32_t* status, int32_t n_meas, const int32_t* mtype,
+                     const int32_t* mloc, const int32_t* mend, const double* sigma, const double* z, int32_t* id);
+    // Partition, admit, upload, solve every admitted grid once from a flat
+    // start, and start the workers.
+    int32_t start();
+    // Queue a snapshot for `grid` (count = its measurement count); a breaker
+    // edit (branch >= 0) is applied before the snapshot.  Returns a ticket.
+    int32_t submit(int32_t grid, const double* z, int32_t count, int32_t branch, int32_t closed, int64_t* ticket);
+    // Wait up to timeout_ms (< 0: forever) for a ticket; 1 = done, 0 = timed out.
+    int32_t wait(int64_t ticket, double timeout_ms, ServeResult* out);
+    int32_t get_state(int32_t grid, double* v, double* th);
+    ServeStats stats();
+    void stop();
+    std::string last_error;
+
+private:
+    struct GridData {
+        int32_t n_bus, n_br, n_meas;
+        std::vector<int32_t> bus_type, from, to, status, mtype, mloc, mend;
+        std::vector<double> vset, r, x, b, tap, shift, sigma, z;
+    };
+    struct Request {
+        int64_t ticket;
+        int32_t grid;
+        std::vector<double> z;
+        int32_t branch, closed;
+        int64_t t_submit;
+    };
+    struct Unit {
+        std::unique_ptr<Engine> eng;
+        std::vector<int32_t> grids;                  // fleet grid ids, local order
+        std::vector<std::deque<Request>> pending;    // per local grid
+        int64_t n_pending = 0;
+        bool admitted = false;
+        std::thread worker;
+        std::mutex mu;  // guards pending / n_pending
+        std::condition_variable cv;
+        std::mutex eng_mu;  // serialises engine use (worker vs get_state)
+    };
+    ServeConfig cfg_;
+    std::vector<GridData> fleet_;
+    std::vector<int32_t> unit_of_, local_of_;
+    std::vector<std::unique_ptr<Unit>> units_;
+    bool started_ = false;
+    std::atomic<bool> stopping_{false};
+    std::mutex res_mu_;
+    std::condition_variable res_cv_;
+    std::unordered_map<int64_t, ServeResult> results_;
+    int64_t next_ticket_ = 1;
+    std::mutex st_mu_;
+    ServeStats stats_;
+    void run_unit(Unit* u);
+    void finish(int64_t ticket, const ServeResult& r);
+};
+
+}  // namespace sle_gb300

@@ -740,4 +740,108 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     return true;
 }
 
+
+namespace {
+template <typename T>
+void append_shift(std::vector<T>& dst, const std::vector<T>& src, T shift, bool keep_negative = false) {
+    for (T v : src) dst.push_back((keep_negative && v < 0) ? v : static_cast<T>(v + shift));
+}
+// CSR row pointers: drop the leading 0 of every part after the first.
+template <typename T>
+void append_ptr(std::vector<T>& dst, const std::vector<T>& src, T shift) {
+    if (dst.empty()) dst.push_back(0);
+    for (size_t i = 1; i < src.size(); ++i) dst.push_back(static_cast<T>(src[i] + shift));
+}
+}  // namespace
+
+void merge_plans(const std::vector<const Plan*>& parts, const std::vector<int32_t>& br_count, Plan& M) {
+    M = Plan();
+    int32_t bus0 = 0, br0 = 0, m0 = 0, st0 = 0, ns0 = 0;
+    int32_t y0 = 0, h0 = 0, tg0 = 0;
+    int64_t rows0 = 0, su0 = 0, pair0 = 0, lx0 = 0, u0 = 0;
+    int32_t maxl = 0;
+    for (const Plan* P : parts) maxl = std::max(maxl, P->n_levels);
+    for (size_t g = 0; g < parts.size(); ++g) {
+        const Plan& P = *parts[g];
+        if (g == 0) M.slack = P.slack;
+        append_ptr(M.y_ptr, P.y_ptr, y0);
+        append_shift(M.y_col, P.y_col, bus0);
+        for (int32_t v : P.y_src) M.y_src.push_back(v < 0 ? v : (((v >> 1) + br0) << 1) | (v & 1));
+        M.y_hpos_t.insert(M.y_hpos_t.end(), P.y_hpos_t.begin(), P.y_hpos_t.end());
+        M.y_hpos_v.insert(M.y_hpos_v.end(), P.y_hpos_v.begin(), P.y_hpos_v.end());
+        append_ptr(M.h_ptr, P.h_ptr, h0);
+        append_shift(M.h_col, P.h_col, st0);
+        append_shift(M.h_row, P.h_row, m0);
+        M.m_kind.insert(M.m_kind.end(), P.m_kind.begin(), P.m_kind.end());
+        M.m_fpos.insert(M.m_fpos.end(), P.m_fpos.begin(), P.m_fpos.end());
+        append_shift(M.bus_perm, P.bus_perm, bus0);
+        append_shift(M.bus_ps_theta, P.bus_ps_theta, st0, true);
+        append_shift(M.bus_ps_v, P.bus_ps_v, st0, true);
+        append_shift(M.state_of_ps, P.state_of_ps, st0);
+        append_ptr(M.sn_c0, P.sn_c0, st0);
+        M.sn_f.insert(M.sn_f.end(), P.sn_f.begin(), P.sn_f.end());
+        append_shift(M.sn_parent, P.sn_parent, ns0, true);
+        append_ptr(M.sn_rows_off, P.sn_rows_off, rows0);
+        append_shift(M.sn_rows, P.sn_rows, st0);
+        append_ptr(M.sn_lx_off, P.sn_lx_off, lx0);
+        append_ptr(M.sn_u_off, P.sn_u_off, u0);
+        append_ptr(M.sn_su_off, P.sn_su_off, su0);
+        append_ptr(M.sn_child_ptr, P.sn_child_ptr, static_cast<int32_t>(M.sn_child.size()));
+        append_shift(M.sn_child, P.sn_child, ns0);
+        M.sn_relmap.insert(M.sn_relmap.end(), P.sn_relmap.begin(), P.sn_relmap.end());
+        append_ptr(M.sn_tgt_ptr, P.sn_tgt_ptr, tg0);
+        M.tgt_local.insert(M.tgt_local.end(), P.tgt_local.begin(), P.tgt_local.end());
+        append_ptr(M.tgt_pair_ptr, P.tgt_pair_ptr, pair0);
+        append_shift(M.pair_a, P.pair_a, h0);
+        append_shift(M.pair_b, P.pair_b, h0);
+        append_ptr(M.rhs_ptr, P.rhs_ptr, static_cast<int32_t>(M.rhs_h.size()));
+        append_shift(M.rhs_h, P.rhs_h, h0);
+        M.nnz_l += P.nnz_l;
+        M.flops += P.flops;
+        M.max_front = std::max(M.max_front, P.max_front);
+        M.lx_size += P.lx_size;
+        M.u_size += P.u_size;
+        M.su_size += P.su_size;
+        bus0 += P.n_bus;
+        br0 += br_count[g];
+        m0 += P.n_meas;
+        st0 += P.n_state;
+        ns0 += P.n_super;
+        y0 += static_cast<int32_t>(P.y_col.size());
+        h0 += static_cast<int32_t>(P.h_col.size());
+        tg0 += static_cast<int32_t>(P.tgt_local.size());
+        rows0 += static_cast<int64_t>(P.sn_rows.size());
+        su0 += P.su_size;
+        pair0 += static_cast<int64_t>(P.pair_a.size());
+        lx0 += P.lx_size;
+        u0 += P.u_size;
+    }
+    if (M.y_ptr.empty()) M.y_ptr.push_back(0);
+    if (M.h_ptr.empty()) M.h_ptr.push_back(0);
+    if (M.sn_c0.empty()) M.sn_c0.push_back(0);
+    if (M.sn_rows_off.empty()) M.sn_rows_off.push_back(0);
+    if (M.sn_lx_off.empty()) M.sn_lx_off.push_back(0);
+    if (M.sn_u_off.empty()) M.sn_u_off.push_back(0);
+    if (M.sn_su_off.empty()) M.sn_su_off.push_back(0);
+    if (M.sn_child_ptr.empty()) M.sn_child_ptr.push_back(0);
+    if (M.sn_tgt_ptr.empty()) M.sn_tgt_ptr.push_back(0);
+    if (M.tgt_pair_ptr.empty()) M.tgt_pair_ptr.push_back(0);
+    if (M.rhs_ptr.empty()) M.rhs_ptr.push_back(0);
+    M.n_bus = bus0;
+    M.n_meas = m0;
+    M.n_state = st0;
+    M.n_super = ns0;
+    M.n_levels = maxl;
+    M.lvl_ptr.assign(maxl + 1, 0);
+    for (int32_t l = 0; l < maxl; ++l) {
+        int32_t off = 0;
+        for (const Plan* P : parts) {
+            if (l < P->n_levels)
+                for (int32_t x = P->lvl_ptr[l]; x < P->lvl_ptr[l + 1]; ++x) M.lvl_sn.push_back(P->lvl_sn[x] + off);
+            off += P->n_super;
+        }
+        M.lvl_ptr[l + 1] = static_cast<int32_t>(M.lvl_sn.size());
+    }
+}
+
 }  // namespace sle_gb300

@@ -116,6 +116,14 @@ struct Plan {
 // Builds the plan; returns false and sets err on invalid input.
 bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& plan, std::string& err);
 
+// Block-diagonal union of independent grids' plans (a batch): every index
+// array is shifted by the preceding grids' counts (buses, branches, rows,
+// states, Ybus and H entries, supernodes, targets, pairs), so the batch is a
+// plan of one grid whose elimination forest is the union of the grids'
+// forests.  Level l of the batch is the union of the grids' levels l.
+// Branch offsets come from br_count (branches per grid).
+void merge_plans(const std::vector<const Plan*>& parts, const std::vector<int32_t>& br_count, Plan& out);
+
 // Bus-level helpers exposed for tests / the oracle cross-check.
 // Adjacency of the bus graph (CSR, sorted, no self loops).
 void bus_graph(const Topology& t, const std::vector<int32_t>& y_ptr, const std::vector<int32_t>& y_col,

@@ -72,6 +72,31 @@ class SLE_Result(ctypes.Structure):
                 ("bad_data_count", ctypes.c_int32)]
 
 
+class SLE_ExGridResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("iterations", ctypes.c_int32), ("max_mismatch", ctypes.c_double),
+                ("objective", ctypes.c_double)]
+
+
+class SLE_ExServerConfig(ctypes.Structure):
+    _fields_ = [("use_double_precision", ctypes.c_int32), ("max_iterations", ctypes.c_int32),
+                ("tolerance", ctypes.c_double), ("robust", ctypes.c_int32), ("huber_gamma", ctypes.c_double),
+                ("bucket_bus", ctypes.c_int32 * 4), ("own_unit_bus", ctypes.c_int32), ("device_id", ctypes.c_int32),
+                ("memory_budget", ctypes.c_size_t)]
+
+
+class SLE_ExServeResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("iterations", ctypes.c_int32), ("max_mismatch", ctypes.c_double),
+                ("objective", ctypes.c_double), ("admitted", ctypes.c_int32), ("batch_size", ctypes.c_int32),
+                ("t_submit_ns", ctypes.c_int64), ("t_start_ns", ctypes.c_int64), ("t_done_ns", ctypes.c_int64)]
+
+
+class SLE_ExServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("rejected", ctypes.c_int64),
+                ("passes", ctypes.c_int64), ("grid_solves", ctypes.c_int64), ("units", ctypes.c_int32),
+                ("admitted_units", ctypes.c_int32), ("grids", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("device_bytes", ctypes.c_size_t), ("budget_bytes", ctypes.c_size_t)]
+
+
 class SLE_Config(ctypes.Structure):
     _fields_ = [("device_id", ctypes.c_int32), ("max_buses", ctypes.c_size_t), ("max_branches", ctypes.c_size_t),
                 ("max_measurements", ctypes.c_size_t), ("max_switching_devices", ctypes.c_size_t),
@@ -218,6 +243,24 @@ SLE_SIGNATURES = {
     "sle_ExTimer": (I, [H, I, P(D)]),
     "sle_ExGetStats": (I, [H, P(SLE_ExStats)]),
     "sle_ExResetStats": (I, [H]),
+    "sle_ExBatchAddGrid": (I, [H, I, P(I), P(D), I, P(I), P(I), P(D), P(D), P(D), P(D), P(D), P(I), I, P(I), P(I),
+                               P(I), P(D), P(D), P(I)]),
+    "sle_ExBatchGridCount": (I, [H]),
+    "sle_ExBatchUpdateTelemetry": (I, [H, I, P(D), I]),
+    "sle_ExBatchSolve": (I, [H, I, P(I), P(ctypes.c_uint8), I, D, I, D, P(SLE_ExGridResult)]),
+    "sle_ExBatchGetState": (I, [H, I, P(D), P(D)]),
+    "sle_ExBatchSetBranchStatus": (I, [H, I, I, I]),
+    "sle_ExServerDefaultConfig": (None, [P(SLE_ExServerConfig)]),
+    "sle_ExServerCreate": (I, [P(ctypes.c_void_p), P(SLE_ExServerConfig)]),
+    "sle_ExServerDestroy": (None, [ctypes.c_void_p]),
+    "sle_ExServerAddGrid": (I, [ctypes.c_void_p, I, P(I), P(D), I, P(I), P(I), P(D), P(D), P(D), P(D), P(D), P(I), I,
+                                P(I), P(I), P(I), P(D), P(D), P(I)]),
+    "sle_ExServerStart": (I, [ctypes.c_void_p]),
+    "sle_ExServerSubmit": (I, [ctypes.c_void_p, I, P(D), I, I, I, P(ctypes.c_int64)]),
+    "sle_ExServerWait": (I, [ctypes.c_void_p, ctypes.c_int64, D, P(SLE_ExServeResult)]),
+    "sle_ExServerGetState": (I, [ctypes.c_void_p, I, P(D), P(D)]),
+    "sle_ExServerGetStats": (I, [ctypes.c_void_p, P(SLE_ExServerStats)]),
+    "sle_ExServerLastError": (S, [ctypes.c_void_p]),
 }
 
 

@@ -9,7 +9,13 @@ Named workloads (seed = 0x5E00 + index):
               (54,200 rows), taps on 15 % of branches; flat start, then
               hot-start updates that re-noise 1 % of the rows each.
   grid200k    200,000 buses / 280,000 branches, same mix (1,084,000 rows),
-              2 % gross errors of +-(10..30) sigma, Huber gamma = 1.5.
+              2 % gross errors of +-(10..30) sigma on telemetry rows, Huber
+              gamma = 1.5.
+  batch512    512 independent grids, n = round(30 (5000/30)^U) buses
+              (log-uniform), round(1.4 n) branches, the grid10k mix; grid i
+              seeded 0x5E03 ^ (i * 0x9E3779B97F4A7C15).
+  fleet200    200 grids with n ~ Zipf(1.2) truncated to [30, 200000], the
+              grid10k mix; grid i seeded 0x5E04 ^ (i * 0x9E3779B97F4A7C15).
 """
 import ctypes
 
@@ -85,6 +91,34 @@ class SyntheticGrid:
             self.close()
         except Exception:
             pass
+
+
+GOLDEN = 0x9E3779B97F4A7C15
+MASK64 = (1 << 64) - 1
+
+
+def grid_seed(base, i):
+    return (base ^ ((i * GOLDEN) & MASK64)) & MASK64
+
+
+def batch_sizes(count=512, seed=0x5E03, lo=30, hi=5000):
+    L = segen_lib()
+    return [L.segen_draw_loguniform(seed, i, lo, hi) for i in range(count)]
+
+
+def fleet_sizes(count=200, seed=0x5E04, s=1.2, lo=30, hi=200000):
+    L = segen_lib()
+    return [L.segen_draw_zipf(seed, i, s, lo, hi) for i in range(count)]
+
+
+def batch_grids(count=512, seed=0x5E03, lo=30, hi=5000):
+    """The batched-form workload: `count` independent grids of log-uniform size."""
+    return [SyntheticGrid(n, int(round(1.4 * n)), grid_seed(seed, i)) for i, n in enumerate(batch_sizes(count, seed, lo, hi))]
+
+
+def fleet_grids(count=200, seed=0x5E04):
+    """The serving-form fleet: `count` grids of Zipf(1.2) size in [30, 200000]."""
+    return [SyntheticGrid(n, int(round(1.4 * n)), grid_seed(seed, i)) for i, n in enumerate(fleet_sizes(count, seed))]
 
 
 def make(name):
