@@ -174,11 +174,13 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExBatchSetBranchStatus(SLE_Handle handle, in
 
 /* ---- Serving runtime (no counterpart in the reference) --------------------
  * A resident fleet of grids answering measurement snapshots and breaker
- * edits as they arrive.  Small grids share batch units (the sle_ExBatch
- * machinery), grids of at least own_unit_bus buses get a unit of their own;
- * each unit has its own stream and worker thread, and solves every grid
- * with a pending request in one pass, hot-started from the grid's last state
- * (continuous batching: requests arriving during a pass join the next one).
+ * edits as they arrive.  Grids share batch units by size (the sle_ExBatch
+ * machinery); grids of at least own_unit_bus buses get a unit of their own.
+ * Each unit has its own stream and worker thread and runs its batch one
+ * Gauss-Newton iteration at a time: between iterations, grids with a pending
+ * request join the batch (hot-started from their last state), and after each
+ * iteration the grids that finished answer and leave (iteration-level
+ * continuous batching).
  * Units are admitted in order while their device arenas fit the memory
  * budget; requests for grids of units left out complete at once with
  * admitted = 0.  Thread-safe: submit / wait may be called from any thread. */
@@ -202,7 +204,7 @@ typedef struct SLE_ExServeResult {
     double max_mismatch;
     double objective;
     int32_t admitted;    /* 0: the grid's unit is outside the memory budget */
-    int32_t batch_size;  /* grids solved in the same pass */
+    int32_t batch_size;  /* grids in the batch at the iteration that finished it */
     int64_t t_submit_ns, t_start_ns, t_done_ns; /* steady clock */
 } SLE_ExServeResult;
 

@@ -382,9 +382,10 @@ int32_t Engine::upload() {
             batch_.iters = c.take<int32_t>(G);
             batch_.mismatch = c.take<double>(G);
             batch_.objective = c.take<double>(G);
-            uint8_t* af = c.take<uint8_t>(2 * static_cast<size_t>(G));  // active, then flat
+            uint8_t* af = c.take<uint8_t>(3 * static_cast<size_t>(G));  // active, flat, retire
             batch_.active = af;
             batch_.flat = af + G;
+            batch_.retire = af + 2 * static_cast<size_t>(G);
             batch_.running = c.take<int32_t>(1);
         } else {
             batch_ = DevBatch{};
@@ -551,7 +552,7 @@ int32_t Engine::upload() {
             h_batch_in_ = nullptr;
             h_batch_out_ = nullptr;
             h_batch_cap_ = 0;
-            chk(cudaMallocHost(reinterpret_cast<void**>(&h_batch_in_), 2 * static_cast<size_t>(G)));
+            chk(cudaMallocHost(reinterpret_cast<void**>(&h_batch_in_), 3 * static_cast<size_t>(G)));
             chk(cudaMallocHost(&h_batch_out_, out_bytes));
             if (e == cudaSuccess) h_batch_cap_ = G;
         }
@@ -1460,6 +1461,125 @@ int32_t Engine::batch_set_branch_status(int32_t grid, int32_t branch, int32_t cl
     if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
     if (e != cudaSuccess) return set_cuda_error(e, "breaker edit");
     return 0;
+}
+
+
+// ---------------------------------------------------------------------------
+// Stream mode: grids join and leave the running batch between iterations.
+// ---------------------------------------------------------------------------
+int32_t Engine::stream_begin(const SolveRequest& rq) {
+    if (!batch_mode()) {
+        last_error = "no batch grids";
+        return -4;
+    }
+    if (!init_ || !uploaded_ || model.structure_dirty) {
+        const int32_t rc = upload();
+        if (rc) return rc;
+    }
+    cudaSetDevice(cfg.device_id);
+    if (model.values_dirty) {
+        const int32_t rc = sync_measurements();
+        if (rc) return rc;
+    }
+    stream_rq_ = rq;
+    const int32_t G = static_cast<int32_t>(grids_.size());
+    in_flight_.assign(G, 0);
+    stream_iters_.assign(G, 0);
+    std::memset(h_batch_in_, 0, 3 * static_cast<size_t>(G));
+    // every grid starts out of the batch
+    cudaError_t e = cudaMemcpyAsync(const_cast<uint8_t*>(batch_.active), h_batch_in_, 3 * static_cast<size_t>(G),
+                                    cudaMemcpyHostToDevice, st_);
+    if (e == cudaSuccess) e = launch_batch_begin(net_, work_, batch_, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "stream begin");
+    return 0;
+}
+
+int32_t Engine::stream_activate(int32_t n, const int32_t* ids, const uint8_t* flat) {
+    const int32_t G = static_cast<int32_t>(grids_.size());
+    if (n <= 0) return 0;
+    std::memset(h_batch_in_, 0, 3 * static_cast<size_t>(G));
+    for (int32_t i = 0; i < n; ++i) {
+        const int32_t g = ids[i];
+        if (g < 0 || g >= G || in_flight_[g]) {
+            last_error = "grid index out of range or already in the batch";
+            return -4;
+        }
+        h_batch_in_[g] = 1;
+        h_batch_in_[G + g] = (flat && flat[i]) ? 1 : 0;
+        in_flight_[g] = 1;
+        stream_iters_[g] = 0;
+    }
+    cudaError_t e = cudaMemcpyAsync(const_cast<uint8_t*>(batch_.active), h_batch_in_, 2 * static_cast<size_t>(G),
+                                    cudaMemcpyHostToDevice, st_);
+    if (e == cudaSuccess) e = launch_batch_activate(net_, work_, batch_, st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "stream activate");
+    return 0;
+}
+
+int32_t Engine::stream_step(std::vector<int32_t>& done, std::vector<GridResult>& res) {
+    done.clear();
+    res.clear();
+    const int32_t G = static_cast<int32_t>(grids_.size());
+    bool any = false;
+    for (int32_t g = 0; g < G && !any; ++g) any = in_flight_[g] != 0;
+    if (!any) return 0;
+    const SolveParams sp = params(stream_rq_);
+    if (run_iteration(sp, true) != 0) return -3;
+    if (h_status_->flags & FLAG_TIMEOUT) {
+        last_error = "factorisation dataflow wait timed out";
+        return -3;
+    }
+    char* ob = static_cast<char*>(h_batch_out_);
+    uint32_t* h_flags = reinterpret_cast<uint32_t*>(ob);
+    int32_t* h_iters = reinterpret_cast<int32_t*>(ob + 4 * static_cast<size_t>(G));
+    double* h_mis = reinterpret_cast<double*>(ob + 8 * static_cast<size_t>(G));
+    double* h_obj = reinterpret_cast<double*>(ob + 16 * static_cast<size_t>(G));
+    cudaError_t e = cudaMemcpyAsync(h_flags, batch_.flags, 4 * static_cast<size_t>(G), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_iters, batch_.iters, 4 * static_cast<size_t>(G), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_mis, batch_.mismatch, 8 * static_cast<size_t>(G), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "stream step");
+    for (int32_t g = 0; g < G; ++g) {
+        if (!in_flight_[g]) continue;
+        ++stream_iters_[g];
+        if ((h_flags[g] & FLAG_FROZEN) || stream_iters_[g] >= stream_rq_.max_iterations) done.push_back(g);
+    }
+    if (done.empty()) return 0;
+    // final evaluation of the finished grids (and, harmlessly, of the running
+    // ones) for their objective; then they leave the batch
+    std::memset(h_batch_in_ + 2 * static_cast<size_t>(G), 0, G);
+    for (int32_t g : done) h_batch_in_[2 * static_cast<size_t>(G) + g] = 1;
+    SolveParams spf = sp;
+    spf.skip_flags = FLAG_INACTIVE;
+    e = launch_evaluate(net_, work_, spf, st_);
+    if (e == cudaSuccess) e = launch_batch_objective(net_, work_, batch_, st_);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(const_cast<uint8_t*>(batch_.retire), h_batch_in_ + 2 * static_cast<size_t>(G), G,
+                            cudaMemcpyHostToDevice, st_);
+    if (e == cudaSuccess) e = launch_batch_retire(batch_, st_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_obj, batch_.objective, 8 * static_cast<size_t>(G), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "stream retire");
+    for (int32_t g : done) {
+        const uint32_t fl = h_flags[g];
+        GridResult r;
+        r.status = (fl & FLAG_SINGULAR) ? CONV_SINGULAR
+                   : (fl & FLAG_NONFINITE) ? CONV_DIVERGED
+                   : (fl & FLAG_CONVERGED) ? CONV_OK
+                                           : CONV_MAXIT;
+        r.iterations = h_iters[g];
+        r.max_mismatch = h_mis[g];
+        r.objective = h_obj[g];
+        res.push_back(r);
+        in_flight_[g] = 0;
+    }
+    stale_ = DL_ALL;
+    return 0;
+}
+
+bool Engine::stream_in_flight(int32_t grid) const {
+    return grid >= 0 && grid < static_cast<int32_t>(in_flight_.size()) && in_flight_[grid] != 0;
 }
 
 }  // namespace sle_gb300

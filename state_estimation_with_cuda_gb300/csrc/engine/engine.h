@@ -155,6 +155,15 @@ public:
     int32_t batch_get_state(int32_t grid, double* v, double* th);
     int32_t batch_set_branch_status(int32_t grid, int32_t branch, int32_t closed);
     bool batch_mode() const { return !grids_.empty(); }
+    // Stream mode of a batch (iteration-level continuous batching): after
+    // stream_begin every grid is out of the batch; stream_activate adds grids
+    // (their telemetry already set), stream_step runs one Gauss-Newton
+    // iteration for the grids in the batch and returns those that finished
+    // (converged, diverged, singular or at max_iterations), which leave it.
+    int32_t stream_begin(const SolveRequest& rq);
+    int32_t stream_activate(int32_t n, const int32_t* ids, const uint8_t* flat);
+    int32_t stream_step(std::vector<int32_t>& done, std::vector<GridResult>& res);
+    bool stream_in_flight(int32_t grid) const;
     // Admission: when non-zero, upload() refuses (-10, nothing allocated) a
     // model whose device arena would exceed this many bytes.
     size_t budget_bytes = 0;
@@ -205,6 +214,9 @@ private:
     uint8_t* h_batch_in_ = nullptr;   // pinned [2 * G]: active, flat
     void* h_batch_out_ = nullptr;     // pinned: flags, iters, mismatch, objective, running
     size_t h_batch_cap_ = 0;
+    SolveRequest stream_rq_{};
+    std::vector<uint8_t> in_flight_;
+    std::vector<int32_t> stream_iters_;
     int32_t analyze_batch();
     std::vector<int64_t> lay_lx_off_, lay_u_off_;
     std::vector<int32_t> lay_u_ld_, h_pcol_;

@@ -159,6 +159,7 @@ struct DevBatch {
     const uint8_t* active;    // [n_grids] 1 = solve this grid
     const uint8_t* flat;      // [n_grids] 1 = flat start first
     int32_t* running;         // [1] grids still iterating after this step
+    const uint8_t* retire;    // [n_grids] 1 = leave the running batch (stream mode)
 };
 
 struct SolveParams {
@@ -248,6 +249,11 @@ cudaError_t launch_batch_begin(const DevNet& net, const DevWork& w, const DevBat
 cudaError_t launch_batch_update(const DevNet& net, const DevFactor& f, const DevWork& w, const DevBatch& b,
                                 const SolveParams& sp, const double* step, cudaStream_t st);
 cudaError_t launch_batch_objective(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st);
+// Stream mode (grids join and leave between iterations): activate the grids
+// with active[g] = 1 (flags cleared, flat start if flat[g]), leaving the
+// others as they are; retire the grids with retire[g] = 1 (frozen, inactive).
+cudaError_t launch_batch_activate(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st);
+cudaError_t launch_batch_retire(const DevBatch& b, cudaStream_t st);
 
 // Largest front of the high-occupancy dataflow phase.
 constexpr int32_t kFlowSmallF = 64;

@@ -505,6 +505,28 @@ __global__ void k_batch_begin(DevNet net, DevWork w, DevBatch b) {
     }
 }
 
+// Stream mode: grids with active[g] join the running batch.
+__global__ void k_batch_activate(DevNet net, DevWork w, DevBatch b) {
+    const int g = blockIdx.x;
+    if (!b.active[g]) return;
+    if (threadIdx.x == 0) {
+        b.flags[g] = 0u;
+        b.iters[g] = 0;
+        b.mismatch[g] = 0.0;
+    }
+    if (!b.flat[g]) return;
+    for (int i = b.bus_off[g] + threadIdx.x; i < b.bus_off[g + 1]; i += blockDim.x) {
+        const int t = net.bus_type[i];
+        w.v[i] = (t == 1 || t == 2) ? net.v_setpoint[i] : 1.0;
+        w.th[i] = 0.0;
+    }
+}
+
+__global__ void k_batch_retire(DevBatch b) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < b.n_grids && b.retire[g]) b.flags[g] |= FLAG_FROZEN | FLAG_INACTIVE;
+}
+
 // Batch a13: one block per grid.  A grid that is frozen takes no step; a grid
 // whose factorisation flagged a non-positive pivot stops as singular without
 // applying the step; otherwise x += dx (slack angle fixed, V clamped) and the
@@ -584,6 +606,20 @@ cudaError_t launch_batch_update(const DevNet& net, const DevFactor& f, const Dev
                                 const SolveParams& sp, const double* step, cudaStream_t st) {
     if (b.n_grids <= 0) return cudaSuccess;
     k_batch_update<<<b.n_grids, kBlock, 0, st>>>(net, f, w, b, sp, step);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_activate(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st) {
+    if (b.n_grids <= 0) return cudaSuccess;
+    k_batch_activate<<<b.n_grids, kBlock, 0, st>>>(net, w, b);
+    ++g_kernel_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_retire(const DevBatch& b, cudaStream_t st) {
+    if (b.n_grids <= 0) return cudaSuccess;
+    k_batch_retire<<<(b.n_grids + kBlock - 1) / kBlock, kBlock, 0, st>>>(b);
     ++g_kernel_launches;
     return cudaGetLastError();
 }

@@ -249,6 +249,10 @@ void Server::finish(int64_t ticket, const ServeResult& r) {
     res_cv_.notify_all();
 }
 
+// Iteration-level continuous batching: between two Gauss-Newton iterations
+// of the unit's batch, every grid with a pending request that is not already
+// in the batch joins it (its breaker edit and snapshot applied first); after
+// the iteration, grids that finished answer their request and leave.
 void Server::run_unit(Unit* u) {
     SolveRequest rq;
     rq.mode = Mode::PRECISION;
@@ -256,56 +260,103 @@ void Server::run_unit(Unit* u) {
     rq.tolerance = cfg_.tolerance;
     rq.robust = cfg_.robust;
     rq.huber_gamma = cfg_.huber_gamma;
-    std::vector<Request> take;
-    std::vector<int32_t> ids;
+    {
+        std::lock_guard<std::mutex> lk(u->eng_mu);
+        if (u->eng->stream_begin(rq) != 0) {
+            // the unit cannot run: answer everything it receives as failed
+            for (;;) {
+                std::unique_lock<std::mutex> lk2(u->mu);
+                u->cv.wait(lk2, [&] { return stopping_.load() || u->n_pending > 0; });
+                if (stopping_ && u->n_pending == 0) return;
+                for (auto& q : u->pending)
+                    while (!q.empty()) {
+                        ServeResult r;
+                        r.status = CONV_DIVERGED;
+                        r.t_submit_ns = q.front().t_submit;
+                        r.t_start_ns = r.t_done_ns = now_ns();
+                        finish(q.front().ticket, r);
+                        q.pop_front();
+                        --u->n_pending;
+                    }
+            }
+        }
+    }
+    struct Running {
+        Request req;
+        int64_t t_start;
+    };
+    std::unordered_map<int32_t, Running> active;  // local grid -> its request
+    std::vector<Request> starting;
+    std::vector<int32_t> ids, done;
     std::vector<Engine::GridResult> res;
     for (;;) {
-        take.clear();
+        starting.clear();
         {
             std::unique_lock<std::mutex> lk(u->mu);
-            u->cv.wait(lk, [&] { return stopping_ || u->n_pending > 0; });
-            if (stopping_ && u->n_pending == 0) return;
-            for (auto& q : u->pending) {
-                if (q.empty()) continue;
-                take.push_back(std::move(q.front()));
+            if (active.empty()) u->cv.wait(lk, [&] { return stopping_.load() || u->n_pending > 0; });
+            if (stopping_ && u->n_pending == 0 && active.empty()) return;
+            for (size_t lid = 0; lid < u->pending.size(); ++lid) {
+                auto& q = u->pending[lid];
+                if (q.empty() || active.count(static_cast<int32_t>(lid))) continue;
+                starting.push_back(std::move(q.front()));
                 q.pop_front();
                 --u->n_pending;
             }
         }
         const int64_t t0 = now_ns();
-        ids.resize(take.size());
-        res.assign(take.size(), Engine::GridResult{});
         int32_t rc = 0;
+        ids.clear();
         {
             std::lock_guard<std::mutex> lk(u->eng_mu);
-            for (size_t i = 0; i < take.size() && rc == 0; ++i) {
-                const int32_t lid = local_of_[take[i].grid];
-                ids[i] = lid;
-                if (take[i].branch >= 0) rc = u->eng->batch_set_branch_status(lid, take[i].branch, take[i].closed);
-                if (rc == 0) rc = u->eng->batch_set_telemetry(lid, take[i].z.data(), static_cast<int32_t>(take[i].z.size()));
+            for (auto& r : starting) {
+                const int32_t lid = local_of_[r.grid];
+                if (rc == 0 && r.branch >= 0) rc = u->eng->batch_set_branch_status(lid, r.branch, r.closed);
+                if (rc == 0) rc = u->eng->batch_set_telemetry(lid, r.z.data(), static_cast<int32_t>(r.z.size()));
+                ids.push_back(lid);
             }
-            if (rc == 0) rc = u->eng->batch_solve(static_cast<int32_t>(ids.size()), ids.data(), nullptr, rq, res.data());
+            if (rc == 0 && !ids.empty()) rc = u->eng->stream_activate(static_cast<int32_t>(ids.size()), ids.data(), nullptr);
+            for (auto& r : starting) active[local_of_[r.grid]] = Running{std::move(r), t0};
+            if (rc == 0) rc = u->eng->stream_step(done, res);
         }
         const int64_t t1 = now_ns();
-        for (size_t i = 0; i < take.size(); ++i) {
-            ServeResult r;
-            if (rc == 0) {
+        const int32_t in_batch = static_cast<int32_t>(active.size());
+        int64_t completed = 0;
+        if (rc != 0) {
+            // an engine error ends every request in the batch
+            for (auto& kv : active) {
+                ServeResult r;
+                r.status = CONV_DIVERGED;
+                r.batch_size = in_batch;
+                r.t_submit_ns = kv.second.req.t_submit;
+                r.t_start_ns = kv.second.t_start;
+                r.t_done_ns = t1;
+                finish(kv.second.req.ticket, r);
+                ++completed;
+            }
+            active.clear();
+            std::lock_guard<std::mutex> lk(u->eng_mu);
+            u->eng->stream_begin(rq);
+        } else {
+            for (size_t i = 0; i < done.size(); ++i) {
+                auto it = active.find(done[i]);
+                if (it == active.end()) continue;
+                ServeResult r;
                 r.status = res[i].status;
                 r.iterations = res[i].iterations;
                 r.max_mismatch = res[i].max_mismatch;
                 r.objective = res[i].objective;
-            } else {
-                r.status = CONV_DIVERGED;
+                r.batch_size = in_batch;
+                r.t_submit_ns = it->second.req.t_submit;
+                r.t_start_ns = it->second.t_start;
+                r.t_done_ns = t1;
+                finish(it->second.req.ticket, r);
+                active.erase(it);
+                ++completed;
             }
-            r.batch_size = static_cast<int32_t>(take.size());
-            r.t_submit_ns = take[i].t_submit;
-            r.t_start_ns = t0;
-            r.t_done_ns = t1;
-            finish(take[i].ticket, r);
         }
         std::lock_guard<std::mutex> lk(st_mu_);
-        stats_.completed += static_cast<int64_t>(take.size());
-        stats_.grid_solves += static_cast<int64_t>(take.size());
+        stats_.completed += completed;
+        stats_.grid_solves += completed;
         ++stats_.passes;
     }
 }

@@ -5,11 +5,13 @@
 // batch Engine whose Gauss-Newton loop solves all grids with pending
 // requests together.  A grid at or above `own_unit_bus` gets a unit of its
 // own.  Every unit has its own CUDA stream and worker thread, so the units'
-// work overlaps on the device.  A worker takes, for every grid of its unit, the
-// oldest pending request and solves them as one batch; requests that arrive
-// meanwhile wait for the unit's next pass (continuous batching).  Each grid
-// hot-starts from its last state.  A grid stops on its own convergence
-// test, so its result does not depend on which other requests share the pass.
+// work overlaps on the device.  A unit's worker runs its batch one
+// Gauss-Newton iteration at a time; between iterations every grid with a
+// pending request that is not already in the batch joins it (its oldest
+// request), and after each iteration the grids that finished answer and
+// leave (iteration-level continuous batching).  Each grid hot-starts from its
+// last state and stops on its own convergence test, so its result does not
+// depend on which other requests share the batch.
 //
 // Admission: units are made resident in order (small units first) while the
 // sum of their device arenas stays within the memory budget; requests for
@@ -52,12 +54,12 @@ struct ServeResult {
     double max_mismatch = 0.0;
     double objective = 0.0;
     int32_t admitted = 1;
-    int32_t batch_size = 0;  // grids solved in the same pass
+    int32_t batch_size = 0;  // grids in the batch at the iteration that finished this request
     int64_t t_submit_ns = 0, t_start_ns = 0, t_done_ns = 0;  // steady clock
 };
 
 struct ServeStats {
-    int64_t submitted = 0, completed = 0, rejected = 0, passes = 0, grid_solves = 0;
+    int64_t submitted = 0, completed = 0, rejected = 0, passes = 0, grid_solves = 0;  // passes = iterations run
     int32_t units = 0, admitted_units = 0, grids = 0;
     size_t device_bytes = 0, budget_bytes = 0;
 };
