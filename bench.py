@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid10k-steps", type=int, default=40)
     ap.add_argument("--skip-extra", action="store_true", help="headline legs only")
+    ap.add_argument("--only", choices=["batch512", "grid200k", "grid10k"],
+                    help="run one secondary configuration alone and print its object (for profiling)")
     return ap.parse_args()
 
 
@@ -451,16 +453,19 @@ def run_per_grid_fp64(stream, local, lo, hi):
 
 
 def run_batch512():
-    from state_estimation_with_cuda_gb300 import BatchEstimator, workloads
+    """Batched form with the autotuned schedule (tuned.json: size buckets solved
+    concurrently, phase-A width); falls back to one bucket of all grids."""
+    from state_estimation_with_cuda_gb300 import workloads
+    from state_estimation_with_cuda_gb300.tune import BatchSet, tuned_config
 
+    best = tuned_config().get("batch", {}).get("best", {})
+    bounds = tuple(best.get("bucket_bus", ()))
+    width = best.get("flow_small_f")
     grids = workloads.batch_grids(512)
     snaps = [[g.renoise(u).copy() for g in grids] for u in range(3)]
     out = {}
     for mixed in (True, False):
-        b = BatchEstimator(mixed=mixed)
-        for g in grids:
-            b.add_grid(g)
-        b.upload_model()
+        b = BatchSet(grids, bounds, mixed=mixed, flow_small_f=width)
         b.solve(flat_start=True)
         times, its = [], []
         for u in range(3):
@@ -477,9 +482,12 @@ def run_batch512():
                                              "iterations_mean": round(float(np.mean(its)), 3),
                                              "iterations_max": int(max(its))}
     out["config"] = ("512 grids, log-uniform 30..5000 buses (%d buses, %d rows); hot start after a 1%% re-noise; "
-                     "all grids in one batch (one pass of each kernel per Gauss-Newton step)"
-                     % (sum(g.n_bus for g in grids), sum(g.n_meas for g in grids)))
+                     "size buckets %s (one batch each, solved concurrently), phase-A width %s; "
+                     "wall clock including the telemetry copies"
+                     % (sum(g.n_bus for g in grids), sum(g.n_meas for g in grids), list(bounds) or "[all]",
+                        width or 64))
     out["unit"] = "solves/s"
+    out["schedule_source"] = "tuned.json" if best else "defaults"
     return out
 
 
@@ -633,6 +641,23 @@ def main():
     args = parse()
     world, rank, local = dist_setup()
     lo, hi = args.warmup, args.warmup + args.steps
+    if args.only:
+        if args.only == "batch512":
+            out = run_batch512()
+        elif args.only == "grid200k":
+            out = run_grid200k()
+        else:
+            from state_estimation_with_cuda_gb300 import workloads
+
+            a10 = argparse.Namespace(**vars(args))
+            a10.steps, a10.warmup = args.grid10k_steps, 3
+            g10 = workloads.make("grid10k")
+            snaps10 = [g10.renoise(u).copy() for u in range(a10.warmup + a10.steps)]
+            out = summarize_leg(run_leg(a10, g10, snaps10, local, True, world),
+                                run_leg(a10, g10, snaps10, local, False, world), g10, a10, world)
+        if rank == 0:
+            print(json.dumps({"only": args.only, **out}))
+        return
     if args.impl == "reference":
         if rank != 0:
             return

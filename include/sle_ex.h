@@ -48,7 +48,11 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
  *                           (default 0: the Gauss-Newton loop itself re-forms
  *                           the FP64 residual and gradient every step)
  *   "big_front_flops"       FP64: fronts with more factor flops than this use
- *                           the tiled multi-CTA kernels (re-uploads) */
+ *                           the tiled multi-CTA kernels (re-uploads)
+ *   "dataflow"              1 (default): persistent dataflow kernels for the
+ *                           fronts below the tiled ones and for the solves
+ *   "flow_small_f"          widest front of the high-occupancy dataflow phase
+ *                           (default 64, at most 128; re-uploads) */
 SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* key, double value);
 
 typedef struct SLE_ExPlanInfo {

@@ -331,8 +331,17 @@ class Server:
     """Serving runtime (sle_ExServer*; no reference counterpart): a resident
     fleet answering snapshots as they arrive, with continuous batching."""
 
-    def __init__(self, mixed=True, max_iterations=20, tolerance=1e-6, bucket_bus=(300, 2000, 20000, 0),
-                 own_unit_bus=1 << 30, memory_budget=0, robust=False, huber_gamma=1.5, device_id=0):
+    def __init__(self, mixed=True, max_iterations=20, tolerance=1e-6, bucket_bus=None, own_unit_bus=None,
+                 memory_budget=0, robust=False, huber_gamma=1.5, device_id=0):
+        """bucket_bus / own_unit_bus default to the autotuned values shipped in
+        tuned.json (see tune.py), else (300, 2000, 20000, 0) / no own units."""
+        from .tune import tuned_config
+
+        best = tuned_config().get("serving", {}).get("best", {})
+        if bucket_bus is None:
+            bucket_bus = tuple(best.get("bucket_bus", (300, 2000, 20000, 0)))
+        if own_unit_bus is None:
+            own_unit_bus = int(best.get("own_unit_bus", 1 << 30))
         self.lib = N.sle_lib()
         c = N.SLE_ExServerConfig()
         self.lib.sle_ExServerDefaultConfig(ctypes.byref(c))

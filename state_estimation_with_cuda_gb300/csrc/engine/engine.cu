@@ -175,7 +175,8 @@ void Engine::build_schedule() {
     }
     // Dataflow phases: a front whose subtree holds no big front is factorised
     // by the persistent kernels (phase A if no front of its subtree is wider
-    // than kFlowSmallF, phase B otherwise); the rest stays level-synchronous.
+    // than cfg.flow_small_f, phase B otherwise); the rest stays level-synchronous.
+    const int32_t flow_small_f = std::max(8, std::min(cfg.flow_small_f, kFlowSmallFMax));
     std::vector<char> sub_big(ns, 0);
     std::vector<int32_t> sub_maxf(ns, 0);
     for (int32_t l = 0; l < nl; ++l)
@@ -191,7 +192,7 @@ void Engine::build_schedule() {
         }
     flow_phase_.assign(ns, 0);
     for (int32_t s = 0; s < ns; ++s)
-        if (cfg.dataflow && !sub_big[s]) flow_phase_[s] = sub_maxf[s] <= kFlowSmallF ? 1 : 2;
+        if (cfg.dataflow && !sub_big[s]) flow_phase_[s] = sub_maxf[s] <= flow_small_f ? 1 : 2;
     int64_t lx = 0, uu = 0;
     for (int32_t s = 0; s < ns; ++s) {
         const int64_t f = P.sn_f[s], nc = P.sn_c0[s + 1] - P.sn_c0[s];

@@ -42,6 +42,7 @@ struct EngineConfig {
     double big_front_flops = 2.0e5;  // FP64: fronts above this many factor flops use the tiled multi-CTA path
     int32_t refine_steps = 0;        // mixed precision: extra refinement steps per Gauss-Newton step
     int32_t dataflow = 1;            // persistent dataflow kernels below the big fronts and for the solves
+    int32_t flow_small_f = 64;       // widest front of the high-occupancy dataflow phase (<= kFlowSmallFMax)
 };
 
 enum class Mode : int32_t { REALTIME = 0, PRECISION = 1 };

@@ -548,21 +548,44 @@ __global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, 
         D[i + j * ld] = (i >= j) ? B[(p0 + i) + (int64_t)(p0 + j) * f] : T(0);
     }
     __syncthreads();
-    // one warp factors the tile in registers: lane i owns row i
+    // one warp factors the tile, lane i owning row i: FP32 in registers with
+    // shuffles; FP64 through shared memory (a shuffle moves half a double, so
+    // the register form is slower for FP64)
     if (threadIdx.x < 32) {
         const int i = threadIdx.x;
-        T a[kTile];
+        if constexpr (sizeof(T) == 4) {
+            T a[kTile];
 #pragma unroll
-        for (int j = 0; j < kTile; ++j) a[j] = (i < pb && j <= i) ? D[i + j * ld] : T(0);
-        T inv;
-        const bool bad = warp_potrf<T, kTile>(a, pb, i, &inv);
-        if (bad && i == 0) atomicOr(singular_flags(F, W, s), FLAG_SINGULAR);
+            for (int j = 0; j < kTile; ++j) a[j] = (i < pb && j <= i) ? D[i + j * ld] : T(0);
+            T inv;
+            const bool bad = warp_potrf<T, kTile>(a, pb, i, &inv);
+            if (bad && i == 0) atomicOr(singular_flags(F, W, s), FLAG_SINGULAR);
 #pragma unroll
-        for (int j = 0; j < kTile; ++j)
-            if (i < pb && j <= i) D[i + j * ld] = a[j];
-        if (i < pb) {
-            rdiag[i] = inv;
-            reinterpret_cast<T*>(W.rdiag)[F.sn_c0[s] + p0 + i] = inv;
+            for (int j = 0; j < kTile; ++j)
+                if (i < pb && j <= i) D[i + j * ld] = a[j];
+            if (i < pb) {
+                rdiag[i] = inv;
+                reinterpret_cast<T*>(W.rdiag)[F.sn_c0[s] + p0 + i] = inv;
+            }
+        } else {
+            for (int k = 0; k < pb; ++k) {
+                if (i == k) {
+                    T sq, inv;
+                    pivot(D[k + k * ld], &sq, &inv, singular_flags(F, W, s));
+                    D[k + k * ld] = sq;
+                    rdiag[k] = inv;
+                    reinterpret_cast<T*>(W.rdiag)[F.sn_c0[s] + p0 + k] = inv;
+                }
+                __syncwarp();
+                const T inv = rdiag[k];
+                if (i > k && i < pb) D[i + k * ld] *= inv;
+                __syncwarp();
+                if (i > k && i < pb) {
+                    const T lik = D[i + k * ld];
+                    for (int j = k + 1; j <= i; ++j) D[i + j * ld] -= lik * D[j + k * ld];
+                }
+                __syncwarp();
+            }
         }
     }
     __syncthreads();
@@ -582,47 +605,48 @@ __global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, 
     }
 }
 
-// Panel step p, part 2 (one CTA per row tile ti > p): X = A L_dd^-T with the
-// diagonal tile factored by part 1.
+// Panel step p, part 2: X = A L_dd^-T for the row tiles ti > p.  One warp
+// per row tile and one lane per row: forward substitution in registers
+// against the factored diagonal tile, staged transposed in shared memory.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_big_trsm(DevFactor F, T* lx, const void* Wrdiag, const int4* work, int p) {
-    constexpr int ld = kTile + 1;
-    __shared__ T D[kTile * ld];
-    __shared__ T A[kTile * ld];
-    __shared__ T rdiag[kTile];
-    const int4 wk = work[blockIdx.x];
+constexpr int kTrsmWarps = sizeof(T) == 4 ? 8 : 4;
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kTrsmWarps<T>) k_big_trsm(DevFactor F, T* lx, const void* Wrdiag,
+                                                                 const int4* work, int n_work, int p) {
+    __shared__ T lt[kTrsmWarps<T>][kTile][kTile + 1];
+    __shared__ T rinv[kTrsmWarps<T>][kTile];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int item = blockIdx.x * kTrsmWarps<T> + warp;
+    if (item >= n_work) return;  // the whole warp; no block barrier follows
+    const int4 wk = work[item];
     const int s = wk.x, ti = wk.y;
     const int f = F.sn_f[s];
     const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
+    const T* Bc = lx + F.sn_lx_off[s];
     T* B = lx + F.sn_lx_off[s];
     const int p0 = p * kTile;
     const int pb = min(kTile, nc - p0);
-    const int r0 = ti * kTile, nr = min(kTile, f - r0);
-    const int c0s = F.sn_c0[s];
-    for (int x = threadIdx.x; x < pb * pb; x += blockDim.x) {
-        const int i = x % pb, j = x / pb;
-        D[i + j * ld] = (i >= j) ? B[(p0 + i) + (int64_t)(p0 + j) * f] : T(0);
-    }
-    for (int x = threadIdx.x; x < nr * pb; x += blockDim.x) {
-        const int i = x % nr, j = x / nr;
-        A[i + j * ld] = B[(r0 + i) + (int64_t)(p0 + j) * f];
-    }
-    __syncthreads();
-    if (threadIdx.x < pb) rdiag[threadIdx.x] = reinterpret_cast<const T*>(Wrdiag)[c0s + p0 + threadIdx.x];
-    __syncthreads();
-    // column sweep: all rows of the tile advance together, one column per step
-    for (int c = 0; c < pb; ++c) {
-        if (threadIdx.x < nr) A[threadIdx.x + c * ld] *= rdiag[c];
-        __syncthreads();
-        for (int x = threadIdx.x; x < nr * (pb - c - 1); x += blockDim.x) {
-            const int i = x % nr, j = c + 1 + x / nr;
-            A[i + j * ld] -= A[i + c * ld] * D[j + c * ld];
+    for (int c = 0; c < pb; ++c)
+        lt[warp][c][lane] = (lane < pb && lane > c) ? Bc[(p0 + lane) + (int64_t)(p0 + c) * f] : T(0);
+    if (lane < pb) rinv[warp][lane] = reinterpret_cast<const T*>(Wrdiag)[F.sn_c0[s] + p0 + lane];
+    __syncwarp();
+    const int r = ti * kTile + lane;
+    if (r < f) {
+        T x[kTile];
+#pragma unroll
+        for (int c = 0; c < kTile; ++c) x[c] = (c < pb) ? Bc[r + (int64_t)(p0 + c) * f] : T(0);
+#pragma unroll
+        for (int c = 0; c < kTile; ++c) {
+            if (c < pb) {
+                x[c] *= rinv[warp][c];
+#pragma unroll
+                for (int c2 = c + 1; c2 < kTile; ++c2) x[c2] -= x[c] * lt[warp][c][c2];
+            }
         }
-        __syncthreads();
-    }
-    for (int x = threadIdx.x; x < nr * pb; x += blockDim.x) {
-        const int i = x % nr, j = x / nr;
-        B[(r0 + i) + (int64_t)(p0 + j) * f] = A[i + j * ld];
+#pragma unroll
+        for (int c = 0; c < kTile; ++c)
+            if (c < pb) B[r + (int64_t)(p0 + c) * f] = x[c];
     }
 }
 
@@ -860,6 +884,9 @@ cudaError_t prepare_impl() {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_front_flow<T, kPanel, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)front_smem<T>(small_front_max<T>()));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_front_flow<T, kPanelSmall, kMinBlocksA<T>>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)front_smem<T>(kFlowSmallFMax));
     const int mx = (int)solve_smem<double>(16384);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fwd<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bwd<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -915,7 +942,8 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
                     ++g_kernel_launches;
                 }
                 if (npan > 0) {
-                    k_big_trsm<T><<<npan, kThreads, 0, st>>>(F, lx, W.rdiag, ls.d_pan + ls.h_pan_ptr[slot], p);
+                    k_big_trsm<T><<<(npan + kTrsmWarps<T> - 1) / kTrsmWarps<T>, 32 * kTrsmWarps<T>, 0, st>>>(
+                        F, lx, W.rdiag, ls.d_pan + ls.h_pan_ptr[slot], npan, p);
                     ++g_kernel_launches;
                 }
                 if (nupd > 0) {

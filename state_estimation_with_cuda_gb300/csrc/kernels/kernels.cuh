@@ -223,7 +223,7 @@ struct LevelSchedule {
     const int32_t* h_lvl_maxf = nullptr;    // [n_levels] largest front per level
     const int64_t* h_lvl_maxpanel = nullptr;  // [n_levels] largest f * nc per level
     // dataflow phases of the factorisation (fronts below every big front):
-    // A = fronts whose whole subtree has f <= kFlowSmallF, B = the rest.  A
+    // A = fronts whose whole subtree has f <= flow_small_f, B = the rest.  A
     // CTA claims an initially ready front of its phase (no children in the
     // phase) and, when it completes the last child of a parent in the same
     // phase, goes on with that parent; CTAs exit when nothing is left.
@@ -255,8 +255,9 @@ cudaError_t launch_batch_objective(const DevNet& net, const DevWork& w, const De
 cudaError_t launch_batch_activate(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st);
 cudaError_t launch_batch_retire(const DevBatch& b, cudaStream_t st);
 
-// Largest front of the high-occupancy dataflow phase.
-constexpr int32_t kFlowSmallF = 64;
+// Largest front the high-occupancy dataflow phase may hold (its kernel keeps
+// 16-column panels and a register budget for several CTAs per SM).
+constexpr int32_t kFlowSmallFMax = 128;
 
 // Resident-CTA grid sizes of the persistent dataflow kernels (0 = cannot run).
 struct FlowGrids {
