@@ -164,6 +164,13 @@ class Estimator:
     def flat_start(self):
         self._check(self.lib.sle_ApplyFlatStart(self.h))
 
+    def check_observability(self):
+        """(observable, islands): topological check, on the device once uploaded."""
+        obs = ctypes.c_int32()
+        isl = ctypes.c_int32()
+        self._check(self.lib.sle_CheckObservability(self.h, ctypes.byref(obs), ctypes.byref(isl)))
+        return bool(obs.value), isl.value
+
     # -- results ------------------------------------------------------------------------
     def counts(self):
         return (self.lib.sle_GetBusCount(self.h), self.lib.sle_GetBranchCount(self.h),

@@ -692,25 +692,31 @@ SLE_API SLE_StatusCode SLE_CALL sle_SolveWithConfig(SLE_Handle handle, const SLE
 
 SLE_API SLE_StatusCode SLE_CALL sle_CheckObservability(SLE_Handle handle, int32_t* is_observable, int32_t* islands) {
     if (!handle) return SLE_ERROR_INVALID_HANDLE;
-    // Topological check (sle_engine.cu:684-753): union-find over closed
-    // branches, then enough measurements for the states.
-    auto& M = E(handle)->model;
+    // Topological check (sle_engine.cu:684-753): one island over the closed
+    // branches and at least as many active rows as states.  On an uploaded
+    // model the islands are labelled on the device; before the first upload
+    // the host model is checked the same way.
+    Engine* en = E(handle);
+    auto& M = en->model;
     const int32_t n = M.n_bus();
-    std::vector<int32_t> par(n);
-    for (int32_t i = 0; i < n; ++i) par[i] = i;
-    auto find = [&](int32_t x) {
-        while (par[x] != x) x = par[x] = par[par[x]];
-        return x;
-    };
-    for (int32_t k = 0; k < M.n_branch(); ++k)
-        if (M.br_closed[k]) {
-            const int32_t a = find(M.br_from[k]), b = find(M.br_to[k]);
-            if (a != b) par[a] = b;
-        }
-    int32_t count = 0;
-    for (int32_t i = 0; i < n; ++i) count += (find(i) == i);
-    int32_t active = 0;
-    for (int32_t q = 0; q < M.n_meas(); ++q) active += M.m_active[q];
+    int32_t count = 0, active = 0;
+    if (en->uploaded() && !M.structure_dirty && !en->batch_mode()) {
+        if (en->check_islands(&count, &active) != 0) return fail(SLE_ERROR_CUDA_FAILURE, en->last_error);
+    } else {
+        std::vector<int32_t> par(n);
+        for (int32_t i = 0; i < n; ++i) par[i] = i;
+        auto find = [&](int32_t x) {
+            while (par[x] != x) x = par[x] = par[par[x]];
+            return x;
+        };
+        for (int32_t k = 0; k < M.n_branch(); ++k)
+            if (M.br_closed[k]) {
+                const int32_t a = find(M.br_from[k]), b = find(M.br_to[k]);
+                if (a != b) par[a] = b;
+            }
+        for (int32_t i = 0; i < n; ++i) count += (find(i) == i);
+        for (int32_t q = 0; q < M.n_meas(); ++q) active += M.m_active[q];
+    }
     const bool obs = n > 0 && count == 1 && active >= 2 * n - 1;
     if (is_observable) *is_observable = obs ? 1 : 0;
     if (islands) *islands = count;

@@ -92,7 +92,8 @@ int32_t Engine::initialize() {
         return -4;
     }
     if ((e = cudaSetDevice(cfg.device_id)) != cudaSuccess) return set_cuda_error(e, "cudaSetDevice");
-    if ((e = cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking)) != cudaSuccess) return set_cuda_error(e, "stream");
+    if ((e = cudaStreamCreateWithPriority(&st_, cudaStreamNonBlocking, cfg.stream_priority)) != cudaSuccess)
+        return set_cuda_error(e, "stream");
     cudaEventCreate(&ev0_);
     cudaEventCreate(&ev1_);
     if ((e = cudaMallocHost(&h_status_, sizeof(DevStatus))) != cudaSuccess) return set_cuda_error(e, "cudaMallocHost");
@@ -442,6 +443,8 @@ int32_t Engine::upload() {
         work_.ocnt = c.take<int32_t>(nparts);
         work_.status = c.take<DevStatus>(1);
         work_.grid_flags = batch_mode() ? batch_.flags : nullptr;
+        isl_parent_ = c.take<int32_t>(n);
+        isl_out_ = c.take<int32_t>(4);
     };
     Carver dry(nullptr);
     layout(dry);
@@ -717,7 +720,7 @@ int32_t Engine::stage_begin(int32_t stage) {
 }
 
 void Engine::stage_end(int32_t stage, int32_t mark, int64_t launches_before) {
-    stats.launches[stage] += g_kernel_launches.load() - launches_before;
+    stats.launches[stage] += t_kernel_launches - launches_before;
     stats.calls[stage] += 1;
     if (mark >= 0) cudaEventRecord(ev_pool_[mark + 1], st_);
 }
@@ -741,10 +744,10 @@ int32_t Engine::enqueue_iteration(const SolveParams& sp, bool refactor, int64_t*
     };
     auto stage = [&](int32_t st, auto&& fn) {
         if (e != cudaSuccess) return;
-        const int64_t l0 = g_kernel_launches.load();
+        const int64_t l0 = t_kernel_launches;
         const int32_t mk = stage_begin(st);
         e = fn();
-        if (per_stage) per_stage[st] += g_kernel_launches.load() - l0;
+        if (per_stage) per_stage[st] += t_kernel_launches - l0;
         if (mk >= 0) cudaEventRecord(ev_pool_[mk + 1], st_);
     };
     stage(ST_EVALUATE, [&] { return launch_evaluate(net_, work_, sp, st_); });
@@ -803,11 +806,12 @@ int32_t Engine::run_iteration(const SolveParams& sp, bool refactor) {
             cudaGraph_t graph = nullptr;
             cudaError_t e = cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal);
             if (e != cudaSuccess) return set_cuda_error(e, "graph capture");
-            const int64_t before = g_kernel_launches.load();
+            const int64_t before = t_kernel_launches;
             const int32_t rc = enqueue_iteration(sp, refactor, g.launches);
             e = cudaStreamEndCapture(st_, &graph);
-            g.total = g_kernel_launches.load() - before;
+            g.total = t_kernel_launches - before;
             g_kernel_launches -= g.total;  // counted when the graph runs
+            t_kernel_launches -= g.total;
             if (rc) {
                 if (graph) cudaGraphDestroy(graph);
                 return rc;
@@ -920,7 +924,7 @@ int32_t Engine::solve(const SolveRequest& rq, SolveResult& out) {
     if (diverged) factor_valid_ = false;
     // final evaluation at the returned state: objective, residuals, bad data
     {
-        const int64_t l0 = g_kernel_launches.load();
+        const int64_t l0 = t_kernel_launches;
         const int32_t mk = stage_begin(ST_OTHER);
         launch_evaluate(net_, work_, sp, st_);
         launch_objective(net_, work_, cfg.bad_data_threshold, st_);
@@ -1091,6 +1095,26 @@ int32_t Engine::factor_and_solve_noalloc(const double* rhs_orig, double* x_orig)
         return -3;
     }
     return (h_status_->flags & FLAG_SINGULAR) ? -7 : 0;
+}
+
+int32_t Engine::check_islands(int32_t* islands, int32_t* active_rows) {
+    if (!uploaded_) {
+        last_error = "no model on the device";
+        return -4;
+    }
+    cudaSetDevice(cfg.device_id);
+    cudaError_t e = launch_islands(net_, isl_parent_, isl_out_, 1000, st_);
+    int32_t out[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, isl_out_, sizeof(out), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "islands");
+    if (out[2] < 0) {
+        last_error = "island labelling did not settle";
+        return -3;
+    }
+    if (islands) *islands = out[0];
+    if (active_rows) *active_rows = out[1];
+    return 0;
 }
 
 int32_t Engine::max_solve_front() const {

@@ -43,6 +43,7 @@ struct EngineConfig {
     int32_t refine_steps = 0;        // mixed precision: extra refinement steps per Gauss-Newton step
     int32_t dataflow = 1;            // persistent dataflow kernels below the big fronts and for the solves
     int32_t flow_small_f = 64;       // widest front of the high-occupancy dataflow phase (<= kFlowSmallFMax)
+    int32_t stream_priority = 0;     // CUDA stream priority of the engine's stream (lower = more urgent)
 };
 
 enum class Mode : int32_t { REALTIME = 0, PRECISION = 1 };
@@ -115,6 +116,9 @@ public:
     // model needs more scratch than kNoAllocScratchBytes.
     int32_t factor_and_solve_noalloc(const double* rhs_orig, double* x_orig);
     int32_t export_ybus(std::vector<double>& g, std::vector<double>& b);
+    // Topological islands of the uploaded network (closed branches) and the
+    // active measurement rows, computed on the device.
+    int32_t check_islands(int32_t* islands, int32_t* active_rows);
     int32_t export_eval(double* hval, double* hx, double* rhs_orig);
 
     // Measurement hooks.
@@ -207,6 +211,8 @@ private:
     int8_t* d_phase_ = nullptr;
     int32_t* d_phase_nchild_ = nullptr;
     int32_t* d_nchild_ = nullptr;
+    int32_t* isl_parent_ = nullptr;
+    int32_t* isl_out_ = nullptr;
     int32_t max_solve_front() const;
     // batch state
     std::vector<GridSpan> grids_;

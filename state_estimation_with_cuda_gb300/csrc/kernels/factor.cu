@@ -901,7 +901,7 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
     T* gv = reinterpret_cast<T*>(W.gvals);
     if (ls.n_tgt > 0) {
         k_gain_values<T, HV><<<grid_for(ls.n_tgt, 256), 256, 0, st>>>(net, F, W, hval, gv, ls.n_tgt);
-        ++g_kernel_launches;
+        count_launches(1);
     }
     if (ls.flow_a_n + ls.flow_b_n > 0) {
         cudaError_t e = cudaMemsetAsync(W.flow, 0, sizeof(int) * (size_t)(F.n_super + 8), st);
@@ -911,13 +911,13 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
             const int mf = ls.flow_a_maxf;
             k_front_flow<T, kPanelSmall, kMinBlocksA<T>><<<ls.flow_a_grid, kThreads, front_smem<T>(mf), st>>>(
                 F, W, gv, lx, ub, ls.d_flow_a, ls.flow_a_n, ls.d_phase, 1, ls.d_phase_nchild, counters + 0, W.flow);
-            ++g_kernel_launches;
+            count_launches(1);
         }
         if (ls.flow_b_n > 0) {
             const int mf = ls.flow_b_maxf;
             k_front_flow<T, kPanel, 1><<<ls.flow_b_grid, kThreads, front_smem<T>(mf), st>>>(
                 F, W, gv, lx, ub, ls.d_flow_b, ls.flow_b_n, ls.d_phase, 2, ls.d_phase_nchild, counters + 1, W.flow);
-            ++g_kernel_launches;
+            count_launches(1);
         }
     }
     for (int l = 0; l < ls.n_levels; ++l) {
@@ -926,12 +926,12 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
             const int mf = ls.h_small_maxf[l];
             k_front_small<T><<<ns, kThreads, front_smem<T>(mf), st>>>(F, W, gv, lx, ub,
                                                                                   ls.d_small + ls.h_small_ptr[l]);
-            ++g_kernel_launches;
+            count_launches(1);
         }
         const int na = ls.h_asm_ptr[l + 1] - ls.h_asm_ptr[l];
         if (na > 0) {
             k_big_assemble<T><<<na, kThreads, 0, st>>>(F, gv, lx, ub, ls.d_asm + ls.h_asm_ptr[l]);
-            ++g_kernel_launches;
+            count_launches(1);
             for (int p = 0; p < ls.h_lvl_panels[l]; ++p) {
                 const int slot = ls.h_step_ptr[l] + p;
                 const int npot = ls.h_pot_ptr[slot + 1] - ls.h_pot_ptr[slot];
@@ -939,16 +939,16 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
                 const int nupd = ls.h_upd_ptr[slot + 1] - ls.h_upd_ptr[slot];
                 if (npot > 0) {
                     k_big_potrf<T><<<npot, kThreads, 0, st>>>(F, W, lx, ls.d_pot + ls.h_pot_ptr[slot], p);
-                    ++g_kernel_launches;
+                    count_launches(1);
                 }
                 if (npan > 0) {
                     k_big_trsm<T><<<(npan + kTrsmWarps<T> - 1) / kTrsmWarps<T>, 32 * kTrsmWarps<T>, 0, st>>>(
                         F, lx, W.rdiag, ls.d_pan + ls.h_pan_ptr[slot], npan, p);
-                    ++g_kernel_launches;
+                    count_launches(1);
                 }
                 if (nupd > 0) {
                     k_big_update<T><<<nupd, kThreads, 0, st>>>(F, lx, ls.d_upd + ls.h_upd_ptr[slot], p);
-                    ++g_kernel_launches;
+                    count_launches(1);
                 }
             }
         }
@@ -972,7 +972,7 @@ cudaError_t solve_impl(const DevFactor& F, const DevWork& W, const LevelSchedule
                                                              counters + 0, fwd_done);
         k_bwd_flow<T, T><<<ls.solve_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_down, ns, counters + 1,
                                                                 bwd_done);
-        g_kernel_launches += 2;
+        count_launches(2);
         return cudaGetLastError();
     }
     for (int l = 0; l < ls.n_levels; ++l) {
@@ -980,7 +980,7 @@ cudaError_t solve_impl(const DevFactor& F, const DevWork& W, const LevelSchedule
         if (n > 0) {
             k_fwd<T, T><<<n, kThreads, solve_smem<T>(ls.h_lvl_maxf[l]), st>>>(F, lx, rdiag, sv,
                                                                                ls.d_all + ls.h_all_ptr[l]);
-            ++g_kernel_launches;
+            count_launches(1);
         }
     }
     for (int l = ls.n_levels - 1; l >= 0; --l) {
@@ -988,7 +988,7 @@ cudaError_t solve_impl(const DevFactor& F, const DevWork& W, const LevelSchedule
         if (n > 0) {
             k_bwd<T, T><<<n, kThreads, solve_smem<T>(ls.h_lvl_maxf[l]), st>>>(F, lx, rdiag, sv,
                                                                                ls.d_all + ls.h_all_ptr[l]);
-            ++g_kernel_launches;
+            count_launches(1);
         }
     }
     return cudaGetLastError();
@@ -1049,7 +1049,7 @@ cudaError_t launch_gain_export(const DevNet& net, const DevFactor& F, const DevW
                                cudaStream_t st) {
     if (n_tgt > 0) {
         k_gain_export<double><<<grid_for(n_tgt, 256), 256, 0, st>>>(net, F, W, W.hval, n_tgt, out);
-        ++g_kernel_launches;
+        count_launches(1);
     }
     return cudaGetLastError();
 }
@@ -1149,7 +1149,7 @@ cudaError_t launch_factor_solve_noalloc(const DevNet& net, const DevFactor& F, c
     if (e != cudaSuccess) return e;
     if (n > 0) {
         k_state_to_ps<<<grid_for(n, 256), 256, 0, st>>>(net, F, d_rhs, W2.rhs);
-        ++g_kernel_launches;
+        count_launches(1);
     }
     e = factor_impl<double, double>(net, F, W2, ls, W2.hval, W2.lx, W2.u, st);
     if (e == cudaSuccess)
@@ -1158,7 +1158,7 @@ cudaError_t launch_factor_solve_noalloc(const DevNet& net, const DevFactor& F, c
     if (e != cudaSuccess) return e;
     if (n > 0) {
         k_ps_to_state<<<grid_for(n, 256), 256, 0, st>>>(net, F, W2.sol, d_x);
-        ++g_kernel_launches;
+        count_launches(1);
     }
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(x_host, d_x, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, st);

@@ -249,6 +249,14 @@ cudaError_t launch_batch_begin(const DevNet& net, const DevWork& w, const DevBat
 cudaError_t launch_batch_update(const DevNet& net, const DevFactor& f, const DevWork& w, const DevBatch& b,
                                 const SolveParams& sp, const double* step, cudaStream_t st);
 cudaError_t launch_batch_objective(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st);
+// Topological islands (connected components over closed branches) on the
+// device: parent[n_bus] is scratch, out[0] = islands, out[1] = active rows.
+// Hooking of component roots along every closed branch (the larger root
+// points at the smaller) alternates with pointer jumping until no branch
+// joins two components; bounded by `max_rounds` (out[2] = rounds used, -1
+// when the bound was hit).
+cudaError_t launch_islands(const DevNet& net, int32_t* parent, int32_t* out, int32_t max_rounds, cudaStream_t st);
+
 // Stream mode (grids join and leave between iterations): activate the grids
 // with active[g] = 1 (flags cleared, flat start if flat[g]), leaving the
 // others as they are; retire the grids with retire[g] = 1 (frozen, inactive).
@@ -296,6 +304,13 @@ cudaError_t launch_solve32(const DevFactor& f, const DevWork& w, const LevelSche
 
 // Kernels launched by this library since load (all engines of the process).
 extern std::atomic<int64_t> g_kernel_launches;
+// Launches issued by the calling thread (graph captures count their own
+// launches without seeing other threads').
+extern thread_local int64_t t_kernel_launches;
+inline void count_launches(int64_t n) {
+    g_kernel_launches += n;
+    t_kernel_launches += n;
+}
 
 // Largest front (rows) handled by the single-CTA shared-memory kernel:
 // 160 x 160 doubles or 224 x 224 floats (<= 200 KiB of shared memory).

@@ -505,6 +505,48 @@ __global__ void k_batch_begin(DevNet net, DevWork w, DevBatch b) {
     }
 }
 
+// f2: islands of the closed-branch graph (the reference's topological check,
+// sle_engine.cu:684-753, on the device).
+__global__ void k_island_init(DevNet net, int32_t* parent, int32_t* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < net.n_bus) parent[i] = i;
+    if (i == 0) {
+        out[0] = 0;
+        out[1] = 0;
+        out[3] = 0;
+    }
+}
+
+__device__ __forceinline__ int island_root(const int32_t* parent, int x) {
+    for (int guard = 0; guard < 64 && parent[x] != x; ++guard) x = parent[x];
+    return x;
+}
+
+// out[3] = 1 when some branch joined two components this round
+__global__ void k_island_hook(DevNet net, int32_t* parent, int32_t* out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= net.n_branch || !net.br_closed[k]) return;
+    const int a = island_root(parent, net.br_from[k]);
+    const int b = island_root(parent, net.br_to[k]);
+    if (a == b) return;
+    atomicMin(parent + max(a, b), min(a, b));
+    out[3] = 1;
+}
+
+__global__ void k_island_jump(DevNet net, int32_t* parent) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= net.n_bus) return;
+    int p = parent[i];
+    for (int guard = 0; guard < 64 && parent[p] != p; ++guard) p = parent[p];
+    parent[i] = p;
+}
+
+__global__ void k_island_count(DevNet net, const int32_t* parent, int32_t* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < net.n_bus && parent[i] == i) atomicAdd(out + 0, 1);
+    if (i < net.n_meas && net.m_active[i]) atomicAdd(out + 1, 1);
+}
+
 // Stream mode: grids with active[g] join the running batch.
 __global__ void k_batch_activate(DevNet net, DevWork w, DevBatch b) {
     const int g = blockIdx.x;
@@ -598,7 +640,7 @@ inline int nblocks(int n) { return (n + kBlock - 1) / kBlock; }
 cudaError_t launch_batch_begin(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st) {
     if (b.n_grids <= 0) return cudaSuccess;
     k_batch_begin<<<b.n_grids, kBlock, 0, st>>>(net, w, b);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
 }
 
@@ -606,47 +648,78 @@ cudaError_t launch_batch_update(const DevNet& net, const DevFactor& f, const Dev
                                 const SolveParams& sp, const double* step, cudaStream_t st) {
     if (b.n_grids <= 0) return cudaSuccess;
     k_batch_update<<<b.n_grids, kBlock, 0, st>>>(net, f, w, b, sp, step);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
+}
+
+cudaError_t launch_islands(const DevNet& net, int32_t* parent, int32_t* out, int32_t max_rounds, cudaStream_t st) {
+    const int nb = nblocks(std::max(net.n_bus, 1));
+    k_island_init<<<nb, kBlock, 0, st>>>(net, parent, out);
+    count_launches(1);
+    int32_t rounds = 0, joined = 1;
+    cudaError_t e = cudaSuccess;
+    while (joined && e == cudaSuccess) {
+        if (rounds == max_rounds) {
+            rounds = -1;
+            break;
+        }
+        e = cudaMemsetAsync(out + 3, 0, sizeof(int32_t), st);
+        if (net.n_branch > 0 && e == cudaSuccess) {
+            k_island_hook<<<nblocks(net.n_branch), kBlock, 0, st>>>(net, parent, out);
+            count_launches(1);
+        }
+        k_island_jump<<<nb, kBlock, 0, st>>>(net, parent);
+        count_launches(1);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&joined, out + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        ++rounds;
+    }
+    if (e != cudaSuccess) return e;
+    k_island_count<<<nblocks(std::max(std::max(net.n_bus, net.n_meas), 1)), kBlock, 0, st>>>(net, parent, out);
+    count_launches(1);
+    e = cudaMemcpyAsync(out + 2, &rounds, sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
 cudaError_t launch_batch_activate(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st) {
     if (b.n_grids <= 0) return cudaSuccess;
     k_batch_activate<<<b.n_grids, kBlock, 0, st>>>(net, w, b);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batch_retire(const DevBatch& b, cudaStream_t st) {
     if (b.n_grids <= 0) return cudaSuccess;
     k_batch_retire<<<(b.n_grids + kBlock - 1) / kBlock, kBlock, 0, st>>>(b);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batch_objective(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st) {
     if (b.n_grids <= 0) return cudaSuccess;
     k_batch_objective<<<b.n_grids, kBlock, 0, st>>>(net, w, b);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
 }
 
 std::atomic<int64_t> g_kernel_launches{0};
+thread_local int64_t t_kernel_launches = 0;
 
 cudaError_t launch_admittance_and_ybus(const DevNet& net, cudaStream_t st) {
     if (net.n_branch > 0) {
         k_admittance<<<nblocks(net.n_branch), kBlock, 0, st>>>(net);
-        ++g_kernel_launches;
+        count_launches(1);
     }
     k_ybus<<<nblocks(net.n_bus), kBlock, 0, st>>>(net);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_evaluate(const DevNet& net, const DevWork& w, const SolveParams& sp, cudaStream_t st) {
     if (net.n_meas <= 0) return cudaSuccess;
     k_evaluate<<<nblocks(net.n_meas), kBlock, 0, st>>>(net, w, sp);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
 }
 
@@ -654,16 +727,16 @@ cudaError_t launch_objective(const DevNet& net, const DevWork& w, double bad_thr
     const int nb = net.n_meas > 0 ? nblocks(net.n_meas) : 0;
     if (nb > 0) {
         k_objective_part<<<nb, kBlock, 0, st>>>(net, w, bad_threshold);
-        ++g_kernel_launches;
+        count_launches(1);
     }
     k_objective<<<1, 1024, 0, st>>>(net, w, nb);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_rhs(const DevNet& net, const DevFactor& f, const DevWork& w, cudaStream_t st) {
     k_rhs<<<nblocks(f.n_state), kBlock, 0, st>>>(net, f, w);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
 }
 
@@ -672,50 +745,50 @@ cudaError_t launch_update(const DevNet& net, const DevFactor& f, const DevWork& 
     const int nb = nblocks(net.n_bus);
     k_update<<<nb, kBlock, 0, st>>>(net, f, w, sp, step);
     k_update_finalize<<<1, 1024, 0, st>>>(w, nb, sp.tol);
-    g_kernel_launches += 2;
+    count_launches(2);
     return cudaGetLastError();
 }
 
 cudaError_t launch_to_fp32(const DevFactor& f, const DevWork& w, cudaStream_t st) {
     k_to_fp32<<<nblocks(f.n_state), kBlock, 0, st>>>(f, w);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_refine_begin(const DevFactor& f, const DevWork& w, cudaStream_t st) {
     k_refine_begin<<<nblocks(f.n_state), kBlock, 0, st>>>(f, w);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_refine_residual(const DevNet& net, const DevFactor& f, const DevWork& w, cudaStream_t st) {
     if (net.n_meas > 0) {
         k_refine_spmv<<<nblocks(net.n_meas), kBlock, 0, st>>>(net, w);
-        ++g_kernel_launches;
+        count_launches(1);
     }
     k_refine_rhs<<<nblocks(f.n_state), kBlock, 0, st>>>(net, f, w);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_refine_accumulate(const DevFactor& f, const DevWork& w, cudaStream_t st) {
     k_refine_accumulate<<<nblocks(f.n_state), kBlock, 0, st>>>(f, w);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_flat_start(const DevNet& net, const DevWork& w, cudaStream_t st) {
     k_flat_start<<<nblocks(net.n_bus), kBlock, 0, st>>>(net, w);
-    ++g_kernel_launches;
+    count_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_results(const DevNet& net, const DevWork& w, cudaStream_t st) {
     k_injections<<<nblocks(net.n_bus), kBlock, 0, st>>>(net, w);
-    ++g_kernel_launches;
+    count_launches(1);
     if (net.n_branch > 0) {
         k_flows<<<nblocks(net.n_branch), kBlock, 0, st>>>(net, w);
-        ++g_kernel_launches;
+        count_launches(1);
     }
     return cudaGetLastError();
 }

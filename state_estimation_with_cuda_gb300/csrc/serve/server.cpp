@@ -97,12 +97,25 @@ int32_t Server::start() {
         }
         budget = static_cast<size_t>(0.9 * static_cast<double>(fr));
     }
+    // stream priorities: units of smaller grids are more urgent (their
+    // requests are short and plentiful), so their kernels are scheduled first
+    int least = 0, greatest = 0;
+    cudaSetDevice(cfg_.device_id);
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    const int32_t nparts = static_cast<int32_t>(parts.size());
     // build every unit's batch model, then analyse them in parallel (host only)
     for (auto& members : parts) {
         auto u = std::make_unique<Unit>();
         EngineConfig ec;
         ec.device_id = cfg_.device_id;
         ec.use_double_precision = cfg_.use_double_precision;
+        {
+            // parts are ordered small to large: spread them over the priority range
+            const int32_t pi = static_cast<int32_t>(units_.size());
+            const int span = least - greatest;  // >= 0; greatest is the most urgent
+            ec.stream_priority = nparts > 1 ? greatest + static_cast<int>((static_cast<int64_t>(span) * pi) / (nparts - 1))
+                                            : least;
+        }
         u->eng = std::make_unique<Engine>(ec);
         u->grids = members;
         u->pending.resize(members.size());

@@ -207,3 +207,28 @@ def test_mixed_precision_hot_start_sequence_grid10k(refine):
         v, th = e.voltages()
         assert res.status == 0
         assert max(np.abs(v - ov).max(), np.abs(th - oth).max()) < 1e-6
+
+
+def _degree_one_branches(g, count):
+    deg = np.bincount(np.concatenate([g.br_from, g.br_to]), minlength=g.n_bus)
+    leaves = [k for k in range(g.n_branch) if deg[g.br_from[k]] == 1 or deg[g.br_to[k]] == 1]
+    return leaves[:count]
+
+
+@pytest.mark.parametrize("n_open", [0, 1, 5])
+def test_islands_on_device_match_host(n_open):
+    """Opening n branches that each isolate a leaf bus leaves n + 1 islands;
+    the device labelling (uploaded model) agrees with the host check."""
+    g = SyntheticGrid(3000, 4200, 0x5E31)
+    status = np.ones(g.n_branch, np.int32)
+    for k in _degree_one_branches(g, n_open):
+        status[k] = 0
+    g.br_status = status
+    e = Estimator()
+    e.load_network(g)
+    host = e.check_observability()
+    e.upload_model()
+    dev = e.check_observability()
+    assert dev == host
+    assert dev[1] == n_open + 1
+    e.close()
