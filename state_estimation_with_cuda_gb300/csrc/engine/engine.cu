@@ -150,10 +150,10 @@ void Engine::build_schedule() {
     sch_all_.clear();
     sch_asm_.clear();
     sch_pot_.clear();
-    sch_pan_.clear();
     sch_upd_.clear();
     sch_pot_ptr_.assign(1, 0);
     sch_pan_ptr_.assign(1, 0);
+    sch_pan_.clear();
     sch_upd_ptr_.assign(1, 0);
     sch_flow_a_.clear();
     sch_flow_b_.clear();
@@ -250,7 +250,8 @@ void Engine::build_schedule() {
                 const int32_t pb = std::min(kTile, nc - p * kTile);
                 const int32_t q0 = p * kTile + pb;
                 sch_pot_.push_back(make_int4(s, p, 0, 0));
-                for (int32_t ti = p + 1; ti < tiles; ++ti) sch_pan_.push_back(make_int4(s, ti, 0, 0));
+                if (!mixed_)  // FP64: the panel's row tiles below go to the multi-CTA solve
+                    for (int32_t ti = p + 1; ti < tiles; ++ti) sch_pan_.push_back(make_int4(s, ti, 0, 0));
                 if (q0 < f)
                     for (int32_t tj = q0 / kTile; tj < tiles; ++tj)
                         for (int32_t ti = tj; ti < tiles; ++ti) sch_upd_.push_back(make_int4(s, ti, tj, 0));

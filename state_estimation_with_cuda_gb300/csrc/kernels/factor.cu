@@ -531,7 +531,8 @@ __global__ void __launch_bounds__(kThreads) k_big_assemble(DevFactor F, const T*
 }
 
 // Panel step p, part 1 (one CTA per front): factor the diagonal tile in
-// place and solve the rows of tile p below the panel's last column.
+// place, then solve the rows below it against it (FP32: the whole column
+// panel; FP64: tile p only, the rest by k_big_trsm); then the trailing update.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, T* lx, const int4* work, int p) {
     constexpr int ld = kTile + 1;
@@ -593,21 +594,36 @@ __global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, 
         const int i = x % pb, j = x / pb;
         if (i >= j) B[(p0 + i) + (int64_t)(p0 + j) * f] = D[i + j * ld];
     }
-    const int r = p0 + pb + threadIdx.x;
-    if (threadIdx.x < kTile && r < min(p0 + kTile, f)) {
+    // rows below the diagonal block, one per thread: x = a L_dd^-T by forward
+    // substitution in registers (volatile reads keep the compiler from
+    // hoisting the factor into registers across rows).  FP32: the whole
+    // column panel; FP64: the rest of tile p only (k_big_trsm takes the
+    // tiles below on many CTAs).
+    const volatile T* Dv = D;
+    const int r_end = (sizeof(T) == 4) ? f : min(p0 + kTile, f);
+#pragma unroll 1
+    for (int r = p0 + pb + threadIdx.x; r < r_end; r += blockDim.x) {
         T x[kTile];
-        for (int c = 0; c < pb; ++c) {
-            T a = B[r + (int64_t)(p0 + c) * f];
-            for (int k = 0; k < c; ++k) a -= x[k] * D[c + k * ld];
-            x[c] = a * rdiag[c];
+#pragma unroll
+        for (int c = 0; c < kTile; ++c) x[c] = (c < pb) ? B[r + (int64_t)(p0 + c) * f] : T(0);
+#pragma unroll
+        for (int c = 0; c < kTile; ++c) {
+            if (c < pb) {
+                x[c] *= rdiag[c];
+#pragma unroll
+                for (int c2 = c + 1; c2 < kTile; ++c2) x[c2] -= x[c] * Dv[c2 + c * ld];
+            }
         }
-        for (int c = 0; c < pb; ++c) B[r + (int64_t)(p0 + c) * f] = x[c];
+#pragma unroll
+        for (int c = 0; c < kTile; ++c)
+            if (c < pb) B[r + (int64_t)(p0 + c) * f] = x[c];
     }
 }
 
-// Panel step p, part 2: X = A L_dd^-T for the row tiles ti > p.  One warp
-// per row tile and one lane per row: forward substitution in registers
-// against the factored diagonal tile, staged transposed in shared memory.
+// FP64 panel step p, part 2: X = A L_dd^-T for the row tiles ti > p, spread
+// over CTAs (one SM's FP64 rate cannot carry a whole panel).  One warp per
+// row tile and one lane per row: forward substitution in registers against
+// the factored diagonal tile, staged transposed in shared memory.
 template <typename T>
 constexpr int kTrsmWarps = sizeof(T) == 4 ? 8 : 4;
 
@@ -935,16 +951,18 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
             for (int p = 0; p < ls.h_lvl_panels[l]; ++p) {
                 const int slot = ls.h_step_ptr[l] + p;
                 const int npot = ls.h_pot_ptr[slot + 1] - ls.h_pot_ptr[slot];
-                const int npan = ls.h_pan_ptr[slot + 1] - ls.h_pan_ptr[slot];
                 const int nupd = ls.h_upd_ptr[slot + 1] - ls.h_upd_ptr[slot];
                 if (npot > 0) {
                     k_big_potrf<T><<<npot, kThreads, 0, st>>>(F, W, lx, ls.d_pot + ls.h_pot_ptr[slot], p);
                     count_launches(1);
                 }
-                if (npan > 0) {
-                    k_big_trsm<T><<<(npan + kTrsmWarps<T> - 1) / kTrsmWarps<T>, 32 * kTrsmWarps<T>, 0, st>>>(
-                        F, lx, W.rdiag, ls.d_pan + ls.h_pan_ptr[slot], npan, p);
-                    count_launches(1);
+                if constexpr (sizeof(T) == 8) {
+                    const int npan = ls.h_pan_ptr[slot + 1] - ls.h_pan_ptr[slot];
+                    if (npan > 0) {
+                        k_big_trsm<T><<<(npan + kTrsmWarps<T> - 1) / kTrsmWarps<T>, 32 * kTrsmWarps<T>, 0, st>>>(
+                            F, lx, W.rdiag, ls.d_pan + ls.h_pan_ptr[slot], npan, p);
+                        count_launches(1);
+                    }
                 }
                 if (nupd > 0) {
                     k_big_update<T><<<nupd, kThreads, 0, st>>>(F, lx, ls.d_upd + ls.h_upd_ptr[slot], p);

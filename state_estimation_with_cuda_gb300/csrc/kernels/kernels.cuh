@@ -214,7 +214,7 @@ struct LevelSchedule {
     const int32_t* h_step_ptr = nullptr;    // [n_levels+1] first step slot of a level
     const int32_t* h_pot_ptr = nullptr;     // [n_slots+1] offsets into d_pot
     const int4* d_pot = nullptr;            // (big front) diagonal-tile factorisations
-    const int32_t* h_pan_ptr = nullptr;     // [n_slots+1] offsets into d_pan
+    const int32_t* h_pan_ptr = nullptr;     // [n_slots+1] offsets into d_pan (FP64 only)
     const int4* d_pan = nullptr;            // (big front, row tile below the panel)
     const int32_t* h_upd_ptr = nullptr;     // [n_slots+1] offsets into d_upd
     const int4* d_upd = nullptr;            // (big front, row tile, column tile)
