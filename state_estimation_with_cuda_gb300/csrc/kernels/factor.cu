@@ -95,7 +95,7 @@ __device__ __forceinline__ bool front_frozen(const DevFactor& F, const DevWork& 
 
 // L_kk = sqrt(d) and 1 / L_kk for a positive finite d (the caller checks).
 __device__ __forceinline__ void pivot_value(float d, float* sq, float* inv) {
-    const float y = __frsqrt_rn(d);
+    const float y = rsqrtf(d);  // the FP32 factor is a preconditioner of FP64 steps
     *sq = d * y;
     *inv = y;
 }
@@ -118,9 +118,9 @@ __device__ __forceinline__ const T* update_of(const DevFactor& F, const T* lx, c
     return (F.sn_u_big[c] ? lx : ub) + F.sn_u_off[c];
 }
 
-// Each child's relative map is staged in shared memory (relbuf, >= m ints)
-// and the update entries are loaded four per lane before they are scattered,
-// so several global loads are in flight per lane.
+// Each child's relative map is staged in shared memory (relbuf, >= m ints);
+// each warp loads four columns of update entries, four rows per lane, before
+// it scatters them, so sixteen global loads are in flight per lane.
 template <typename T>
 __device__ __forceinline__ void extend_add_child(const DevFactor& F, const T* lx, const T* ubase, int c, T* dst,
                                                  int ldd, int tid, int nth, int* relbuf) {
@@ -131,21 +131,34 @@ __device__ __forceinline__ void extend_add_child(const DevFactor& F, const T* lx
     for (int i = tid; i < m; i += nth) relbuf[i] = rel[i];
     __syncthreads();
     const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
-    for (int j = warp; j < m; j += nwarp) {
-        const int pj = relbuf[j] * ldd;
-        const T* Uj = U + (int64_t)j * uld;
-        for (int i0 = j + lane; i0 < m; i0 += 128) {
-            T u[4];
+    // a warp takes four columns at a time and issues all their loads (up to
+    // sixteen per lane) before the scatter-adds, so L2 latency is paid once
+    // per group instead of once per column
+    for (int jb = warp; jb < m; jb += 4 * nwarp) {
+        for (int ib = 0;; ib += 128) {
+            T u[4][4];
 #pragma unroll
-            for (int t = 0; t < 4; ++t) {
-                const int i = i0 + 32 * t;
-                u[t] = (i < m) ? __ldcg(Uj + i) : T(0);
+            for (int q = 0; q < 4; ++q) {
+                const int j = jb + q * nwarp;
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int i = j + ib + lane + 32 * t;
+                    u[q][t] = (j < m && i < m) ? __ldcg(U + (int64_t)j * uld + i) : T(0);
+                }
             }
 #pragma unroll
-            for (int t = 0; t < 4; ++t) {
-                const int i = i0 + 32 * t;
-                if (i < m) dst[relbuf[i] + pj] += u[t];
+            for (int q = 0; q < 4; ++q) {
+                const int j = jb + q * nwarp;
+                if (j < m) {
+                    const int pj = relbuf[j] * ldd;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const int i = j + ib + lane + 32 * t;
+                        if (i < m) dst[relbuf[i] + pj] += u[q][t];
+                    }
+                }
             }
+            if (jb + ib + 128 >= m) break;  // column jb has the most rows (m - jb)
         }
     }
 }
@@ -724,17 +737,38 @@ __device__ void front_fwd(const DevFactor& F, const T* lx, const T* rdiag, const
     const T* L = lx + F.sn_lx_off[s];
     for (int i = tid; i < f; i += nth) v[i] = (i < nc) ? rhs[c0 + i] : V(0);
     __syncthreads();
-    for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) {
-        const int c = F.sn_child[ci];
-        const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
-        const V* su = sub + F.sn_su_off[c];
-        const int* rel = F.sn_relmap + F.sn_su_off[c];
-        for (int i = tid; i < m; i += nth) {
-            const V val = __ldcg(su + i);
-            const int r = rel[i];
-            v[r] += val;
+    // children's update vectors, eight children at a time: every thread issues
+    // its loads for all eight before the ordered adds (one barrier per child
+    // keeps the sum order fixed)
+    const int cp0 = F.sn_child_ptr[s], cp1 = F.sn_child_ptr[s + 1];
+    for (int cb = cp0; cb < cp1; cb += 8) {
+        V val[8];
+        int row[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            row[u] = -1;
+            val[u] = V(0);
+            if (cb + u < cp1) {
+                const int c = F.sn_child[cb + u];
+                const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
+                if (tid < m) {
+                    const int64_t o = F.sn_su_off[c];
+                    val[u] = __ldcg(sub + o + tid);
+                    row[u] = F.sn_relmap[o + tid];
+                }
+            }
         }
-        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (cb + u < cp1) {
+                if (row[u] >= 0) v[row[u]] += val[u];
+                const int c = F.sn_child[cb + u];
+                const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
+                const int64_t o = F.sn_su_off[c];
+                for (int i = tid + nth; i < m; i += nth) v[F.sn_relmap[o + i]] += __ldcg(sub + o + i);
+                __syncthreads();
+            }
+        }
     }
     constexpr int ld = kTile + 1;
     for (int k0 = 0; k0 < nc; k0 += kTile) {
