@@ -52,7 +52,8 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
  *   "dataflow"              1 (default): persistent dataflow kernels for the
  *                           fronts below the tiled ones and for the solves
  *   "flow_small_f"          widest front of the high-occupancy dataflow phase
- *                           (default 64, at most 128; re-uploads) */
+ *                           (0 = default: 128 mixed, 64 FP64; at most 128;
+ *                           re-uploads) */
 SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* key, double value);
 
 typedef struct SLE_ExPlanInfo {

@@ -177,7 +177,8 @@ void Engine::build_schedule() {
     // Dataflow phases: a front whose subtree holds no big front is factorised
     // by the persistent kernels (phase A if no front of its subtree is wider
     // than cfg.flow_small_f, phase B otherwise); the rest stays level-synchronous.
-    const int32_t flow_small_f = std::max(8, std::min(cfg.flow_small_f, kFlowSmallFMax));
+    const int32_t want_f = cfg.flow_small_f > 0 ? cfg.flow_small_f : (mixed_ ? 128 : 64);
+    const int32_t flow_small_f = std::max(8, std::min(want_f, kFlowSmallFMax));
     std::vector<char> sub_big(ns, 0);
     std::vector<int32_t> sub_maxf(ns, 0);
     for (int32_t l = 0; l < nl; ++l)
@@ -372,6 +373,7 @@ int32_t Engine::upload() {
         fac_.bus_ps_v = c.take<int32_t>(n);
         fac_.sn_u_ld = c.take<int32_t>(ns);
         fac_.sn_u_big = c.take<uint8_t>(ns);
+        fac_.sn_pw = c.take<int8_t>(ns);
         fac_.sn_grid = batch_mode() ? c.take<int32_t>(ns) : nullptr;
         fac_.tgt_grid = batch_mode() ? c.take<int32_t>(P.tgt_local.size()) : nullptr;
         fac_.ps_grid = batch_mode() ? c.take<int32_t>(P.n_state) : nullptr;
@@ -577,6 +579,12 @@ int32_t Engine::upload() {
         chk(put(d_phase_, ph, st_));
     }
     chk(put(d_phase_nchild_, phase_nchild_, st_));
+    {
+        // phase-A fronts are factorised with kPanelFlowA-column panels, all others kTile
+        std::vector<int8_t> pw(ns);
+        for (int32_t x = 0; x < ns; ++x) pw[x] = static_cast<int8_t>(flow_phase_[x] == 1 ? kPanelFlowA : kTile);
+        chk(put(const_cast<int8_t*>(fac_.sn_pw), pw, st_));
+    }
     chk(put(d_nchild_, nchild_, st_));
     chk(put(work_.v, model.bus_v, st_));
     chk(put(work_.th, model.bus_th, st_));

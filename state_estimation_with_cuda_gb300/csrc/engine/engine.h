@@ -42,7 +42,8 @@ struct EngineConfig {
     double big_front_flops = 2.0e5;  // FP64: fronts above this many factor flops use the tiled multi-CTA path
     int32_t refine_steps = 0;        // mixed precision: extra refinement steps per Gauss-Newton step
     int32_t dataflow = 1;            // persistent dataflow kernels below the big fronts and for the solves
-    int32_t flow_small_f = 64;       // widest front of the high-occupancy dataflow phase (<= kFlowSmallFMax)
+    int32_t flow_small_f = 0;        // widest front of the high-occupancy dataflow phase (<= kFlowSmallFMax;
+                                     // 0: 128 for the mixed pipeline, 64 for FP64)
     int32_t stream_priority = 0;     // CUDA stream priority of the engine's stream (lower = more urgent)
 };
 

@@ -118,47 +118,67 @@ __device__ __forceinline__ const T* update_of(const DevFactor& F, const T* lx, c
     return (F.sn_u_big[c] ? lx : ub) + F.sn_u_off[c];
 }
 
-// Each child's relative map is staged in shared memory (relbuf, >= m ints);
-// each warp loads four columns of update entries, four rows per lane, before
-// it scatters them, so sixteen global loads are in flight per lane.
+// Extend-add of every child of front s with no barrier between children:
+// warp w owns the front's target columns t with t % nwarp == w and walks the
+// children in order, adding only into its own columns, so no two warps touch
+// the same entry and each entry's additions keep the children's order.  Per
+// child, the warp selects its columns 32 at a time (ballot over the relative
+// map), then loads up to four of them (four rows per lane each) before it
+// scatters them.  The caller follows with a block barrier.
 template <typename T>
-__device__ __forceinline__ void extend_add_child(const DevFactor& F, const T* lx, const T* ubase, int c, T* dst,
-                                                 int ldd, int tid, int nth, int* relbuf) {
-    const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
-    const T* U = update_of<T>(F, lx, ubase, c);
-    const int uld = F.sn_u_ld[c];
-    const int* rel = F.sn_relmap + F.sn_su_off[c];
-    for (int i = tid; i < m; i += nth) relbuf[i] = rel[i];
-    __syncthreads();
-    const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
-    // a warp takes four columns at a time and issues all their loads (up to
-    // sixteen per lane) before the scatter-adds, so L2 latency is paid once
-    // per group instead of once per column
-    for (int jb = warp; jb < m; jb += 4 * nwarp) {
-        for (int ib = 0;; ib += 128) {
-            T u[4][4];
+__device__ __forceinline__ void extend_add_children(const DevFactor& F, const T* lx, const T* ubase, int s, T* dst,
+                                                    int ldd) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) {
+        const int c = F.sn_child[ci];
+        const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
+        const T* U = update_of<T>(F, lx, ubase, c);
+        const int uld = F.sn_u_ld[c];
+        const int* rel = F.sn_relmap + F.sn_su_off[c];
+        for (int j0 = 0; j0 < m; j0 += 32) {
+            const int jl = j0 + lane;
+            const int tj = (jl < m) ? rel[jl] : -1;
+            unsigned own = __ballot_sync(0xffffffffu, tj >= 0 && (tj % nwarp) == warp);
+            while (own) {
+                int js[4];
+                int cnt = 0;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int j = jb + q * nwarp;
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    const int i = j + ib + lane + 32 * t;
-                    u[q][t] = (j < m && i < m) ? __ldcg(U + (int64_t)j * uld + i) : T(0);
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int j = jb + q * nwarp;
-                if (j < m) {
-                    const int pj = relbuf[j] * ldd;
-#pragma unroll
-                    for (int t = 0; t < 4; ++t) {
-                        const int i = j + ib + lane + 32 * t;
-                        if (i < m) dst[relbuf[i] + pj] += u[q][t];
+                for (int q = 0; q < 4; ++q) {
+                    js[q] = -1;
+                    if (own) {
+                        const int b = __ffs(own) - 1;
+                        own &= own - 1;
+                        js[q] = j0 + b;
+                        ++cnt;
                     }
                 }
+                const int jmin = js[0];  // the smallest column has the most rows
+                for (int ib = 0;; ib += 128) {
+                    T u[4][4];
+                    int ri[4][4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+#pragma unroll
+                        for (int t = 0; t < 4; ++t) {
+                            const int j = js[q];
+                            const int i = j + ib + lane + 32 * t;
+                            const bool ok = j >= 0 && i < m;
+                            u[q][t] = ok ? __ldcg(U + (int64_t)j * uld + i) : T(0);
+                            ri[q][t] = ok ? rel[i] : -1;
+                        }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int j = js[q];
+                        if (j < 0) continue;
+                        const int pj = __shfl_sync(0xffffffffu, tj, j - j0) * ldd;
+#pragma unroll
+                        for (int t = 0; t < 4; ++t)
+                            if (ri[q][t] >= 0) dst[ri[q][t] + pj] += u[q][t];
+                    }
+                    if (jmin + ib + 128 >= m) break;
+                }
+                (void)cnt;
             }
-            if (jb + ib + 128 >= m) break;  // column jb has the most rows (m - jb)
         }
     }
 }
@@ -178,7 +198,7 @@ __device__ __forceinline__ void extend_add_child(const DevFactor& F, const T* lx
 //       A22 -= X X^T, two vector loads and sixteen FMAs per panel column.
 // ---------------------------------------------------------------------------
 constexpr int kPanel = 32;  // widest panel of the in-shared-memory factorisation
-static_assert(kThreads >= kSmallFrontMax32, "one thread per front row");
+static_assert(kThreads - 32 >= kSmallFrontMax32, "one thread per front row besides warp 0");
 
 template <typename T>
 __device__ __forceinline__ void load4(const T* p, T (&v)[4]);
@@ -239,12 +259,43 @@ __device__ __forceinline__ bool warp_potrf(T (&a)[KP], int kb, int lane, T* inv_
     return bad;
 }
 
+// FP32 factors store L11^-1 in each diagonal block's slot, so that the solves
+// multiply by it (independent dot products) instead of sweeping the triangle
+// one column at a time.  FP64 keeps L11 there: at this GPU's FP64 rate the
+// inversion costs the factorisation more than the solves save.
+template <typename T>
+constexpr bool kInvDiag = sizeof(T) == 4;
+
+// Inverse of a kb x kb lower-triangular block held in shared memory as
+// lt[c][r] = L[r][c] (r > c) with reciprocal diagonal rinv: lane j forms
+// column j of L^-1 = L^-1 e_j by the same right-looking substitution as the
+// panel's row solve (a chain of kb multiply/FMA steps; the updates of a step
+// are independent) and writes rows i >= j to dst[i + j * ld].
+template <typename T, int KP, int LTLD>
+__device__ __forceinline__ void warp_trinv(const T (*lt)[LTLD], const T* rinv, int kb, int lane, T* dst, int ld) {
+    T x[KP];
+#pragma unroll
+    for (int i = 0; i < KP; ++i) x[i] = (i == lane) ? T(1) : T(0);
+#pragma unroll
+    for (int c = 0; c < KP; ++c) {
+        if (c < kb) {
+            x[c] *= rinv[c];
+#pragma unroll
+            for (int c2 = c + 1; c2 < KP; ++c2) x[c2] -= x[c] * lt[c][c2];
+        }
+    }
+    if (lane < kb) {
+#pragma unroll
+        for (int i = 0; i < KP; ++i)
+            if (i >= lane && i < kb) dst[i + lane * ld] = x[i];
+    }
+}
+
 // Shared-memory scratch of one front besides the front itself.
 template <typename T>
 struct FrontSmem {
     T lt[kPanel][kPanel + 1];  // lt[c][r] = L11[r][c] of the current panel
     T rinv[kPanel];            // 1 / L11[c][c]
-    int relbuf[kSmallFrontMax32];
 };
 
 // Assembles and partially factorises front s in shared memory (Fm holds
@@ -270,10 +321,8 @@ __device__ void front_factor(const DevFactor& F, const DevWork& W, const T* gv, 
         }
     }
     __syncthreads();
-    for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) {
-        extend_add_child<T>(F, lx, ub, F.sn_child[ci], Fm, ldf, tid, nth, sm.relbuf);
-        __syncthreads();
-    }
+    extend_add_children<T>(F, lx, ub, s, Fm, ldf);
+    __syncthreads();
     T* rdg = reinterpret_cast<T*>(W.rdiag) + F.sn_c0[s];
 #pragma unroll 1
     for (int k0 = 0; k0 < nc; k0 += KP) {
@@ -301,10 +350,15 @@ __device__ void front_factor(const DevFactor& F, const DevWork& W, const T* gv, 
                 }
         }
         __syncthreads();
-        // (2) rows below the block: x = a L11^-T, one row per thread (f <= kThreads)
+        // (2) FP32: warp 0 writes the inverse of the diagonal block into its
+        // slot.  The other threads (FP64: all): rows below the block,
+        // x = a L11^-T, one row per thread (f - q0 < kThreads - 32)
         const int q0 = k0 + kb;
-        {
-            const int r = q0 + tid;
+        constexpr int kInvThreads = kInvDiag<T> ? 32 : 0;
+        if (kInvDiag<T> && warp == 0) {
+            warp_trinv<T, KP, kPanel + 1>(sm.lt, sm.rinv, kb, lane, Fm + k0 + k0 * ldf, ldf);
+        } else {
+            const int r = q0 + tid - kInvThreads;
             if (r < f) {
                 T x[KP];
 #pragma unroll
@@ -387,7 +441,7 @@ __device__ void front_factor(const DevFactor& F, const DevWork& W, const T* gv, 
 // Panel widths: fronts of the high-occupancy dataflow phase (f <= 64) use
 // 16-column panels and a register budget for several CTAs per SM; the rest
 // use 32-column panels and the full register file (one CTA per SM anyway).
-constexpr int kPanelSmall = 16;
+constexpr int kPanelSmall = kPanelFlowA;
 template <typename T>
 constexpr int kMinBlocksA = sizeof(T) == 4 ? 3 : 2;
 
@@ -603,47 +657,55 @@ __global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, 
         }
     }
     __syncthreads();
-    for (int x = threadIdx.x; x < pb * pb; x += blockDim.x) {
-        const int i = x % pb, j = x / pb;
-        if (i >= j) B[(p0 + i) + (int64_t)(p0 + j) * f] = D[i + j * ld];
-    }
-    // rows below the diagonal block, one per thread: x = a L_dd^-T by forward
-    // substitution in registers (volatile reads keep the compiler from
-    // hoisting the factor into registers across rows).  FP32: the whole
-    // column panel; FP64: the rest of tile p only (k_big_trsm takes the
-    // tiles below on many CTAs).
-    const volatile T* Dv = D;
-    const int r_end = (sizeof(T) == 4) ? f : min(p0 + kTile, f);
-#pragma unroll 1
-    for (int r = p0 + pb + threadIdx.x; r < r_end; r += blockDim.x) {
-        T x[kTile];
-#pragma unroll
-        for (int c = 0; c < kTile; ++c) x[c] = (c < pb) ? B[r + (int64_t)(p0 + c) * f] : T(0);
-#pragma unroll
-        for (int c = 0; c < kTile; ++c) {
-            if (c < pb) {
-                x[c] *= rdiag[c];
-#pragma unroll
-                for (int c2 = c + 1; c2 < kTile; ++c2) x[c2] -= x[c] * Dv[c2 + c * ld];
-            }
+    // Warp 0 writes the diagonal tile's slot: L_dd^-1 for FP32, L_dd for
+    // FP64.  Warps 1..: rows below the diagonal block, one per thread,
+    // x = a L_dd^-T by forward substitution in registers (volatile reads keep
+    // the compiler from hoisting the factor into registers across rows).
+    // FP32: the whole column panel; FP64: the rest of tile p only (k_big_trsm
+    // takes the tiles below on many CTAs).
+    if (threadIdx.x < 32) {
+        const int i = threadIdx.x;
+        if constexpr (kInvDiag<T>) {
+            warp_trinv<T, kTile, kTile + 1>(reinterpret_cast<const T (*)[kTile + 1]>(D), rdiag, pb, i,
+                                            B + p0 + (int64_t)p0 * f, f);
+        } else {
+            for (int j = 0; j < pb; ++j)
+                if (i >= j && i < pb) B[(p0 + i) + (int64_t)(p0 + j) * f] = D[i + j * ld];
         }
+    } else {
+        const volatile T* Dv = D;
+        const int r_end = (sizeof(T) == 4) ? f : min(p0 + kTile, f);
+#pragma unroll 1
+        for (int r = p0 + pb + threadIdx.x - 32; r < r_end; r += blockDim.x - 32) {
+            T x[kTile];
 #pragma unroll
-        for (int c = 0; c < kTile; ++c)
-            if (c < pb) B[r + (int64_t)(p0 + c) * f] = x[c];
+            for (int c = 0; c < kTile; ++c) x[c] = (c < pb) ? B[r + (int64_t)(p0 + c) * f] : T(0);
+#pragma unroll
+            for (int c = 0; c < kTile; ++c) {
+                if (c < pb) {
+                    x[c] *= rdiag[c];
+#pragma unroll
+                    for (int c2 = c + 1; c2 < kTile; ++c2) x[c2] -= x[c] * Dv[c2 + c * ld];
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < kTile; ++c)
+                if (c < pb) B[r + (int64_t)(p0 + c) * f] = x[c];
+        }
     }
 }
 
 // FP64 panel step p, part 2: X = A L_dd^-T for the row tiles ti > p, spread
 // over CTAs (one SM's FP64 rate cannot carry a whole panel).  One warp per
-// row tile and one lane per row: forward substitution in registers against
-// the factored diagonal tile, staged transposed in shared memory.
+// row tile and one lane per row, forward substitution in registers against
+// the diagonal tile staged in shared memory.
 template <typename T>
 constexpr int kTrsmWarps = sizeof(T) == 4 ? 8 : 4;
 
 template <typename T>
 __global__ void __launch_bounds__(32 * kTrsmWarps<T>) k_big_trsm(DevFactor F, T* lx, const void* Wrdiag,
                                                                  const int4* work, int n_work, int p) {
-    __shared__ T lt[kTrsmWarps<T>][kTile][kTile + 1];
+    __shared__ T lt[kTrsmWarps<T>][kTile][kTile + 1];  // lt[w][c][r] = L_dd[r][c]
     __shared__ T rinv[kTrsmWarps<T>][kTile];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int item = blockIdx.x * kTrsmWarps<T> + warp;
@@ -652,19 +714,18 @@ __global__ void __launch_bounds__(32 * kTrsmWarps<T>) k_big_trsm(DevFactor F, T*
     const int s = wk.x, ti = wk.y;
     const int f = F.sn_f[s];
     const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
-    const T* Bc = lx + F.sn_lx_off[s];
     T* B = lx + F.sn_lx_off[s];
     const int p0 = p * kTile;
     const int pb = min(kTile, nc - p0);
     for (int c = 0; c < pb; ++c)
-        lt[warp][c][lane] = (lane < pb && lane > c) ? Bc[(p0 + lane) + (int64_t)(p0 + c) * f] : T(0);
+        lt[warp][c][lane] = (lane < pb && lane > c) ? B[(p0 + lane) + (int64_t)(p0 + c) * f] : T(0);
     if (lane < pb) rinv[warp][lane] = reinterpret_cast<const T*>(Wrdiag)[F.sn_c0[s] + p0 + lane];
     __syncwarp();
     const int r = ti * kTile + lane;
     if (r < f) {
         T x[kTile];
 #pragma unroll
-        for (int c = 0; c < kTile; ++c) x[c] = (c < pb) ? Bc[r + (int64_t)(p0 + c) * f] : T(0);
+        for (int c = 0; c < kTile; ++c) x[c] = (c < pb) ? B[r + (int64_t)(p0 + c) * f] : T(0);
 #pragma unroll
         for (int c = 0; c < kTile; ++c) {
             if (c < pb) {
@@ -714,9 +775,10 @@ __global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, T* lx, con
 // Solves.  Forward (bottom-up): v = [b of own columns; 0] + children's update
 // vectors; y = L11^-1 v1; update vector = v2 - L21 y.
 // Backward (top-down): x1 = L11^-T (y - L21^T x_rows).
-// Blocked by kTile columns: the diagonal tile is staged in shared memory and
-// swept by one warp; the rectangular update below (forward) or the dot
-// products against the solved rows (backward) use every thread with
+// Blocked by columns: each diagonal block is staged in shared memory and
+// applied by one warp (FP32: a mat-vec with the stored L11^-1, one lane per
+// row; FP64: a column sweep); the rectangular update below (forward) or the
+// dot products against the solved rows (backward) use every thread with
 // coalesced reads of the column-major panel.
 // ---------------------------------------------------------------------------
 struct SolveVecs {
@@ -770,22 +832,38 @@ __device__ void front_fwd(const DevFactor& F, const T* lx, const T* rdiag, const
             }
         }
     }
+    // blocks of the factor's panel width (FP32: the diagonal slots hold
+    // L11^-1) or of kTile (FP64: L11 with its reciprocal diagonal)
+    const int bw = kInvDiag<T> ? (F.sn_pw ? F.sn_pw[s] : kTile) : kTile;
     constexpr int ld = kTile + 1;
-    for (int k0 = 0; k0 < nc; k0 += kTile) {
-        const int kb = min(kTile, nc - k0);
+    for (int k0 = 0; k0 < nc; k0 += bw) {
+        const int kb = min(bw, nc - k0);
         for (int x = tid; x < kb * kb; x += nth) {
             const int i = x % kb, j = x / kb;
-            D[i + j * ld] = (i == j) ? rdiag[c0 + k0 + i] : L[(k0 + i) + (int64_t)(k0 + j) * f];
+            if constexpr (kInvDiag<T>)
+                D[i + j * ld] = (i >= j) ? L[(k0 + i) + (int64_t)(k0 + j) * f] : T(0);
+            else
+                D[i + j * ld] = (i == j) ? rdiag[c0 + k0 + i] : L[(k0 + i) + (int64_t)(k0 + j) * f];
         }
         __syncthreads();
         if (tid < 32) {
-            for (int k = 0; k < kb; ++k) {
-                const V yk = v[k0 + k] * static_cast<V>(D[k + k * ld]);
+            if constexpr (kInvDiag<T>) {
+                // y = L11^-1 v: one lane per row, independent dot products
+                V y = V(0);
+                if (tid < kb)
+                    for (int j = 0; j <= tid; ++j) y += static_cast<V>(D[tid + j * ld]) * v[k0 + j];
                 __syncwarp();
-                const int i = k + 1 + tid;
-                if (i < kb) v[k0 + i] -= static_cast<V>(D[i + k * ld]) * yk;
-                if (tid == 0) v[k0 + k] = yk;
-                __syncwarp();
+                if (tid < kb) v[k0 + tid] = y;
+            } else {
+                // column sweep, lane i updating row k + 1 + i
+                for (int k = 0; k < kb; ++k) {
+                    const V yk = v[k0 + k] * static_cast<V>(D[k + k * ld]);
+                    __syncwarp();
+                    const int i = k + 1 + tid;
+                    if (i < kb) v[k0 + i] -= static_cast<V>(D[i + k * ld]) * yk;
+                    if (tid == 0) v[k0 + k] = yk;
+                    __syncwarp();
+                }
             }
         }
         __syncthreads();
@@ -818,10 +896,12 @@ __device__ void front_bwd(const DevFactor& F, const T* lx, const T* rdiag, const
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     for (int r = threadIdx.x; r < f; r += blockDim.x) x[r] = (r < nc) ? __ldcg(sol + c0 + r) : __ldcg(sol + rows[r]);
     __syncthreads();
+    // blocks as in the forward sweep, last first; x1 = L11^-T t
+    const int bw = kInvDiag<T> ? (F.sn_pw ? F.sn_pw[s] : kTile) : kTile;
     constexpr int ld = kTile + 1;
-    const int nblk = (nc + kTile - 1) / kTile;
+    const int nblk = (nc + bw - 1) / bw;
     for (int b = nblk - 1; b >= 0; --b) {
-        const int k0 = b * kTile, kb = min(kTile, nc - k0);
+        const int k0 = b * bw, kb = min(bw, nc - k0);
         for (int k = k0 + warp; k < k0 + kb; k += nwarp) {
             V acc = V(0);
             for (int r = k0 + kb + lane; r < f; r += 32) acc += static_cast<V>(L[r + (int64_t)k * f]) * x[r];
@@ -830,17 +910,31 @@ __device__ void front_bwd(const DevFactor& F, const T* lx, const T* rdiag, const
         }
         for (int q = threadIdx.x; q < kb * kb; q += blockDim.x) {
             const int i = q % kb, j = q / kb;
-            D[i + j * ld] = (i == j) ? rdiag[c0 + k0 + i] : L[(k0 + i) + (int64_t)(k0 + j) * f];
+            if constexpr (kInvDiag<T>)
+                D[i + j * ld] = (i >= j) ? L[(k0 + i) + (int64_t)(k0 + j) * f] : T(0);
+            else
+                D[i + j * ld] = (i == j) ? rdiag[c0 + k0 + i] : L[(k0 + i) + (int64_t)(k0 + j) * f];
         }
         __syncthreads();
         if (threadIdx.x < 32) {
-            for (int k = kb - 1; k >= 0; --k) {
-                const V xk = x[k0 + k] * static_cast<V>(D[k + k * ld]);
+            if constexpr (kInvDiag<T>) {
+                // x = (L11^-1)^T t: one lane per column of L11^-1
+                const int c = threadIdx.x;
+                V val = V(0);
+                if (c < kb)
+                    for (int i = c; i < kb; ++i) val += static_cast<V>(D[i + c * ld]) * x[k0 + i];
                 __syncwarp();
-                const int i = threadIdx.x;
-                if (i < k) x[k0 + i] -= static_cast<V>(D[k + i * ld]) * xk;
-                if (threadIdx.x == 0) x[k0 + k] = xk;
-                __syncwarp();
+                if (c < kb) x[k0 + c] = val;
+            } else {
+                // column sweep from the last, lane i updating row i < k
+                for (int k = kb - 1; k >= 0; --k) {
+                    const V xk = x[k0 + k] * static_cast<V>(D[k + k * ld]);
+                    __syncwarp();
+                    const int i = threadIdx.x;
+                    if (i < k) x[k0 + i] -= static_cast<V>(D[k + i * ld]) * xk;
+                    if (threadIdx.x == 0) x[k0 + k] = xk;
+                    __syncwarp();
+                }
             }
         }
         __syncthreads();

@@ -104,6 +104,9 @@ struct DevFactor {
     const int32_t* sn_grid;  // batch: grid of each front (nullptr for one grid)
     const int32_t* tgt_grid; // batch: grid of each gain target
     const int32_t* ps_grid;  // batch: grid of each permuted state
+    // columns per panel of each front's factorisation (16 or 32); the
+    // diagonal block of every panel is stored inverted (L11^-1) in L
+    const int8_t* sn_pw;
 };
 
 // Mutable per-iteration state (device).
@@ -266,6 +269,8 @@ cudaError_t launch_batch_retire(const DevBatch& b, cudaStream_t st);
 // Largest front the high-occupancy dataflow phase may hold (its kernel keeps
 // 16-column panels and a register budget for several CTAs per SM).
 constexpr int32_t kFlowSmallFMax = 128;
+// Panel width of the high-occupancy phase's fronts (all others use 32).
+constexpr int32_t kPanelFlowA = 16;
 
 // Resident-CTA grid sizes of the persistent dataflow kernels (0 = cannot run).
 struct FlowGrids {
