@@ -215,20 +215,64 @@ void Engine::build_schedule() {
     lay_u_off_[ns] = uu;
     lay_lx_size_ = lx;
     lay_u_size_ = uu;
+    // every front by level (solves without dataflow, backward order)
+    std::vector<int32_t> lvl_of(ns, 0);
     for (int32_t l = 0; l < nl; ++l) {
-        std::vector<int32_t> bigs;
         for (int32_t x = P.lvl_ptr[l]; x < P.lvl_ptr[l + 1]; ++x) {
             const int32_t s = P.lvl_sn[x];
+            lvl_of[s] = l;
             sch_all_.push_back(s);
             sch_maxf_[l] = std::max(sch_maxf_[l], P.sn_f[s]);
             sch_maxpanel_[l] = std::max<int64_t>(sch_maxpanel_[l],
                                                  static_cast<int64_t>(P.sn_f[s]) * (P.sn_c0[s + 1] - P.sn_c0[s]));
+            if (flow_phase_[s] == 1) flow_a_maxf_ = std::max(flow_a_maxf_, P.sn_f[s]);
+            if (flow_phase_[s] == 2) flow_b_maxf_ = std::max(flow_b_maxf_, P.sn_f[s]);
+        }
+        sch_all_ptr_[l + 1] = static_cast<int32_t>(sch_all_.size());
+    }
+    // Level-synchronous fronts (not in a dataflow phase) are grouped either
+    // by height (levels from the leaves, as above) or by depth (distance from
+    // the root, deepest first).  Either order completes children first; the
+    // one with fewer launches wins.  In a batch the wide fronts sit just below
+    // each grid's root, so depth lines them up across grids where height does
+    // not, and the union needs about as many panel steps as its largest grid.
+    std::vector<int32_t> depth(ns, 0);
+    int32_t dmax = 0;
+    for (int32_t s = ns - 1; s >= 0; --s) {  // parents follow their children
+        const int32_t p = P.sn_parent[s];
+        depth[s] = p >= 0 ? depth[p] + 1 : 0;
+        if (flow_phase_[s] == 0) dmax = std::max(dmax, depth[s]);
+    }
+    const int32_t per_panel = mixed_ ? 2 : 3;  // launches per panel step
+    auto sync_cost = [&](bool by_depth) {
+        std::vector<int32_t> pan(nl, 0);
+        std::vector<char> has_small(nl, 0), has_big(nl, 0);
+        for (int32_t s = 0; s < ns; ++s) {
+            if (flow_phase_[s] != 0) continue;
+            const int32_t l = by_depth ? dmax - depth[s] : lvl_of[s];
+            if (big[s]) {
+                has_big[l] = 1;
+                pan[l] = std::max(pan[l], (P.sn_c0[s + 1] - P.sn_c0[s] + kTile - 1) / kTile);
+            } else {
+                has_small[l] = 1;
+            }
+        }
+        int64_t c = 0;
+        for (int32_t l = 0; l < nl; ++l) c += static_cast<int64_t>(pan[l]) * per_panel + has_small[l] + has_big[l];
+        return c;
+    };
+    const bool by_depth = dmax < nl && sync_cost(true) < sync_cost(false);
+    std::vector<std::vector<int32_t>> sync_lvl(nl);
+    for (int32_t l = 0; l < nl; ++l)
+        for (int32_t x = P.lvl_ptr[l]; x < P.lvl_ptr[l + 1]; ++x) {
+            const int32_t s = P.lvl_sn[x];
+            if (flow_phase_[s] == 0) sync_lvl[by_depth ? dmax - depth[s] : l].push_back(s);
+        }
+    for (int32_t l = 0; l < nl; ++l) {
+        std::vector<int32_t> bigs;
+        for (int32_t s : sync_lvl[l]) {
             if (big[s]) {
                 bigs.push_back(s);
-            } else if (flow_phase_[s] == 1) {
-                flow_a_maxf_ = std::max(flow_a_maxf_, P.sn_f[s]);
-            } else if (flow_phase_[s] == 2) {
-                flow_b_maxf_ = std::max(flow_b_maxf_, P.sn_f[s]);
             } else {
                 sch_small_.push_back(s);
                 sch_small_maxf_[l] = std::max(sch_small_maxf_[l], P.sn_f[s]);
@@ -263,7 +307,6 @@ void Engine::build_schedule() {
         }
         sch_small_ptr_[l + 1] = static_cast<int32_t>(sch_small_.size());
         sch_asm_ptr_[l + 1] = static_cast<int32_t>(sch_asm_.size());
-        sch_all_ptr_[l + 1] = static_cast<int32_t>(sch_all_.size());
     }
     // every front, top-down, for the backward dataflow sweep
     sch_down_.assign(sch_all_.rbegin(), sch_all_.rend());
@@ -392,6 +435,27 @@ int32_t Engine::upload() {
             batch_.flat = af + G;
             batch_.retire = af + 2 * static_cast<size_t>(G);
             batch_.running = c.take<int32_t>(1);
+            // items of kBatchChunk buses / rows, a grid's items adjacent
+            auto items = [&](bool rows, std::vector<int2>& it, std::vector<int32_t>& ptr) {
+                it.clear();
+                ptr.assign(1, 0);
+                for (int32_t g = 0; g < G; ++g) {
+                    const int32_t a = rows ? grids_[g].m0 : grids_[g].bus0;
+                    const int32_t n = rows ? grids_[g].nm : grids_[g].nbus;
+                    for (int32_t k = 0; k < n; k += kBatchChunk) it.push_back(make_int2(g, a + k));
+                    ptr.push_back(static_cast<int32_t>(it.size()));
+                }
+            };
+            items(false, bus_items_, bus_item_ptr_);
+            items(true, row_items_, row_item_ptr_);
+            batch_.n_bus_items = static_cast<int32_t>(bus_items_.size());
+            batch_.n_row_items = static_cast<int32_t>(row_items_.size());
+            batch_.bus_items = c.take<int2>(bus_items_.size());
+            batch_.bus_item_ptr = c.take<int32_t>(G + 1);
+            batch_.row_items = c.take<int2>(row_items_.size());
+            batch_.row_item_ptr = c.take<int32_t>(G + 1);
+            batch_.part = c.take<double>(std::max<size_t>(1, std::max(bus_items_.size(), row_items_.size())));
+            batch_.part_bad = c.take<int32_t>(std::max<size_t>(1, bus_items_.size()));
         } else {
             batch_ = DevBatch{};
         }
@@ -408,6 +472,13 @@ int32_t Engine::upload() {
         d_phase_ = c.take<int8_t>(ns);
         d_phase_nchild_ = c.take<int32_t>(ns);
         d_nchild_ = c.take<int32_t>(ns);
+        d_ready_n_ = c.take<int32_t>(4);
+        {
+            const int32_t src_n[4] = {static_cast<int32_t>(sch_flow_a_.size()), static_cast<int32_t>(sch_flow_b_.size()),
+                                      static_cast<int32_t>(sch_up_.size()), static_cast<int32_t>(sch_down_.size())};
+            for (int l = 0; l < 4; ++l) d_cmp_[l] = batch_mode() ? c.take<int32_t>(src_n[l]) : nullptr;
+            d_chunk_cnt_ = batch_mode() ? c.take<int32_t>(std::max(1, ready_chunks(src_n))) : nullptr;
+        }
         // work
         work_.v = c.take<double>(n);
         work_.th = c.take<double>(n);
@@ -552,6 +623,10 @@ int32_t Engine::upload() {
         }
         chk(put(const_cast<int32_t*>(batch_.bus_off), boff, st_));
         chk(put(const_cast<int32_t*>(batch_.meas_off), moff, st_));
+        chk(put(const_cast<int2*>(batch_.bus_items), bus_items_, st_));
+        chk(put(const_cast<int32_t*>(batch_.bus_item_ptr), bus_item_ptr_, st_));
+        chk(put(const_cast<int2*>(batch_.row_items), row_items_, st_));
+        chk(put(const_cast<int32_t*>(batch_.row_item_ptr), row_item_ptr_, st_));
         const size_t out_bytes = static_cast<size_t>(G) * (4 + 4 + 8 + 8) + 8;
         if (h_batch_cap_ < static_cast<size_t>(G)) {
             if (h_batch_in_) cudaFreeHost(h_batch_in_);
@@ -586,6 +661,18 @@ int32_t Engine::upload() {
         chk(put(const_cast<int8_t*>(fac_.sn_pw), pw, st_));
     }
     chk(put(d_nchild_, nchild_, st_));
+    {
+        const std::vector<int32_t> n4 = {static_cast<int32_t>(sch_flow_a_.size()),
+                                         static_cast<int32_t>(sch_flow_b_.size()),
+                                         static_cast<int32_t>(sch_up_.size()), static_cast<int32_t>(sch_down_.size())};
+        chk(put(d_ready_n_, n4, st_));
+        // until the first compaction the batch lists are the full ones (every
+        // factor or solve launch then finds valid lists)
+        const int32_t* src[4] = {d_flow_a_, d_flow_b_, d_up_, d_down_};
+        for (int l = 0; l < 4; ++l)
+            if (d_cmp_[l] && n4[l] > 0)
+                chk(cudaMemcpyAsync(d_cmp_[l], src[l], sizeof(int32_t) * n4[l], cudaMemcpyDeviceToDevice, st_));
+    }
     chk(put(work_.v, model.bus_v, st_));
     chk(put(work_.th, model.bus_th, st_));
     chk(put(work_.z, model.m_value, st_));
@@ -635,6 +722,23 @@ int32_t Engine::upload() {
         sched_.solve_maxf = ms;
         sched_.solve_grid = std::max(1, std::min(g.solve, ns));
         sched_.up_grid = std::max(1, std::min(g.solve, sched_.up_n));
+        // claim-list lengths on the device; a batch claims from compacted copies
+        const int32_t* src[4] = {d_flow_a_, d_flow_b_, d_up_, d_down_};
+        const int32_t src_n[4] = {sched_.flow_a_n, sched_.flow_b_n, sched_.up_n, static_cast<int32_t>(sch_down_.size())};
+        sched_.d_ready_n = d_ready_n_;
+        sched_.compact = batch_mode() ? 1 : 0;
+        sched_.d_chunk_cnt = d_chunk_cnt_;
+        for (int l = 0; l < 4; ++l) {
+            sched_.src_lists[l] = src[l];
+            sched_.src_n[l] = src_n[l];
+            sched_.cmp_lists[l] = d_cmp_[l];
+        }
+        if (sched_.compact) {
+            sched_.d_flow_a = d_cmp_[0];
+            sched_.d_flow_b = d_cmp_[1];
+            sched_.d_up = d_cmp_[2];
+            sched_.d_down = d_cmp_[3];
+        }
     }
 
     if (h_stage_n_ < static_cast<size_t>(m)) {
@@ -759,6 +863,7 @@ int32_t Engine::enqueue_iteration(const SolveParams& sp, bool refactor, int64_t*
         if (per_stage) per_stage[st] += t_kernel_launches - l0;
         if (mk >= 0) cudaEventRecord(ev_pool_[mk + 1], st_);
     };
+    if (sched_.compact) stage(ST_OTHER, [&] { return launch_ready_compact(fac_, work_, sched_, st_); });
     stage(ST_EVALUATE, [&] { return launch_evaluate(net_, work_, sp, st_); });
     if (!mixed_) {
         if (refactor) stage(ST_FACTOR, [&] { return launch_factor(net_, fac_, work_, sched_, st_); });
@@ -1396,7 +1501,7 @@ int32_t Engine::batch_solve(int32_t n, const int32_t* ids, const uint8_t* flat, 
     SolveParams spf = sp;
     spf.skip_flags = FLAG_INACTIVE;  // converged grids need their final residuals
     e = launch_evaluate(net_, work_, spf, st_);
-    if (e == cudaSuccess) e = launch_batch_objective(net_, work_, batch_, st_);
+    if (e == cudaSuccess) e = launch_batch_objective(net_, work_, batch_, 0u, st_);
     cudaEventRecord(ev1_, st_);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_flags, batch_.flags, 4 * static_cast<size_t>(G), cudaMemcpyDeviceToHost, st_);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_iters, batch_.iters, 4 * static_cast<size_t>(G), cudaMemcpyDeviceToHost, st_);
@@ -1580,17 +1685,18 @@ int32_t Engine::stream_step(std::vector<int32_t>& done, std::vector<GridResult>&
         if ((h_flags[g] & FLAG_FROZEN) || stream_iters_[g] >= stream_rq_.max_iterations) done.push_back(g);
     }
     if (done.empty()) return 0;
-    // final evaluation of the finished grids (and, harmlessly, of the running
-    // ones) for their objective; then they leave the batch
+    // final evaluation and objective of the finished grids only (marked
+    // FLAG_FINAL); then they leave the batch
     std::memset(h_batch_in_ + 2 * static_cast<size_t>(G), 0, G);
     for (int32_t g : done) h_batch_in_[2 * static_cast<size_t>(G) + g] = 1;
     SolveParams spf = sp;
     spf.skip_flags = FLAG_INACTIVE;
-    e = launch_evaluate(net_, work_, spf, st_);
-    if (e == cudaSuccess) e = launch_batch_objective(net_, work_, batch_, st_);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(const_cast<uint8_t*>(batch_.retire), h_batch_in_ + 2 * static_cast<size_t>(G), G,
-                            cudaMemcpyHostToDevice, st_);
+    spf.need_flags = FLAG_FINAL;
+    e = cudaMemcpyAsync(const_cast<uint8_t*>(batch_.retire), h_batch_in_ + 2 * static_cast<size_t>(G), G,
+                        cudaMemcpyHostToDevice, st_);
+    if (e == cudaSuccess) e = launch_batch_mark_final(batch_, st_);
+    if (e == cudaSuccess) e = launch_evaluate(net_, work_, spf, st_);
+    if (e == cudaSuccess) e = launch_batch_objective(net_, work_, batch_, FLAG_FINAL, st_);
     if (e == cudaSuccess) e = launch_batch_retire(batch_, st_);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_obj, batch_.objective, 8 * static_cast<size_t>(G), cudaMemcpyDeviceToHost, st_);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st_);

@@ -212,6 +212,11 @@ private:
     int8_t* d_phase_ = nullptr;
     int32_t* d_phase_nchild_ = nullptr;
     int32_t* d_nchild_ = nullptr;
+    int32_t* d_ready_n_ = nullptr;               // [4] claim-list lengths
+    int32_t* d_cmp_[4] = {nullptr, nullptr, nullptr, nullptr};  // batch: compacted claim lists
+    int32_t* d_chunk_cnt_ = nullptr;             // batch: compaction scratch
+    std::vector<int2> bus_items_, row_items_;    // batch: per-grid reduction items
+    std::vector<int32_t> bus_item_ptr_, row_item_ptr_;
     int32_t* isl_parent_ = nullptr;
     int32_t* isl_out_ = nullptr;
     int32_t max_solve_front() const;

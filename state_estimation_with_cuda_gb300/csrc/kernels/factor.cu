@@ -518,15 +518,16 @@ __device__ __forceinline__ int continue_up(const DevFactor& F, const int8_t* pha
 
 template <typename T, int KP, int kMinBlocks>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) k_front_flow(DevFactor F, DevWork W, const T* gv, T* lx,
-                                                                     T* ub, const int* ready, int n_ready,
+                                                                     T* ub, const int* ready, const int* n_ready,
                                                                      const int8_t* phase, int ph,
                                                                      const int32_t* nchild, int* counter, int* cnt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ FrontSmem<T> sm;
     __shared__ int slot;
+    const int nr = *n_ready;
     for (;;) {
         const int item = claim(counter, &slot);
-        if (item >= n_ready) break;
+        if (item >= nr) break;
         int s = ready[item];
         while (s >= 0) {
             if (!front_frozen(F, W, s))
@@ -550,9 +551,11 @@ __device__ __forceinline__ int lower_bound_i32(const int* a, int lo, int hi, int
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_big_assemble(DevFactor F, const T* gv, T* lx, T* ub, const int4* work) {
+__global__ void __launch_bounds__(kThreads) k_big_assemble(DevFactor F, DevWork W, const T* gv, T* lx, T* ub,
+                                                           const int4* work) {
     const int4 wk = work[blockIdx.x];
     const int s = wk.x, tj = wk.y;
+    if (front_frozen(F, W, s)) return;  // the whole CTA, before any barrier
     const int f = F.sn_f[s];
     T* B = lx + F.sn_lx_off[s];
     const int c0 = tj * kTile, c1 = min(c0 + kTile, f);
@@ -606,6 +609,7 @@ __global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, 
     __shared__ T D[kTile * ld];
     __shared__ T rdiag[kTile];
     const int s = work[blockIdx.x].x;
+    if (front_frozen(F, W, s)) return;  // the whole CTA, before any barrier
     const int f = F.sn_f[s];
     const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
     T* B = lx + F.sn_lx_off[s];
@@ -703,8 +707,8 @@ template <typename T>
 constexpr int kTrsmWarps = sizeof(T) == 4 ? 8 : 4;
 
 template <typename T>
-__global__ void __launch_bounds__(32 * kTrsmWarps<T>) k_big_trsm(DevFactor F, T* lx, const void* Wrdiag,
-                                                                 const int4* work, int n_work, int p) {
+__global__ void __launch_bounds__(32 * kTrsmWarps<T>) k_big_trsm(DevFactor F, DevWork W, T* lx, const int4* work,
+                                                                 int n_work, int p) {
     __shared__ T lt[kTrsmWarps<T>][kTile][kTile + 1];  // lt[w][c][r] = L_dd[r][c]
     __shared__ T rinv[kTrsmWarps<T>][kTile];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -712,6 +716,7 @@ __global__ void __launch_bounds__(32 * kTrsmWarps<T>) k_big_trsm(DevFactor F, T*
     if (item >= n_work) return;  // the whole warp; no block barrier follows
     const int4 wk = work[item];
     const int s = wk.x, ti = wk.y;
+    if (front_frozen(F, W, s)) return;  // the whole warp
     const int f = F.sn_f[s];
     const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
     T* B = lx + F.sn_lx_off[s];
@@ -719,7 +724,7 @@ __global__ void __launch_bounds__(32 * kTrsmWarps<T>) k_big_trsm(DevFactor F, T*
     const int pb = min(kTile, nc - p0);
     for (int c = 0; c < pb; ++c)
         lt[warp][c][lane] = (lane < pb && lane > c) ? B[(p0 + lane) + (int64_t)(p0 + c) * f] : T(0);
-    if (lane < pb) rinv[warp][lane] = reinterpret_cast<const T*>(Wrdiag)[F.sn_c0[s] + p0 + lane];
+    if (lane < pb) rinv[warp][lane] = reinterpret_cast<const T*>(W.rdiag)[F.sn_c0[s] + p0 + lane];
     __syncwarp();
     const int r = ti * kTile + lane;
     if (r < f) {
@@ -743,11 +748,12 @@ __global__ void __launch_bounds__(32 * kTrsmWarps<T>) k_big_trsm(DevFactor F, T*
 // Trailing update of step p: tile (ti, tj) -= A_i A_j^T over the panel's
 // columns, restricted to rows >= cols >= p0 + pb.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, T* lx, const int4* work, int p) {
+__global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, DevWork W, T* lx, const int4* work, int p) {
     __shared__ T Ai[kTile][kTile + 1];
     __shared__ T Aj[kTile][kTile + 1];
     const int4 wk = work[blockIdx.x];
     const int s = wk.x, ti = wk.y, tj = wk.z;
+    if (front_frozen(F, W, s)) return;  // the whole CTA, before any barrier
     const int f = F.sn_f[s];
     const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
     T* B = lx + F.sn_lx_off[s];
@@ -961,14 +967,15 @@ __global__ void __launch_bounds__(kThreads) k_bwd(DevFactor F, const T* lx, cons
 // Forward sweep by continuation from the leaves (see continue_up).
 template <typename T, typename V>
 __global__ void __launch_bounds__(kThreads) k_fwd_flow(DevFactor F, DevWork W, const T* lx, const T* rdiag,
-                                                       SolveVecs sv, const int* ready, int n_ready,
+                                                       SolveVecs sv, const int* ready, const int* n_ready,
                                                        const int32_t* nchild, int* counter, int* cnt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ T D[kTile * (kTile + 1)];
     __shared__ int slot;
+    const int nr = *n_ready;
     for (;;) {
         const int item = claim(counter, &slot);
-        if (item >= n_ready) break;
+        if (item >= nr) break;
         int s = ready[item];
         while (s >= 0) {
             if (!front_frozen(F, W, s)) front_fwd<T, V>(F, lx, rdiag, sv, s, reinterpret_cast<V*>(smem_raw), D);
@@ -981,14 +988,15 @@ __global__ void __launch_bounds__(kThreads) k_fwd_flow(DevFactor F, DevWork W, c
 // Backward sweep as dataflow: order = fronts top-down, waits on the parent.
 template <typename T, typename V>
 __global__ void __launch_bounds__(kThreads) k_bwd_flow(DevFactor F, DevWork W, const T* lx, const T* rdiag,
-                                                       SolveVecs sv, const int* order, int n_items, int* counter,
-                                                       int* done) {
+                                                       SolveVecs sv, const int* order, const int* n_items,
+                                                       int* counter, int* done) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ T D[kTile * (kTile + 1)];
     __shared__ int slot;
+    const int ni = *n_items;
     for (;;) {
         const int item = claim(counter, &slot);
-        if (item >= n_items) break;
+        if (item >= ni) break;
         const int s = order[item];
         if (front_frozen(F, W, s)) {
             if (threadIdx.x == 0) publish_done(done + s);
@@ -1003,6 +1011,86 @@ __global__ void __launch_bounds__(kThreads) k_bwd_flow(DevFactor F, DevWork W, c
         if (threadIdx.x == 0) publish_done(done + s);
     }
 }
+
+// ---------------------------------------------------------------------------
+// Claim-list compaction for a batch.  The four lists (phase A, phase B,
+// forward leaves, backward order) are cut into chunks of kCompactChunk
+// entries, one CTA each.  Pass 1 counts each chunk's fronts whose grid is not
+// frozen; pass 2 offsets a chunk by the counts of the chunks before it in
+// the same list and writes its kept entries in their original order (the
+// claim order carries the critical-path priority and, for the backward
+// sweep, parents before children).  A frozen grid's fronts form whole trees
+// of their own, so no kept front has a dropped child or parent.
+// ---------------------------------------------------------------------------
+struct ReadyLists {
+    const int* src[4];
+    int* dst[4];
+    int n[4];
+    int chunk0[5];  // first chunk of each list; chunk0[4] = all chunks
+};
+
+__device__ __forceinline__ int list_of_chunk(const ReadyLists& R, int b) {
+    int l = 0;
+    while (l < 3 && b >= R.chunk0[l + 1]) ++l;
+    return l;
+}
+
+__device__ __forceinline__ bool claim_kept(const DevFactor& F, const DevWork& W, const ReadyLists& R, int l, int i) {
+    return i < R.n[l] && !(W.grid_flags[F.sn_grid[R.src[l][i]]] & FLAG_FROZEN);
+}
+
+constexpr int kCompactThreads = 256;
+static_assert(kCompactChunk % kCompactThreads == 0, "whole rounds per chunk");
+
+__global__ void __launch_bounds__(kCompactThreads) k_ready_count(DevFactor F, DevWork W, ReadyLists R, int* chunk_cnt) {
+    const int b = blockIdx.x;
+    const int l = list_of_chunk(R, b);
+    const int base = (b - R.chunk0[l]) * kCompactChunk;
+    int total = 0;
+    for (int r = 0; r < kCompactChunk; r += kCompactThreads)
+        total += __syncthreads_count(claim_kept(F, W, R, l, base + r + threadIdx.x));
+    if (threadIdx.x == 0) chunk_cnt[b] = total;
+}
+
+__global__ void __launch_bounds__(kCompactThreads) k_ready_compact(DevFactor F, DevWork W, ReadyLists R,
+                                                                    const int* chunk_cnt, int* counts) {
+    __shared__ int warp_n[kCompactThreads / 32];
+    __shared__ int s_off;
+    const int b = blockIdx.x;
+    const int l = list_of_chunk(R, b);
+    const int base = (b - R.chunk0[l]) * kCompactChunk;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // offset of this chunk: kept entries of the list's earlier chunks
+    int part = 0;
+    for (int q = R.chunk0[l] + threadIdx.x; q < b; q += kCompactThreads) part += chunk_cnt[q];
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+    if (lane == 0) warp_n[warp] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < kCompactThreads / 32; ++w) t += warp_n[w];
+        s_off = t;
+    }
+    __syncthreads();
+    int off = s_off;
+    for (int r = 0; r < kCompactChunk; r += kCompactThreads) {
+        const int i = base + r + threadIdx.x;
+        const bool keep = claim_kept(F, W, R, l, i);
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        __syncthreads();  // warp_n of the previous round has been read
+        if (lane == 0) warp_n[warp] = __popc(m);
+        __syncthreads();
+        int before = 0, all = 0;
+        for (int w = 0; w < kCompactThreads / 32; ++w) {
+            before += (w < warp) ? warp_n[w] : 0;
+            all += warp_n[w];
+        }
+        if (keep) R.dst[l][off + before + __popc(m & ((1u << lane) - 1u))] = R.src[l][i];
+        off += all;
+    }
+    if (threadIdx.x == 0 && b == R.chunk0[l + 1] - 1) counts[l] = off;
+}
+
 
 template <typename HV>
 __global__ void k_gain_export(DevNet net, DevFactor F, DevWork W, const HV* hval, int n_tgt, double* out) {
@@ -1054,13 +1142,13 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
         if (ls.flow_a_n > 0) {
             const int mf = ls.flow_a_maxf;
             k_front_flow<T, kPanelSmall, kMinBlocksA<T>><<<ls.flow_a_grid, kThreads, front_smem<T>(mf), st>>>(
-                F, W, gv, lx, ub, ls.d_flow_a, ls.flow_a_n, ls.d_phase, 1, ls.d_phase_nchild, counters + 0, W.flow);
+                F, W, gv, lx, ub, ls.d_flow_a, ls.d_ready_n + 0, ls.d_phase, 1, ls.d_phase_nchild, counters + 0, W.flow);
             count_launches(1);
         }
         if (ls.flow_b_n > 0) {
             const int mf = ls.flow_b_maxf;
             k_front_flow<T, kPanel, 1><<<ls.flow_b_grid, kThreads, front_smem<T>(mf), st>>>(
-                F, W, gv, lx, ub, ls.d_flow_b, ls.flow_b_n, ls.d_phase, 2, ls.d_phase_nchild, counters + 1, W.flow);
+                F, W, gv, lx, ub, ls.d_flow_b, ls.d_ready_n + 1, ls.d_phase, 2, ls.d_phase_nchild, counters + 1, W.flow);
             count_launches(1);
         }
     }
@@ -1074,7 +1162,7 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
         }
         const int na = ls.h_asm_ptr[l + 1] - ls.h_asm_ptr[l];
         if (na > 0) {
-            k_big_assemble<T><<<na, kThreads, 0, st>>>(F, gv, lx, ub, ls.d_asm + ls.h_asm_ptr[l]);
+            k_big_assemble<T><<<na, kThreads, 0, st>>>(F, W, gv, lx, ub, ls.d_asm + ls.h_asm_ptr[l]);
             count_launches(1);
             for (int p = 0; p < ls.h_lvl_panels[l]; ++p) {
                 const int slot = ls.h_step_ptr[l] + p;
@@ -1088,12 +1176,12 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
                     const int npan = ls.h_pan_ptr[slot + 1] - ls.h_pan_ptr[slot];
                     if (npan > 0) {
                         k_big_trsm<T><<<(npan + kTrsmWarps<T> - 1) / kTrsmWarps<T>, 32 * kTrsmWarps<T>, 0, st>>>(
-                            F, lx, W.rdiag, ls.d_pan + ls.h_pan_ptr[slot], npan, p);
+                            F, W, lx, ls.d_pan + ls.h_pan_ptr[slot], npan, p);
                         count_launches(1);
                     }
                 }
                 if (nupd > 0) {
-                    k_big_update<T><<<nupd, kThreads, 0, st>>>(F, lx, ls.d_upd + ls.h_upd_ptr[slot], p);
+                    k_big_update<T><<<nupd, kThreads, 0, st>>>(F, W, lx, ls.d_upd + ls.h_upd_ptr[slot], p);
                     count_launches(1);
                 }
             }
@@ -1114,10 +1202,10 @@ cudaError_t solve_impl(const DevFactor& F, const DevWork& W, const LevelSchedule
         cudaError_t e = cudaMemsetAsync(fwd_done, 0, sizeof(int) * (size_t)(2 * ns + 8), st);
         if (e != cudaSuccess) return e;
         const size_t smem = solve_smem<T>(ls.solve_maxf);
-        k_fwd_flow<T, T><<<ls.up_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_up, ls.up_n, ls.d_nchild,
-                                                             counters + 0, fwd_done);
-        k_bwd_flow<T, T><<<ls.solve_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_down, ns, counters + 1,
-                                                                bwd_done);
+        k_fwd_flow<T, T><<<ls.up_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_up, ls.d_ready_n + 2,
+                                                             ls.d_nchild, counters + 0, fwd_done);
+        k_bwd_flow<T, T><<<ls.solve_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_down, ls.d_ready_n + 3,
+                                                                counters + 1, bwd_done);
         count_launches(2);
         return cudaGetLastError();
     }
@@ -1159,6 +1247,23 @@ FlowGrids flow_grids_impl(int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf) {
 }
 
 }  // namespace
+
+cudaError_t launch_ready_compact(const DevFactor& F, const DevWork& W, const LevelSchedule& ls, cudaStream_t st) {
+    ReadyLists R;
+    R.chunk0[0] = 0;
+    for (int l = 0; l < 4; ++l) {
+        R.src[l] = ls.src_lists[l];
+        R.dst[l] = ls.cmp_lists[l];
+        R.n[l] = ls.src_n[l];
+        R.chunk0[l + 1] = R.chunk0[l] + (R.n[l] + kCompactChunk - 1) / kCompactChunk;
+    }
+    const int nb = R.chunk0[4];
+    if (nb == 0 || !W.grid_flags) return cudaSuccess;
+    k_ready_count<<<nb, kCompactThreads, 0, st>>>(F, W, R, ls.d_chunk_cnt);
+    k_ready_compact<<<nb, kCompactThreads, 0, st>>>(F, W, R, ls.d_chunk_cnt, ls.d_ready_n);
+    count_launches(2);
+    return cudaGetLastError();
+}
 
 FlowGrids flow_grids(bool mixed, int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf) {
     return mixed ? flow_grids_impl<float>(maxf_a, maxf_b, solve_maxf)

@@ -15,6 +15,7 @@ enum StatusFlag : uint32_t {
     FLAG_TIMEOUT = 8u,    // a dataflow wait gave up (bounded spin)
     FLAG_FROZEN = 16u,    // batch: this grid takes no further steps (inactive or finished)
     FLAG_INACTIVE = 32u,  // batch: this grid is not part of the current solve
+    FLAG_FINAL = 64u,     // batch: the grid's final evaluation and objective are due
 };
 
 // Per-solve scalars kept on the device; read back once per iteration.
@@ -163,7 +164,20 @@ struct DevBatch {
     const uint8_t* flat;      // [n_grids] 1 = flat start first
     int32_t* running;         // [1] grids still iterating after this step
     const uint8_t* retire;    // [n_grids] 1 = leave the running batch (stream mode)
+    // Per-grid reductions spread over many CTAs: a grid's buses (rows) are cut
+    // into items of kBatchChunk consecutive entries, items of a grid adjacent;
+    // item k = (grid, first entry).  Each item writes a partial, and one thread
+    // per grid combines its items' partials in item order (deterministic).
+    const int2* bus_items;       // [n_bus_items]
+    const int32_t* bus_item_ptr; // [n_grids + 1]
+    int32_t n_bus_items;
+    const int2* row_items;       // [n_row_items]
+    const int32_t* row_item_ptr; // [n_grids + 1]
+    int32_t n_row_items;
+    double* part;                // [max(n_bus_items, n_row_items)] partial max |dx| or sum w r^2
+    int32_t* part_bad;           // [n_bus_items] non-finite step seen
 };
+constexpr int kBatchChunk = 2048;
 
 struct SolveParams {
     int32_t exact_jacobian;  // 1: analytic derivatives of h(x); 0: the reference's formulas
@@ -173,6 +187,7 @@ struct SolveParams {
     double tol;
     double vmin, vmax;
     uint32_t skip_flags;     // batch: grids whose flags intersect this mask are not evaluated
+    uint32_t need_flags;     // batch: only grids whose flags hold every bit of this mask are evaluated
 };
 
 // Upload-time kernels.
@@ -244,14 +259,42 @@ struct LevelSchedule {
     const int32_t* d_nchild = nullptr;       // [n_super] children
     const int32_t* d_down = nullptr;
     int32_t solve_maxf = 0, solve_grid = 0, up_grid = 0;
+    // Lengths of the four claim lists (A, B, up, down) as the kernels read
+    // them, on the device.  In a batch the lists above are compacted copies:
+    // before every iteration launch_ready_compact keeps, in order, the
+    // entries of src_lists whose grid takes the step, so that fronts of
+    // frozen grids are never claimed and a pass costs what its active grids
+    // cost.  Outside a batch the lists are the full ones and the lengths fixed.
+    int32_t* d_ready_n = nullptr;
+    int32_t compact = 0;
+    const int32_t* src_lists[4] = {nullptr, nullptr, nullptr, nullptr};
+    int32_t* cmp_lists[4] = {nullptr, nullptr, nullptr, nullptr};
+    int32_t src_n[4] = {0, 0, 0, 0};
+    int32_t* d_chunk_cnt = nullptr;  // [ready_chunks(src_n)] scratch
 };
+
+// Entries per CTA of the claim-list compaction.
+constexpr int kCompactChunk = 2048;
+inline int32_t ready_chunks(const int32_t* n) {
+    int32_t c = 0;
+    for (int l = 0; l < 4; ++l) c += (n[l] + kCompactChunk - 1) / kCompactChunk;
+    return c;
+}
+// Batch: stable compaction of the claim lists to the fronts of grids that are
+// not frozen (two launches).
+cudaError_t launch_ready_compact(const DevFactor& f, const DevWork& w, const LevelSchedule& ls, cudaStream_t st);
 
 // Batch control: begin (flags, flat starts), per-grid update + convergence,
 // per-grid objective at the final state.
 cudaError_t launch_batch_begin(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st);
 cudaError_t launch_batch_update(const DevNet& net, const DevFactor& f, const DevWork& w, const DevBatch& b,
                                 const SolveParams& sp, const double* step, cudaStream_t st);
-cudaError_t launch_batch_objective(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st);
+// Objective of every grid that is not inactive and whose flags hold `need`.
+cudaError_t launch_batch_objective(const DevNet& net, const DevWork& w, const DevBatch& b, uint32_t need,
+                                   cudaStream_t st);
+// Stream mode: FLAG_FINAL on the grids with retire[g] = 1 (their final
+// evaluation follows); launch_batch_retire then freezes them and clears it.
+cudaError_t launch_batch_mark_final(const DevBatch& b, cudaStream_t st);
 // Topological islands (connected components over closed branches) on the
 // device: parent[n_bus] is scratch, out[0] = islands, out[1] = active rows.
 // Hooking of component roots along every closed branch (the larger root

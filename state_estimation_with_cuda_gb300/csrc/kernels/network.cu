@@ -158,7 +158,11 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
     __shared__ double sh[32];
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     double obj = 0.0;
-    const bool skip = q < net.n_meas && net.meas_grid && (w.grid_flags[net.meas_grid[q]] & sp.skip_flags);
+    bool skip = false;
+    if (q < net.n_meas && net.meas_grid) {
+        const uint32_t gf = w.grid_flags[net.meas_grid[q]];
+        skip = (gf & sp.skip_flags) || (gf & sp.need_flags) != sp.need_flags;
+    }
     if (q < net.n_meas && !skip) {
         const int kind = net.m_kind[q];
         const int ty = net.m_type[q];
@@ -566,32 +570,27 @@ __global__ void k_batch_activate(DevNet net, DevWork w, DevBatch b) {
 
 __global__ void k_batch_retire(DevBatch b) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g < b.n_grids && b.retire[g]) b.flags[g] |= FLAG_FROZEN | FLAG_INACTIVE;
+    if (g < b.n_grids && b.retire[g]) b.flags[g] = (b.flags[g] | FLAG_FROZEN | FLAG_INACTIVE) & ~FLAG_FINAL;
 }
 
-// Batch a13: one block per grid.  A grid that is frozen takes no step; a grid
-// whose factorisation flagged a non-positive pivot stops as singular without
-// applying the step; otherwise x += dx (slack angle fixed, V clamped) and the
-// grid stops when max |dx| < tol (converged) or dx is not finite (diverged),
-// exactly as the single-grid loop decides after its step.
-__global__ void __launch_bounds__(kBlock) k_batch_update(DevNet net, DevFactor f, DevWork w, DevBatch b,
-                                                         SolveParams sp, const double* step) {
+// Batch a13, spread over CTAs: each item applies the step to its buses and
+// writes its max |dx| and whether a step entry was not finite; then one
+// thread per grid combines its items and decides, exactly as the single-grid
+// loop does after its step: a frozen grid takes no step; a grid whose
+// factorisation flagged a non-positive pivot stops as singular without
+// applying the step; otherwise it stops when max |dx| < tol (converged) or
+// dx is not finite (diverged).
+__global__ void __launch_bounds__(kBlock) k_batch_update_part(DevFactor f, DevWork w, DevBatch b, SolveParams sp,
+                                                              const double* step) {
     __shared__ double sh[32];
-    __shared__ int bad;
-    const int g = blockIdx.x;
+    const int2 it = b.bus_items[blockIdx.x];
+    const int g = it.x;
     const uint32_t fl = b.flags[g];
-    if (fl & FLAG_FROZEN) return;
-    if (fl & FLAG_SINGULAR) {
-        if (threadIdx.x == 0) {
-            b.flags[g] = fl | FLAG_FROZEN;
-            b.iters[g] += 1;
-        }
-        return;
-    }
-    if (threadIdx.x == 0) bad = 0;
-    __syncthreads();
+    if (fl & (FLAG_FROZEN | FLAG_SINGULAR)) return;  // the whole CTA
+    const int end = min(it.y + kBatchChunk, b.bus_off[g + 1]);
     double mx = 0.0;
-    for (int i = b.bus_off[g] + threadIdx.x; i < b.bus_off[g + 1]; i += blockDim.x) {
+    int bad = 0;
+    for (int i = it.y + threadIdx.x; i < end; i += blockDim.x) {
         const int pt = f.bus_ps_theta[i];
         const double dv = step[f.bus_ps_v[i]];
         double dt = 0.0;
@@ -608,30 +607,71 @@ __global__ void __launch_bounds__(kBlock) k_batch_update(DevNet net, DevFactor f
         if (m != m) m = 0.0;
         mx = fmax(mx, m);
     }
+    bad = __syncthreads_or(bad);
     const double m = block_max(mx, sh);
     if (threadIdx.x == 0) {
-        b.mismatch[g] = m;
-        b.iters[g] += 1;
-        if (bad) {
-            b.flags[g] = fl | FLAG_NONFINITE | FLAG_FROZEN;
-        } else if (m < sp.tol) {
-            b.flags[g] = fl | FLAG_CONVERGED | FLAG_FROZEN;
-        } else {
-            atomicAdd(b.running, 1);
-        }
+        b.part[blockIdx.x] = m;
+        b.part_bad[blockIdx.x] = bad;
     }
 }
 
-// Batch objective sum w r^2 over each grid's rows in a fixed order.
-__global__ void __launch_bounds__(kBlock) k_batch_objective(DevNet net, DevWork w, DevBatch b) {
+__global__ void k_batch_update_fin(DevBatch b, double tol) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= b.n_grids) return;
+    const uint32_t fl = b.flags[g];
+    if (fl & FLAG_FROZEN) return;
+    if (fl & FLAG_SINGULAR) {
+        b.flags[g] = fl | FLAG_FROZEN;
+        b.iters[g] += 1;
+        return;
+    }
+    double m = 0.0;
+    int bad = 0;
+    for (int k = b.bus_item_ptr[g]; k < b.bus_item_ptr[g + 1]; ++k) {
+        m = fmax(m, b.part[k]);
+        bad |= b.part_bad[k];
+    }
+    b.mismatch[g] = m;
+    b.iters[g] += 1;
+    if (bad) {
+        b.flags[g] = fl | FLAG_NONFINITE | FLAG_FROZEN;
+    } else if (m < tol) {
+        b.flags[g] = fl | FLAG_CONVERGED | FLAG_FROZEN;
+    } else {
+        atomicAdd(b.running, 1);
+    }
+}
+
+// Objective sum w r^2 of each selected grid (not inactive, flags holding
+// `need`): per item in row order, then per grid over its items in order.
+__global__ void __launch_bounds__(kBlock) k_batch_objective_part(DevNet net, DevWork w, DevBatch b, uint32_t need) {
     __shared__ double sh[32];
-    const int g = blockIdx.x;
+    const int2 it = b.row_items[blockIdx.x];
+    const uint32_t fl = b.flags[it.x];
+    if ((fl & FLAG_INACTIVE) || (fl & need) != need) return;  // the whole CTA
+    const int end = min(it.y + kBatchChunk, b.meas_off[it.x + 1]);
     double acc = 0.0;
-    for (int q = b.meas_off[g] + threadIdx.x; q < b.meas_off[g + 1]; q += blockDim.x)
+    for (int q = it.y + threadIdx.x; q < end; q += blockDim.x)
         if (net.m_kind[q] != 5) acc += net.m_w[q] * w.r[q] * w.r[q];
     const double tot = block_sum(acc, sh);
-    if (threadIdx.x == 0) b.objective[g] = tot;
+    if (threadIdx.x == 0) b.part[blockIdx.x] = tot;
 }
+
+__global__ void k_batch_objective_fin(DevBatch b, uint32_t need) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= b.n_grids) return;
+    const uint32_t fl = b.flags[g];
+    if ((fl & FLAG_INACTIVE) || (fl & need) != need) return;
+    double t = 0.0;
+    for (int k = b.row_item_ptr[g]; k < b.row_item_ptr[g + 1]; ++k) t += b.part[k];
+    b.objective[g] = t;
+}
+
+__global__ void k_batch_mark_final(DevBatch b) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < b.n_grids && b.retire[g]) b.flags[g] |= FLAG_FINAL;
+}
+
 
 inline int nblocks(int n) { return (n + kBlock - 1) / kBlock; }
 
@@ -647,7 +687,11 @@ cudaError_t launch_batch_begin(const DevNet& net, const DevWork& w, const DevBat
 cudaError_t launch_batch_update(const DevNet& net, const DevFactor& f, const DevWork& w, const DevBatch& b,
                                 const SolveParams& sp, const double* step, cudaStream_t st) {
     if (b.n_grids <= 0) return cudaSuccess;
-    k_batch_update<<<b.n_grids, kBlock, 0, st>>>(net, f, w, b, sp, step);
+    if (b.n_bus_items > 0) {
+        k_batch_update_part<<<b.n_bus_items, kBlock, 0, st>>>(f, w, b, sp, step);
+        count_launches(1);
+    }
+    k_batch_update_fin<<<nblocks(b.n_grids), kBlock, 0, st>>>(b, sp.tol);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -696,9 +740,21 @@ cudaError_t launch_batch_retire(const DevBatch& b, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_objective(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st) {
+cudaError_t launch_batch_objective(const DevNet& net, const DevWork& w, const DevBatch& b, uint32_t need,
+                                   cudaStream_t st) {
     if (b.n_grids <= 0) return cudaSuccess;
-    k_batch_objective<<<b.n_grids, kBlock, 0, st>>>(net, w, b);
+    if (b.n_row_items > 0) {
+        k_batch_objective_part<<<b.n_row_items, kBlock, 0, st>>>(net, w, b, need);
+        count_launches(1);
+    }
+    k_batch_objective_fin<<<nblocks(b.n_grids), kBlock, 0, st>>>(b, need);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_mark_final(const DevBatch& b, cudaStream_t st) {
+    if (b.n_grids <= 0) return cudaSuccess;
+    k_batch_mark_final<<<nblocks(b.n_grids), kBlock, 0, st>>>(b);
     count_launches(1);
     return cudaGetLastError();
 }
