@@ -53,7 +53,11 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
  *                           fronts below the tiled ones and for the solves
  *   "flow_small_f"          widest front of the high-occupancy dataflow phase
  *                           (0 = default: 128 mixed, 64 FP64; at most 128;
- *                           re-uploads) */
+ *                           re-uploads)
+ *   "warp_fronts"           fronts whose whole subtree is at most 32 wide are
+ *                           factorised and solved one per warp: 1 on, 0 off,
+ *                           -1 (default) for each grid with at least 4096 of
+ *                           them (re-uploads) */
 SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* key, double value);
 
 typedef struct SLE_ExPlanInfo {

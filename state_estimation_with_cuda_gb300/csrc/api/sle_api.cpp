@@ -1151,6 +1151,7 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* k
     else if (k == "big_front_flops") { c.big_front_flops = value; E(handle)->model.structure_dirty = true; }
     else if (k == "dataflow") { c.dataflow = value != 0.0 ? 1 : 0; E(handle)->model.structure_dirty = true; }
     else if (k == "flow_small_f") { c.flow_small_f = static_cast<int32_t>(value); E(handle)->model.structure_dirty = true; }
+    else if (k == "warp_fronts") { c.warp_fronts = value < 0.0 ? -1 : (value != 0.0 ? 1 : 0); E(handle)->model.structure_dirty = true; }
     else return fail(SLE_ERROR_INVALID_ARGUMENT, "unknown option");
     return SLE_OK;
 }

@@ -150,12 +150,14 @@ void Engine::build_schedule() {
     sch_all_.clear();
     sch_asm_.clear();
     sch_pot_.clear();
+    n_pot_pairs_ = 0;
     sch_upd_.clear();
     sch_pot_ptr_.assign(1, 0);
     sch_pan_ptr_.assign(1, 0);
     sch_pan_.clear();
     sch_upd_ptr_.assign(1, 0);
     sch_flow_a_.clear();
+    sch_flow_w_.clear();
     sch_flow_b_.clear();
     sch_down_.clear();
     sch_up_.clear();
@@ -192,9 +194,33 @@ void Engine::build_schedule() {
                 sub_maxf[p] = std::max(sub_maxf[p], sub_maxf[s]);
             }
         }
+    // The warp phase is decided per grid (by default: from kWarpPhaseMinFronts
+    // candidate fronts of that grid on), so that a grid of a batch runs the
+    // same kernels, and gets the same result, as when it is solved alone.
+    std::vector<int32_t> front_grid(ns, 0);
+    int32_t n_groups = 1;
+    if (batch_mode()) {
+        int64_t total = 0;
+        for (const Plan& gp : grid_plans_) total += gp.n_super;
+        if (total == ns) {
+            int32_t x = 0;
+            n_groups = static_cast<int32_t>(grid_plans_.size());
+            for (int32_t g = 0; g < n_groups; ++g)
+                for (int32_t k = 0; k < grid_plans_[g].n_super; ++k) front_grid[x++] = g;
+        }
+    }
+    std::vector<int32_t> n_warp(n_groups, 0);
+    for (int32_t s = 0; s < ns; ++s)
+        if (cfg.dataflow && !sub_big[s] && sub_maxf[s] <= kWarpFrontMax) ++n_warp[front_grid[s]];
+    std::vector<char> warp_phase(n_groups, 0);
+    for (int32_t g = 0; g < n_groups; ++g)
+        warp_phase[g] = cfg.warp_fronts > 0 || (cfg.warp_fronts < 0 && n_warp[g] >= kWarpPhaseMinFronts);
     flow_phase_.assign(ns, 0);
     for (int32_t s = 0; s < ns; ++s)
-        if (cfg.dataflow && !sub_big[s]) flow_phase_[s] = sub_maxf[s] <= flow_small_f ? 1 : 2;
+        if (cfg.dataflow && !sub_big[s])
+            flow_phase_[s] = (warp_phase[front_grid[s]] && sub_maxf[s] <= kWarpFrontMax)
+                                 ? 3
+                                 : (sub_maxf[s] <= flow_small_f ? 1 : 2);
     int64_t lx = 0, uu = 0;
     for (int32_t s = 0; s < ns; ++s) {
         const int64_t f = P.sn_f[s], nc = P.sn_c0[s + 1] - P.sn_c0[s];
@@ -294,7 +320,14 @@ void Engine::build_schedule() {
                 const int32_t tiles = (f + kTile - 1) / kTile;
                 const int32_t pb = std::min(kTile, nc - p * kTile);
                 const int32_t q0 = p * kTile + pb;
-                sch_pot_.push_back(make_int4(s, p, 0, 0));
+                if (mixed_) {
+                    // one CTA per kPanelRows rows below the diagonal block
+                    const int32_t nch = std::max(1, (f - q0 + kPanelRows - 1) / kPanelRows);
+                    for (int32_t k = 0; k < nch; ++k) sch_pot_.push_back(make_int4(s, k, nch, n_pot_pairs_));
+                    ++n_pot_pairs_;
+                } else {
+                    sch_pot_.push_back(make_int4(s, p, 0, 0));
+                }
                 if (!mixed_)  // FP64: the panel's row tiles below go to the multi-CTA solve
                     for (int32_t ti = p + 1; ti < tiles; ++ti) sch_pan_.push_back(make_int4(s, ti, 0, 0));
                 if (q0 < f)
@@ -309,7 +342,11 @@ void Engine::build_schedule() {
         sch_asm_ptr_[l + 1] = static_cast<int32_t>(sch_asm_.size());
     }
     // every front, top-down, for the backward dataflow sweep
-    sch_down_.assign(sch_all_.rbegin(), sch_all_.rend());
+    // every front top-down for the backward sweeps: warp fronts apart
+    sch_down_.clear();
+    sch_down_w_.clear();
+    for (auto it = sch_all_.rbegin(); it != sch_all_.rend(); ++it)
+        (flow_phase_[*it] == 3 ? sch_down_w_ : sch_down_).push_back(*it);
     // continuation sweeps: children counts and initially ready fronts, the
     // ones with the most factor work on their path to the root first
     phase_nchild_.assign(ns, 0);
@@ -320,16 +357,18 @@ void Engine::build_schedule() {
         const double f = P.sn_f[s], nc = P.sn_c0[s + 1] - P.sn_c0[s];
         up_cost[s] = f * f * nc + (p >= 0 ? up_cost[p] : 0.0);
         if (p >= 0) {
-            ++nchild_[p];
+            if (flow_phase_[s] != 3) ++nchild_[p];  // the CTA forward sweep counts no warp fronts
             if (flow_phase_[p] != 0 && flow_phase_[p] == flow_phase_[s]) ++phase_nchild_[p];
         }
     }
     for (int32_t s = 0; s < ns; ++s) {
+        if (flow_phase_[s] == 3 && phase_nchild_[s] == 0) sch_flow_w_.push_back(s);
         if (flow_phase_[s] == 1 && phase_nchild_[s] == 0) sch_flow_a_.push_back(s);
         if (flow_phase_[s] == 2 && phase_nchild_[s] == 0) sch_flow_b_.push_back(s);
-        if (nchild_[s] == 0) sch_up_.push_back(s);
+        if (flow_phase_[s] != 3 && nchild_[s] == 0) sch_up_.push_back(s);
     }
     auto by_cost = [&](int32_t a, int32_t b) { return up_cost[a] > up_cost[b] || (up_cost[a] == up_cost[b] && a < b); };
+    std::sort(sch_flow_w_.begin(), sch_flow_w_.end(), by_cost);
     std::sort(sch_flow_a_.begin(), sch_flow_a_.end(), by_cost);
     std::sort(sch_flow_b_.begin(), sch_flow_b_.end(), by_cost);
     std::sort(sch_up_.begin(), sch_up_.end(), by_cost);
@@ -463,20 +502,23 @@ int32_t Engine::upload() {
         d_all_ = c.take<int32_t>(sch_all_.size());
         d_asm_ = c.take<int4>(sch_asm_.size());
         d_pot_ = c.take<int4>(sch_pot_.size());
+        d_pot_cnt_ = c.take<int32_t>(std::max(1, n_pot_pairs_));
         d_pan_ = c.take<int4>(sch_pan_.size());
         d_upd_ = c.take<int4>(sch_upd_.size());
         d_flow_a_ = c.take<int32_t>(sch_flow_a_.size());
         d_flow_b_ = c.take<int32_t>(sch_flow_b_.size());
         d_down_ = c.take<int32_t>(sch_down_.size());
         d_up_ = c.take<int32_t>(sch_up_.size());
+        d_flow_w_ = c.take<int32_t>(sch_flow_w_.size());
+        d_down_w_ = c.take<int32_t>(sch_down_w_.size());
         d_phase_ = c.take<int8_t>(ns);
         d_phase_nchild_ = c.take<int32_t>(ns);
         d_nchild_ = c.take<int32_t>(ns);
-        d_ready_n_ = c.take<int32_t>(4);
+        d_ready_n_ = c.take<int32_t>(kReadyLists);
         {
-            const int32_t src_n[4] = {static_cast<int32_t>(sch_flow_a_.size()), static_cast<int32_t>(sch_flow_b_.size()),
-                                      static_cast<int32_t>(sch_up_.size()), static_cast<int32_t>(sch_down_.size())};
-            for (int l = 0; l < 4; ++l) d_cmp_[l] = batch_mode() ? c.take<int32_t>(src_n[l]) : nullptr;
+            int32_t src_n[kReadyLists];
+            for (int l = 0; l < kReadyLists; ++l) src_n[l] = static_cast<int32_t>(claim_list(l).size());
+            for (int l = 0; l < kReadyLists; ++l) d_cmp_[l] = batch_mode() ? c.take<int32_t>(src_n[l]) : nullptr;
             d_chunk_cnt_ = batch_mode() ? c.take<int32_t>(std::max(1, ready_chunks(src_n))) : nullptr;
         }
         // work
@@ -649,29 +691,30 @@ int32_t Engine::upload() {
     chk(put(d_flow_b_, sch_flow_b_, st_));
     chk(put(d_down_, sch_down_, st_));
     chk(put(d_up_, sch_up_, st_));
+    chk(put(d_flow_w_, sch_flow_w_, st_));
+    chk(put(d_down_w_, sch_down_w_, st_));
     {
         std::vector<int8_t> ph(flow_phase_.begin(), flow_phase_.end());
         chk(put(d_phase_, ph, st_));
     }
     chk(put(d_phase_nchild_, phase_nchild_, st_));
     {
-        // phase-A fronts are factorised with kPanelFlowA-column panels, all others kTile
+        // phase-A fronts are factorised with kPanelFlowA-column panels, all
+        // others (warp fronts: one block of at most kWarpFrontMax) kTile
         std::vector<int8_t> pw(ns);
         for (int32_t x = 0; x < ns; ++x) pw[x] = static_cast<int8_t>(flow_phase_[x] == 1 ? kPanelFlowA : kTile);
         chk(put(const_cast<int8_t*>(fac_.sn_pw), pw, st_));
     }
     chk(put(d_nchild_, nchild_, st_));
     {
-        const std::vector<int32_t> n4 = {static_cast<int32_t>(sch_flow_a_.size()),
-                                         static_cast<int32_t>(sch_flow_b_.size()),
-                                         static_cast<int32_t>(sch_up_.size()), static_cast<int32_t>(sch_down_.size())};
-        chk(put(d_ready_n_, n4, st_));
+        std::vector<int32_t> nl(kReadyLists);
+        for (int l = 0; l < kReadyLists; ++l) nl[l] = static_cast<int32_t>(claim_list(l).size());
+        chk(put(d_ready_n_, nl, st_));
         // until the first compaction the batch lists are the full ones (every
         // factor or solve launch then finds valid lists)
-        const int32_t* src[4] = {d_flow_a_, d_flow_b_, d_up_, d_down_};
-        for (int l = 0; l < 4; ++l)
-            if (d_cmp_[l] && n4[l] > 0)
-                chk(cudaMemcpyAsync(d_cmp_[l], src[l], sizeof(int32_t) * n4[l], cudaMemcpyDeviceToDevice, st_));
+        for (int l = 0; l < kReadyLists; ++l)
+            if (d_cmp_[l] && nl[l] > 0)
+                chk(cudaMemcpyAsync(d_cmp_[l], claim_dev(l), sizeof(int32_t) * nl[l], cudaMemcpyDeviceToDevice, st_));
     }
     chk(put(work_.v, model.bus_v, st_));
     chk(put(work_.th, model.bus_th, st_));
@@ -693,6 +736,8 @@ int32_t Engine::upload() {
     sched_.h_step_ptr = sch_step_ptr_.data();
     sched_.h_pot_ptr = sch_pot_ptr_.data();
     sched_.d_pot = d_pot_;
+    sched_.d_pot_cnt = d_pot_cnt_;
+    sched_.n_pot_pairs = n_pot_pairs_;
     sched_.h_pan_ptr = sch_pan_ptr_.data();
     sched_.d_pan = d_pan_;
     sched_.h_upd_ptr = sch_upd_ptr_.data();
@@ -704,6 +749,12 @@ int32_t Engine::upload() {
     {
         const int32_t ms = max_solve_front();
         FlowGrids g = flow_grids(mixed_, flow_a_maxf_, flow_b_maxf_, ms);
+        sched_.d_flow_w = d_flow_w_;
+        sched_.flow_w_n = static_cast<int32_t>(sch_flow_w_.size());
+        sched_.flow_w_grid = std::max(1, std::min(g.w, sched_.flow_w_n));
+        sched_.d_down_w = d_down_w_;
+        sched_.down_w_n = static_cast<int32_t>(sch_down_w_.size());
+        sched_.solve_w_grid = std::max(1, std::min(g.wsolve, std::max(sched_.flow_w_n, sched_.down_w_n)));
         sched_.d_flow_a = d_flow_a_;
         sched_.flow_a_n = static_cast<int32_t>(sch_flow_a_.size());
         sched_.flow_a_maxf = flow_a_maxf_;
@@ -723,14 +774,12 @@ int32_t Engine::upload() {
         sched_.solve_grid = std::max(1, std::min(g.solve, ns));
         sched_.up_grid = std::max(1, std::min(g.solve, sched_.up_n));
         // claim-list lengths on the device; a batch claims from compacted copies
-        const int32_t* src[4] = {d_flow_a_, d_flow_b_, d_up_, d_down_};
-        const int32_t src_n[4] = {sched_.flow_a_n, sched_.flow_b_n, sched_.up_n, static_cast<int32_t>(sch_down_.size())};
         sched_.d_ready_n = d_ready_n_;
         sched_.compact = batch_mode() ? 1 : 0;
         sched_.d_chunk_cnt = d_chunk_cnt_;
-        for (int l = 0; l < 4; ++l) {
-            sched_.src_lists[l] = src[l];
-            sched_.src_n[l] = src_n[l];
+        for (int l = 0; l < kReadyLists; ++l) {
+            sched_.src_lists[l] = claim_dev(l);
+            sched_.src_n[l] = static_cast<int32_t>(claim_list(l).size());
             sched_.cmp_lists[l] = d_cmp_[l];
         }
         if (sched_.compact) {
@@ -738,6 +787,8 @@ int32_t Engine::upload() {
             sched_.d_flow_b = d_cmp_[1];
             sched_.d_up = d_cmp_[2];
             sched_.d_down = d_cmp_[3];
+            sched_.d_flow_w = d_cmp_[4];
+            sched_.d_down_w = d_cmp_[5];
         }
     }
 

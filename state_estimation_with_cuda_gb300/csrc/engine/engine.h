@@ -44,6 +44,8 @@ struct EngineConfig {
     int32_t dataflow = 1;            // persistent dataflow kernels below the big fronts and for the solves
     int32_t flow_small_f = 0;        // widest front of the high-occupancy dataflow phase (<= kFlowSmallFMax;
                                      // 0: 128 for the mixed pipeline, 64 for FP64)
+    int32_t warp_fronts = -1;        // warp phase for fronts whose subtree is at most kWarpFrontMax wide:
+                                     // 1 on, 0 off, -1 per grid with at least kWarpPhaseMinFronts of them
     int32_t stream_priority = 0;     // CUDA stream priority of the engine's stream (lower = more urgent)
 };
 
@@ -202,18 +204,32 @@ private:
         sch_pot_ptr_, sch_pan_ptr_, sch_upd_ptr_, sch_all_ptr_, sch_all_, sch_maxf_;
     std::vector<int4> sch_asm_, sch_pot_, sch_pan_, sch_upd_;
     std::vector<int64_t> sch_maxpanel_;
-    std::vector<int32_t> sch_flow_a_, sch_flow_b_, sch_down_, sch_up_, phase_nchild_, nchild_;
+    std::vector<int32_t> sch_flow_a_, sch_flow_b_, sch_down_, sch_up_, sch_flow_w_, sch_down_w_, phase_nchild_, nchild_;
     std::vector<char> flow_phase_;
     int32_t flow_a_maxf_ = 0, flow_b_maxf_ = 0;
     int32_t* d_flow_a_ = nullptr;
     int32_t* d_flow_b_ = nullptr;
     int32_t* d_down_ = nullptr;
     int32_t* d_up_ = nullptr;
+    int32_t* d_flow_w_ = nullptr;
+    int32_t* d_down_w_ = nullptr;
+    // the claim lists in LevelSchedule::src_lists order (A, B, up, down, warp, warp down)
+    const std::vector<int32_t>& claim_list(int l) const {
+        const std::vector<int32_t>* v[kReadyLists] = {&sch_flow_a_, &sch_flow_b_, &sch_up_, &sch_down_, &sch_flow_w_,
+                                                      &sch_down_w_};
+        return *v[l];
+    }
+    int32_t* claim_dev(int l) const {
+        int32_t* v[kReadyLists] = {d_flow_a_, d_flow_b_, d_up_, d_down_, d_flow_w_, d_down_w_};
+        return v[l];
+    }
     int8_t* d_phase_ = nullptr;
     int32_t* d_phase_nchild_ = nullptr;
     int32_t* d_nchild_ = nullptr;
     int32_t* d_ready_n_ = nullptr;               // [4] claim-list lengths
-    int32_t* d_cmp_[4] = {nullptr, nullptr, nullptr, nullptr};  // batch: compacted claim lists
+    int32_t* d_pot_cnt_ = nullptr;               // FP32 tiled fronts: per (front, step) tile readers
+    int32_t n_pot_pairs_ = 0;
+    int32_t* d_cmp_[kReadyLists] = {};  // batch: compacted claim lists
     int32_t* d_chunk_cnt_ = nullptr;             // batch: compaction scratch
     std::vector<int2> bus_items_, row_items_;    // batch: per-grid reduction items
     std::vector<int32_t> bus_item_ptr_, row_item_ptr_;

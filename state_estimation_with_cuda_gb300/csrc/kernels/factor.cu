@@ -291,6 +291,119 @@ __device__ __forceinline__ void warp_trinv(const T (*lt)[LTLD], const T* rinv, i
     }
 }
 
+constexpr int kWarpsPerCta = kThreads / 32;
+constexpr int kWtLd = kWarpFrontMax + 1;
+
+template <typename T>
+struct WarpTile {
+    T a[kWarpFrontMax * kWtLd];  // a[c * kWtLd + r] = front entry (r, c)
+    T rinv[kWarpFrontMax];
+};
+
+__device__ __forceinline__ int warp_claim(int* counter) {
+    int item = 0;
+    if ((threadIdx.x & 31) == 0) item = atomicAdd(counter, 1);
+    return __shfl_sync(0xffffffffu, item, 0);
+}
+
+// Lane 0 counts finished front s into its parent when the parent belongs to
+// the same phase; returns the parent when this completed its last child.
+__device__ __forceinline__ int warp_continue_up(const DevFactor& F, const int8_t* phase, int ph, const int32_t* nchild,
+                                                int* cnt, int s) {
+    __syncwarp();
+    int nxt = -1;
+    if ((threadIdx.x & 31) == 0) {
+        const int p = F.sn_parent[s];
+        if (p >= 0 && phase[p] == ph) {
+            __threadfence();
+            if (atomicAdd(cnt + p, 1) + 1 == nchild[p]) {
+                __threadfence();
+                nxt = p;
+            }
+        }
+    }
+    nxt = __shfl_sync(0xffffffffu, nxt, 0);
+    __syncwarp();
+    return nxt;
+}
+
+template <typename T>
+__device__ void warp_front_factor(const DevFactor& F, const DevWork& W, const T* gv, T* lx, T* ub, int s,
+                                  WarpTile<T>& t) {
+    const int lane = threadIdx.x & 31;
+    const int f = F.sn_f[s];
+    const int c0 = F.sn_c0[s];
+    const int nc = F.sn_c0[s + 1] - c0;
+    for (int c = 0; c < f; ++c) t.a[c * kWtLd + lane] = T(0);
+    __syncwarp();
+    {
+        // original entries, four per lane in flight
+        const int tg0 = F.sn_tgt_ptr[s], tg1 = F.sn_tgt_ptr[s + 1];
+        for (int tb = tg0; tb < tg1; tb += 128) {
+            T g[4];
+            int l[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int tg = tb + lane + 32 * q;
+                l[q] = tg < tg1 ? F.tgt_local[tg] : -1;  // row + col * f
+                g[q] = tg < tg1 ? gv[tg] : T(0);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (l[q] >= 0) {
+                    const int c = l[q] / f;
+                    t.a[c * kWtLd + (l[q] - c * f)] = g[q];
+                }
+        }
+    }
+    __syncwarp();
+    for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) {
+        const int ch = F.sn_child[ci];
+        const int m = F.sn_f[ch] - (F.sn_c0[ch + 1] - F.sn_c0[ch]);  // < kWarpFrontMax: the parent holds m rows
+        const T* U = update_of<T>(F, lx, ub, ch);
+        const int uld = F.sn_u_ld[ch];
+        const int ri = lane < m ? F.sn_relmap[F.sn_su_off[ch] + lane] : 0;
+        for (int j = 0; j < m; j += 4) {
+            T u[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                u[q] = (j + q < m && lane >= j + q && lane < m) ? __ldcg(U + lane + (int64_t)(j + q) * uld) : T(0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int rj = __shfl_sync(0xffffffffu, ri, (j + q) & 31);
+                if (j + q < m && lane >= j + q && lane < m) t.a[rj * kWtLd + ri] += u[q];
+            }
+        }
+        __syncwarp();
+    }
+    T a[kWarpFrontMax];
+#pragma unroll
+    for (int j = 0; j < kWarpFrontMax; ++j) a[j] = (lane < f && j <= lane) ? t.a[j * kWtLd + lane] : T(0);
+    T inv;
+    const bool bad = warp_potrf<T, kWarpFrontMax>(a, nc, lane, &inv);
+    if (bad && lane == 0) atomicOr(singular_flags(F, W, s), FLAG_SINGULAR);
+    if (lane < nc) reinterpret_cast<T*>(W.rdiag)[c0 + lane] = inv;
+    T* L = lx + F.sn_lx_off[s];
+    const int row0 = kInvDiag<T> ? nc : 0;  // FP32 writes its diagonal block as L11^-1 below
+#pragma unroll
+    for (int c = 0; c < kWarpFrontMax; ++c)
+        if (c < nc && lane < f && lane >= c && lane >= row0) L[lane + c * f] = a[c];
+    const int m = f - nc;
+    T* Uo = ub + F.sn_u_off[s];
+#pragma unroll
+    for (int j = 0; j < kWarpFrontMax; ++j)
+        if (j >= nc && lane >= j && lane < f) Uo[(lane - nc) + (j - nc) * m] = a[j];
+    if constexpr (kInvDiag<T>) {
+        __syncwarp();
+#pragma unroll
+        for (int c = 0; c < kWarpFrontMax; ++c)
+            if (c <= lane && lane < nc) t.a[c * kWtLd + lane] = a[c];
+        if (lane < nc) t.rinv[lane] = inv;
+        __syncwarp();
+        warp_trinv<T, kWarpFrontMax, kWtLd>(reinterpret_cast<const T (*)[kWtLd]>(t.a), t.rinv, nc, lane, L, f);
+    }
+}
+
 // Shared-memory scratch of one front besides the front itself.
 template <typename T>
 struct FrontSmem {
@@ -600,11 +713,16 @@ __global__ void __launch_bounds__(kThreads) k_big_assemble(DevFactor F, DevWork 
     }
 }
 
-// Panel step p, part 1 (one CTA per front): factor the diagonal tile in
-// place, then solve the rows below it against it (FP32: the whole column
-// panel; FP64: tile p only, the rest by k_big_trsm); then the trailing update.
+// FP64 panel step p, part 1 (one CTA per front): one warp factors the
+// diagonal tile through shared memory (a shuffle moves half a double, so the
+// register form is slower for FP64) and writes L_dd back; the other warps
+// solve the rows of tile p below the block (x = a L_dd^-T by forward
+// substitution in registers; volatile reads keep the compiler from hoisting
+// the factor into registers across rows).  k_big_trsm takes the row tiles
+// below on many CTAs; then the trailing update.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, T* lx, const int4* work, int p) {
+    static_assert(sizeof(T) == 8, "FP32 panels use k_big_panel32");
     constexpr int ld = kTile + 1;
     __shared__ T D[kTile * ld];
     __shared__ T rdiag[kTile];
@@ -620,65 +738,35 @@ __global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, 
         D[i + j * ld] = (i >= j) ? B[(p0 + i) + (int64_t)(p0 + j) * f] : T(0);
     }
     __syncthreads();
-    // one warp factors the tile, lane i owning row i: FP32 in registers with
-    // shuffles; FP64 through shared memory (a shuffle moves half a double, so
-    // the register form is slower for FP64)
     if (threadIdx.x < 32) {
         const int i = threadIdx.x;
-        if constexpr (sizeof(T) == 4) {
-            T a[kTile];
-#pragma unroll
-            for (int j = 0; j < kTile; ++j) a[j] = (i < pb && j <= i) ? D[i + j * ld] : T(0);
-            T inv;
-            const bool bad = warp_potrf<T, kTile>(a, pb, i, &inv);
-            if (bad && i == 0) atomicOr(singular_flags(F, W, s), FLAG_SINGULAR);
-#pragma unroll
-            for (int j = 0; j < kTile; ++j)
-                if (i < pb && j <= i) D[i + j * ld] = a[j];
-            if (i < pb) {
-                rdiag[i] = inv;
-                reinterpret_cast<T*>(W.rdiag)[F.sn_c0[s] + p0 + i] = inv;
+        for (int k = 0; k < pb; ++k) {
+            if (i == k) {
+                T sq, inv;
+                pivot(D[k + k * ld], &sq, &inv, singular_flags(F, W, s));
+                D[k + k * ld] = sq;
+                rdiag[k] = inv;
+                reinterpret_cast<T*>(W.rdiag)[F.sn_c0[s] + p0 + k] = inv;
             }
-        } else {
-            for (int k = 0; k < pb; ++k) {
-                if (i == k) {
-                    T sq, inv;
-                    pivot(D[k + k * ld], &sq, &inv, singular_flags(F, W, s));
-                    D[k + k * ld] = sq;
-                    rdiag[k] = inv;
-                    reinterpret_cast<T*>(W.rdiag)[F.sn_c0[s] + p0 + k] = inv;
-                }
-                __syncwarp();
-                const T inv = rdiag[k];
-                if (i > k && i < pb) D[i + k * ld] *= inv;
-                __syncwarp();
-                if (i > k && i < pb) {
-                    const T lik = D[i + k * ld];
-                    for (int j = k + 1; j <= i; ++j) D[i + j * ld] -= lik * D[j + k * ld];
-                }
-                __syncwarp();
+            __syncwarp();
+            const T inv = rdiag[k];
+            if (i > k && i < pb) D[i + k * ld] *= inv;
+            __syncwarp();
+            if (i > k && i < pb) {
+                const T lik = D[i + k * ld];
+                for (int j = k + 1; j <= i; ++j) D[i + j * ld] -= lik * D[j + k * ld];
             }
+            __syncwarp();
         }
     }
     __syncthreads();
-    // Warp 0 writes the diagonal tile's slot: L_dd^-1 for FP32, L_dd for
-    // FP64.  Warps 1..: rows below the diagonal block, one per thread,
-    // x = a L_dd^-T by forward substitution in registers (volatile reads keep
-    // the compiler from hoisting the factor into registers across rows).
-    // FP32: the whole column panel; FP64: the rest of tile p only (k_big_trsm
-    // takes the tiles below on many CTAs).
     if (threadIdx.x < 32) {
         const int i = threadIdx.x;
-        if constexpr (kInvDiag<T>) {
-            warp_trinv<T, kTile, kTile + 1>(reinterpret_cast<const T (*)[kTile + 1]>(D), rdiag, pb, i,
-                                            B + p0 + (int64_t)p0 * f, f);
-        } else {
-            for (int j = 0; j < pb; ++j)
-                if (i >= j && i < pb) B[(p0 + i) + (int64_t)(p0 + j) * f] = D[i + j * ld];
-        }
+        for (int j = 0; j < pb; ++j)
+            if (i >= j && i < pb) B[(p0 + i) + (int64_t)(p0 + j) * f] = D[i + j * ld];
     } else {
         const volatile T* Dv = D;
-        const int r_end = (sizeof(T) == 4) ? f : min(p0 + kTile, f);
+        const int r_end = min(p0 + kTile, f);
 #pragma unroll 1
         for (int r = p0 + pb + threadIdx.x - 32; r < r_end; r += blockDim.x - 32) {
             T x[kTile];
@@ -695,6 +783,119 @@ __global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, 
 #pragma unroll
             for (int c = 0; c < kTile; ++c)
                 if (c < pb) B[r + (int64_t)(p0 + c) * f] = x[c];
+        }
+    }
+}
+
+// FP32 panel step p of the tiled fronts in one launch.  The rows below the
+// diagonal block are cut into chunks of kPanelRows, one CTA each.  Every CTA
+// factors the 32 x 32 diagonal block itself (warp 0, in registers) and
+// inverts it while the other warps stage the chunk's rows of the panel; then
+// it solves the chunk as X = A L_dd^-T = A (L_dd^-1)^T, a register-tiled
+// product with 4 x 4 outputs per thread.  The CTA that reads the diagonal
+// tile last (a counter per front and step) writes L_dd^-1 into it for the
+// solves: no CTA reads an overwritten tile, and none waits for another.
+__global__ void __launch_bounds__(kThreads) k_big_panel32(DevFactor F, DevWork W, float* lx, const int4* work, int p,
+                                                          int* step_cnt) {
+    static_assert(kThreads == 256 && kPanelRows == 128 && kTile == 32, "thread tiling below");
+    constexpr int ld = kTile + 1;
+    constexpr int lt_ld = kTile + 4;       // 16-byte aligned rows
+    constexpr int as_ld = kPanelRows + 4;  // 16-byte aligned rows
+    __shared__ float D[kTile * ld];        // D[i + j * ld] = L_dd[i][j]
+    __shared__ float rdiag[kTile];
+    __shared__ __align__(16) float Lt[kTile * lt_ld];  // Lt[k][c] = L_dd^-1[c][k]
+    __shared__ __align__(16) float As[kTile * as_ld];  // As[k][r] = A[r0 + r][k], then X
+    __shared__ int last;
+    const int4 wk = work[blockIdx.x];
+    const int s = wk.x, chunk = wk.y, nchunk = wk.z, pair = wk.w;
+    if (front_frozen(F, W, s)) return;  // the whole CTA, before any barrier
+    const int f = F.sn_f[s];
+    const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
+    float* B = lx + F.sn_lx_off[s];
+    const int p0 = p * kTile;
+    const int pb = min(kTile, nc - p0);
+    const int r0 = p0 + pb + chunk * kPanelRows;    // first row of the chunk
+    const int nr = max(0, min(kPanelRows, f - r0));  // its rows
+    const int tid = threadIdx.x;
+    {
+        // all staging loads in flight before the first shared-memory store:
+        // thread (j, i) with i = tid % 32 reads column j = tid / 32 + 8 q of
+        // the diagonal tile and rows i + 32 u of the chunk's column
+        constexpr int kQ = kTile / (kThreads / 32);  // columns per thread
+        const int i = tid & 31, j0 = tid >> 5;
+        float dv[kQ], av[kQ][kPanelRows / 32];
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) {
+            const int j = j0 + q * (kThreads / 32);
+            const float* col = B + (int64_t)(p0 + j) * f;
+            dv[q] = (j < pb && i < pb && i >= j) ? col[p0 + i] : 0.f;
+#pragma unroll
+            for (int u = 0; u < kPanelRows / 32; ++u) {
+                const int r = i + 32 * u;
+                av[q][u] = (j < pb && r < nr) ? col[r0 + r] : 0.f;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) {
+            const int j = j0 + q * (kThreads / 32);
+            D[i + j * ld] = dv[q];
+            Lt[j * lt_ld + i] = 0.f;
+#pragma unroll
+            for (int u = 0; u < kPanelRows / 32; ++u) As[j * as_ld + i + 32 * u] = av[q][u];
+        }
+    }
+    __syncthreads();
+    if (tid == 0) last = (atomicAdd(step_cnt + pair, 1) == nchunk - 1);  // this CTA's tile reads are done
+    if (tid < 32) {
+        const int i = tid;
+        float a[kTile];
+#pragma unroll
+        for (int j = 0; j < kTile; ++j) a[j] = (i < pb && j <= i) ? D[i + j * ld] : 0.f;
+        float inv;
+        const bool bad = warp_potrf<float, kTile>(a, pb, i, &inv);
+        if (bad && i == 0 && chunk == 0) atomicOr(singular_flags(F, W, s), FLAG_SINGULAR);
+#pragma unroll
+        for (int j = 0; j < kTile; ++j)
+            if (i < pb && j <= i) D[i + j * ld] = a[j];
+        if (i < pb) rdiag[i] = inv;
+        if (chunk == 0 && i < pb) reinterpret_cast<float*>(W.rdiag)[F.sn_c0[s] + p0 + i] = inv;
+        __syncwarp();
+        warp_trinv<float, kTile, ld>(reinterpret_cast<const float (*)[ld]>(D), rdiag, pb, i, Lt, lt_ld);
+    }
+    __syncthreads();
+    {
+        // thread (rg, cg): rows 4rg..4rg+3, columns 4cg..4cg+3 of the chunk
+        const int cg = tid & 7, rg = tid >> 3;
+        float acc[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+#pragma unroll 8
+        for (int k = 0; k < kTile; ++k) {
+            const float4 a4 = *reinterpret_cast<const float4*>(&As[k * as_ld + 4 * rg]);
+            const float4 l4 = *reinterpret_cast<const float4*>(&Lt[k * lt_ld + 4 * cg]);
+            const float av[4] = {a4.x, a4.y, a4.z, a4.w}, lv[4] = {l4.x, l4.y, l4.z, l4.w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int v = 0; v < 4; ++v) acc[u][v] += av[u] * lv[v];
+        }
+        __syncthreads();  // every read of A is done
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+            *reinterpret_cast<float4*>(&As[(4 * cg + v) * as_ld + 4 * rg]) =
+                make_float4(acc[0][v], acc[1][v], acc[2][v], acc[3][v]);
+    }
+    __syncthreads();
+    for (int x = tid; x < kTile * kPanelRows; x += kThreads) {
+        const int r = x % kPanelRows, k = x / kPanelRows;
+        if (r < nr && k < pb) B[(r0 + r) + (int64_t)(p0 + k) * f] = As[k * as_ld + r];
+    }
+    if (last) {
+        for (int x = tid; x < pb * pb; x += kThreads) {
+            const int i = x % pb, j = x / pb;
+            if (i >= j) B[(p0 + i) + (int64_t)(p0 + j) * f] = Lt[j * lt_ld + i];
         }
     }
 }
@@ -792,6 +993,114 @@ struct SolveVecs {
     void* sol;        // [n_state] solution, permuted (V)
     void* su;         // solve update vectors (V)
 };
+
+// Forward step of a warp front: v = [b of own columns; 0] + children's update
+// vectors (in child order), y = L11^-1 v1, update vector v2 - L21 y.
+template <typename T, typename V>
+__device__ void warp_front_fwd(const DevFactor& F, const T* lx, const T* rdiag, const SolveVecs& sv, int s, V* v) {
+    const V* rhs = reinterpret_cast<const V*>(sv.rhs);
+    V* sol = reinterpret_cast<V*>(sv.sol);
+    V* sub = reinterpret_cast<V*>(sv.su);
+    const int lane = threadIdx.x & 31;
+    const int f = F.sn_f[s];
+    const int c0 = F.sn_c0[s];
+    const int nc = F.sn_c0[s + 1] - c0;
+    const T* L = lx + F.sn_lx_off[s];
+    const V rd = (!kInvDiag<T> && lane < nc) ? static_cast<V>(rdiag[c0 + lane]) : V(0);
+    v[lane] = (lane < nc) ? rhs[c0 + lane] : V(0);
+    __syncwarp();
+    const int cp0 = F.sn_child_ptr[s], cp1 = F.sn_child_ptr[s + 1];
+    for (int cb = cp0; cb < cp1; cb += 8) {
+        V val[8];
+        int row[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            row[u] = -1;
+            val[u] = V(0);
+            if (cb + u < cp1) {
+                const int c = F.sn_child[cb + u];
+                const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
+                if (lane < m) {
+                    const int64_t o = F.sn_su_off[c];
+                    val[u] = __ldcg(sub + o + lane);
+                    row[u] = F.sn_relmap[o + lane];
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (row[u] >= 0) v[row[u]] += val[u];
+            __syncwarp();
+        }
+    }
+    V y = V(0);
+    if constexpr (kInvDiag<T>) {
+        if (lane < nc)
+            for (int j = 0; j <= lane; ++j) y += static_cast<V>(L[lane + j * f]) * v[j];
+        __syncwarp();
+        if (lane < nc) v[lane] = y;
+    } else {
+        for (int k = 0; k < nc; ++k) {
+            const V yk = v[k] * __shfl_sync(0xffffffffu, rd, k);
+            __syncwarp();
+            if (lane > k && lane < nc) v[lane] -= static_cast<V>(L[lane + k * f]) * yk;
+            if (lane == 0) v[k] = yk;
+            __syncwarp();
+        }
+        y = lane < nc ? v[lane] : V(0);
+    }
+    __syncwarp();
+    if (lane < nc) {
+        sol[c0 + lane] = y;
+    } else if (lane < f) {
+        V acc = v[lane];
+        for (int k = 0; k < nc; ++k) acc -= static_cast<V>(L[lane + k * f]) * v[k];
+        sub[F.sn_su_off[s] + (lane - nc)] = acc;
+    }
+    __syncwarp();
+}
+
+// Backward step of a warp front: t = y - L21^T x2, x1 = L11^-T t (lane c
+// computes column c).
+template <typename T, typename V>
+__device__ void warp_front_bwd(const DevFactor& F, const T* lx, const T* rdiag, const SolveVecs& sv, int s, V* x) {
+    V* sol = reinterpret_cast<V*>(sv.sol);
+    const int lane = threadIdx.x & 31;
+    const int f = F.sn_f[s];
+    const int c0 = F.sn_c0[s];
+    const int nc = F.sn_c0[s + 1] - c0;
+    const int* rows = F.sn_rows + F.sn_rows_off[s];
+    const T* L = lx + F.sn_lx_off[s];
+    const V rd = (!kInvDiag<T> && lane < nc) ? static_cast<V>(rdiag[c0 + lane]) : V(0);
+    x[lane] = lane < f ? (lane < nc ? __ldcg(sol + c0 + lane) : __ldcg(sol + rows[lane])) : V(0);
+    __syncwarp();
+    V t = V(0);
+    if (lane < nc) {
+        t = x[lane];
+        for (int r = nc; r < f; ++r) t -= static_cast<V>(L[r + lane * f]) * x[r];
+    }
+    __syncwarp();
+    if (lane < nc) x[lane] = t;
+    __syncwarp();
+    if constexpr (kInvDiag<T>) {
+        V val = V(0);
+        if (lane < nc)
+            for (int i = lane; i < nc; ++i) val += static_cast<V>(L[i + lane * f]) * x[i];
+        __syncwarp();
+        if (lane < nc) x[lane] = val;
+    } else {
+        for (int k = nc - 1; k >= 0; --k) {
+            const V xk = x[k] * __shfl_sync(0xffffffffu, rd, k);
+            __syncwarp();
+            if (lane < k) x[lane] -= static_cast<V>(L[k + lane * f]) * xk;
+            if (lane == 0) x[k] = xk;
+            __syncwarp();
+        }
+    }
+    __syncwarp();
+    if (lane < nc) sol[c0 + lane] = x[lane];
+    __syncwarp();
+}
 
 template <typename T, typename V>
 __device__ void front_fwd(const DevFactor& F, const T* lx, const T* rdiag, const SolveVecs& sv, int s, V* v, T* D) {
@@ -1013,8 +1322,87 @@ __global__ void __launch_bounds__(kThreads) k_bwd_flow(DevFactor F, DevWork W, c
 }
 
 // ---------------------------------------------------------------------------
-// Claim-list compaction for a batch.  The four lists (phase A, phase B,
-// forward leaves, backward order) are cut into chunks of kCompactChunk
+// Warp fronts: a front whose whole subtree is at most kWarpFrontMax wide is
+// handled by one warp (eight fronts per CTA, no block barriers).  Factor: the
+// front is assembled in the warp's tile in shared memory (original entries,
+// then the children's update matrices in child order), loaded row per lane
+// into registers and partially factorised there (the first nc pivots, which
+// also leave the Schur complement in the trailing columns), then L (FP32:
+// with L11^-1 in its diagonal block) and the update matrix are written out.
+// Solves: the forward and backward steps of the same fronts, a lane per row.
+// A warp continues with the parent when it completes the parent's last child
+// in the same phase, as the CTA sweeps do.
+// ---------------------------------------------------------------------------
+template <typename T>
+constexpr int kMinBlocksW = sizeof(T) == 4 ? 2 : 1;
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads, kMinBlocksW<T>) k_front_warp(DevFactor F, DevWork W, const T* gv, T* lx,
+                                                                         T* ub, const int* ready, const int* n_ready,
+                                                                         const int8_t* phase, int ph,
+                                                                         const int32_t* nchild, int* counter,
+                                                                         int* cnt) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    WarpTile<T>& t = reinterpret_cast<WarpTile<T>*>(smem_raw)[threadIdx.x >> 5];
+    const int nr = *n_ready;
+    for (;;) {
+        const int item = warp_claim(counter);
+        if (item >= nr) break;
+        int s = ready[item];
+        while (s >= 0) {
+            if (!front_frozen(F, W, s)) warp_front_factor<T>(F, W, gv, lx, ub, s, t);
+            s = warp_continue_up(F, phase, ph, nchild, cnt, s);
+        }
+    }
+}
+
+template <typename T, typename V>
+__global__ void __launch_bounds__(kThreads) k_fwd_warp(DevFactor F, DevWork W, const T* lx, const T* rdiag,
+                                                       SolveVecs sv, const int* ready, const int* n_ready,
+                                                       const int8_t* phase, int ph, const int32_t* nchild,
+                                                       int* counter, int* cnt) {
+    __shared__ V vw[kWarpsPerCta][kWarpFrontMax];
+    V* v = vw[threadIdx.x >> 5];
+    const int nr = *n_ready;
+    for (;;) {
+        const int item = warp_claim(counter);
+        if (item >= nr) break;
+        int s = ready[item];
+        while (s >= 0) {
+            if (!front_frozen(F, W, s)) warp_front_fwd<T, V>(F, lx, rdiag, sv, s, v);
+            s = warp_continue_up(F, phase, ph, nchild, cnt, s);
+        }
+    }
+}
+
+// Backward steps of the warp fronts in top-down order, each waiting (bounded)
+// on its parent's flag; parents outside the warp phase finished in the CTA
+// sweep before this launch.
+template <typename T, typename V>
+__global__ void __launch_bounds__(kThreads) k_bwd_warp(DevFactor F, DevWork W, const T* lx, const T* rdiag,
+                                                       SolveVecs sv, const int* order, const int* n_items,
+                                                       int* counter, int* done) {
+    __shared__ V xw[kWarpsPerCta][kWarpFrontMax];
+    V* x = xw[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int ni = *n_items;
+    for (;;) {
+        const int item = warp_claim(counter);
+        if (item >= ni) break;
+        const int s = order[item];
+        if (!front_frozen(F, W, s)) {
+            if (lane == 0 && F.sn_parent[s] >= 0) wait_done(done + F.sn_parent[s], &W.status->flags);
+            __syncwarp();
+            warp_front_bwd<T, V>(F, lx, rdiag, sv, s, x);
+        }
+        if (lane == 0) publish_done(done + s);
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Claim-list compaction for a batch.  The lists (phase A, phase B, forward
+// leaves, backward order, warp phase, warp backward order) are cut into chunks of kCompactChunk
 // entries, one CTA each.  Pass 1 counts each chunk's fronts whose grid is not
 // frozen; pass 2 offsets a chunk by the counts of the chunks before it in
 // the same list and writes its kept entries in their original order (the
@@ -1023,15 +1411,15 @@ __global__ void __launch_bounds__(kThreads) k_bwd_flow(DevFactor F, DevWork W, c
 // of their own, so no kept front has a dropped child or parent.
 // ---------------------------------------------------------------------------
 struct ReadyLists {
-    const int* src[4];
-    int* dst[4];
-    int n[4];
-    int chunk0[5];  // first chunk of each list; chunk0[4] = all chunks
+    const int* src[kReadyLists];
+    int* dst[kReadyLists];
+    int n[kReadyLists];
+    int chunk0[kReadyLists + 1];  // first chunk of each list; the last entry = all chunks
 };
 
 __device__ __forceinline__ int list_of_chunk(const ReadyLists& R, int b) {
     int l = 0;
-    while (l < 3 && b >= R.chunk0[l + 1]) ++l;
+    while (l < kReadyLists - 1 && b >= R.chunk0[l + 1]) ++l;
     return l;
 }
 
@@ -1124,6 +1512,10 @@ cudaError_t prepare_impl() {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bwd<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fwd_flow<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bwd_flow<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_front_warp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(WarpTile<T>) * kWarpsPerCta));
+
     return e;
 }
 
@@ -1135,10 +1527,16 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
         k_gain_values<T, HV><<<grid_for(ls.n_tgt, 256), 256, 0, st>>>(net, F, W, hval, gv, ls.n_tgt);
         count_launches(1);
     }
-    if (ls.flow_a_n + ls.flow_b_n > 0) {
+    if (ls.flow_a_n + ls.flow_b_n + ls.flow_w_n > 0) {
         cudaError_t e = cudaMemsetAsync(W.flow, 0, sizeof(int) * (size_t)(F.n_super + 8), st);
         if (e != cudaSuccess) return e;
         int* counters = W.flow + F.n_super;
+        if (ls.flow_w_n > 0) {
+            k_front_warp<T><<<ls.flow_w_grid, kThreads, sizeof(WarpTile<T>) * kWarpsPerCta, st>>>(
+                F, W, gv, lx, ub, ls.d_flow_w, ls.d_ready_n + 4, ls.d_phase, 3, ls.d_phase_nchild, counters + 2,
+                W.flow);
+            count_launches(1);
+        }
         if (ls.flow_a_n > 0) {
             const int mf = ls.flow_a_maxf;
             k_front_flow<T, kPanelSmall, kMinBlocksA<T>><<<ls.flow_a_grid, kThreads, front_smem<T>(mf), st>>>(
@@ -1151,6 +1549,10 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
                 F, W, gv, lx, ub, ls.d_flow_b, ls.d_ready_n + 1, ls.d_phase, 2, ls.d_phase_nchild, counters + 1, W.flow);
             count_launches(1);
         }
+    }
+    if (sizeof(T) == 4 && ls.n_pot_pairs > 0) {
+        cudaError_t e = cudaMemsetAsync(ls.d_pot_cnt, 0, sizeof(int) * (size_t)ls.n_pot_pairs, st);
+        if (e != cudaSuccess) return e;
     }
     for (int l = 0; l < ls.n_levels; ++l) {
         const int ns = ls.h_small_ptr[l + 1] - ls.h_small_ptr[l];
@@ -1169,7 +1571,11 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
                 const int npot = ls.h_pot_ptr[slot + 1] - ls.h_pot_ptr[slot];
                 const int nupd = ls.h_upd_ptr[slot + 1] - ls.h_upd_ptr[slot];
                 if (npot > 0) {
-                    k_big_potrf<T><<<npot, kThreads, 0, st>>>(F, W, lx, ls.d_pot + ls.h_pot_ptr[slot], p);
+                    if constexpr (sizeof(T) == 4)
+                        k_big_panel32<<<npot, kThreads, 0, st>>>(F, W, lx, ls.d_pot + ls.h_pot_ptr[slot], p,
+                                                                 ls.d_pot_cnt);
+                    else
+                        k_big_potrf<T><<<npot, kThreads, 0, st>>>(F, W, lx, ls.d_pot + ls.h_pot_ptr[slot], p);
                     count_launches(1);
                 }
                 if constexpr (sizeof(T) == 8) {
@@ -1202,11 +1608,25 @@ cudaError_t solve_impl(const DevFactor& F, const DevWork& W, const LevelSchedule
         cudaError_t e = cudaMemsetAsync(fwd_done, 0, sizeof(int) * (size_t)(2 * ns + 8), st);
         if (e != cudaSuccess) return e;
         const size_t smem = solve_smem<T>(ls.solve_maxf);
-        k_fwd_flow<T, T><<<ls.up_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_up, ls.d_ready_n + 2,
-                                                             ls.d_nchild, counters + 0, fwd_done);
-        k_bwd_flow<T, T><<<ls.solve_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_down, ls.d_ready_n + 3,
-                                                                counters + 1, bwd_done);
-        count_launches(2);
+        // warp fronts first going up, last coming down
+        if (ls.flow_w_n > 0) {
+            k_fwd_warp<T, T><<<ls.solve_w_grid, kThreads, 0, st>>>(F, W, lx, rdiag, sv, ls.d_flow_w, ls.d_ready_n + 4,
+                                                                   ls.d_phase, 3, ls.d_phase_nchild, counters + 2,
+                                                                   fwd_done);
+            count_launches(1);
+        }
+        if (ls.up_n > 0) {
+            k_fwd_flow<T, T><<<ls.up_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_up, ls.d_ready_n + 2,
+                                                                 ls.d_nchild, counters + 0, fwd_done);
+            k_bwd_flow<T, T><<<ls.solve_grid, kThreads, smem, st>>>(F, W, lx, rdiag, sv, ls.d_down, ls.d_ready_n + 3,
+                                                                    counters + 1, bwd_done);
+            count_launches(2);
+        }
+        if (ls.down_w_n > 0) {
+            k_bwd_warp<T, T><<<ls.solve_w_grid, kThreads, 0, st>>>(F, W, lx, rdiag, sv, ls.d_down_w, ls.d_ready_n + 5,
+                                                                   counters + 3, bwd_done);
+            count_launches(1);
+        }
         return cudaGetLastError();
     }
     for (int l = 0; l < ls.n_levels; ++l) {
@@ -1230,7 +1650,7 @@ cudaError_t solve_impl(const DevFactor& F, const DevWork& W, const LevelSchedule
 
 template <typename T>
 FlowGrids flow_grids_impl(int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf) {
-    FlowGrids g{0, 0, 0};
+    FlowGrids g{0, 0, 0, 0, 0};
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return g;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return g;
@@ -1242,6 +1662,8 @@ FlowGrids flow_grids_impl(int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf) {
     g.a = resident((const void*)k_front_flow<T, kPanelSmall, kMinBlocksA<T>>, front_smem<T>(maxf_a));
     g.b = resident((const void*)k_front_flow<T, kPanel, 1>, front_smem<T>(maxf_b));
     if (solve_maxf <= 16384) g.solve = resident((const void*)k_fwd_flow<T, T>, solve_smem<T>(solve_maxf));
+    g.w = resident((const void*)k_front_warp<T>, sizeof(WarpTile<T>) * kWarpsPerCta);
+    g.wsolve = std::min(resident((const void*)k_fwd_warp<T, T>, 0), resident((const void*)k_bwd_warp<T, T>, 0));
     cudaGetLastError();
     return g;
 }
@@ -1251,13 +1673,13 @@ FlowGrids flow_grids_impl(int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf) {
 cudaError_t launch_ready_compact(const DevFactor& F, const DevWork& W, const LevelSchedule& ls, cudaStream_t st) {
     ReadyLists R;
     R.chunk0[0] = 0;
-    for (int l = 0; l < 4; ++l) {
+    for (int l = 0; l < kReadyLists; ++l) {
         R.src[l] = ls.src_lists[l];
         R.dst[l] = ls.cmp_lists[l];
         R.n[l] = ls.src_n[l];
         R.chunk0[l + 1] = R.chunk0[l] + (R.n[l] + kCompactChunk - 1) / kCompactChunk;
     }
-    const int nb = R.chunk0[4];
+    const int nb = R.chunk0[kReadyLists];
     if (nb == 0 || !W.grid_flags) return cudaSuccess;
     k_ready_count<<<nb, kCompactThreads, 0, st>>>(F, W, R, ls.d_chunk_cnt);
     k_ready_compact<<<nb, kCompactThreads, 0, st>>>(F, W, R, ls.d_chunk_cnt, ls.d_ready_n);

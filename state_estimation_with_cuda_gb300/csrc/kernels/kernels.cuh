@@ -231,7 +231,9 @@ struct LevelSchedule {
     const int32_t* h_lvl_panels = nullptr;  // [n_levels] panel steps of the level
     const int32_t* h_step_ptr = nullptr;    // [n_levels+1] first step slot of a level
     const int32_t* h_pot_ptr = nullptr;     // [n_slots+1] offsets into d_pot
-    const int4* d_pot = nullptr;            // (big front) diagonal-tile factorisations
+    const int4* d_pot = nullptr;            // FP64: (big front); FP32: (big front, chunk, chunks, step pair)
+    int32_t* d_pot_cnt = nullptr;           // FP32: [n_pot_pairs] CTAs of a (front, step) done reading its tile
+    int32_t n_pot_pairs = 0;
     const int32_t* h_pan_ptr = nullptr;     // [n_slots+1] offsets into d_pan (FP64 only)
     const int4* d_pan = nullptr;            // (big front, row tile below the panel)
     const int32_t* h_upd_ptr = nullptr;     // [n_slots+1] offsets into d_upd
@@ -259,25 +261,33 @@ struct LevelSchedule {
     const int32_t* d_nchild = nullptr;       // [n_super] children
     const int32_t* d_down = nullptr;
     int32_t solve_maxf = 0, solve_grid = 0, up_grid = 0;
-    // Lengths of the four claim lists (A, B, up, down) as the kernels read
-    // them, on the device.  In a batch the lists above are compacted copies:
-    // before every iteration launch_ready_compact keeps, in order, the
-    // entries of src_lists whose grid takes the step, so that fronts of
-    // frozen grids are never claimed and a pass costs what its active grids
-    // cost.  Outside a batch the lists are the full ones and the lengths fixed.
+    // warp phase: initially ready warp fronts (factor and forward sweep) and
+    // every warp front top-down (backward sweep)
+    const int32_t* d_flow_w = nullptr;
+    int32_t flow_w_n = 0, flow_w_grid = 0;
+    const int32_t* d_down_w = nullptr;
+    int32_t down_w_n = 0, solve_w_grid = 0;
+    // Lengths of the claim lists (A, B, up, down, warp, warp down) as the
+    // kernels read them, on the device.  In a batch the lists above are
+    // compacted copies: before every iteration launch_ready_compact keeps, in
+    // order, the entries of src_lists whose grid takes the step, so that
+    // fronts of frozen grids are never claimed and a pass costs what its
+    // active grids cost.  Outside a batch the lists are the full ones and the
+    // lengths fixed.
     int32_t* d_ready_n = nullptr;
     int32_t compact = 0;
-    const int32_t* src_lists[4] = {nullptr, nullptr, nullptr, nullptr};
-    int32_t* cmp_lists[4] = {nullptr, nullptr, nullptr, nullptr};
-    int32_t src_n[4] = {0, 0, 0, 0};
+    const int32_t* src_lists[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int32_t* cmp_lists[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int32_t src_n[6] = {0, 0, 0, 0, 0, 0};
     int32_t* d_chunk_cnt = nullptr;  // [ready_chunks(src_n)] scratch
 };
 
-// Entries per CTA of the claim-list compaction.
+// Claim lists and entries per CTA of their compaction.
+constexpr int kReadyLists = 6;
 constexpr int kCompactChunk = 2048;
 inline int32_t ready_chunks(const int32_t* n) {
     int32_t c = 0;
-    for (int l = 0; l < 4; ++l) c += (n[l] + kCompactChunk - 1) / kCompactChunk;
+    for (int l = 0; l < kReadyLists; ++l) c += (n[l] + kCompactChunk - 1) / kCompactChunk;
     return c;
 }
 // Batch: stable compaction of the claim lists to the fronts of grids that are
@@ -314,10 +324,16 @@ cudaError_t launch_batch_retire(const DevBatch& b, cudaStream_t st);
 constexpr int32_t kFlowSmallFMax = 128;
 // Panel width of the high-occupancy phase's fronts (all others use 32).
 constexpr int32_t kPanelFlowA = 16;
+// Fronts whose whole subtree is at most this wide are factorised and solved
+// one front per warp (the warp phase, dataflow phase id 3).  The phase adds a
+// phase boundary to the factorisation and to each sweep, so by default a
+// grid uses it when it has at least kWarpPhaseMinFronts such fronts.
+constexpr int32_t kWarpFrontMax = 32;
+constexpr int32_t kWarpPhaseMinFronts = 4096;
 
 // Resident-CTA grid sizes of the persistent dataflow kernels (0 = cannot run).
 struct FlowGrids {
-    int32_t a, b, solve;
+    int32_t a, b, solve, w, wsolve;
 };
 FlowGrids flow_grids(bool mixed, int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf);
 
@@ -338,6 +354,8 @@ cudaError_t launch_factor_solve_noalloc(const DevNet& net, const DevFactor& F, c
 
 // Tile edge of the big-front kernels.
 constexpr int kTile = 32;
+// Rows per CTA of the FP32 panel solve of a tiled front.
+constexpr int kPanelRows = 128;
 
 // Sets the kernel attributes (dynamic shared memory limits) on the current
 // device; call before launching or capturing the factorisation.
