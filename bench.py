@@ -71,7 +71,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid10k-steps", type=int, default=40)
     ap.add_argument("--skip-extra", action="store_true", help="headline legs only")
-    ap.add_argument("--only", choices=["batch512", "grid200k", "grid10k"],
+    ap.add_argument("--union-passes", type=int, default=3, help="profiled passes of the batch roofline leg")
+    ap.add_argument("--only", choices=["batch512", "grid200k", "grid10k", "union_roofline"],
                     help="run one secondary configuration alone and print its object (for profiling)")
     return ap.parse_args()
 
@@ -306,6 +307,8 @@ def roofline(leg, g, mixed):
     achieved = sb[dom] / (per_call_ms * 1e-3) / 1e9 if per_call_ms > 0 else 0.0
     kernel = {"evaluate": "k_evaluate", "factor": "front_factorisation", "rhs": "k_rhs", "solve": "front_solves",
               "update": "k_update"}[dom]
+    if info.n_bus > 100000:  # the batch union: its own committed summary
+        kernel = "union_" + kernel
     return {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 2), "peak": peak, "peak_kind": peak_kind,
             "unit": "GB/s", "frac": round(achieved / peak, 5), "traffic": profile_traffic(kernel),
             "algorithmic_bytes_per_call": int(sb[dom])}
@@ -491,6 +494,48 @@ def run_batch512():
     return out
 
 
+def run_union_roofline(local, passes=3):
+    """Throughput-regime roofline: one Gauss-Newton pass of the 512-grid batch
+    with every grid taking the step (flat start), stages timed with CUDA events
+    (profiling on, so no graphs), L2 flushed before the pass; the dominant
+    stage against its algorithmic bytes on the union's plan.  The single
+    grid10k leg keeps its own roofline: one grid of that size is bound by the
+    elimination tree's serial chain, not by HBM."""
+    from state_estimation_with_cuda_gb300 import BatchEstimator, native, workloads
+
+    grids = workloads.batch_grids(512)
+    b = BatchEstimator(mixed=True)
+    b.set_config(enable_profiling=1, device_id=local)
+    for g in grids:
+        b.add_grid(g)
+    b.upload_model()
+    b.solve(flat_start=True, max_iterations=1)  # warm-up
+    lib = b.lib
+    names = ["evaluate", "factor", "rhs", "solve", "update", "final"]
+    best = None
+    for _ in range(passes):
+        b._check(lib.sle_ExFlushL2(b.h, FLUSH_BYTES))
+        lib.sle_ExResetStats(b.h)
+        b.solve(flat_start=True, max_iterations=1)
+        st = native.SLE_ExStats()
+        lib.sle_ExGetStats(b.h, ctypes.byref(st))
+        leg = {"stage_ms": {names[i]: st.ms[i] for i in range(6)},
+               "stage_calls": {names[i]: st.calls[i] for i in range(6)},
+               "stage_launches": {names[i]: st.launches[i] for i in range(6)}}
+        if best is None or sum(leg["stage_ms"].values()) < sum(best["stage_ms"].values()):
+            best = leg
+    best["info"] = b.plan_info()
+    b.close()
+    union = argparse.Namespace(m_type=np.concatenate([g.m_type for g in grids]))
+    r = roofline(best, union, True)
+    r["workload"] = ("one Gauss-Newton pass of the 512-grid batch (%d buses, %d rows), every grid active, mixed "
+                     "precision, L2 flushed before the pass" % (sum(g.n_bus for g in grids),
+                                                               sum(g.n_meas for g in grids)))
+    r["stages_ms"] = {k: round(v, 4) for k, v in best["stage_ms"].items()}
+    r["stage_launches"] = best["stage_launches"]
+    return r
+
+
 def run_grid200k():
     from state_estimation_with_cuda_gb300 import Estimator, workloads
 
@@ -562,6 +607,7 @@ def run_gb300(args, world, rank, local):
         if not args.skip_extra:
             extra["batch512"] = run_batch512()
             extra["grid200k"] = run_grid200k()
+            extra["union_roofline"] = run_union_roofline(local)
     g10 = None
     if not args.skip_extra:
         from state_estimation_with_cuda_gb300 import workloads
@@ -644,6 +690,8 @@ def main():
     if args.only:
         if args.only == "batch512":
             out = run_batch512()
+        elif args.only == "union_roofline":
+            out = run_union_roofline(local, args.union_passes)
         elif args.only == "grid200k":
             out = run_grid200k()
         else:
@@ -686,9 +734,13 @@ def main():
             out["cpu_baseline"] = {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
                                    "sample": "the first %d timed requests of the stream, in arrival order "
                                              "(%.1f s of CPU solves)" % (len(times), sum(times))}
-        out["roofline"] = out.get("grid10k", {}).get("mixed", {}).get("roofline")
-        if out["roofline"]:
-            out["roofline"] = dict(out["roofline"], workload="grid10k hot start (the factorisation stage)")
+        # the dominant stage where the GPU is loaded (a batch pass, as the served
+        # units run under load); grid10k's latency-bound figure stays in its leg
+        out["roofline"] = out.pop("union_roofline", None)
+        if not out["roofline"]:
+            out["roofline"] = out.get("grid10k", {}).get("mixed", {}).get("roofline")
+            if out["roofline"]:
+                out["roofline"] = dict(out["roofline"], workload="grid10k hot start (the factorisation stage)")
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

@@ -533,6 +533,8 @@ int32_t Engine::upload() {
         work_.rhs = c.take<double>(P.n_state);
         work_.sol = c.take<double>(P.n_state);
         work_.hval32 = mixed_ ? c.take<float>(nnz_h) : nullptr;
+        work_.hw = mixed_ ? nullptr : c.take<double>(nnz_h);
+        work_.hw32 = mixed_ ? c.take<float>(nnz_h) : nullptr;
         work_.b0 = c.take<double>(P.n_state);
         work_.dx = c.take<double>(P.n_state);
         work_.hdx = c.take<double>(m);
@@ -1563,6 +1565,7 @@ int32_t Engine::batch_solve(int32_t n, const int32_t* ids, const uint8_t* flat, 
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ev0_, ev1_);
     last_.time_ms = ms;
+    collect_stage_times();
     for (int32_t i = 0; i < n; ++i) {
         const int32_t g = ids[i];
         const uint32_t fl = h_flags[g];
@@ -1730,6 +1733,7 @@ int32_t Engine::stream_step(std::vector<int32_t>& done, std::vector<GridResult>&
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_mis, batch_.mismatch, 8 * static_cast<size_t>(G), cudaMemcpyDeviceToHost, st_);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
     if (e != cudaSuccess) return set_cuda_error(e, "stream step");
+    collect_stage_times();
     for (int32_t g = 0; g < G; ++g) {
         if (!in_flight_[g]) continue;
         ++stream_iters_[g];

@@ -29,14 +29,15 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// G entry = sum over its pairs (a, b) of (w h_a) h_b, the weighted entry
+// hw[a] written by the evaluation (FP64: the same product, so the same sum).
 template <typename HV>
-__device__ __forceinline__ double gain_entry(const DevNet& net, const DevFactor& F, const DevWork& W, const HV* hval,
-                                             int tg) {
+__device__ __forceinline__ double gain_entry(const DevFactor& F, const HV* hval, const HV* hw, int tg) {
     double acc = 0.0;
     const int64_t p1 = F.tgt_pair_ptr[tg + 1];
     for (int64_t p = F.tgt_pair_ptr[tg]; p < p1; ++p) {
         const int a = F.pair_a[p], b = F.pair_b[p];
-        acc += W.w_eff[net.h_row[a]] * static_cast<double>(hval[a]) * static_cast<double>(hval[b]);
+        acc += static_cast<double>(hw[a]) * static_cast<double>(hval[b]);
     }
     return acc;
 }
@@ -45,10 +46,10 @@ __device__ __forceinline__ double gain_entry(const DevNet& net, const DevFactor&
 // dependent gathers are hidden by occupancy instead of sitting on the
 // elimination tree's critical path.
 template <typename T, typename HV>
-__global__ void k_gain_values(DevNet net, DevFactor F, DevWork W, const HV* hval, T* gv, int n_tgt) {
+__global__ void k_gain_values(DevFactor F, DevWork W, const HV* hval, const HV* hw, T* gv, int n_tgt) {
     for (int tg = blockIdx.x * blockDim.x + threadIdx.x; tg < n_tgt; tg += gridDim.x * blockDim.x) {
         if (F.tgt_grid && (W.grid_flags[F.tgt_grid[tg]] & FLAG_FROZEN)) continue;
-        gv[tg] = static_cast<T>(gain_entry(net, F, W, hval, tg));
+        gv[tg] = static_cast<T>(gain_entry(F, hval, hw, tg));
     }
 }
 
@@ -225,13 +226,15 @@ __device__ __forceinline__ void store4<double>(double* p, const double (&v)[4]) 
     reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
 }
 
-// Factors the kb x kb diagonal block held by one warp in registers: lane i
-// owns row i in a[] (entries j <= i, zeros elsewhere and for lanes >= kb).
-// Fully unrolled and branch-free: the chain from one pivot to the next is a
-// shuffle, a reciprocal square root and two FMAs, and the remaining shuffles
-// and updates of a step overlap with it.  On return a[] is row i of L and
-// *inv_out = 1 / L_ii; returns true if a pivot was not positive and finite
-// (then replaced by 1).
+// Eliminates the first kb columns of the rows held by one warp in registers:
+// lane i owns row i in a[] (entries j <= i, zeros elsewhere); the remaining
+// columns receive the Schur complement update.  Fully unrolled and
+// branch-free (a branch per column, even one always taken, keeps the next
+// step's shuffles from overlapping the pivot chain): the chain from one pivot
+// to the next is a shuffle, a reciprocal square root and two FMAs, and the
+// remaining shuffles and updates of a step overlap with it.  On return a[] is
+// row i of L and *inv_out = 1 / L_ii; returns true if a pivot was not
+// positive and finite (then replaced by 1).
 template <typename T, int KP>
 __device__ __forceinline__ bool warp_potrf(T (&a)[KP], int kb, int lane, T* inv_out) {
     bool bad = false;
@@ -378,7 +381,10 @@ __device__ void warp_front_factor(const DevFactor& F, const DevWork& W, const T*
     }
     T a[kWarpFrontMax];
 #pragma unroll
-    for (int j = 0; j < kWarpFrontMax; ++j) a[j] = (lane < f && j <= lane) ? t.a[j * kWtLd + lane] : T(0);
+    for (int j = 0; j < kWarpFrontMax; ++j) {
+        a[j] = T(0);
+        if (j < f) a[j] = (lane < f && j <= lane) ? t.a[j * kWtLd + lane] : T(0);
+    }
     T inv;
     const bool bad = warp_potrf<T, kWarpFrontMax>(a, nc, lane, &inv);
     if (bad && lane == 0) atomicOr(singular_flags(F, W, s), FLAG_SINGULAR);
@@ -387,17 +393,23 @@ __device__ void warp_front_factor(const DevFactor& F, const DevWork& W, const T*
     const int row0 = kInvDiag<T> ? nc : 0;  // FP32 writes its diagonal block as L11^-1 below
 #pragma unroll
     for (int c = 0; c < kWarpFrontMax; ++c)
-        if (c < nc && lane < f && lane >= c && lane >= row0) L[lane + c * f] = a[c];
+        if (c < nc) {
+            if (lane < f && lane >= c && lane >= row0) L[lane + c * f] = a[c];
+        }
     const int m = f - nc;
     T* Uo = ub + F.sn_u_off[s];
 #pragma unroll
     for (int j = 0; j < kWarpFrontMax; ++j)
-        if (j >= nc && lane >= j && lane < f) Uo[(lane - nc) + (j - nc) * m] = a[j];
+        if (j >= nc && j < f) {
+            if (lane >= j && lane < f) Uo[(lane - nc) + (j - nc) * m] = a[j];
+        }
     if constexpr (kInvDiag<T>) {
         __syncwarp();
 #pragma unroll
         for (int c = 0; c < kWarpFrontMax; ++c)
-            if (c <= lane && lane < nc) t.a[c * kWtLd + lane] = a[c];
+            if (c < nc) {
+                if (c <= lane && lane < nc) t.a[c * kWtLd + lane] = a[c];
+            }
         if (lane < nc) t.rinv[lane] = inv;
         __syncwarp();
         warp_trinv<T, kWarpFrontMax, kWtLd>(reinterpret_cast<const T (*)[kWtLd]>(t.a), t.rinv, nc, lane, L, f);
@@ -1481,9 +1493,9 @@ __global__ void __launch_bounds__(kCompactThreads) k_ready_compact(DevFactor F, 
 
 
 template <typename HV>
-__global__ void k_gain_export(DevNet net, DevFactor F, DevWork W, const HV* hval, int n_tgt, double* out) {
+__global__ void k_gain_export(DevFactor F, const HV* hval, const HV* hw, int n_tgt, double* out) {
     for (int tg = blockIdx.x * blockDim.x + threadIdx.x; tg < n_tgt; tg += gridDim.x * blockDim.x)
-        out[tg] = gain_entry(net, F, W, hval, tg);
+        out[tg] = gain_entry(F, hval, hw, tg);
 }
 
 inline int grid_for(int64_t n, int threads) {
@@ -1521,10 +1533,11 @@ cudaError_t prepare_impl() {
 
 template <typename T, typename HV>
 cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W, const LevelSchedule& ls, const HV* hval,
+                        const HV* hw,
                         T* lx, T* ub, cudaStream_t st) {
     T* gv = reinterpret_cast<T*>(W.gvals);
     if (ls.n_tgt > 0) {
-        k_gain_values<T, HV><<<grid_for(ls.n_tgt, 256), 256, 0, st>>>(net, F, W, hval, gv, ls.n_tgt);
+        k_gain_values<T, HV><<<grid_for(ls.n_tgt, 256), 256, 0, st>>>(F, W, hval, hw, gv, ls.n_tgt);
         count_launches(1);
     }
     if (ls.flow_a_n + ls.flow_b_n + ls.flow_w_n > 0) {
@@ -1700,7 +1713,7 @@ cudaError_t prepare_factor_kernels() {
 
 cudaError_t launch_factor32(const DevNet& net, const DevFactor& F, const DevWork& W, const LevelSchedule& ls,
                             cudaStream_t st) {
-    return factor_impl<float, float>(net, F, W, ls, W.hval32, W.lx32, W.u32, st);
+    return factor_impl<float, float>(net, F, W, ls, W.hval32, W.hw32, W.lx32, W.u32, st);
 }
 
 cudaError_t launch_solve32(const DevFactor& F, const DevWork& W, const LevelSchedule& ls, cudaStream_t st) {
@@ -1710,7 +1723,7 @@ cudaError_t launch_solve32(const DevFactor& F, const DevWork& W, const LevelSche
 
 cudaError_t launch_factor(const DevNet& net, const DevFactor& F, const DevWork& W, const LevelSchedule& ls,
                           cudaStream_t st) {
-    return factor_impl<double, double>(net, F, W, ls, W.hval, W.lx, W.u, st);
+    return factor_impl<double, double>(net, F, W, ls, W.hval, W.hw, W.lx, W.u, st);
 }
 
 cudaError_t launch_solve(const DevFactor& F, const DevWork& W, const LevelSchedule& ls, cudaStream_t st) {
@@ -1721,7 +1734,7 @@ cudaError_t launch_solve(const DevFactor& F, const DevWork& W, const LevelSchedu
 cudaError_t launch_gain_export(const DevNet& net, const DevFactor& F, const DevWork& W, int32_t n_tgt, double* out,
                                cudaStream_t st) {
     if (n_tgt > 0) {
-        k_gain_export<double><<<grid_for(n_tgt, 256), 256, 0, st>>>(net, F, W, W.hval, n_tgt, out);
+        k_gain_export<double><<<grid_for(n_tgt, 256), 256, 0, st>>>(F, W.hval, W.hw, n_tgt, out);
         count_launches(1);
     }
     return cudaGetLastError();
@@ -1824,7 +1837,7 @@ cudaError_t launch_factor_solve_noalloc(const DevNet& net, const DevFactor& F, c
         k_state_to_ps<<<grid_for(n, 256), 256, 0, st>>>(net, F, d_rhs, W2.rhs);
         count_launches(1);
     }
-    e = factor_impl<double, double>(net, F, W2, ls, W2.hval, W2.lx, W2.u, st);
+    e = factor_impl<double, double>(net, F, W2, ls, W2.hval, W2.hw, W2.lx, W2.u, st);
     if (e == cudaSuccess)
         e = solve_impl<double>(F, W2, ls, W2.lx, reinterpret_cast<const double*>(W2.rdiag),
                                SolveVecs{W2.rhs, W2.sol, W2.su}, st);

@@ -121,6 +121,8 @@ struct DevWork {
     double* wr;       // [n_meas] w_eff * r
     double* hval;     // [nnz_H]
     float* hval32;    // [nnz_H] FP32 copy (mixed-precision pipeline)
+    double* hw;       // [nnz_H] FP64 pipeline: w_eff(row) * H entry, the gain sums' first factor
+    float* hw32;      // [nnz_H] mixed pipeline: the same product rounded to FP32
     double* rhs;      // [n_state] permuted
     double* sol;      // [n_state] permuted (y after forward, x after backward)
     double* b0;       // [n_state] permuted gradient H^T W r of the iteration (mixed)

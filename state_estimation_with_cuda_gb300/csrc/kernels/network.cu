@@ -272,6 +272,12 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
         w.r[q] = rr;
         w.w_eff[q] = we;
         w.wr[q] = we * rr;
+        // weighted H entries for the gain sums G_ij = sum (w h_a) h_b
+        if (sp.mixed && w.hw32) {
+            for (int x = 0; x < nh; ++x) w.hw32[base + x] = static_cast<float>(we * hrow[x]);
+        } else if (!sp.mixed && w.hw) {
+            for (int x = 0; x < nh; ++x) w.hw[base + x] = we * hrow[x];
+        }
     }
     const double s = block_sum(obj, sh);
     if (threadIdx.x == 0) w.part[blockIdx.x] = s;
