@@ -379,40 +379,63 @@ __device__ void warp_front_factor(const DevFactor& F, const DevWork& W, const T*
         }
         __syncwarp();
     }
-    T a[kWarpFrontMax];
-#pragma unroll
-    for (int j = 0; j < kWarpFrontMax; ++j) {
-        a[j] = T(0);
-        if (j < f) a[j] = (lane < f && j <= lane) ? t.a[j * kWtLd + lane] : T(0);
+    // Right-looking elimination of the first nc columns in the tile, lane i
+    // owning row i; the trailing columns receive the Schur complement.  The
+    // loops are bounded by the front's own size (warp fronts are narrow:
+    // median 16 rows, 4 columns), which keeps the kernel small enough for the
+    // instruction cache.
+    T my_inv = T(0);
+    bool bad = false;
+    for (int k = 0; k < nc; ++k) {
+        T d = t.a[k * kWtLd + k];
+        const bool badk = !(d > T(0)) || !isfinite(d);
+        bad |= badk;
+        d = badk ? T(1) : d;
+        T sq, inv;
+        pivot_value(d, &sq, &inv);
+        const bool below = lane > k && lane < f;
+        const T lik = below ? t.a[k * kWtLd + lane] * inv : T(0);
+        __syncwarp();  // column k read by every lane before it is overwritten
+        if (lane == k) {
+            t.a[k * kWtLd + k] = sq;
+            my_inv = inv;
+        }
+        if (below) t.a[k * kWtLd + lane] = lik;
+        __syncwarp();
+        if (below)
+            for (int j = k + 1; j <= lane; ++j) t.a[j * kWtLd + lane] -= lik * t.a[k * kWtLd + j];
+        __syncwarp();
     }
-    T inv;
-    const bool bad = warp_potrf<T, kWarpFrontMax>(a, nc, lane, &inv);
     if (bad && lane == 0) atomicOr(singular_flags(F, W, s), FLAG_SINGULAR);
-    if (lane < nc) reinterpret_cast<T*>(W.rdiag)[c0 + lane] = inv;
+    if (lane < nc) reinterpret_cast<T*>(W.rdiag)[c0 + lane] = my_inv;
     T* L = lx + F.sn_lx_off[s];
     const int row0 = kInvDiag<T> ? nc : 0;  // FP32 writes its diagonal block as L11^-1 below
-#pragma unroll
-    for (int c = 0; c < kWarpFrontMax; ++c)
-        if (c < nc) {
-            if (lane < f && lane >= c && lane >= row0) L[lane + c * f] = a[c];
-        }
+    if (lane < f)
+        for (int c = 0; c < nc; ++c)
+            if (lane >= c && lane >= row0) L[lane + c * f] = t.a[c * kWtLd + lane];
     const int m = f - nc;
     T* Uo = ub + F.sn_u_off[s];
-#pragma unroll
-    for (int j = 0; j < kWarpFrontMax; ++j)
-        if (j >= nc && j < f) {
-            if (lane >= j && lane < f) Uo[(lane - nc) + (j - nc) * m] = a[j];
-        }
+    for (int j = nc; j < f; ++j)
+        if (lane >= j && lane < f) Uo[(lane - nc) + (j - nc) * m] = t.a[j * kWtLd + lane];
     if constexpr (kInvDiag<T>) {
+        // column j of L11^-1 by forward substitution, lane j; its entries
+        // x_i (i > j) are kept transposed in the tile's free upper triangle,
+        // at (row j, column i)
+        if (lane < nc) t.rinv[lane] = my_inv;
         __syncwarp();
-#pragma unroll
-        for (int c = 0; c < kWarpFrontMax; ++c)
-            if (c < nc) {
-                if (c <= lane && lane < nc) t.a[c * kWtLd + lane] = a[c];
+        if (lane < nc) {
+            const int j = lane;
+            for (int i = j + 1; i < nc; ++i) {
+                T acc = -t.a[j * kWtLd + i] * my_inv;  // L_ij x_j with x_j = 1 / L_jj
+                for (int k = j + 1; k < i; ++k) acc -= t.a[k * kWtLd + i] * t.a[k * kWtLd + j];
+                t.a[i * kWtLd + j] = acc * t.rinv[i];
             }
-        if (lane < nc) t.rinv[lane] = inv;
+        }
         __syncwarp();
-        warp_trinv<T, kWarpFrontMax, kWtLd>(reinterpret_cast<const T (*)[kWtLd]>(t.a), t.rinv, nc, lane, L, f);
+        // L11^-1 into the diagonal block: lane i writes row i
+        if (lane < nc)
+            for (int j = 0; j <= lane; ++j)
+                L[lane + j * f] = (j == lane) ? my_inv : t.a[lane * kWtLd + j];
     }
 }
 
@@ -1346,7 +1369,7 @@ __global__ void __launch_bounds__(kThreads) k_bwd_flow(DevFactor F, DevWork W, c
 // in the same phase, as the CTA sweeps do.
 // ---------------------------------------------------------------------------
 template <typename T>
-constexpr int kMinBlocksW = sizeof(T) == 4 ? 2 : 1;
+constexpr int kMinBlocksW = sizeof(T) == 4 ? 4 : 2;
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads, kMinBlocksW<T>) k_front_warp(DevFactor F, DevWork W, const T* gv, T* lx,
