@@ -460,6 +460,7 @@ int32_t Engine::upload() {
         fac_.tgt_grid = batch_mode() ? c.take<int32_t>(P.tgt_local.size()) : nullptr;
         fac_.ps_grid = batch_mode() ? c.take<int32_t>(P.n_state) : nullptr;
         net_.meas_grid = batch_mode() ? c.take<int32_t>(m) : nullptr;
+        net_.bus_grid = batch_mode() ? c.take<int32_t>(n) : nullptr;
         if (batch_mode()) {
             const int32_t G = static_cast<int32_t>(grids_.size());
             batch_.n_grids = G;
@@ -533,6 +534,7 @@ int32_t Engine::upload() {
         work_.rhs = c.take<double>(P.n_state);
         work_.sol = c.take<double>(P.n_state);
         work_.hval32 = mixed_ ? c.take<float>(nnz_h) : nullptr;
+        work_.bus_cs = c.take<double2>(n);
         work_.hw = mixed_ ? nullptr : c.take<double>(nnz_h);
         work_.hw32 = mixed_ ? c.take<float>(nnz_h) : nullptr;
         work_.b0 = c.take<double>(P.n_state);
@@ -664,6 +666,10 @@ int32_t Engine::upload() {
             chk(put(const_cast<int32_t*>(fac_.tgt_grid), tg, st_));
             chk(put(const_cast<int32_t*>(fac_.ps_grid), pg, st_));
             chk(put(const_cast<int32_t*>(net_.meas_grid), mg, st_));
+            std::vector<int32_t> bg(n);
+            for (int32_t g = 0; g < G; ++g)
+                for (int32_t i = boff[g]; i < boff[g + 1]; ++i) bg[i] = g;
+            chk(put(const_cast<int32_t*>(net_.bus_grid), bg, st_));
         }
         chk(put(const_cast<int32_t*>(batch_.bus_off), boff, st_));
         chk(put(const_cast<int32_t*>(batch_.meas_off), moff, st_));

@@ -72,6 +72,7 @@ struct DevNet {
     const int32_t* h_row;
     const int32_t* h_pcol;   // column of each H entry in the permuted state order
     const int32_t* meas_grid;  // batch: grid of each measurement row (nullptr for one grid)
+    const int32_t* bus_grid;   // batch: grid of each bus (nullptr for one grid)
 };
 
 // Factorisation plan (device).
@@ -121,6 +122,7 @@ struct DevWork {
     double* wr;       // [n_meas] w_eff * r
     double* hval;     // [nnz_H]
     float* hval32;    // [nnz_H] FP32 copy (mixed-precision pipeline)
+    double2* bus_cs;  // [n_bus] (cos theta, sin theta) of the state being evaluated
     double* hw;       // [nnz_H] FP64 pipeline: w_eff(row) * H entry, the gain sums' first factor
     float* hw32;      // [nnz_H] mixed pipeline: the same product rounded to FP32
     double* rhs;      // [n_state] permuted

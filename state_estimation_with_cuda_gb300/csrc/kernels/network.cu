@@ -97,14 +97,12 @@ struct FlowTerms {
     double d[4];  // theta_i, V_i, theta_j, V_j
 };
 
-// a4 + a8 flow rows: value of P/Q at one end and its derivatives.
-__device__ FlowTerms flow_terms(const DevNet& net, const double* v, const double* th, int k, bool is_q,
-                                bool to_end, bool exact) {
+// a4 + a8 flow rows: value of P/Q at one end and its derivatives, given
+// s, c = sin, cos of theta_i - theta_j - shift.
+__device__ FlowTerms flow_terms_sc(const DevNet& net, const double* v, int k, bool is_q, bool to_end, bool exact,
+                                   double s, double c) {
     const int i = net.br_from[k], j = net.br_to[k];
     const double Vi = v[i], Vj = v[j];
-    const double t = th[i] - th[j] - net.br_shift[k];
-    double s, c;
-    sincos(t, &s, &c);
     const double g = net.br_g[k], b = net.br_b[k];
     const double A = fmax(net.br_tap[k], kEps);
     const double inv = 1.0 / A, a2 = A * A;
@@ -146,6 +144,54 @@ __device__ FlowTerms flow_terms(const DevNet& net, const double* v, const double
     return f;
 }
 
+__device__ FlowTerms flow_terms(const DevNet& net, const double* v, const double* th, int k, bool is_q,
+                                bool to_end, bool exact) {
+    double s, c;
+    sincos(th[net.br_from[k]] - th[net.br_to[k]] - net.br_shift[k], &s, &c);
+    return flow_terms_sc(net, v, k, is_q, to_end, exact, s, c);
+}
+
+// sin and cos of theta_i - theta_j from the buses' (cos, sin): four FMAs in
+// place of an FP64 sincos per use (the evaluation meets each angle difference
+// in up to eight rows); absolute error a few ulps of 1.
+__device__ __forceinline__ void angle_diff(const double2 a, const double2 b, double* s, double* c) {
+    *c = a.x * b.x + a.y * b.y;
+    *s = a.y * b.x - a.x * b.y;
+}
+
+// sin and cos of theta_i - theta_j - shift of branch k.
+__device__ __forceinline__ void branch_angle(const DevNet& net, const double2* cs, int k, double* s, double* c) {
+    angle_diff(cs[net.br_from[k]], cs[net.br_to[k]], s, c);
+    const double phi = net.br_shift[k];
+    if (phi != 0.0) {
+        double sp, cp;
+        sincos(phi, &sp, &cp);
+        const double c2 = *c * cp + *s * sp;
+        *s = *s * cp - *c * sp;
+        *c = c2;
+    }
+}
+
+__device__ __forceinline__ FlowTerms flow_terms_cs(const DevNet& net, const double* v, const double2* cs, int k,
+                                                   bool is_q, bool to_end, bool exact) {
+    double s, c;
+    branch_angle(net, cs, k, &s, &c);
+    return flow_terms_sc(net, v, k, is_q, to_end, exact, s, c);
+}
+
+// cos and sin of every bus angle of the grids being evaluated.
+__global__ void k_bus_trig(DevNet net, DevWork w, SolveParams sp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= net.n_bus) return;
+    if (net.bus_grid) {
+        const uint32_t gf = w.grid_flags[net.bus_grid[i]];
+        if ((gf & sp.skip_flags) || (gf & sp.need_flags) != sp.need_flags) return;
+    }
+    double s, c;
+    sincos(w.th[i], &s, &c);
+    w.bus_cs[i] = make_double2(c, s);
+}
+
 __device__ __forceinline__ void put_flow(double* hrow, int fpos, const double d[4]) {
     for (int x = 0; x < 4; ++x) {
         const int p = (fpos >> (8 * x)) & 0xFF;
@@ -181,7 +227,8 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
             if (nh > 0) hrow[0] = 1.0;
         } else if (kind == 2) {  // P/Q injection or pseudo
             const bool isq = (ty == 3 || ty == 8);
-            const double Vi = w.v[loc], ti = w.th[loc];
+            const double Vi = w.v[loc];
+            const double2 cs_i = w.bus_cs[loc];
             double dVi = 0.0, dTi = 0.0;
             const int e0 = net.y_ptr[loc], e1 = net.y_ptr[loc + 1];
             for (int e = e0; e < e1; ++e) {
@@ -200,7 +247,7 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
                 } else {
                     const double Vj = w.v[j];
                     double s, c;
-                    sincos(ti - w.th[j], &s, &c);
+                    angle_diff(cs_i, w.bus_cs[j], &s, &c);
                     const double gcbs = G * c + B * s, gsbc = G * s - B * c;
                     double dTj, dVj;
                     if (!isq) {
@@ -226,12 +273,12 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
             hrow[net.y_hpos_v[e0]] += dVi;
         } else if (kind == 3) {  // P/Q flow
             const bool to_end = net.m_end[q] != 0;
-            const FlowTerms f = flow_terms(net, w.v, w.th, loc, ty == 5, to_end, exact);
+            const FlowTerms f = flow_terms_cs(net, w.v, w.bus_cs, loc, ty == 5, to_end, exact);
             hv = f.val;
             put_flow(hrow, net.m_fpos[q], f.d);
         } else if (kind == 4) {  // current magnitude
             const bool to_end = net.m_end[q] != 0;
-            const FlowTerms fp = flow_terms(net, w.v, w.th, loc, false, to_end, exact);
+            const FlowTerms fp = flow_terms_cs(net, w.v, w.bus_cs, loc, false, to_end, exact);
             const int ib = to_end ? net.br_to[loc] : net.br_from[loc];
             const double ve = w.v[ib];
             const double vs = fmax(ve, kEps);
@@ -239,11 +286,11 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
             double d[4];
             if (!exact) {  // the reference reuses the P-flow derivatives
                 hv = 0.0;
-                const FlowTerms fq = flow_terms(net, w.v, w.th, loc, true, to_end, exact);
+                const FlowTerms fq = flow_terms_cs(net, w.v, w.bus_cs, loc, true, to_end, exact);
                 hv = sqrt(fp.val * fp.val + fq.val * fq.val) / vs * on;
                 for (int x = 0; x < 4; ++x) d[x] = fp.d[x];
             } else {
-                const FlowTerms fq = flow_terms(net, w.v, w.th, loc, true, to_end, exact);
+                const FlowTerms fq = flow_terms_cs(net, w.v, w.bus_cs, loc, true, to_end, exact);
                 const double S = sqrt(fp.val * fp.val + fq.val * fq.val);
                 hv = S / vs * on;
                 for (int x = 0; x < 4; ++x)
@@ -780,8 +827,9 @@ cudaError_t launch_admittance_and_ybus(const DevNet& net, cudaStream_t st) {
 
 cudaError_t launch_evaluate(const DevNet& net, const DevWork& w, const SolveParams& sp, cudaStream_t st) {
     if (net.n_meas <= 0) return cudaSuccess;
+    k_bus_trig<<<nblocks(net.n_bus), kBlock, 0, st>>>(net, w, sp);
     k_evaluate<<<nblocks(net.n_meas), kBlock, 0, st>>>(net, w, sp);
-    count_launches(1);
+    count_launches(2);
     return cudaGetLastError();
 }
 
