@@ -330,9 +330,11 @@ void Engine::build_schedule() {
                 }
                 if (!mixed_)  // FP64: the panel's row tiles below go to the multi-CTA solve
                     for (int32_t ti = p + 1; ti < tiles; ++ti) sch_pan_.push_back(make_int4(s, ti, 0, 0));
-                if (q0 < f)
-                    for (int32_t tj = q0 / kTile; tj < tiles; ++tj)
-                        for (int32_t ti = tj; ti < tiles; ++ti) sch_upd_.push_back(make_int4(s, ti, tj, 0));
+                if (q0 < f) {
+                    const int32_t ut = (f + kUpdTile - 1) / kUpdTile;
+                    for (int32_t tj = q0 / kUpdTile; tj < ut; ++tj)
+                        for (int32_t ti = tj; ti < ut; ++ti) sch_upd_.push_back(make_int4(s, ti, tj, 0));
+                }
             }
             sch_pot_ptr_.push_back(static_cast<int32_t>(sch_pot_.size()));
             sch_pan_ptr_.push_back(static_cast<int32_t>(sch_pan_.size()));

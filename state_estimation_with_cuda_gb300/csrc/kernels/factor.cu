@@ -981,12 +981,19 @@ __global__ void __launch_bounds__(32 * kTrsmWarps<T>) k_big_trsm(DevFactor F, De
     }
 }
 
-// Trailing update of step p: tile (ti, tj) -= A_i A_j^T over the panel's
-// columns, restricted to rows >= cols >= p0 + pb.
+// Trailing update of step p: the kUpdTile x kUpdTile tile (ti, tj) -= A_i A_j^T
+// over the panel's columns, restricted to rows >= cols >= p0 + pb.  The two
+// row blocks of the panel are staged k-major in shared memory; thread
+// (tr, tc) accumulates rows tr + 16u and columns tc + 16v (u, v < 2) in
+// registers, four shared loads per four FMAs (a thread per output needed
+// two per FMA), and its read-modify-writes of a column touch 16 consecutive
+// rows per half warp.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, DevWork W, T* lx, const int4* work, int p) {
-    __shared__ T Ai[kTile][kTile + 1];
-    __shared__ T Aj[kTile][kTile + 1];
+    static_assert(kThreads == 256 && kUpdTile == 32, "thread tiling below");
+    constexpr int ld = kUpdTile + 1;
+    __shared__ T Ai[kTile * ld];  // Ai[k * ld + r] = A(R0 + r, p0 + k)
+    __shared__ T Aj[kTile * ld];
     const int4 wk = work[blockIdx.x];
     const int s = wk.x, ti = wk.y, tj = wk.z;
     if (front_frozen(F, W, s)) return;  // the whole CTA, before any barrier
@@ -996,20 +1003,35 @@ __global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, DevWork W,
     const int p0 = p * kTile;
     const int pb = min(kTile, nc - p0);
     const int q0 = p0 + pb;
-    const int R0 = ti * kTile, C0 = tj * kTile;
-    for (int x = threadIdx.x; x < kTile * pb; x += blockDim.x) {
-        const int rr = x % kTile, kk = x / kTile;
-        Ai[rr][kk] = (R0 + rr < f) ? B[(R0 + rr) + (int64_t)(p0 + kk) * f] : T(0);
-        Aj[rr][kk] = (C0 + rr < f) ? B[(C0 + rr) + (int64_t)(p0 + kk) * f] : T(0);
+    const int R0 = ti * kUpdTile, C0 = tj * kUpdTile;
+    for (int x = threadIdx.x; x < kUpdTile * kTile; x += kThreads) {
+        const int r = x % kUpdTile, k = x / kUpdTile;
+        const T* col = B + (int64_t)(p0 + k) * f;
+        Ai[k * ld + r] = (k < pb && R0 + r < f) ? col[R0 + r] : T(0);
+        Aj[k * ld + r] = (k < pb && C0 + r < f) ? col[C0 + r] : T(0);
     }
     __syncthreads();
-    const int rr = threadIdx.x % kTile;
-    for (int cq = threadIdx.x / kTile; cq < kTile; cq += blockDim.x / kTile) {
-        const int gr = R0 + rr, gc = C0 + cq;
-        if (gr >= f || gc >= f || gr < gc || gc < q0) continue;
-        T acc = T(0);
-        for (int k = 0; k < pb; ++k) acc += Ai[rr][k] * Aj[cq][k];
-        B[gr + (int64_t)gc * f] -= acc;
+    const int tr = threadIdx.x & 15, tc = threadIdx.x >> 4;
+    T acc[2][2] = {{T(0), T(0)}, {T(0), T(0)}};
+#pragma unroll 4
+    for (int k = 0; k < pb; ++k) {
+        const T a0 = Ai[k * ld + tr], a1 = Ai[k * ld + tr + 16];
+        const T b0 = Aj[k * ld + tc], b1 = Aj[k * ld + tc + 16];
+        acc[0][0] += a0 * b0;
+        acc[0][1] += a0 * b1;
+        acc[1][0] += a1 * b0;
+        acc[1][1] += a1 * b1;
+    }
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+        const int gc = C0 + tc + 16 * v;
+        if (gc < q0 || gc >= f) continue;
+        T* dst = B + (int64_t)gc * f;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int gr = R0 + tr + 16 * u;
+            if (gr >= gc && gr < f) dst[gr] -= acc[u][v];
+        }
     }
 }
 

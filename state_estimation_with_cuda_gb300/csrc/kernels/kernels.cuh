@@ -360,6 +360,9 @@ cudaError_t launch_factor_solve_noalloc(const DevNet& net, const DevFactor& F, c
 constexpr int kTile = 32;
 // Rows per CTA of the FP32 panel solve of a tiled front.
 constexpr int kPanelRows = 128;
+// Edge of the trailing-update tiles of a tiled front (one CTA each; 64 left a
+// single grid's step on too few SMs: grid200k FP64 179 -> 203 ms).
+constexpr int kUpdTile = 32;
 
 // Sets the kernel attributes (dynamic shared memory limits) on the current
 // device; call before launching or capturing the factorisation.
