@@ -72,6 +72,21 @@ typedef struct SLE_ExPlanInfo {
 /* Symbolic plan statistics (uploads the model if needed). */
 SLE_API SLE_StatusCode SLE_CALL sle_ExGetPlanInfo(SLE_Handle handle, SLE_ExPlanInfo* info);
 
+typedef struct SLE_ExScheduleInfo {
+    int32_t n_warp, n_phase_a, n_phase_b, n_sync; /* fronts per factorisation phase (warp, dataflow A and B,
+                                                      level-synchronous) */
+    int32_t warp_ready, a_ready, b_ready;         /* initially ready fronts of the dataflow phases */
+    int32_t up_ready, down_n, down_warp_n;        /* forward-sweep leaves; backward-sweep fronts (CTA, warp) */
+    int32_t sync_levels, panel_steps;             /* non-empty synchronous levels; tiled-front panel steps */
+    int32_t by_depth, pad;                        /* 1: synchronous levels ordered by depth from the root */
+    int64_t launches_by_height, launches_by_depth; /* cost of the synchronous part under either order */
+} SLE_ExScheduleInfo;
+
+/* Kernel schedule of the current model and options (no counterpart in the
+ * reference).  Host-only before the first upload (it runs the symbolic
+ * analysis if needed); afterwards it reports the uploaded schedule. */
+SLE_API SLE_StatusCode SLE_CALL sle_ExGetScheduleInfo(SLE_Handle handle, SLE_ExScheduleInfo* info);
+
 /* Ybus in canonical CSR order: row_ptr[n_bus+1], col/g/b[nnz_ybus]. */
 SLE_API SLE_StatusCode SLE_CALL sle_ExGetYbus(SLE_Handle handle, int32_t* row_ptr, int32_t* col, SLE_Real* g,
                                               SLE_Real* b);

@@ -214,6 +214,13 @@ class Estimator:
         return idx[:cnt.value].copy()
 
     # -- stage-level access (sle_ex.h) ------------------------------------------------------
+    def schedule_info(self):
+        """Kernel schedule of the current model and options (host-only before
+        the first upload): fronts per phase, ready lists, panel steps."""
+        info = N.SLE_ExScheduleInfo()
+        self._check(self.lib.sle_ExGetScheduleInfo(self.h, ctypes.byref(info)))
+        return info
+
     def plan_info(self):
         info = N.SLE_ExPlanInfo()
         self._check(self.lib.sle_ExGetPlanInfo(self.h, ctypes.byref(info)))

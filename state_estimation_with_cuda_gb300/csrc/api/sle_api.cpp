@@ -1156,6 +1156,29 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* k
     return SLE_OK;
 }
 
+SLE_API SLE_StatusCode SLE_CALL sle_ExGetScheduleInfo(SLE_Handle handle, SLE_ExScheduleInfo* info) {
+    if (!handle || !info) return SLE_ERROR_INVALID_ARGUMENT;
+    sle_gb300::Engine::ScheduleInfo si;
+    if (E(handle)->schedule_info(si) != 0) return fail(SLE_ERROR_MODEL_INCOMPLETE, E(handle)->last_error);
+    std::memset(info, 0, sizeof(*info));
+    info->n_warp = si.n_warp;
+    info->n_phase_a = si.n_phase_a;
+    info->n_phase_b = si.n_phase_b;
+    info->n_sync = si.n_sync;
+    info->warp_ready = si.warp_ready;
+    info->a_ready = si.a_ready;
+    info->b_ready = si.b_ready;
+    info->up_ready = si.up_ready;
+    info->down_n = si.down_n;
+    info->down_warp_n = si.down_warp_n;
+    info->sync_levels = si.sync_levels;
+    info->panel_steps = si.panel_steps;
+    info->by_depth = si.by_depth;
+    info->launches_by_height = si.launches_by_height;
+    info->launches_by_depth = si.launches_by_depth;
+    return SLE_OK;
+}
+
 SLE_API SLE_StatusCode SLE_CALL sle_ExGetPlanInfo(SLE_Handle handle, SLE_ExPlanInfo* info) {
     if (!handle || !info) return SLE_ERROR_INVALID_ARGUMENT;
     Engine* e = E(handle);

@@ -287,7 +287,10 @@ void Engine::build_schedule() {
         for (int32_t l = 0; l < nl; ++l) c += static_cast<int64_t>(pan[l]) * per_panel + has_small[l] + has_big[l];
         return c;
     };
-    const bool by_depth = dmax < nl && sync_cost(true) < sync_cost(false);
+    sync_cost_height_ = sync_cost(false);
+    sync_cost_depth_ = dmax < nl ? sync_cost(true) : sync_cost_height_;
+    const bool by_depth = dmax < nl && sync_cost_depth_ < sync_cost_height_;
+    sync_by_depth_ = by_depth ? 1 : 0;
     std::vector<std::vector<int32_t>> sync_lvl(nl);
     for (int32_t l = 0; l < nl; ++l)
         for (int32_t x = P.lvl_ptr[l]; x < P.lvl_ptr[l + 1]; ++x) {
@@ -374,6 +377,38 @@ void Engine::build_schedule() {
     std::sort(sch_flow_a_.begin(), sch_flow_a_.end(), by_cost);
     std::sort(sch_flow_b_.begin(), sch_flow_b_.end(), by_cost);
     std::sort(sch_up_.begin(), sch_up_.end(), by_cost);
+}
+
+int32_t Engine::schedule_info(ScheduleInfo& out) {
+    if (!uploaded_) {
+        // host-only: the schedule is rebuilt at upload anyway
+        if (!(analyzed_ && !model.structure_dirty)) {
+            const int32_t rc = analyze();
+            if (rc) return rc;
+        }
+        mixed_ = cfg.use_double_precision == 0;
+        build_schedule();
+    }
+    out = ScheduleInfo();
+    for (char ph : flow_phase_) {
+        out.n_warp += ph == 3;
+        out.n_phase_a += ph == 1;
+        out.n_phase_b += ph == 2;
+        out.n_sync += ph == 0;
+    }
+    out.warp_ready = static_cast<int32_t>(sch_flow_w_.size());
+    out.a_ready = static_cast<int32_t>(sch_flow_a_.size());
+    out.b_ready = static_cast<int32_t>(sch_flow_b_.size());
+    out.up_ready = static_cast<int32_t>(sch_up_.size());
+    out.down_n = static_cast<int32_t>(sch_down_.size());
+    out.down_warp_n = static_cast<int32_t>(sch_down_w_.size());
+    for (size_t l = 0; l + 1 < sch_small_ptr_.size(); ++l)
+        out.sync_levels += (sch_small_ptr_[l + 1] > sch_small_ptr_[l] || sch_asm_ptr_[l + 1] > sch_asm_ptr_[l]) ? 1 : 0;
+    for (int32_t p : sch_panels_) out.panel_steps += p;
+    out.by_depth = sync_by_depth_;
+    out.launches_by_height = sync_cost_height_;
+    out.launches_by_depth = sync_cost_depth_;
+    return 0;
 }
 
 int32_t Engine::upload() {

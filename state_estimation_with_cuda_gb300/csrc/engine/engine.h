@@ -99,6 +99,14 @@ public:
 
     int32_t initialize();
     int32_t analyze();  // host-only symbolic analysis of the current model
+    // Schedule summary (host-only before the first upload).
+    struct ScheduleInfo {
+        int32_t n_warp = 0, n_phase_a = 0, n_phase_b = 0, n_sync = 0;
+        int32_t warp_ready = 0, a_ready = 0, b_ready = 0, up_ready = 0, down_n = 0, down_warp_n = 0;
+        int32_t sync_levels = 0, panel_steps = 0, by_depth = 0;
+        int64_t launches_by_height = 0, launches_by_depth = 0;
+    };
+    int32_t schedule_info(ScheduleInfo& out);
     int32_t upload();
     int32_t update_telemetry(const double* z, int32_t count);
     int32_t sync_measurements();
@@ -206,6 +214,8 @@ private:
     std::vector<int64_t> sch_maxpanel_;
     std::vector<int32_t> sch_flow_a_, sch_flow_b_, sch_down_, sch_up_, sch_flow_w_, sch_down_w_, phase_nchild_, nchild_;
     std::vector<char> flow_phase_;
+    int32_t sync_by_depth_ = 0;
+    int64_t sync_cost_height_ = 0, sync_cost_depth_ = 0;
     int32_t flow_a_maxf_ = 0, flow_b_maxf_ = 0;
     int32_t* d_flow_a_ = nullptr;
     int32_t* d_flow_b_ = nullptr;

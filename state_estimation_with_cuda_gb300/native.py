@@ -137,6 +137,13 @@ class SLE_ExPlanInfo(ctypes.Structure):
                 ("factor_flops", ctypes.c_double), ("device_bytes", ctypes.c_size_t)]
 
 
+class SLE_ExScheduleInfo(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in (
+        "n_warp", "n_phase_a", "n_phase_b", "n_sync", "warp_ready", "a_ready", "b_ready", "up_ready", "down_n",
+        "down_warp_n", "sync_levels", "panel_steps", "by_depth", "pad")] + [
+        ("launches_by_height", ctypes.c_int64), ("launches_by_depth", ctypes.c_int64)]
+
+
 class SLE_ExStats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_int64 * 6), ("ms", ctypes.c_double * 6), ("calls", ctypes.c_int64 * 6),
                 ("iterations", ctypes.c_int64), ("solves", ctypes.c_int64), ("total_launches", ctypes.c_int64)]
@@ -230,6 +237,7 @@ SLE_SIGNATURES = {
                               P(I), P(D), P(D)]),
     "sle_ExSetOption": (I, [H, S, D]),
     "sle_ExGetPlanInfo": (I, [H, P(SLE_ExPlanInfo)]),
+    "sle_ExGetScheduleInfo": (I, [H, P(SLE_ExScheduleInfo)]),
     "sle_ExGetYbus": (I, [H, P(I), P(I), P(D), P(D)]),
     "sle_ExEvaluateAt": (I, [H, P(D), P(D), I]),
     "sle_ExGetJacobian": (I, [H, P(I), P(I), P(D), P(D), P(D)]),

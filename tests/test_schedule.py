@@ -1,0 +1,103 @@
+"""Kernel schedule (host logic, no GPU): which fronts each factorisation phase
+takes, the per-grid warp-phase decision, and the order of the
+level-synchronous part.  sle_ExGetScheduleInfo builds the schedule on the
+host before the first upload.
+
+* A grid uses the warp phase (one front per warp for subtrees at most 32 wide)
+  from 4096 such fronts on; the option forces it on or off.
+* In a batch the decision is per grid: the batch's warp fronts are exactly
+  those of its grids that use the phase alone (each grid runs the kernels it
+  runs alone).
+* Every front belongs to exactly one phase and one backward sweep.
+* The synchronous levels are ordered by depth or by height, whichever needs
+  fewer launches; in a batch, depth lines up the grids' tiled fronts so the
+  union needs far fewer panel steps than its grids one after another.
+"""
+import pytest
+
+from state_estimation_with_cuda_gb300 import BatchEstimator, Estimator
+from state_estimation_with_cuda_gb300.workloads import SyntheticGrid, grid_seed
+
+WARP_MIN = 4096
+
+
+def schedule(grids, warp=None, mixed=True):
+    if len(grids) == 1:
+        e = Estimator()
+        e.set_option("use_double_precision", 0 if mixed else 1)
+        if warp is not None:
+            e.set_option("warp_fronts", warp)
+        e.load_network(grids[0])
+    else:
+        e = BatchEstimator(mixed=mixed)
+        if warp is not None:
+            e.set_option("warp_fronts", warp)
+        for g in grids:
+            e.add_grid(g)
+    si, pi = e.schedule_info(), e.plan_info()
+    e.close()
+    return si, pi
+
+
+def check_partition(si, pi):
+    assert si.n_warp + si.n_phase_a + si.n_phase_b + si.n_sync == pi.n_super
+    assert si.down_n + si.down_warp_n == pi.n_super
+    assert si.down_warp_n == si.n_warp
+    assert si.warp_ready <= si.n_warp and si.a_ready <= si.n_phase_a and si.b_ready <= si.n_phase_b
+
+
+@pytest.fixture(scope="module")
+def grids():
+    small = SyntheticGrid(2000, 2800, grid_seed(0x5E51, 0))
+    big = SyntheticGrid(20000, 28000, grid_seed(0x5E51, 1))
+    return small, big
+
+
+def test_warp_phase_threshold_and_option(grids):
+    small, big = grids
+    s0, sp = schedule([small])
+    b0, bp = schedule([big])
+    for si, pi in ((s0, sp), (b0, bp)):
+        check_partition(si, pi)
+    assert s0.n_warp == 0  # below the threshold
+    assert b0.n_warp >= WARP_MIN
+    s1, _ = schedule([small], warp=1)
+    b_off, _ = schedule([big], warp=0)
+    assert s1.n_warp > 0 and s1.warp_ready > 0
+    assert b_off.n_warp == 0 and b_off.n_phase_a > b0.n_phase_a
+    # forcing the phase moves fronts between the dataflow phases only
+    assert s1.n_sync == s0.n_sync and b_off.n_sync == b0.n_sync
+
+
+def test_batch_decides_the_warp_phase_per_grid(grids):
+    small, big = grids
+    s0, _ = schedule([small])
+    b0, _ = schedule([big])
+    u, up = schedule([small, big])
+    check_partition(u, up)
+    assert u.n_warp == b0.n_warp + s0.n_warp
+    assert u.n_phase_a == b0.n_phase_a + s0.n_phase_a
+    assert u.warp_ready == b0.warp_ready + s0.warp_ready
+    # forced on, the small grid's fronts join too
+    s1, _ = schedule([small], warp=1)
+    b1, _ = schedule([big], warp=1)
+    u1, _ = schedule([small, big], warp=1)
+    assert u1.n_warp == s1.n_warp + b1.n_warp
+
+
+def test_synchronous_order_is_the_cheaper_and_aligns_a_batch():
+    h1 = SyntheticGrid(60000, 84000, grid_seed(0x5E51, 2))
+    h2 = SyntheticGrid(50000, 70000, grid_seed(0x5E51, 3))
+    a, _ = schedule([h1])
+    b, _ = schedule([h2])
+    u, up = schedule([h1, h2])
+    check_partition(u, up)
+    for si in (a, b, u):
+        assert si.panel_steps > 0
+        assert si.by_depth == (si.launches_by_depth < si.launches_by_height)
+        assert min(si.launches_by_depth, si.launches_by_height) > 0
+    # both grids' tiled fronts sit just below their roots: by depth they share
+    # panel steps instead of running one after the other
+    assert u.by_depth == 1
+    assert u.panel_steps < a.panel_steps + b.panel_steps
+    assert u.panel_steps <= max(a.panel_steps, b.panel_steps) + min(a.panel_steps, b.panel_steps) // 2
