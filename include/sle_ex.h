@@ -57,7 +57,15 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
  *   "warp_fronts"           fronts whose whole subtree is at most 32 wide are
  *                           factorised and solved one per warp: 1 on, 0 off,
  *                           -1 (default) for each grid with at least 4096 of
- *                           them (re-uploads) */
+ *                           them (re-uploads)
+ *   "spin_limit"            polls (about 64 ns each) after which a dataflow
+ *                           wait of the solves gives up; the call then fails
+ *                           with SLE_ERROR_CUDA_FAILURE and the message
+ *                           "factorisation dataflow wait timed out" instead
+ *                           of the GPU hanging (default 4194304)
+ *   "hold_front"            failure-path test hook: the backward sweep never
+ *                           publishes this front's completion, so the waits
+ *                           of its children run out (-1, the default: none) */
 SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* key, double value);
 
 typedef struct SLE_ExPlanInfo {
@@ -116,6 +124,11 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExFactorSolve(SLE_Handle handle, const SLE_R
  *     (one-time set-up); make that first call before any stream capture.
  *   - Every call on a device shares the array: calls that overlap in time
  *     (two threads, two handles) race and must be serialised by the caller.
+ *   - Like sle_ExFactorSolve, the call also overwrites the handle's own
+ *     factor, right-hand side and solution buffers in its device arena, so
+ *     it must not overlap a solve or another stage call on the same handle.
+ *   - The handle's device (SLE_Config.device_id) is made current for the
+ *     call and the caller's current device is restored afterwards.
  *   - A model whose scratch exceeds 16 MiB is rejected with
  *     SLE_ERROR_INVALID_ARGUMENT and a message giving the bytes it needs.
  * FP64 pipeline only (use_double_precision = 1), after sle_ExEvaluateAt. */
@@ -205,9 +218,15 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExBatchSetBranchStatus(SLE_Handle handle, in
  * request join the batch (hot-started from their last state), and after each
  * iteration the grids that finished answer and leave (iteration-level
  * continuous batching).
- * Units are admitted in order while their device arenas fit the memory
- * budget; requests for grids of units left out complete at once with
- * admitted = 0.  Thread-safe: submit / wait may be called from any thread. */
+ * Residency follows a device-memory budget: at start, units are made
+ * resident in order (small units first) while their arenas fit; a unit left
+ * out is made resident when a request for one of its grids arrives, after
+ * evicting idle units (least recently used first; their states are kept on
+ * the host and restored when they come back), so every request completes
+ * and its result is the one the grid gives while resident.  Only a unit
+ * whose arena alone exceeds the budget is never admitted: its requests
+ * complete at once with admitted = 0.  Thread-safe: submit / wait may be
+ * called from any thread. */
 typedef struct SLE_ExServer SLE_ExServer;
 
 typedef struct SLE_ExServerConfig {
@@ -235,7 +254,9 @@ typedef struct SLE_ExServeResult {
 typedef struct SLE_ExServerStats {
     int64_t submitted, completed, rejected, passes, grid_solves;
     int32_t units, admitted_units, grids, pad;
-    size_t device_bytes, budget_bytes;
+    size_t device_bytes, budget_bytes;  /* device_bytes: arenas resident now */
+    int64_t admissions, evictions;      /* residency changes after start */
+    int32_t resident_units, pad2;
 } SLE_ExServerStats;
 
 /* Defaults of SLE_ExServerConfig. */
@@ -257,6 +278,13 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExServerStart(SLE_ExServer* server);
  * return); branch >= 0 opens (closed = 0) or closes that branch first. */
 SLE_API SLE_StatusCode SLE_CALL sle_ExServerSubmit(SLE_ExServer* server, int32_t grid, const SLE_Real* values,
                                                    int32_t count, int32_t branch, int32_t closed, int64_t* ticket);
+/* As sle_ExServerSubmit; when the request completes, the grid's |V| and
+ * theta (its n_bus values each) are written to v_out / theta_out (either may
+ * be NULL) before the ticket is ready.  The buffers belong to the caller and
+ * must stay valid until sle_ExServerWait has returned the ticket. */
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerSubmitEx(SLE_ExServer* server, int32_t grid, const SLE_Real* values,
+                                                     int32_t count, int32_t branch, int32_t closed, SLE_Real* v_out,
+                                                     SLE_Real* theta_out, int64_t* ticket);
 /* Wait for a ticket: returns 1 when done (result filled), 0 on timeout
  * (timeout_ms < 0 waits forever), negative on error.  A ticket is read once. */
 SLE_API int32_t SLE_CALL sle_ExServerWait(SLE_ExServer* server, int64_t ticket, double timeout_ms,

@@ -53,6 +53,7 @@ def lib():
         L.or_bad_data.argtypes = [ctypes.c_void_p, P(D), D, P(I), I]
         L.or_ordering.argtypes = [ctypes.c_void_p, P(I)]
         L.or_symbolic.argtypes = [ctypes.c_void_p, P(I), P(I), P(I)]
+        L.or_results.argtypes = [ctypes.c_void_p, P(D), P(D), P(D), P(D), P(D), P(D), P(D), P(D)]
         L.or_threads.restype = I
         _lib = L
     return _lib
@@ -145,6 +146,14 @@ class Oracle:
         r = np.empty(self.n_meas)
         self.L.or_wls(self.h, _dp(z), _dp(v), _dp(theta), ctypes.byref(p), ctypes.byref(res), _dp(r))
         return v, theta, res, r
+
+    def results(self, v, theta):
+        """(p_inj, q_inj, pf, qf, pt, qt) at the state (v, theta)."""
+        v = np.ascontiguousarray(v, np.float64)
+        theta = np.ascontiguousarray(theta, np.float64)
+        out = [np.empty(self.n_bus), np.empty(self.n_bus)] + [np.empty(self.n_branch) for _ in range(4)]
+        self.L.or_results(self.h, _dp(v), _dp(theta), *[_dp(a) for a in out])
+        return out
 
     def bad_data(self, r, threshold):
         r = np.ascontiguousarray(r, np.float64)

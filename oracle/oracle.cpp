@@ -2,6 +2,7 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <limits>
 #include <cmath>
 #include <cstring>
 #include <set>
@@ -637,8 +638,11 @@ void or_wls(OrGrid* g, const double* z, double* v, double* th, const OrParams* p
                 if (a != a) a = 0.0;
                 mx = std::max(mx, a);
             }
-            res->max_mismatch = mx;
-            converged = mx < p->tolerance;
+            // a non-finite step: the reference's max reduction yields NaN
+            // (kernels.cu:557-574,752-782), "NaN < tol" fails, and the
+            // validity flag makes the step diverged (wls_solver.cu:493-517)
+            res->max_mismatch = bad ? std::numeric_limits<double>::quiet_NaN() : mx;
+            converged = !bad && mx < p->tolerance;
             diverged = bad;
             res->iterations = it + 1;
         }
@@ -699,6 +703,37 @@ void or_symbolic(OrGrid* g, const int32_t* bus_perm, int32_t* parent, int32_t* c
             for (int x : s)
                 if (x != p) higher[p].insert(x);
         }
+    }
+}
+
+void or_results(OrGrid* g, const double* v, const double* th, double* p_inj, double* q_inj, double* pf, double* qf,
+                double* pt, double* qt) {
+    // bus injections from Ybus at (v, th) (kernels.cu:129-230) and both-end
+    // branch flows (kernels.cu:241-333), the arrays the reference's result
+    // accessors read after a solve (sle_engine.cu:841-977)
+    for (int i = 0; i < g->n; ++i) {
+        double P = 0.0, Q = 0.0;
+        for (int e = g->yptr[i]; e < g->yptr[i + 1]; ++e) {
+            const int j = g->ycol[e];
+            const double ang = th[i] - th[j];
+            const double c = std::cos(ang), s = std::sin(ang);
+            P += v[i] * v[j] * (g->yg[e] * c + g->yb[e] * s);
+            Q += v[i] * v[j] * (g->yg[e] * s - g->yb[e] * c);
+        }
+        if (p_inj) p_inj[i] = P;
+        if (q_inj) q_inj[i] = Q;
+    }
+    double d[4];
+    for (int k = 0; k < g->nbr; ++k) {
+        double val;
+        flow(*g, v, th, k, false, false, true, val, d);
+        if (pf) pf[k] = val;
+        flow(*g, v, th, k, true, false, true, val, d);
+        if (qf) qf[k] = val;
+        flow(*g, v, th, k, false, true, true, val, d);
+        if (pt) pt[k] = val;
+        flow(*g, v, th, k, true, true, true, val, d);
+        if (qt) qt[k] = val;
     }
 }
 

@@ -105,6 +105,11 @@ void or_ordering(OrGrid* g, int32_t* bus_perm);
  * graph under the given ordering, by explicit symbolic elimination. */
 void or_symbolic(OrGrid* g, const int32_t* bus_perm, int32_t* parent, int32_t* colcount);
 
+/* Bus P/Q injections [n_bus] and branch flows P/Q at the from and to ends
+ * [n_branch] at the state (v, th).  Any output may be NULL. */
+void or_results(OrGrid* g, const double* v, const double* th, double* p_inj, double* q_inj, double* pf, double* qf,
+                double* pt, double* qt);
+
 /* Number of OpenMP threads the oracle uses. */
 int32_t or_threads(void);
 

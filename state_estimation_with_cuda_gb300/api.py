@@ -213,6 +213,17 @@ class Estimator:
         self._check(self.lib.sle_IdentifyBadData(self.h, threshold, _ip(idx), m, ctypes.byref(cnt)))
         return idx[:cnt.value].copy()
 
+    def last_error(self):
+        err = self.lib.sle_GetLastError(self.h)
+        return err.decode() if err else ""
+
+    def stats(self):
+        """Per-stage launch counts, Gauss-Newton iterations and solves of this
+        handle (sle_ExGetStats)."""
+        st = N.SLE_ExStats()
+        self._check(self.lib.sle_ExGetStats(self.h, ctypes.byref(st)))
+        return st
+
     # -- stage-level access (sle_ex.h) ------------------------------------------------------
     def schedule_info(self):
         """Kernel schedule of the current model and options (host-only before
@@ -392,11 +403,23 @@ class Server:
     def start(self):
         self._check(self.lib.sle_ExServerStart(self.s))
 
-    def submit(self, gid, z, branch=-1, closed=1):
+    def submit(self, gid, z, branch=-1, closed=1, out=None):
+        """Queue a snapshot; `out` = (v, theta) float64 arrays of the grid's
+        bus count receive the state when the request completes (they must stay
+        alive until wait() returns the ticket)."""
         z = np.ascontiguousarray(z, np.float64)
         t = ctypes.c_int64()
-        self._check(self.lib.sle_ExServerSubmit(self.s, int(gid), _dp(z), len(z), int(branch), int(closed),
-                                                ctypes.byref(t)))
+        if out is None:
+            self._check(self.lib.sle_ExServerSubmit(self.s, int(gid), _dp(z), len(z), int(branch), int(closed),
+                                                    ctypes.byref(t)))
+        else:
+            v, th = out
+            n = self.sizes[gid][0]
+            if v.dtype != np.float64 or th.dtype != np.float64 or len(v) < n or len(th) < n or \
+                    not v.flags.c_contiguous or not th.flags.c_contiguous:
+                raise ValueError("out buffers must be contiguous float64 arrays of the grid's bus count")
+            self._check(self.lib.sle_ExServerSubmitEx(self.s, int(gid), _dp(z), len(z), int(branch), int(closed),
+                                                      _dp(v), _dp(th), ctypes.byref(t)))
         return t.value
 
     def wait(self, ticket, timeout_ms=-1.0):

@@ -1021,6 +1021,13 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExServerSubmit(SLE_ExServer* s, int32_t grid
     return server_rc(s, s->srv.submit(grid, values, count, branch, closed, ticket));
 }
 
+SLE_API SLE_StatusCode SLE_CALL sle_ExServerSubmitEx(SLE_ExServer* s, int32_t grid, const SLE_Real* values,
+                                                     int32_t count, int32_t branch, int32_t closed, SLE_Real* v_out,
+                                                     SLE_Real* theta_out, int64_t* ticket) {
+    if (!s) return SLE_ERROR_INVALID_HANDLE;
+    return server_rc(s, s->srv.submit(grid, values, count, branch, closed, ticket, v_out, theta_out));
+}
+
 SLE_API int32_t SLE_CALL sle_ExServerWait(SLE_ExServer* s, int64_t ticket, double timeout_ms, SLE_ExServeResult* res) {
     if (!s) return SLE_ERROR_INVALID_HANDLE;
     sle_gb300::ServeResult r;
@@ -1058,6 +1065,10 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExServerGetStats(SLE_ExServer* s, SLE_ExServ
     out->pad = 0;
     out->device_bytes = st.device_bytes;
     out->budget_bytes = st.budget_bytes;
+    out->admissions = st.admissions;
+    out->evictions = st.evictions;
+    out->resident_units = st.resident_units;
+    out->pad2 = 0;
     return SLE_OK;
 }
 
@@ -1152,7 +1163,15 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* k
     else if (k == "dataflow") { c.dataflow = value != 0.0 ? 1 : 0; E(handle)->model.structure_dirty = true; }
     else if (k == "flow_small_f") { c.flow_small_f = static_cast<int32_t>(value); E(handle)->model.structure_dirty = true; }
     else if (k == "warp_fronts") { c.warp_fronts = value < 0.0 ? -1 : (value != 0.0 ? 1 : 0); E(handle)->model.structure_dirty = true; }
-    else return fail(SLE_ERROR_INVALID_ARGUMENT, "unknown option");
+    else if (k == "spin_limit" || k == "hold_front") {
+        if (k == "spin_limit") {
+            if (!(value >= 1.0 && value <= 9.0e15)) return fail(SLE_ERROR_INVALID_ARGUMENT, "spin_limit must be >= 1");
+            c.spin_limit = static_cast<long long>(value);
+        } else {
+            c.hold_front = value < 0.0 ? -1 : static_cast<int32_t>(value);
+        }
+        E(handle)->apply_wait_options();
+    } else return fail(SLE_ERROR_INVALID_ARGUMENT, "unknown option");
     return SLE_OK;
 }
 

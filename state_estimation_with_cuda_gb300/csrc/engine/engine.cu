@@ -38,6 +38,7 @@ inline int nblk(int n) { return (n + 255) / 256; }
 }  // namespace
 
 Engine::~Engine() {
+    const DeviceScope dev_scope(cfg.device_id);
     release_device();
     if (st_) cudaStreamDestroy(st_);
     if (ev0_) cudaEventDestroy(ev0_);
@@ -381,13 +382,18 @@ void Engine::build_schedule() {
 
 int32_t Engine::schedule_info(ScheduleInfo& out) {
     if (!uploaded_) {
-        // host-only: the schedule is rebuilt at upload anyway
+        // Host-only: the schedule of the current options is built into the
+        // engine's schedule members, which upload() rebuilds from scratch
+        // (together with the pipeline precision) before it uses them; the
+        // precision flag of the engine is left as it was.
         if (!(analyzed_ && !model.structure_dirty)) {
             const int32_t rc = analyze();
             if (rc) return rc;
         }
+        const bool mixed_before = mixed_;
         mixed_ = cfg.use_double_precision == 0;
         build_schedule();
+        mixed_ = mixed_before;
     }
     out = ScheduleInfo();
     for (char ph : flow_phase_) {
@@ -412,9 +418,9 @@ int32_t Engine::schedule_info(ScheduleInfo& out) {
 }
 
 int32_t Engine::upload() {
+    const DeviceScope dev_scope(cfg.device_id);
     int32_t rc = initialize();
     if (rc) return rc;
-    cudaSetDevice(cfg.device_id);
     // keep the hot-start state across re-uploads
     if (uploaded_) download_results();
     if (!(reuse_analysis_once && analyzed_)) rc = analyze();
@@ -600,12 +606,15 @@ int32_t Engine::upload() {
         work_.ocnt = c.take<int32_t>(nparts);
         work_.status = c.take<DevStatus>(1);
         work_.grid_flags = batch_mode() ? batch_.flags : nullptr;
+        work_.spin_limit = cfg.spin_limit;
+        work_.hold_front = cfg.hold_front;
         isl_parent_ = c.take<int32_t>(n);
         isl_out_ = c.take<int32_t>(4);
     };
     Carver dry(nullptr);
     layout(dry);
     const size_t need = dry.off + 256;
+    need_bytes = need;
     if (budget_bytes && need > budget_bytes) {
         last_error = "device arena of " + std::to_string(need) + " bytes exceeds the admission budget of " +
                      std::to_string(budget_bytes) + " bytes";
@@ -858,6 +867,7 @@ int32_t Engine::upload() {
 }
 
 int32_t Engine::update_telemetry(const double* z, int32_t count) {
+    const DeviceScope dev_scope(cfg.device_id);
     if (count != model.n_meas()) {
         last_error = "telemetry count does not match the measurement count";
         return -4;
@@ -889,6 +899,7 @@ int32_t Engine::sync_measurements() {
 }
 
 int32_t Engine::flat_start() {
+    const DeviceScope dev_scope(cfg.device_id);
     for (int32_t i = 0; i < model.n_bus(); ++i) {
         const int32_t t = model.bus_type[i];
         model.bus_v[i] = (t == 1 || t == 2) ? model.bus_vset[i] : 1.0;
@@ -995,6 +1006,12 @@ int32_t Engine::enqueue_iteration(const SolveParams& sp, bool refactor, int64_t*
     return 0;
 }
 
+void Engine::apply_wait_options() {
+    work_.spin_limit = cfg.spin_limit;
+    work_.hold_front = cfg.hold_front;
+    drop_graphs();  // the captured launches hold the previous values
+}
+
 void Engine::drop_graphs() {
     for (auto& g : graphs_) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
@@ -1055,6 +1072,7 @@ int32_t Engine::run_iteration(const SolveParams& sp, bool refactor) {
 }
 
 int32_t Engine::solve(const SolveRequest& rq, SolveResult& out) {
+    const DeviceScope dev_scope(cfg.device_id);
     out = SolveResult();
     if (batch_mode()) {
         last_error = "a batch handle is solved with batch_solve";
@@ -1069,7 +1087,6 @@ int32_t Engine::solve(const SolveRequest& rq, SolveResult& out) {
             return rc;
         }
     }
-    cudaSetDevice(cfg.device_id);
     if (model.values_dirty) {
         const int32_t rc = sync_measurements();
         if (rc) return rc;
@@ -1096,7 +1113,12 @@ int32_t Engine::solve(const SolveRequest& rq, SolveResult& out) {
             }
             const uint32_t fl = h_status_->flags;
             if (fl & FLAG_TIMEOUT) {
+                // a failure inside an iteration ends the solve as SINGULAR_MATRIX
+                // (wls_solver.cu:296-300); the message names the cause
                 last_error = "factorisation dataflow wait timed out";
+                out.status = CONV_SINGULAR;
+                factor_valid_ = false;
+                last_ = out;
                 return -3;
             }
             if (fl & FLAG_SINGULAR) {
@@ -1161,7 +1183,20 @@ int32_t Engine::solve(const SolveRequest& rq, SolveResult& out) {
     return 0;
 }
 
+int32_t Engine::evict() {
+    const DeviceScope dev_scope(cfg.device_id);
+    if (!uploaded_) return 0;
+    stale_ |= DL_STATE;  // the device state is the one to keep
+    const int32_t rc = download_results(DL_STATE);
+    if (rc) return rc;
+    const cudaError_t e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "evict");
+    release_device();
+    return 0;
+}
+
 int32_t Engine::download_results(int32_t what) {
+    const DeviceScope dev_scope(cfg.device_id);
     what &= stale_;
     if (!uploaded_ || !what) return 0;
     const int32_t n = model.n_bus(), m = model.n_meas(), nbr = model.n_branch();
@@ -1193,6 +1228,7 @@ int32_t Engine::download_results(int32_t what) {
 }
 
 int32_t Engine::evaluate_at(const double* v, const double* th, int32_t exact) {
+    const DeviceScope dev_scope(cfg.device_id);
     if (!uploaded_ || model.structure_dirty) {
         const int32_t rc = upload();
         if (rc) return rc;
@@ -1220,6 +1256,7 @@ int32_t Engine::evaluate_at(const double* v, const double* th, int32_t exact) {
 }
 
 int32_t Engine::export_gain(std::vector<int32_t>& rows, std::vector<int32_t>& cols, std::vector<double>& vals) {
+    const DeviceScope dev_scope(cfg.device_id);
     const Plan& P = plan_;
     if (mixed_) {
         last_error = "stage access needs the FP64 pipeline (use_double_precision = 1)";
@@ -1249,6 +1286,7 @@ int32_t Engine::export_gain(std::vector<int32_t>& rows, std::vector<int32_t>& co
 }
 
 int32_t Engine::factor_and_solve(const double* rhs_orig, double* x_orig) {
+    const DeviceScope dev_scope(cfg.device_id);
     const Plan& P = plan_;
     if (mixed_) {
         last_error = "stage access needs the FP64 pipeline (use_double_precision = 1)";
@@ -1275,6 +1313,7 @@ int32_t Engine::factor_and_solve(const double* rhs_orig, double* x_orig) {
 }
 
 int32_t Engine::factor_and_solve_noalloc(const double* rhs_orig, double* x_orig) {
+    const DeviceScope dev_scope(cfg.device_id);
     if (batch_mode()) {
         last_error = "not available on a batch handle";
         return -4;
@@ -1308,11 +1347,11 @@ int32_t Engine::factor_and_solve_noalloc(const double* rhs_orig, double* x_orig)
 }
 
 int32_t Engine::check_islands(int32_t* islands, int32_t* active_rows) {
+    const DeviceScope dev_scope(cfg.device_id);
     if (!uploaded_) {
         last_error = "no model on the device";
         return -4;
     }
-    cudaSetDevice(cfg.device_id);
     cudaError_t e = launch_islands(net_, isl_parent_, isl_out_, 1000, st_);
     int32_t out[4] = {0, 0, 0, 0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, isl_out_, sizeof(out), cudaMemcpyDeviceToHost, st_);
@@ -1334,6 +1373,7 @@ int32_t Engine::max_solve_front() const {
 }
 
 int32_t Engine::export_ybus(std::vector<double>& g, std::vector<double>& b) {
+    const DeviceScope dev_scope(cfg.device_id);
     const size_t nnz = plan_.y_col.size();
     g.assign(nnz, 0.0);
     b.assign(nnz, 0.0);
@@ -1345,6 +1385,7 @@ int32_t Engine::export_ybus(std::vector<double>& g, std::vector<double>& b) {
 }
 
 int32_t Engine::export_eval(double* hval, double* hx, double* rhs_orig) {
+    const DeviceScope dev_scope(cfg.device_id);
     const Plan& P = plan_;
     std::vector<double> b(P.n_state);
     cudaError_t e = cudaSuccess;
@@ -1362,6 +1403,7 @@ int32_t Engine::export_eval(double* hval, double* hx, double* rhs_orig) {
 }
 
 int32_t Engine::stage_telemetry(const double* z, int32_t count, int32_t slot) {
+    const DeviceScope dev_scope(cfg.device_id);
     if (!uploaded_ || model.structure_dirty) {
         const int32_t rc = upload();
         if (rc) return rc;
@@ -1392,6 +1434,7 @@ int32_t Engine::stage_telemetry(const double* z, int32_t count, int32_t slot) {
 }
 
 int32_t Engine::use_telemetry(int32_t slot) {
+    const DeviceScope dev_scope(cfg.device_id);
     if (slot < 0 || slot >= n_slots_ || !uploaded_) {
         last_error = "telemetry slot not staged";
         return -4;
@@ -1405,6 +1448,7 @@ int32_t Engine::use_telemetry(int32_t slot) {
 }
 
 int32_t Engine::flush_l2(size_t bytes) {
+    const DeviceScope dev_scope(cfg.device_id);
     int32_t rc = initialize();
     if (rc) return rc;
     if (bytes > scratch_bytes_) {
@@ -1423,6 +1467,7 @@ int32_t Engine::flush_l2(size_t bytes) {
 }
 
 int32_t Engine::timer(int32_t op, double* ms) {
+    const DeviceScope dev_scope(cfg.device_id);
     int32_t rc = initialize();
     if (rc) return rc;
     if (!tm0_) {
@@ -1549,6 +1594,7 @@ int32_t Engine::analyze_batch() {
 
 int32_t Engine::batch_solve(int32_t n, const int32_t* ids, const uint8_t* flat, const SolveRequest& rq,
                             GridResult* out) {
+    const DeviceScope dev_scope(cfg.device_id);
     if (!batch_mode()) {
         last_error = "no batch grids";
         return -4;
@@ -1563,7 +1609,6 @@ int32_t Engine::batch_solve(int32_t n, const int32_t* ids, const uint8_t* flat, 
         const int32_t rc = upload();
         if (rc) return rc;
     }
-    cudaSetDevice(cfg.device_id);
     if (model.values_dirty) {
         const int32_t rc = sync_measurements();
         if (rc) return rc;
@@ -1628,6 +1673,7 @@ int32_t Engine::batch_solve(int32_t n, const int32_t* ids, const uint8_t* flat, 
 }
 
 int32_t Engine::batch_set_telemetry(int32_t grid, const double* z, int32_t count) {
+    const DeviceScope dev_scope(cfg.device_id);
     if (grid < 0 || grid >= static_cast<int32_t>(grids_.size()) || !z) {
         last_error = "grid index out of range";
         return -4;
@@ -1659,6 +1705,7 @@ int32_t Engine::batch_set_telemetry(int32_t grid, const double* z, int32_t count
 }
 
 int32_t Engine::batch_get_state(int32_t grid, double* v, double* th) {
+    const DeviceScope dev_scope(cfg.device_id);
     if (grid < 0 || grid >= static_cast<int32_t>(grids_.size())) {
         last_error = "grid index out of range";
         return -4;
@@ -1678,6 +1725,7 @@ int32_t Engine::batch_get_state(int32_t grid, double* v, double* th) {
 }
 
 int32_t Engine::batch_set_branch_status(int32_t grid, int32_t branch, int32_t closed) {
+    const DeviceScope dev_scope(cfg.device_id);
     if (grid < 0 || grid >= static_cast<int32_t>(grids_.size())) {
         last_error = "grid index out of range";
         return -4;
@@ -1704,6 +1752,7 @@ int32_t Engine::batch_set_branch_status(int32_t grid, int32_t branch, int32_t cl
 // Stream mode: grids join and leave the running batch between iterations.
 // ---------------------------------------------------------------------------
 int32_t Engine::stream_begin(const SolveRequest& rq) {
+    const DeviceScope dev_scope(cfg.device_id);
     if (!batch_mode()) {
         last_error = "no batch grids";
         return -4;
@@ -1712,7 +1761,6 @@ int32_t Engine::stream_begin(const SolveRequest& rq) {
         const int32_t rc = upload();
         if (rc) return rc;
     }
-    cudaSetDevice(cfg.device_id);
     if (model.values_dirty) {
         const int32_t rc = sync_measurements();
         if (rc) return rc;
@@ -1732,6 +1780,7 @@ int32_t Engine::stream_begin(const SolveRequest& rq) {
 }
 
 int32_t Engine::stream_activate(int32_t n, const int32_t* ids, const uint8_t* flat) {
+    const DeviceScope dev_scope(cfg.device_id);
     const int32_t G = static_cast<int32_t>(grids_.size());
     if (n <= 0) return 0;
     std::memset(h_batch_in_, 0, 3 * static_cast<size_t>(G));
@@ -1754,6 +1803,7 @@ int32_t Engine::stream_activate(int32_t n, const int32_t* ids, const uint8_t* fl
 }
 
 int32_t Engine::stream_step(std::vector<int32_t>& done, std::vector<GridResult>& res) {
+    const DeviceScope dev_scope(cfg.device_id);
     done.clear();
     res.clear();
     const int32_t G = static_cast<int32_t>(grids_.size());

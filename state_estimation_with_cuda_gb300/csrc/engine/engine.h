@@ -47,6 +47,26 @@ struct EngineConfig {
     int32_t warp_fronts = -1;        // warp phase for fronts whose subtree is at most kWarpFrontMax wide:
                                      // 1 on, 0 off, -1 per grid with at least kWarpPhaseMinFronts of them
     int32_t stream_priority = 0;     // CUDA stream priority of the engine's stream (lower = more urgent)
+    long long spin_limit = kSpinLimitDefault;  // polls before a dataflow wait gives up (FLAG_TIMEOUT)
+    int32_t hold_front = -1;         // test hook: front whose backward-sweep completion is withheld
+};
+
+// Makes `dev` the calling thread's current device for the lifetime of the
+// object and restores the caller's device afterwards.  Every engine call that
+// touches device memory or the engine's stream opens one, so a handle created
+// for device_id = k works while another device is current (the static
+// scratch of the allocation-free entry point is looked up per current device).
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev) {
+        int cur = -1;
+        if (cudaGetDevice(&cur) == cudaSuccess && cur != dev && cudaSetDevice(dev) == cudaSuccess) prev = cur;
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
 };
 
 enum class Mode : int32_t { REALTIME = 0, PRECISION = 1 };
@@ -136,6 +156,9 @@ public:
     int32_t stage_telemetry(const double* z, int32_t count, int32_t slot);  // host -> device slot
     int32_t use_telemetry(int32_t slot);                                    // device slot -> z (on stream)
     int32_t flush_l2(size_t bytes);                                         // overwrite a scratch buffer
+    // Copies cfg.spin_limit / cfg.hold_front into the device work view (the
+    // next launches use them; captured iteration graphs are dropped).
+    void apply_wait_options();
     int32_t timer(int32_t op, double* ms);                                  // 0 start, 1 stop (+ elapsed)
     StageStats stats;
 
@@ -183,6 +206,11 @@ public:
     // Admission: when non-zero, upload() refuses (-10, nothing allocated) a
     // model whose device arena would exceed this many bytes.
     size_t budget_bytes = 0;
+    // Device arena size of the last upload attempt (set even when refused).
+    size_t need_bytes = 0;
+    // Frees the device arena after copying the state (V, theta) back to the
+    // host model; the next upload() resumes from that state.
+    int32_t evict();
     // Set by a caller that has just run analyze() on the unchanged model (e.g.
     // on a worker thread): the next upload() reuses that plan once.
     bool reuse_analysis_once = false;

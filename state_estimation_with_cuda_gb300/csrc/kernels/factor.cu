@@ -611,12 +611,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_front_small(DevFactor F, DevWor
 // claimed by running CTAs, so progress never depends on CTAs that have not
 // started.  Data produced inside the pass is read with L1-bypassing loads.
 // ---------------------------------------------------------------------------
-constexpr long long kSpinLimit = 1LL << 22;
-
-__device__ __forceinline__ void wait_done(const int* flag, uint32_t* status) {
+__device__ __forceinline__ void wait_done(const int* flag, uint32_t* status, long long limit) {
     long long spins = 0;
     while (atomicAdd(const_cast<int*>(flag), 0) == 0) {
-        if (++spins > kSpinLimit) {
+        if (++spins > limit) {
             atomicOr(status, FLAG_TIMEOUT);
             return;
         }
@@ -1369,12 +1367,13 @@ __global__ void __launch_bounds__(kThreads) k_bwd_flow(DevFactor F, DevWork W, c
             __syncwarp();
             continue;
         }
-        if (threadIdx.x == 0 && F.sn_parent[s] >= 0) wait_done(done + F.sn_parent[s], &W.status->flags);
+        if (threadIdx.x == 0 && F.sn_parent[s] >= 0)
+            wait_done(done + F.sn_parent[s], &W.status->flags, W.spin_limit);
         __syncwarp();
         __syncthreads();
         front_bwd<T, V>(F, lx, rdiag, sv, s, reinterpret_cast<V*>(smem_raw), D);
         __syncthreads();
-        if (threadIdx.x == 0) publish_done(done + s);
+        if (threadIdx.x == 0 && s != W.hold_front) publish_done(done + s);
     }
 }
 
@@ -1448,11 +1447,11 @@ __global__ void __launch_bounds__(kThreads) k_bwd_warp(DevFactor F, DevWork W, c
         if (item >= ni) break;
         const int s = order[item];
         if (!front_frozen(F, W, s)) {
-            if (lane == 0 && F.sn_parent[s] >= 0) wait_done(done + F.sn_parent[s], &W.status->flags);
+            if (lane == 0 && F.sn_parent[s] >= 0) wait_done(done + F.sn_parent[s], &W.status->flags, W.spin_limit);
             __syncwarp();
             warp_front_bwd<T, V>(F, lx, rdiag, sv, s, x);
         }
-        if (lane == 0) publish_done(done + s);
+        if (lane == 0 && s != W.hold_front) publish_done(done + s);
         __syncwarp();
     }
 }

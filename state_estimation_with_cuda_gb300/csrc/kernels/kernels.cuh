@@ -153,7 +153,15 @@ struct DevWork {
     int32_t* ocnt;    //   rows over the threshold per block
     DevStatus* status;
     uint32_t* grid_flags;  // batch: per-grid FLAG_* bits (nullptr for one grid)
+    // Bounded dataflow waits: a wait gives up after spin_limit polls (about
+    // 64 ns each), sets FLAG_TIMEOUT and lets the kernel finish, so the host
+    // reports an error instead of the GPU hanging.
+    long long spin_limit;
+    // Test hook for that path: the backward sweeps never publish this front's
+    // completion (-1: none), so its children's waits run out.
+    int32_t hold_front;
 };
+constexpr long long kSpinLimitDefault = 1LL << 22;
 
 // Batch of independent grids solved together (block-diagonal system).
 struct DevBatch {

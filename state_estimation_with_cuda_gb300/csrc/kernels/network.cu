@@ -497,14 +497,20 @@ __global__ void __launch_bounds__(kBlock) k_update(DevNet net, DevFactor f, DevW
     }
 }
 
+// A step with a non-finite entry (FLAG_NONFINITE from k_update) is never
+// converged and reports a NaN max |dx|: the reference's max reduction turns
+// NaN once a NaN step fills its blocks (kernels.cu:557-574,752-782), so
+// "max |dx| < tol" fails and checkValidityKernel's flag decides: DIVERGED
+// (wls_solver.cu:493-517, 343-352).
 __global__ void k_update_finalize(DevWork w, int nblk, double tol) {
     __shared__ double sh[32];
     double m = 0.0;
     for (int b = threadIdx.x; b < nblk; b += blockDim.x) m = fmax(m, w.part[b]);
     m = block_max(m, sh);
     if (threadIdx.x == 0) {
-        w.status->max_mismatch = m;
-        if (m < tol) atomicOr(&w.status->flags, FLAG_CONVERGED);
+        const bool bad = (w.status->flags & FLAG_NONFINITE) != 0;
+        w.status->max_mismatch = bad ? __longlong_as_double(0x7ff8000000000000LL) : m;
+        if (!bad && m < tol) atomicOr(&w.status->flags, FLAG_CONVERGED);
     }
 }
 
@@ -684,7 +690,7 @@ __global__ void k_batch_update_fin(DevBatch b, double tol) {
         m = fmax(m, b.part[k]);
         bad |= b.part_bad[k];
     }
-    b.mismatch[g] = m;
+    b.mismatch[g] = bad ? __longlong_as_double(0x7ff8000000000000LL) : m;
     b.iters[g] += 1;
     if (bad) {
         b.flags[g] = fl | FLAG_NONFINITE | FLAG_FROZEN;

@@ -158,36 +158,32 @@ int32_t Server::start() {
             last_error = units_[i]->eng->last_error;
             return arc[i];
         }
-    // admission in order (shared units first, then own units by size)
+    // admission in order (shared units first, then own units by size): the
+    // units that fit are made resident now, the others when they are needed
     size_t used = 0;
     for (auto& u : units_) {
         u->eng->budget_bytes = budget > used ? budget - used : 1;
         const int32_t rc = u->eng->upload();
+        u->need = u->eng->need_bytes;
+        u->eng->budget_bytes = 0;
         if (rc == 0) {
-            u->admitted = true;
+            u->resident = true;
             used += u->eng->device_bytes();
         } else if (rc != -10) {
             last_error = u->eng->last_error;
             return rc;
         }
+        u->admitted = u->need <= budget;
     }
-    // first estimate of every admitted grid from a flat start, units in parallel
-    SolveRequest rq;
-    rq.mode = Mode::PRECISION;
-    rq.max_iterations = cfg_.max_iterations;
-    rq.tolerance = cfg_.tolerance;
-    rq.robust = cfg_.robust;
-    rq.huber_gamma = cfg_.huber_gamma;
+    budget_ = budget;
+    used_ = used;
+    // first estimate of every resident grid from a flat start, units in parallel
     std::vector<int32_t> src(U, 0);
     parallel([&](int32_t i) {
         Unit* u = units_[i].get();
-        if (!u->admitted) return;
-        const int32_t n = static_cast<int32_t>(u->grids.size());
-        std::vector<int32_t> ids(n);
-        std::iota(ids.begin(), ids.end(), 0);
-        std::vector<uint8_t> flat(n, 1);
-        std::vector<Engine::GridResult> res(n);
-        src[i] = u->eng->batch_solve(n, ids.data(), flat.data(), rq, res.data());
+        if (!u->resident) return;
+        std::lock_guard<std::mutex> lk(u->eng_mu);
+        src[i] = first_estimates(u);
     });
     for (int32_t i = 0; i < U; ++i)
         if (src[i]) {
@@ -200,7 +196,10 @@ int32_t Server::start() {
         stats_.grids = G;
         stats_.budget_bytes = budget;
         stats_.device_bytes = used;
-        for (auto& u : units_) stats_.admitted_units += u->admitted ? 1 : 0;
+        for (auto& u : units_) {
+            stats_.admitted_units += u->admitted ? 1 : 0;
+            stats_.resident_units += u->resident ? 1 : 0;
+        }
     }
     started_ = true;
     for (auto& u : units_)
@@ -208,7 +207,96 @@ int32_t Server::start() {
     return 0;
 }
 
-int32_t Server::submit(int32_t grid, const double* z, int32_t count, int32_t branch, int32_t closed, int64_t* ticket) {
+SolveRequest Server::request_params() const {
+    SolveRequest rq;
+    rq.mode = Mode::PRECISION;
+    rq.max_iterations = cfg_.max_iterations;
+    rq.tolerance = cfg_.tolerance;
+    rq.robust = cfg_.robust;
+    rq.huber_gamma = cfg_.huber_gamma;
+    return rq;
+}
+
+// The grids' first estimates (flat start, the telemetry given at add_grid),
+// then the stream batch is begun.
+int32_t Server::first_estimates(Unit* u) {
+    const SolveRequest rq = request_params();
+    const int32_t n = static_cast<int32_t>(u->grids.size());
+    std::vector<int32_t> ids(n);
+    std::iota(ids.begin(), ids.end(), 0);
+    std::vector<uint8_t> flat(n, 1);
+    std::vector<Engine::GridResult> res(n);
+    int32_t rc = u->eng->batch_solve(n, ids.data(), flat.data(), rq, res.data());
+    if (rc == 0) u->solved_once = true;
+    return rc;
+}
+
+// Picks the least recently used resident unit whose worker holds no requests
+// (other than `except`), copies its states to the host and frees its arena.
+bool Server::evict_one(const Unit* except) {
+    Unit* best = nullptr;
+    int64_t best_t = 0;
+    for (auto& up : units_) {
+        Unit* v = up.get();
+        if (v == except) continue;
+        std::unique_lock<std::mutex> el(v->eng_mu, std::try_to_lock);
+        if (!el.owns_lock() || !v->resident || v->busy) continue;
+        if (!best || v->last_used_ns < best_t) {
+            best = v;
+            best_t = v->last_used_ns;
+        }
+    }
+    if (!best) return false;
+    std::unique_lock<std::mutex> el(best->eng_mu, std::try_to_lock);
+    if (!el.owns_lock() || !best->resident || best->busy) return false;  // its worker took work meanwhile
+    if (best->eng->evict() != 0) return false;
+    best->resident = false;
+    used_ -= std::min(used_, best->need);
+    std::lock_guard<std::mutex> lk(st_mu_);
+    ++stats_.evictions;
+    --stats_.resident_units;
+    stats_.device_bytes = used_;
+    return true;
+}
+
+// Runs on u's worker with u->busy set (so nothing evicts u meanwhile).
+bool Server::make_resident(Unit* u) {
+    {
+        std::unique_lock<std::mutex> lk(mem_mu_);
+        while (used_ + u->need > budget_) {
+            if (stopping_) return false;
+            if (!evict_one(u)) mem_cv_.wait_for(lk, std::chrono::milliseconds(20));
+        }
+        used_ += u->need;
+    }
+    int32_t rc;
+    {
+        std::lock_guard<std::mutex> el(u->eng_mu);
+        u->eng->reuse_analysis_once = true;  // the plan does not depend on breaker states
+        rc = u->eng->upload();
+        if (rc == 0 && !u->solved_once) rc = first_estimates(u);
+        if (rc == 0) rc = u->eng->stream_begin(request_params());
+        if (rc == 0) {
+            u->resident = true;
+        } else {
+            u->eng->evict();
+        }
+    }
+    std::lock_guard<std::mutex> lk(mem_mu_);
+    if (rc != 0) {
+        used_ -= std::min(used_, u->need);
+        mem_cv_.notify_all();
+        return false;
+    }
+    std::lock_guard<std::mutex> sl(st_mu_);
+    ++stats_.admissions;
+    ++stats_.resident_units;
+    stats_.device_bytes = used_;
+    return true;
+}
+
+int32_t Server::submit(int32_t grid, const double* z, int32_t count, int32_t branch, int32_t closed, int64_t* ticket,
+                       double* v_out, double* th_out) {
     if (!started_) {
         last_error = "server not started";
         return -4;
@@ -244,7 +332,7 @@ int32_t Server::submit(int32_t grid, const double* z, int32_t count, int32_t bra
         finish(t, r);
         return 0;
     }
-    Request rq{t, grid, std::vector<double>(z, z + count), branch, closed, now_ns()};
+    Request rq{t, grid, std::vector<double>(z, z + count), branch, closed, now_ns(), v_out, th_out};
     {
         std::lock_guard<std::mutex> lk(u->mu);
         u->pending[local_of_[grid]].push_back(std::move(rq));
@@ -265,34 +353,24 @@ void Server::finish(int64_t ticket, const ServeResult& r) {
 // Iteration-level continuous batching: between two Gauss-Newton iterations
 // of the unit's batch, every grid with a pending request that is not already
 // in the batch joins it (its breaker edit and snapshot applied first); after
-// the iteration, grids that finished answer their request and leave.
+// the iteration, grids that finished answer their request and leave.  A unit
+// that is not resident is made resident before it takes requests; an idle
+// unit (no request in hand) may be evicted by another unit's worker.
 void Server::run_unit(Unit* u) {
-    SolveRequest rq;
-    rq.mode = Mode::PRECISION;
-    rq.max_iterations = cfg_.max_iterations;
-    rq.tolerance = cfg_.tolerance;
-    rq.robust = cfg_.robust;
-    rq.huber_gamma = cfg_.huber_gamma;
+    const SolveRequest rq = request_params();
     {
         std::lock_guard<std::mutex> lk(u->eng_mu);
-        if (u->eng->stream_begin(rq) != 0) {
-            // the unit cannot run: answer everything it receives as failed
-            for (;;) {
-                std::unique_lock<std::mutex> lk2(u->mu);
-                u->cv.wait(lk2, [&] { return stopping_.load() || u->n_pending > 0; });
-                if (stopping_ && u->n_pending == 0) return;
-                for (auto& q : u->pending)
-                    while (!q.empty()) {
-                        ServeResult r;
-                        r.status = CONV_DIVERGED;
-                        r.t_submit_ns = q.front().t_submit;
-                        r.t_start_ns = r.t_done_ns = now_ns();
-                        finish(q.front().ticket, r);
-                        q.pop_front();
-                        --u->n_pending;
-                    }
-            }
+        if (u->resident && u->eng->stream_begin(rq) != 0) {
+            // the next request brings the unit back (or fails its requests)
+            u->eng->evict();
+            u->resident = false;
+            std::lock_guard<std::mutex> ml(mem_mu_);
+            used_ -= std::min(used_, u->need);
+            std::lock_guard<std::mutex> sl(st_mu_);
+            --stats_.resident_units;
+            stats_.device_bytes = used_;
         }
+        u->last_used_ns = now_ns();
     }
     struct Running {
         Request req;
@@ -302,11 +380,34 @@ void Server::run_unit(Unit* u) {
     std::vector<Request> starting;
     std::vector<int32_t> ids, done;
     std::vector<Engine::GridResult> res;
+    auto fail_all = [&](std::vector<Request>& reqs, int32_t in_batch, int64_t t_start, int64_t t_done) {
+        for (auto& r0 : reqs) {
+            ServeResult r;
+            r.status = CONV_DIVERGED;
+            r.batch_size = in_batch;
+            r.t_submit_ns = r0.t_submit;
+            r.t_start_ns = t_start;
+            r.t_done_ns = t_done;
+            finish(r0.ticket, r);
+        }
+        std::lock_guard<std::mutex> lk(st_mu_);
+        stats_.completed += static_cast<int64_t>(reqs.size());
+    };
     for (;;) {
         starting.clear();
         {
             std::unique_lock<std::mutex> lk(u->mu);
-            if (active.empty()) u->cv.wait(lk, [&] { return stopping_.load() || u->n_pending > 0; });
+            if (active.empty()) {
+                if (u->n_pending == 0) {
+                    {
+                        std::lock_guard<std::mutex> el(u->eng_mu);
+                        u->busy = false;  // evictable while it waits
+                        u->last_used_ns = now_ns();
+                    }
+                    mem_cv_.notify_all();
+                }
+                u->cv.wait(lk, [&] { return stopping_.load() || u->n_pending > 0; });
+            }
             if (stopping_ && u->n_pending == 0 && active.empty()) return;
             for (size_t lid = 0; lid < u->pending.size(); ++lid) {
                 auto& q = u->pending[lid];
@@ -315,6 +416,28 @@ void Server::run_unit(Unit* u) {
                 q.pop_front();
                 --u->n_pending;
             }
+        }
+        bool resident;
+        {
+            std::lock_guard<std::mutex> el(u->eng_mu);
+            u->busy = true;
+            resident = u->resident;
+        }
+        if (!resident && !make_resident(u)) {
+            // stopping, or the unit could not be brought back: its requests fail
+            const int64_t t = now_ns();
+            fail_all(starting, 0, t, t);
+            if (stopping_) {
+                std::lock_guard<std::mutex> lk(u->mu);
+                for (auto& q : u->pending) {
+                    std::vector<Request> rest(std::make_move_iterator(q.begin()), std::make_move_iterator(q.end()));
+                    q.clear();
+                    fail_all(rest, 0, t, t);
+                }
+                u->n_pending = 0;
+                return;
+            }
+            continue;
         }
         const int64_t t0 = now_ns();
         int32_t rc = 0;
@@ -330,6 +453,13 @@ void Server::run_unit(Unit* u) {
             if (rc == 0 && !ids.empty()) rc = u->eng->stream_activate(static_cast<int32_t>(ids.size()), ids.data(), nullptr);
             for (auto& r : starting) active[local_of_[r.grid]] = Running{std::move(r), t0};
             if (rc == 0) rc = u->eng->stream_step(done, res);
+            // states of the finished grids into the callers' buffers, before their tickets complete
+            for (size_t i = 0; rc == 0 && i < done.size(); ++i) {
+                auto it = active.find(done[i]);
+                if (it == active.end() || (!it->second.req.v_out && !it->second.req.th_out)) continue;
+                rc = u->eng->batch_get_state(done[i], it->second.req.v_out, it->second.req.th_out);
+            }
+            u->last_used_ns = now_ns();
         }
         const int64_t t1 = now_ns();
         const int32_t in_batch = static_cast<int32_t>(active.size());
@@ -394,9 +524,10 @@ int32_t Server::get_state(int32_t grid, double* v, double* th) {
     }
     Unit* u = units_[unit_of_[grid]].get();
     if (!u->admitted) {
-        last_error = "grid not resident (admission budget)";
+        last_error = "grid not admitted: its unit's arena exceeds the memory budget";
         return -10;
     }
+    // a unit that is not resident answers from the states saved at eviction
     std::lock_guard<std::mutex> lk(u->eng_mu);
     const int32_t rc = u->eng->batch_get_state(local_of_[grid], v, th);
     if (rc) last_error = u->eng->last_error;
@@ -414,6 +545,10 @@ void Server::stop() {
     for (auto& u : units_) {
         { std::lock_guard<std::mutex> lk(u->mu); }  // a worker between its predicate check and its wait sees the flag
         u->cv.notify_all();
+    }
+    {
+        std::lock_guard<std::mutex> lk(mem_mu_);
+        mem_cv_.notify_all();  // a worker waiting for memory gives up
     }
     for (auto& u : units_)
         if (u->worker.joinable()) u->worker.join();

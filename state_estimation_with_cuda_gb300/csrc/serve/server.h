@@ -13,10 +13,16 @@
 // last state and stops on its own convergence test, so its result does not
 // depend on which other requests share the batch.
 //
-// Admission: units are made resident in order (small units first) while the
-// sum of their device arenas stays within the memory budget; requests for
-// grids of units that were not admitted complete at once with
-// `admitted = 0`.
+// Admission by device-memory budget: at start, units are made resident in
+// order (small units first) while the sum of their device arenas stays
+// within the budget.  A unit left out waits on the host; when a request for
+// one of its grids arrives, its worker makes it resident, evicting idle
+// resident units (least recently used first: their states are copied back
+// to the host and their arenas freed) until it fits, or waiting until a
+// unit goes idle.  An evicted unit resumes from its saved states, so every
+// result is the one the grid gives when it stays resident.  Only a unit
+// whose arena alone exceeds the budget is never admitted: its requests
+// complete at once with `admitted = 0`.
 #pragma once
 
 #include <atomic>
@@ -61,7 +67,9 @@ struct ServeResult {
 struct ServeStats {
     int64_t submitted = 0, completed = 0, rejected = 0, passes = 0, grid_solves = 0;  // passes = iterations run
     int32_t units = 0, admitted_units = 0, grids = 0;
-    size_t device_bytes = 0, budget_bytes = 0;
+    size_t device_bytes = 0, budget_bytes = 0;  // device_bytes: arenas resident now
+    int64_t admissions = 0, evictions = 0;      // residency changes after start
+    int32_t resident_units = 0;
 };
 
 class Server {
@@ -80,7 +88,11 @@ public:
     int32_t start();
     // Queue a snapshot for `grid` (count = its measurement count); a breaker
     // edit (branch >= 0) is applied before the snapshot.  Returns a ticket.
-    int32_t submit(int32_t grid, const double* z, int32_t count, int32_t branch, int32_t closed, int64_t* ticket);
+    // v_out / th_out (either may be null) receive the grid's |V| and theta
+    // when the request completes, before its ticket is ready; the caller
+    // keeps them valid until then.
+    int32_t submit(int32_t grid, const double* z, int32_t count, int32_t branch, int32_t closed, int64_t* ticket,
+                   double* v_out = nullptr, double* th_out = nullptr);
     // Wait up to timeout_ms (< 0: forever) for a ticket; 1 = done, 0 = timed out.
     int32_t wait(int64_t ticket, double timeout_ms, ServeResult* out);
     int32_t get_state(int32_t grid, double* v, double* th);
@@ -100,17 +112,24 @@ private:
         std::vector<double> z;
         int32_t branch, closed;
         int64_t t_submit;
+        double* v_out;
+        double* th_out;
     };
     struct Unit {
         std::unique_ptr<Engine> eng;
         std::vector<int32_t> grids;                  // fleet grid ids, local order
         std::vector<std::deque<Request>> pending;    // per local grid
         int64_t n_pending = 0;
-        bool admitted = false;
+        bool admitted = false;  // its arena fits the budget (it can be made resident)
         std::thread worker;
         std::mutex mu;  // guards pending / n_pending
         std::condition_variable cv;
-        std::mutex eng_mu;  // serialises engine use (worker vs get_state)
+        std::mutex eng_mu;  // serialises engine use (worker, get_state, eviction); guards the fields below
+        bool resident = false;    // arena allocated and the stream batch begun
+        bool busy = false;        // the worker holds requests: not evictable
+        bool solved_once = false; // the grids' first estimates (flat start) are done
+        size_t need = 0;          // arena bytes when resident
+        int64_t last_used_ns = 0;
     };
     ServeConfig cfg_;
     std::vector<GridData> fleet_;
@@ -124,6 +143,14 @@ private:
     int64_t next_ticket_ = 1;
     std::mutex st_mu_;
     ServeStats stats_;
+    // residency: bytes of the resident arenas against the budget
+    size_t budget_ = 0, used_ = 0;
+    std::mutex mem_mu_;  // taken before any unit's eng_mu, never after
+    std::condition_variable mem_cv_;
+    SolveRequest request_params() const;
+    int32_t first_estimates(Unit* u);  // caller holds u->eng_mu
+    bool make_resident(Unit* u);       // worker thread, u->busy set
+    bool evict_one(const Unit* except);  // caller holds mem_mu_
     void run_unit(Unit* u);
     void finish(int64_t ticket, const ServeResult& r);
 };

@@ -94,7 +94,9 @@ class SLE_ExServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("rejected", ctypes.c_int64),
                 ("passes", ctypes.c_int64), ("grid_solves", ctypes.c_int64), ("units", ctypes.c_int32),
                 ("admitted_units", ctypes.c_int32), ("grids", ctypes.c_int32), ("pad", ctypes.c_int32),
-                ("device_bytes", ctypes.c_size_t), ("budget_bytes", ctypes.c_size_t)]
+                ("device_bytes", ctypes.c_size_t), ("budget_bytes", ctypes.c_size_t),
+                ("admissions", ctypes.c_int64), ("evictions", ctypes.c_int64), ("resident_units", ctypes.c_int32),
+                ("pad2", ctypes.c_int32)]
 
 
 class SLE_Config(ctypes.Structure):
@@ -265,6 +267,7 @@ SLE_SIGNATURES = {
                                 P(I), P(I), P(I), P(D), P(D), P(I)]),
     "sle_ExServerStart": (I, [ctypes.c_void_p]),
     "sle_ExServerSubmit": (I, [ctypes.c_void_p, I, P(D), I, I, I, P(ctypes.c_int64)]),
+    "sle_ExServerSubmitEx": (I, [ctypes.c_void_p, I, P(D), I, I, I, P(D), P(D), P(ctypes.c_int64)]),
     "sle_ExServerWait": (I, [ctypes.c_void_p, ctypes.c_int64, D, P(SLE_ExServeResult)]),
     "sle_ExServerGetState": (I, [ctypes.c_void_p, I, P(D), P(D)]),
     "sle_ExServerGetStats": (I, [ctypes.c_void_p, P(SLE_ExServerStats)]),

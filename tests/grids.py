@@ -72,3 +72,40 @@ def state_index(g, bus, which):
     if bus == g.slack:
         return -1
     return bus if bus < g.slack else bus - 1
+
+
+GRID_ARRAYS = ("bus_type", "v_setpoint", "br_from", "br_to", "br_r", "br_x", "br_b", "br_tap", "br_shift",
+               "br_status", "m_type", "m_loc", "m_end", "m_sigma", "z")
+
+
+def copy_grid(g):
+    """A mutable copy of a grid's arrays (SyntheticGrid or namespace)."""
+    c = SimpleNamespace(n_bus=g.n_bus, n_branch=g.n_branch, n_meas=g.n_meas, slack=g.slack)
+    for k in GRID_ARRAYS:
+        setattr(c, k, np.array(getattr(g, k), copy=True))
+    for k in ("v_true", "theta_true"):
+        if hasattr(g, k):
+            setattr(c, k, np.array(getattr(g, k), copy=True))
+    return c
+
+
+def with_current_rows(g, n_branches, sigma=0.008, seed=5):
+    """Copy of a synthetic grid with |I| rows (MEAS_I_MAG = 6) at both ends of
+    `n_branches` seeded branches; their telemetry is h(x_true) from the oracle
+    plus Gaussian noise of `sigma`."""
+    from oracle.binding import Oracle
+
+    c = copy_grid(g)
+    rng = np.random.default_rng(seed)
+    br = np.sort(rng.choice(g.n_branch, size=n_branches, replace=False)).astype(np.int32)
+    c.m_type = np.concatenate([c.m_type, np.full(2 * n_branches, 6, np.int32)])
+    c.m_loc = np.concatenate([c.m_loc, np.repeat(br, 2)])
+    c.m_end = np.concatenate([c.m_end, np.tile(np.array([0, 1], np.int32), n_branches)])
+    c.m_sigma = np.concatenate([c.m_sigma, np.full(2 * n_branches, sigma)])
+    c.n_meas = len(c.m_type)
+    o = Oracle(c)
+    zt = np.concatenate([c.z, np.zeros(2 * n_branches)])
+    hx = o.evaluate(c.v_true, c.theta_true, zt)["hx"]
+    c.z = np.concatenate([c.z, hx[g.n_meas:] + sigma * rng.standard_normal(2 * n_branches)])
+    o.close()
+    return c

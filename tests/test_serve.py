@@ -120,11 +120,19 @@ def test_breaker_request():
     s.close()
 
 
-def test_admission_budget():
+def fleet_bytes(grids):
+    s = server_for(grids)
+    b = s.stats().device_bytes
+    s.close()
+    return b
+
+
+def test_unit_larger_than_the_budget_is_not_admitted():
     grids = fleet()
-    s = server_for(grids, memory_budget=6 << 20)
+    total = fleet_bytes(grids)
+    s = server_for(grids, memory_budget=total // 12)
     st = s.stats()
-    assert 0 < st.admitted_units < st.units
+    assert 0 < st.admitted_units < st.units  # the largest units alone exceed the budget
     assert st.device_bytes <= st.budget_bytes
     outcomes = []
     for i, g in enumerate(grids):
@@ -132,6 +140,53 @@ def test_admission_budget():
         outcomes.append(r.admitted)
         if r.admitted:
             assert r.status == 0
+        else:
+            assert r.status == 4  # NOT_OBSERVABLE: no unit can hold the grid
     assert 0 in outcomes and 1 in outcomes
-    assert s.stats().rejected == outcomes.count(0)
+    st = s.stats()
+    assert st.rejected == outcomes.count(0)
+    assert st.device_bytes <= st.budget_bytes
+    s.close()
+
+
+def test_budget_smaller_than_the_fleet_serves_every_request():
+    """Units are brought in as requests arrive and idle ones are evicted to
+    make room; a grid's states survive eviction on the host, so every result
+    equals the grid solved alone through the same snapshots."""
+    grids = fleet()
+    z0 = [g.z.copy() for g in grids]
+    total = fleet_bytes(grids)
+    s = server_for(grids, memory_budget=int(0.55 * total))
+    st = s.stats()
+    assert st.admitted_units == st.units and st.resident_units < st.units
+    snaps = [[g.renoise(u).copy() for u in range(2)] for g in grids]
+    outs = [[(np.full(g.n_bus, np.nan), np.full(g.n_bus, np.nan)) for _ in range(2)] for g in grids]
+    # round-robin over the grids: every unit is needed again after the others
+    for u in range(2):
+        tickets = [s.submit(i, snaps[i][u], out=outs[i][u]) for i in range(len(grids))]
+        for i, t in enumerate(tickets):
+            r = s.wait(t, 120000.0)
+            assert r is not None and r.admitted == 1 and r.status == 0, (i, u)
+    st = s.stats()
+    assert st.evictions > 0 and st.admissions > 0
+    assert st.device_bytes <= st.budget_bytes
+    assert st.completed == st.submitted == 2 * len(grids) and st.rejected == 0
+    for i, g in enumerate(grids):
+        ref = chain_alone(g, z0[i], snaps[i])
+        for u in range(2):
+            v, th = outs[i][u]
+            assert max(np.abs(v - ref[u][2]).max(), np.abs(th - ref[u][3]).max()) <= SAME, (i, u)
+    s.close()
+
+
+def test_submit_with_state_buffers_returns_the_served_state():
+    grids = fleet()[:5]
+    s = server_for(grids)
+    outs = [(np.empty(g.n_bus), np.empty(g.n_bus)) for g in grids]
+    tickets = [s.submit(i, g.renoise(7), out=outs[i]) for i, g in enumerate(grids)]
+    for i, t in enumerate(tickets):
+        r = s.wait(t, 60000.0)
+        assert r.status == 0
+        v, th = s.state(i)
+        assert np.array_equal(v, outs[i][0]) and np.array_equal(th, outs[i][1])
     s.close()

@@ -70,3 +70,30 @@ def test_noalloc_rejects_models_beyond_the_static_limit():
     assert "bytes of scratch" in msg and str(16 << 20) in msg
     assert np.all(np.isnan(x))  # nothing written
     e.close()
+
+
+def test_noalloc_on_a_handle_whose_device_is_not_current():
+    """A handle binds its own device for the call: with another device made
+    current by a second handle, the static scratch is looked up on (and the
+    kernels run on) the handle's device.  Needs two GPUs."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two GPUs")
+    other = Estimator()
+    other.set_config(device_id=1)
+    other.initialize()  # device 1 is now current on this thread
+    g = SyntheticGrid(2000, 2800, 0x5E01)
+    e = Estimator()
+    e.set_config(device_id=0)
+    e.load_network(g)
+    e.upload_model()
+    v, th = synthetic_state(g)
+    e.evaluate_at(v, th, exact=True)
+    rhs = np.random.default_rng(5).standard_normal(2 * g.n_bus - 1)
+    for _ in range(2):
+        x_ref = e.factor_solve(rhs)
+        rc, x = noalloc_solve(e, rhs)
+        assert rc == api.OK, e.lib.sle_GetLastError(e.h)
+        assert np.abs(x - x_ref).max() <= TOL * np.abs(x_ref).max()
+    e.close()
+    other.close()
