@@ -63,6 +63,14 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
  *                           with SLE_ERROR_CUDA_FAILURE and the message
  *                           "factorisation dataflow wait timed out" instead
  *                           of the GPU hanging (default 4194304)
+ *   "huber_stall"           robust (Huber) solves on one grid: also stop, as
+ *                           converged, when an iteration lowers the Huber
+ *                           objective by no more than this fraction of its
+ *                           previous value (default 0: only the reference's
+ *                           max |dx| < tolerance test).  The reference's
+ *                           reweighting creeps when gross errors sit on
+ *                           critical measurement pairs, whose Huber objective
+ *                           is nearly flat along the states they alone fix
  *   "hold_front"            failure-path test hook: the backward sweep never
  *                           publishes this front's completion, so the waits
  *                           of its children run out (-1, the default: none) */
@@ -163,6 +171,9 @@ typedef struct SLE_ExStats {
     int64_t calls[6];
     int64_t iterations, solves;
     int64_t total_launches; /* kernels this library launched since load */
+    int64_t analyses;       /* symbolic analyses of this handle */
+    int64_t uploads;        /* device arenas built for this handle */
+    int64_t branch_edits;   /* breaker / branch-parameter edits applied on the device */
 } SLE_ExStats;
 
 SLE_API SLE_StatusCode SLE_CALL sle_ExGetStats(SLE_Handle handle, SLE_ExStats* stats);

@@ -16,7 +16,8 @@ P = ctypes.POINTER
 
 class OrParams(ctypes.Structure):
     _fields_ = [("max_iterations", I), ("tolerance", D), ("exact_jacobian", I), ("gain_policy", I),
-                ("robust", I), ("huber_gamma", D), ("flat_start", I), ("realtime", I), ("vmin", D), ("vmax", D)]
+                ("robust", I), ("huber_gamma", D), ("flat_start", I), ("realtime", I), ("vmin", D), ("vmax", D),
+                ("huber_stall", D)]
 
 
 class OrResult(ctypes.Structure):
@@ -136,12 +137,12 @@ class Oracle:
         return st, x
 
     def wls(self, z, v, theta, max_iterations=20, tolerance=1e-6, exact=True, gain_policy=0, robust=False,
-            gamma=1.5, flat_start=True, realtime=False, vmin=0.5, vmax=1.5):
+            gamma=1.5, flat_start=True, realtime=False, vmin=0.5, vmax=1.5, huber_stall=0.0):
         v = np.array(v, np.float64)
         theta = np.array(theta, np.float64)
         z = np.ascontiguousarray(z, np.float64)
         p = OrParams(max_iterations, tolerance, int(exact), gain_policy, int(robust), gamma, int(flat_start),
-                     int(realtime), vmin, vmax)
+                     int(realtime), vmin, vmax, huber_stall)
         res = OrResult()
         r = np.empty(self.n_meas)
         self.L.or_wls(self.h, _dp(z), _dp(v), _dp(theta), ctypes.byref(p), ctypes.byref(res), _dp(r))
@@ -176,3 +177,74 @@ class Oracle:
 
 def threads():
     return lib().or_threads()
+
+
+class RefPin:
+    """The reference's own Ybus / h(x) / Jacobian kernels (FP32, from the
+    cubins in oracle/_ref) run through oracle/refpin.cpp on the GPU."""
+
+    REF_DIR = os.path.join(HERE, "_ref")
+
+    @classmethod
+    def available(cls):
+        return all(os.path.exists(os.path.join(cls.REF_DIR, u + ".cubin")) for u in ("kernels", "sparse_matrix"))
+
+    def __init__(self):
+        L = ctypes.CDLL(os.path.join(HERE, "_build", "librefpin.so"))
+        L.rp_error.restype = ctypes.c_char_p
+        L.rp_open.restype = I
+        L.rp_open.argtypes = [ctypes.c_char_p]
+        U8 = P(ctypes.c_uint8)
+        F = P(ctypes.c_float)
+        L.rp_ybus.restype = I
+        L.rp_ybus.argtypes = [I, I, P(I), P(I), F, F, F, F, F, U8, P(I), P(I), F, F, I]
+        L.rp_evaluate.restype = I
+        L.rp_evaluate.argtypes = [I, I, I, P(I), P(I), F, F, F, F, F, U8, I, U8, P(I), U8, F, F, F, P(I), F]
+        self.L = L
+        if L.rp_open(self.REF_DIR.encode()) != 0:
+            raise RuntimeError(L.rp_error().decode())
+
+    @staticmethod
+    def _branch_arrays(grid):
+        f32 = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+        return [np.ascontiguousarray(grid.br_from, np.int32), np.ascontiguousarray(grid.br_to, np.int32),
+                f32(grid.br_r), f32(grid.br_x), f32(grid.br_b), f32(grid.br_tap), f32(grid.br_shift),
+                np.ascontiguousarray(grid.br_status, np.uint8)]
+
+    @staticmethod
+    def _args(arrs):
+        out = []
+        for a in arrs:
+            t = {np.int32: I, np.float32: ctypes.c_float, np.uint8: ctypes.c_uint8}[a.dtype.type]
+            out.append(a.ctypes.data_as(P(t)))
+        return out
+
+    def ybus(self, grid):
+        """(row_ptr, col, g, b) in the reference kernels' (arrival) order."""
+        br = self._branch_arrays(grid)
+        cap = grid.n_bus + 2 * grid.n_branch
+        ptr = np.empty(grid.n_bus + 1, np.int32)
+        col = np.empty(cap, np.int32)
+        g = np.empty(cap, np.float32)
+        b = np.empty(cap, np.float32)
+        nnz = self.L.rp_ybus(grid.n_bus, grid.n_branch, *self._args(br), *self._args([ptr, col, g, b]), cap)
+        if nnz < 0:
+            raise RuntimeError(self.L.rp_error().decode())
+        return ptr, col[:nnz], g[:nnz], b[:nnz]
+
+    def evaluate(self, grid, v, theta):
+        """h(x) [n_meas] and the Jacobian rows as (col, val) arrays of 10 slots
+        a row in the kernel's write order (-1 = empty slot)."""
+        br = self._branch_arrays(grid)
+        m = grid.n_meas
+        meas = [np.ascontiguousarray(grid.m_type, np.uint8), np.ascontiguousarray(grid.m_loc, np.int32),
+                np.ascontiguousarray(grid.m_end, np.uint8)]
+        st = [np.ascontiguousarray(v, np.float32), np.ascontiguousarray(theta, np.float32)]
+        h = np.empty(m, np.float32)
+        hcol = np.empty(10 * m, np.int32)
+        hval = np.empty(10 * m, np.float32)
+        rc = self.L.rp_evaluate(grid.n_bus, int(grid.slack), grid.n_branch, *self._args(br), m,
+                                *self._args(meas), *self._args(st), *self._args([h, hcol, hval]))
+        if rc != 0:
+            raise RuntimeError(self.L.rp_error().decode())
+        return h, hcol.reshape(m, 10), hval.reshape(m, 10)

@@ -603,14 +603,24 @@ void or_wls(OrGrid* g, const double* z, double* v, double* th, const OrParams* p
     res->status = 5;
     bool converged = false, diverged = false, retry = false;
     int retries = 0;
+    const bool stall_test = p->robust && p->huber_stall > 0.0;
+    double jh_prev = -1.0, jh = 0.0;
     do {
         if (retry) {
             flat();
             g->factor_valid = false;
             converged = diverged = retry = false;
+            jh_prev = -1.0;
         }
         for (int it = 0; it < p->max_iterations && !converged && !diverged; ++it) {
             evaluate(*g, v, th, z, p->exact_jacobian != 0, p->robust != 0, p->huber_gamma);
+            if (stall_test) {  // Huber objective of this evaluation
+                jh = 0.0;
+                for (int q = 0; q < g->m; ++q) {  // every row is active in the oracle
+                    const double u = std::fabs(g->res[q]) / std::max(g->sigma[q], kEps);
+                    jh += u <= p->huber_gamma ? 0.5 * u * u : p->huber_gamma * u - 0.5 * p->huber_gamma * p->huber_gamma;
+                }
+            }
             const bool refactor = !g->factor_valid || p->robust || p->gain_policy == 0;
             if (refactor) {
                 if (!numeric(*g)) {
@@ -644,6 +654,10 @@ void or_wls(OrGrid* g, const double* z, double* v, double* th, const OrParams* p
             res->max_mismatch = bad ? std::numeric_limits<double>::quiet_NaN() : mx;
             converged = !bad && mx < p->tolerance;
             diverged = bad;
+            if (stall_test && !diverged) {
+                if (jh_prev > 0.0 && jh_prev - jh <= p->huber_stall * jh_prev) converged = true;
+                jh_prev = jh;
+            }
             res->iterations = it + 1;
         }
         if (diverged && retries < 2 && !p->realtime) {

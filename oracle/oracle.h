@@ -51,6 +51,8 @@ typedef struct OrParams {
     int32_t flat_start;
     int32_t realtime;        /* 1: no flat-start retries (REALTIME mode) */
     double vmin, vmax;
+    double huber_stall;      /* robust: also converged when the Huber objective of an evaluation falls by no
+                                more than this fraction of the previous one (0: off, the reference's test) */
 } OrParams;
 
 typedef struct OrResult {

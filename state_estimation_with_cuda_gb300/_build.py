@@ -4,6 +4,10 @@ Outputs (in-tree, git-ignored):
   state_estimation_with_cuda_gb300/lib/libsle_gb300.so  C ABI + engine + sm_103a kernels
   state_estimation_with_cuda_gb300/lib/libsegen.so      synthetic grid generator
   oracle/_build/liboracle.so                            CPU FP64 oracle (test infrastructure)
+  oracle/_build/librefpin.so                            harness that runs the reference's own kernels
+                                                        (test infrastructure)
+  oracle/_ref/*.cubin                                   the reference's kernels, built only where its
+                                                        sources are present (oracle/build_ref.py)
 
 Every translation unit is rebuilt only when a source or header it may include
 is newer than its object.
@@ -92,17 +96,39 @@ def build_segen():
 
 def build_oracle():
     os.makedirs(ORACLE_BUILD, exist_ok=True)
-    srcs = sorted(glob.glob(os.path.join(ORACLE, "*.cpp")))
-    hdrs = sorted(glob.glob(os.path.join(ORACLE, "*.h")))
+    srcs = [os.path.join(ORACLE, "oracle.cpp")]
+    hdrs = [os.path.join(ORACLE, "oracle.h")]
     so = os.path.join(ORACLE_BUILD, "liboracle.so")
     if srcs and _stale(so, srcs + hdrs):
         _run(["g++", "-std=c++17", "-O3", "-fPIC", "-shared", "-fopenmp"] + srcs + ["-o", so])
     return so
 
 
+def build_refpin():
+    """The reference-kernel harness (driver API; libcuda resolved at run time)."""
+    os.makedirs(ORACLE_BUILD, exist_ok=True)
+    src = os.path.join(ORACLE, "refpin.cpp")
+    so = os.path.join(ORACLE_BUILD, "librefpin.so")
+    if _stale(so, [src]):
+        _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-I", CUDA_INC, src, "-o", so,
+              "-L", "/usr/local/cuda/lib64/stubs", "-lcuda"])
+    return so
+
+
+def build_ref_kernels():
+    """oracle/_ref cubins from the reference's sources, where they are present."""
+    sys.path.insert(0, ORACLE)
+    try:
+        import build_ref
+    finally:
+        sys.path.pop(0)
+    return build_ref.build()
+
+
 def build_all(verbose=False):
-    with ThreadPoolExecutor(max_workers=3) as ex:
-        futs = [ex.submit(build_core, verbose), ex.submit(build_segen), ex.submit(build_oracle)]
+    with ThreadPoolExecutor(max_workers=5) as ex:
+        futs = [ex.submit(build_core, verbose), ex.submit(build_segen), ex.submit(build_oracle),
+                ex.submit(build_refpin), ex.submit(build_ref_kernels)]
         return [f.result() for f in futs]
 
 

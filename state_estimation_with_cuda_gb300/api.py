@@ -148,6 +148,18 @@ class Estimator:
     def set_switch(self, sd_id, closed):
         self._check(self.lib.sle_SetSwitchStatus(self.h, _b(sd_id), int(bool(closed))))
 
+    def apply_switch_changes(self):
+        self._check(self.lib.sle_ApplySwitchChanges(self.h))
+
+    def set_transformer_tap(self, branch_id, tap):
+        self._check(self.lib.sle_SetTransformerTap(self.h, _b(branch_id), float(tap)))
+
+    def set_phase_shift(self, branch_id, shift):
+        self._check(self.lib.sle_SetTransformerPhaseShift(self.h, _b(branch_id), float(shift)))
+
+    def set_branch_impedance(self, branch_id, r, x, b=0.0, g=0.0):
+        self._check(self.lib.sle_SetBranchImpedance(self.h, _b(branch_id), float(r), float(x), float(b), float(g)))
+
     # -- estimation ------------------------------------------------------------------
     def solve(self, mode=MODE_PRECISION):
         r = N.SLE_Result()

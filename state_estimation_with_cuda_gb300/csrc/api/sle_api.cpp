@@ -412,9 +412,11 @@ SLE_API SLE_StatusCode SLE_CALL sle_UpdateBranch(SLE_Handle handle, const SLE_Br
     auto& M = E(handle)->model;
     const int32_t k = M.find_branch(info->id);
     if (k < 0) return fail(SLE_ERROR_ELEMENT_NOT_FOUND, "Branch not found");
+    bool moved = false;
     if (info->from_bus && info->to_bus) {
         const int32_t f = M.find_bus(info->from_bus), t = M.find_bus(info->to_bus);
         if (f < 0 || t < 0) return fail(SLE_ERROR_ELEMENT_NOT_FOUND, "Bus not found");
+        moved = f != M.br_from[k] || t != M.br_to[k];
         M.br_from[k] = f;
         M.br_to[k] = t;
     }
@@ -425,7 +427,10 @@ SLE_API SLE_StatusCode SLE_CALL sle_UpdateBranch(SLE_Handle handle, const SLE_Br
     M.br_tap[k] = info->tap_ratio;
     M.br_shift[k] = info->phase_shift;
     M.br_xfmr[k] = info->is_transformer;
-    M.structure_dirty = true;
+    if (moved)
+        M.structure_dirty = true;  // new endpoints: a new pattern
+    else
+        M.branch_values_dirty = true;
     return SLE_OK;
 }
 
@@ -436,7 +441,7 @@ SLE_API SLE_StatusCode SLE_CALL sle_SetTransformerTap(SLE_Handle handle, const c
     const int32_t k = M.find_branch(id);
     if (k < 0) return fail(SLE_ERROR_ELEMENT_NOT_FOUND, "Branch not found");
     M.br_tap[k] = tap;
-    M.structure_dirty = true;
+    M.branch_values_dirty = true;  // parameter edit: values only, applied on the device
     return SLE_OK;
 }
 
@@ -446,7 +451,7 @@ SLE_API SLE_StatusCode SLE_CALL sle_SetTransformerPhaseShift(SLE_Handle handle, 
     const int32_t k = M.find_branch(id);
     if (k < 0) return fail(SLE_ERROR_ELEMENT_NOT_FOUND, "Branch not found");
     M.br_shift[k] = shift;
-    M.structure_dirty = true;
+    M.branch_values_dirty = true;  // parameter edit: values only, applied on the device
     return SLE_OK;
 }
 
@@ -460,7 +465,7 @@ SLE_API SLE_StatusCode SLE_CALL sle_SetBranchImpedance(SLE_Handle handle, const 
     M.br_x[k] = x;
     M.br_b[k] = b;
     M.br_g[k] = g;
-    M.structure_dirty = true;
+    M.branch_values_dirty = true;  // parameter edit: values only, applied on the device
     return SLE_OK;
 }
 
@@ -625,11 +630,18 @@ SLE_API SLE_StatusCode SLE_CALL sle_SetSwitchStatus(SLE_Handle handle, const cha
     // Queued in the reference (sle_engine.cu:568-580) and applied before the
     // next solve; here the status is recorded now and takes effect at the next
     // upload, which the next solve performs.
+    // A switched branch is in the uploaded pattern, so the change is a value
+    // edit applied on the device at the next solve (or by
+    // sle_ApplySwitchChanges); a switch added after the analysis of an open
+    // branch needs a new analysis.
     const uint8_t closed = status == SLE_SWITCH_CLOSED ? 1 : 0;
     if (M.sd_closed[s] != closed) {
         M.sd_closed[s] = closed;
         M.br_closed[M.sd_branch[s]] = closed;
-        M.structure_dirty = true;
+        if (E(handle)->branch_in_pattern(M.sd_branch[s]))
+            M.branch_values_dirty = true;
+        else
+            M.structure_dirty = true;
     }
     return SLE_OK;
 }
@@ -645,6 +657,9 @@ SLE_API SLE_SwitchStatus SLE_CALL sle_GetSwitchStatus(SLE_Handle handle, const c
 SLE_API SLE_StatusCode SLE_CALL sle_ApplySwitchChanges(SLE_Handle handle) {
     if (!handle) return SLE_ERROR_INVALID_HANDLE;
     Engine* e = E(handle);
+    if (e->uploaded() && e->model.branch_values_dirty && !e->model.structure_dirty) {
+        if (e->apply_branch_edits() != 0) return fail(SLE_ERROR_CUDA_FAILURE, e->last_error);
+    }
     if (e->uploaded() && e->model.structure_dirty) {
         if (e->upload() != 0) return fail(SLE_ERROR_CUDA_FAILURE, e->last_error);
     }
@@ -700,6 +715,9 @@ SLE_API SLE_StatusCode SLE_CALL sle_CheckObservability(SLE_Handle handle, int32_
     auto& M = en->model;
     const int32_t n = M.n_bus();
     int32_t count = 0, active = 0;
+    if (en->uploaded() && !M.structure_dirty && M.branch_values_dirty && !en->batch_mode()) {
+        if (en->apply_branch_edits() != 0) return fail(SLE_ERROR_CUDA_FAILURE, en->last_error);
+    }
     if (en->uploaded() && !M.structure_dirty && !en->batch_mode()) {
         if (en->check_islands(&count, &active) != 0) return fail(SLE_ERROR_CUDA_FAILURE, en->last_error);
     } else {
@@ -1163,7 +1181,10 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* k
     else if (k == "dataflow") { c.dataflow = value != 0.0 ? 1 : 0; E(handle)->model.structure_dirty = true; }
     else if (k == "flow_small_f") { c.flow_small_f = static_cast<int32_t>(value); E(handle)->model.structure_dirty = true; }
     else if (k == "warp_fronts") { c.warp_fronts = value < 0.0 ? -1 : (value != 0.0 ? 1 : 0); E(handle)->model.structure_dirty = true; }
-    else if (k == "spin_limit" || k == "hold_front") {
+    else if (k == "huber_stall") {
+        if (!(value >= 0.0 && value < 1.0)) return fail(SLE_ERROR_INVALID_ARGUMENT, "huber_stall must be in [0, 1)");
+        c.huber_stall = value;
+    } else if (k == "spin_limit" || k == "hold_front") {
         if (k == "spin_limit") {
             if (!(value >= 1.0 && value <= 9.0e15)) return fail(SLE_ERROR_INVALID_ARGUMENT, "spin_limit must be >= 1");
             c.spin_limit = static_cast<long long>(value);
@@ -1355,6 +1376,9 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExGetStats(SLE_Handle handle, SLE_ExStats* s
     st->iterations = s.iterations;
     st->solves = s.solves;
     st->total_launches = sle_gb300::g_kernel_launches.load();
+    st->analyses = s.analyses;
+    st->uploads = s.uploads;
+    st->branch_edits = s.branch_edits;
     return SLE_OK;
 }
 

@@ -109,6 +109,13 @@ int32_t Engine::analyze() {
         last_error = err;
         return -5;
     }
+    // The pattern holds the closed branches (the reference's rule,
+    // sparse_matrix.cu:357-404) and every branch a switching device can
+    // close, so breaker operations are value edits on the device; an open
+    // switched branch contributes exact zeros.
+    br_in_pattern_.assign(model.br_closed.begin(), model.br_closed.end());
+    for (int32_t k : model.sd_branch)
+        if (k >= 0 && k < model.n_branch()) br_in_pattern_[k] = 1;
     Topology t;
     t.n_bus = model.n_bus();
     t.n_branch = model.n_branch();
@@ -116,7 +123,7 @@ int32_t Engine::analyze() {
     t.slack = model.slack;
     t.br_from = model.br_from.data();
     t.br_to = model.br_to.data();
-    t.br_closed = model.br_closed.data();
+    t.br_closed = br_in_pattern_.data();
     t.m_type = model.m_type.data();
     t.m_loc = model.m_loc.data();
     t.m_end = model.m_end.data();
@@ -129,6 +136,7 @@ int32_t Engine::analyze() {
         return -5;
     }
     analyzed_ = true;
+    ++stats.analyses;
     return 0;
 }
 
@@ -601,6 +609,7 @@ int32_t Engine::upload() {
         work_.pt = c.take<double>(nbr);
         work_.qt = c.take<double>(nbr);
         work_.part = c.take<double>(nparts);
+        work_.hpart = c.take<double>(nparts);
         work_.opart = c.take<double>(nparts);
         work_.oidx = c.take<int32_t>(nparts);
         work_.ocnt = c.take<int32_t>(nparts);
@@ -862,6 +871,8 @@ int32_t Engine::upload() {
     factor_valid_ = false;
     stale_ = 0;
     model.structure_dirty = false;
+    model.branch_values_dirty = false;  // the upload took the current branch values
+    ++stats.uploads;
     model.values_dirty = false;
     return 0;
 }
@@ -922,6 +933,7 @@ SolveParams Engine::params(const SolveRequest& rq) const {
     sp.vmin = cfg.voltage_min_pu;
     sp.vmax = cfg.voltage_max_pu;
     sp.skip_flags = FLAG_FROZEN;
+    sp.huber_objective = (rq.robust && cfg.huber_stall > 0.0 && !batch_mode()) ? 1 : 0;
     return sp;
 }
 
@@ -1087,6 +1099,22 @@ int32_t Engine::solve(const SolveRequest& rq, SolveResult& out) {
             return rc;
         }
     }
+    if (model.branch_values_dirty) {
+        const int32_t rc = apply_branch_edits();
+        if (rc) {
+            out.status = CONV_SINGULAR;
+            last_ = out;
+            return rc;
+        }
+        if (model.structure_dirty) {  // an edit needs a new pattern
+            const int32_t rc2 = upload();
+            if (rc2) {
+                out.status = CONV_NOTOBS;
+                last_ = out;
+                return rc2;
+            }
+        }
+    }
     if (model.values_dirty) {
         const int32_t rc = sync_measurements();
         if (rc) return rc;
@@ -1097,12 +1125,14 @@ int32_t Engine::solve(const SolveRequest& rq, SolveResult& out) {
     const int32_t max_iter = rq.max_iterations;
     bool converged = false, diverged = false, retry = false;
     int32_t retries = 0;
+    double jh_prev = -1.0;  // Huber objective of the previous evaluation (stall test)
     out.status = CONV_RUNNING;
     do {
         if (retry) {
             launch_flat_start(net_, work_, st_);
             converged = diverged = retry = false;
             factor_valid_ = false;
+            jh_prev = -1.0;
         }
         for (int32_t it = 0; it < max_iter && !converged && !diverged; ++it) {
             const bool refactor = !factor_valid_ || rq.robust || cfg.gain_policy == 0;
@@ -1131,6 +1161,14 @@ int32_t Engine::solve(const SolveRequest& rq, SolveResult& out) {
             out.max_mismatch = h_status_->max_mismatch;
             converged = (fl & FLAG_CONVERGED) != 0;
             diverged = (fl & FLAG_NONFINITE) != 0;
+            if (sp.huber_objective && !diverged) {
+                // robust stall test (option huber_stall): the Huber objective of
+                // this iteration's evaluation fell by no more than
+                // huber_stall x its previous value -> the estimate stands
+                const double jh = h_status_->huber_objective;
+                if (jh_prev > 0.0 && jh_prev - jh <= cfg.huber_stall * jh_prev) converged = true;
+                jh_prev = jh;
+            }
             out.iterations = it + 1;
             if (rq.mode == Mode::REALTIME && rq.time_limit_ms > 0.0) {
                 cudaEventRecord(ev1_, st_);
@@ -1183,6 +1221,35 @@ int32_t Engine::solve(const SolveRequest& rq, SolveResult& out) {
     return 0;
 }
 
+int32_t Engine::apply_branch_edits() {
+    if (!model.branch_values_dirty) return 0;
+    if (!uploaded_ || model.structure_dirty) return 0;  // the next upload takes the host values
+    const DeviceScope dev_scope(cfg.device_id);
+    for (int32_t k = 0; k < model.n_branch(); ++k)
+        if (model.br_closed[k] && !branch_in_pattern(k)) {
+            model.structure_dirty = true;  // a branch outside the pattern closed: analyse again
+            return 0;
+        }
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if (e == cudaSuccess) e = x;
+    };
+    chk(put(const_cast<double*>(net_.br_r), model.br_r, st_));
+    chk(put(const_cast<double*>(net_.br_x), model.br_x, st_));
+    chk(put(const_cast<double*>(net_.br_bch), model.br_b, st_));
+    chk(put(const_cast<double*>(net_.br_tap), model.br_tap, st_));
+    chk(put(const_cast<double*>(net_.br_shift), model.br_shift, st_));
+    chk(put(const_cast<uint8_t*>(net_.br_closed), model.br_closed, st_));
+    chk(launch_admittance_and_ybus(net_, st_));
+    chk(cudaStreamSynchronize(st_));
+    if (e != cudaSuccess) return set_cuda_error(e, "branch edits");
+    model.branch_values_dirty = false;
+    factor_valid_ = false;
+    stale_ = DL_ALL;
+    ++stats.branch_edits;
+    return 0;
+}
+
 int32_t Engine::evict() {
     const DeviceScope dev_scope(cfg.device_id);
     if (!uploaded_) return 0;
@@ -1231,6 +1298,11 @@ int32_t Engine::evaluate_at(const double* v, const double* th, int32_t exact) {
     const DeviceScope dev_scope(cfg.device_id);
     if (!uploaded_ || model.structure_dirty) {
         const int32_t rc = upload();
+        if (rc) return rc;
+    }
+    if (model.branch_values_dirty) {
+        int32_t rc = apply_branch_edits();
+        if (rc == 0 && model.structure_dirty) rc = upload();
         if (rc) return rc;
     }
     if (model.values_dirty) sync_measurements();

@@ -48,6 +48,8 @@ struct EngineConfig {
                                      // 1 on, 0 off, -1 per grid with at least kWarpPhaseMinFronts of them
     int32_t stream_priority = 0;     // CUDA stream priority of the engine's stream (lower = more urgent)
     long long spin_limit = kSpinLimitDefault;  // polls before a dataflow wait gives up (FLAG_TIMEOUT)
+    double huber_stall = 0.0;        // robust solves: also stop when the Huber objective falls by no more
+                                     // than this fraction in an iteration (0: the reference's test only)
     int32_t hold_front = -1;         // test hook: front whose backward-sweep completion is withheld
 };
 
@@ -103,6 +105,7 @@ struct StageStats {
     double ms[ST_COUNT] = {0, 0, 0, 0, 0, 0};
     int64_t calls[ST_COUNT] = {0, 0, 0, 0, 0, 0};
     int64_t iterations = 0, solves = 0;
+    int64_t analyses = 0, uploads = 0, branch_edits = 0;
 };
 
 class Engine {
@@ -159,6 +162,17 @@ public:
     // Copies cfg.spin_limit / cfg.hold_front into the device work view (the
     // next launches use them; captured iteration graphs are dropped).
     void apply_wait_options();
+    // Device topology processor for one grid: breaker states and branch
+    // parameters (r, x, charging, tap, phase shift) edited on the host model
+    // reach the device as values -- the branch arrays are copied, admittances
+    // and Ybus recomputed, the factor invalidated -- without a new symbolic
+    // analysis, as long as every edited branch is in the uploaded pattern.
+    int32_t apply_branch_edits();
+    // True when branch k is in the pattern of the current plan (it is closed,
+    // or a switching device can close it), so its edits are value edits.
+    bool branch_in_pattern(int32_t k) const {
+        return analyzed_ && k >= 0 && k < static_cast<int32_t>(br_in_pattern_.size()) && br_in_pattern_[k] != 0;
+    }
     int32_t timer(int32_t op, double* ms);                                  // 0 start, 1 stop (+ elapsed)
     StageStats stats;
 
@@ -221,6 +235,7 @@ public:
 
 private:
     bool init_ = false, analyzed_ = false, uploaded_ = false, factor_valid_ = false;
+    std::vector<uint8_t> br_in_pattern_;  // per branch, of the current plan
     bool mixed_ = false;  // pipeline of the current upload: FP32 gain/factor + FP64 refinement
     int32_t stale_ = 0;  // DL_* mask of host copies older than the device
     cudaStream_t st_ = nullptr;

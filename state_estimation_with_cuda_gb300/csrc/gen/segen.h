@@ -97,8 +97,9 @@ int32_t segen_renoise(SEGrid* g, int32_t update, double frac, double* out);
 /* Toggle the status of branch k (breaker edit) in the generator's copy. */
 void segen_set_status(SEGrid* g, int32_t k, int32_t status);
 
-/* Index of a seeded non-bridge branch (removing it keeps the grid connected),
- * chosen by `draw`; -1 if none exists. */
+/* Index of a seeded switchable branch, chosen by `draw`: closed, not a
+ * bridge (removing it keeps the grid connected) and without flow or current
+ * rows; -1 if none is found. */
 int32_t segen_pick_nonbridge(const SEGrid* g, uint64_t draw);
 
 /* Fleet helpers: grid size draws used by the batched (log-uniform) and

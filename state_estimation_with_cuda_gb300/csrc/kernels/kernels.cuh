@@ -148,6 +148,7 @@ struct DevWork {
     double* pt;
     double* qt;
     double* part;     // block partials: [2 * max_blocks]
+    double* hpart;    // Huber-objective block partials of an evaluation
     double* opart;    // bad-data pass block partials: largest |r| per block
     int32_t* oidx;    //   its row
     int32_t* ocnt;    //   rows over the threshold per block
@@ -200,6 +201,9 @@ struct SolveParams {
     double vmin, vmax;
     uint32_t skip_flags;     // batch: grids whose flags intersect this mask are not evaluated
     uint32_t need_flags;     // batch: only grids whose flags hold every bit of this mask are evaluated
+    int32_t huber_objective; // one grid: also sum the Huber objective of the evaluation into
+                             // DevStatus::huber_objective (the robust solve's stall test)
+    int32_t pad;
 };
 
 // Upload-time kernels.

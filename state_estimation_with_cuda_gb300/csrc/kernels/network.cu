@@ -203,7 +203,7 @@ __device__ __forceinline__ void put_flow(double* hrow, int fpos, const double d[
 __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, SolveParams sp) {
     __shared__ double sh[32];
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    double obj = 0.0;
+    double obj = 0.0, hub = 0.0;
     bool skip = false;
     if (q < net.n_meas && net.meas_grid) {
         const uint32_t gf = w.grid_flags[net.meas_grid[q]];
@@ -312,6 +312,10 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
                 if (!(rn <= sp.huber_gamma)) we = sp.huber_gamma / (sg * fabs(rr) + kEps);
             }
             obj = wb * rr * rr;
+            if (sp.huber_objective) {  // rho(u) = u^2 / 2 inside gamma, gamma |u| - gamma^2 / 2 outside
+                const double u = fabs(rr) / fmax(net.m_sigma[q], kEps);
+                hub = (u <= sp.huber_gamma) ? 0.5 * u * u : sp.huber_gamma * u - 0.5 * sp.huber_gamma * sp.huber_gamma;
+            }
         } else {
             hv = 0.0;
         }
@@ -328,6 +332,20 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
     }
     const double s = block_sum(obj, sh);
     if (threadIdx.x == 0) w.part[blockIdx.x] = s;
+    if (sp.huber_objective) {
+        __syncthreads();  // sh is reused
+        const double hs = block_sum(hub, sh);
+        if (threadIdx.x == 0) w.hpart[blockIdx.x] = hs;
+    }
+}
+
+// Huber objective of the last evaluation (block partials in order).
+__global__ void k_huber_objective(DevWork w, int nblk) {
+    __shared__ double sh[32];
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) acc += w.hpart[b];
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) w.status->huber_objective = acc;
 }
 
 // a11: b = H^T (w r) in permuted state order, one thread per state (gather).
@@ -836,6 +854,10 @@ cudaError_t launch_evaluate(const DevNet& net, const DevWork& w, const SolvePara
     k_bus_trig<<<nblocks(net.n_bus), kBlock, 0, st>>>(net, w, sp);
     k_evaluate<<<nblocks(net.n_meas), kBlock, 0, st>>>(net, w, sp);
     count_launches(2);
+    if (sp.huber_objective) {
+        k_huber_objective<<<1, 1024, 0, st>>>(w, nblocks(net.n_meas));
+        count_launches(1);
+    }
     return cudaGetLastError();
 }
 

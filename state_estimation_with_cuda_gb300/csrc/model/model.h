@@ -59,6 +59,9 @@ struct Model {
     bool structure_dirty = true;
     // true when measurement values changed on the host only
     bool values_dirty = false;
+    // true when branch parameters or switch states changed on the host only
+    // (value edits: the uploaded pattern holds every affected branch)
+    bool branch_values_dirty = false;
 
     int32_t n_bus() const { return static_cast<int32_t>(bus_type.size()); }
     int32_t n_branch() const { return static_cast<int32_t>(br_from.size()); }

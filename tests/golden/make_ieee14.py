@@ -9,7 +9,7 @@ ships: model at :68-270, "true" telemetry at :284-330) and writes
   state_estimation_with_cuda_gb300/csrc/api/ieee14_data.inc
       the same model as a C table, compiled into sle_LoadIEEE14Bus.
 
-Usage:  python tests/golden/make_ieee14.py [path/to/reference]
+Usage:  python tests/golden/make_ieee14.py path/to/reference
 The reference checkout is only needed to regenerate; both outputs are
 committed.
 """
@@ -92,7 +92,9 @@ def c_table(d):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_ieee14.py path/to/reference")
+    ref = sys.argv[1]
     with open(os.path.join(ref, "data", "ieee14bus.h")) as fh:
         src = fh.read()
     d = parse(src)

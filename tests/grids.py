@@ -109,3 +109,86 @@ def with_current_rows(g, n_branches, sigma=0.008, seed=5):
     c.z = np.concatenate([c.z, hx[g.n_meas:] + sigma * rng.standard_normal(2 * n_branches)])
     o.close()
     return c
+
+
+def bounded_degree_grid(n_bus, seed, max_degree=4, n_chords=None, current_rows=8):
+    """A seeded grid whose buses all have at most `max_degree` branches and
+    no parallel branches, so every injection row of the reference's Jacobian
+    fits its fixed 10 slots (2 x 4 neighbours + 2; sparse_matrix.cu:1574-1595).
+    Spanning tree (each bus joins an earlier bus with room) plus chords between
+    nearby buses; parameters drawn as the synthetic workloads draw them
+    (r ~ U(0.01, 0.08), x = r U(3, 8), charging U(0, 0.06), taps U(0.95, 1.05)
+    on 15 % of branches); slack = bus 0; |V| at 30 % of buses, P+Q injection
+    at 60 %, both-end P+Q flows on 70 % of branches, |I| at both ends of
+    `current_rows` branches; telemetry = h(x_true) of the oracle (noise-free:
+    the grid pins formulas, not estimates)."""
+    from oracle.binding import Oracle
+
+    rng = np.random.default_rng(seed)
+    deg = np.zeros(n_bus, np.int64)
+    edges = set()
+    frm, to = [], []
+
+    def add(a, b):
+        frm.append(a)
+        to.append(b)
+        edges.add((min(a, b), max(a, b)))
+        deg[a] += 1
+        deg[b] += 1
+
+    for k in range(1, n_bus):
+        lo = max(0, k - 12)
+        cand = [j for j in range(lo, k) if deg[j] < max_degree - 1] or [j for j in range(k) if deg[j] < max_degree]
+        add(int(rng.choice(cand)), k)
+    n_chords = int(0.4 * n_bus) if n_chords is None else n_chords
+    tries = 0
+    while n_chords > 0 and tries < 50 * n_bus:
+        tries += 1
+        a = int(rng.integers(0, n_bus))
+        b = int(a + rng.integers(1, 10))
+        if b >= n_bus or deg[a] >= max_degree or deg[b] >= max_degree or (a, b) in edges:
+            continue
+        add(a, b)
+        n_chords -= 1
+    nbr = len(frm)
+    g = SimpleNamespace(n_bus=n_bus, n_branch=nbr, slack=0)
+    g.bus_type = np.zeros(n_bus, np.int32)
+    g.bus_type[0] = 2
+    g.v_setpoint = np.ones(n_bus)
+    g.br_from = np.array(frm, np.int32)
+    g.br_to = np.array(to, np.int32)
+    g.br_r = rng.uniform(0.01, 0.08, nbr)
+    g.br_x = g.br_r * rng.uniform(3.0, 8.0, nbr)
+    g.br_b = rng.uniform(0.0, 0.06, nbr)
+    g.br_tap = np.ones(nbr)
+    tapped = rng.choice(nbr, max(1, int(0.15 * nbr)), replace=False)
+    g.br_tap[tapped] = rng.uniform(0.95, 1.05, len(tapped))
+    g.br_shift = np.zeros(nbr)
+    g.br_status = np.ones(nbr, np.int32)
+    g.v_true = rng.uniform(0.97, 1.06, n_bus)
+    g.theta_true = 0.08 * rng.standard_normal(n_bus)
+    g.theta_true[0] = 0.0
+    mt, ml, me = [], [], []
+    for i in np.sort(rng.choice(n_bus, int(0.3 * n_bus), replace=False)):
+        mt.append(0), ml.append(i), me.append(0)
+    for i in np.sort(rng.choice(n_bus, int(0.6 * n_bus), replace=False)):
+        mt += [2, 3]
+        ml += [i, i]
+        me += [0, 0]
+    for k in np.sort(rng.choice(nbr, int(0.7 * nbr), replace=False)):
+        mt += [4, 5, 4, 5]
+        ml += [k] * 4
+        me += [0, 0, 1, 1]
+    for k in np.sort(rng.choice(nbr, current_rows, replace=False)):
+        mt += [6, 6]
+        ml += [k, k]
+        me += [0, 1]
+    g.m_type = np.array(mt, np.int32)
+    g.m_loc = np.array(ml, np.int32)
+    g.m_end = np.array(me, np.int32)
+    g.n_meas = len(mt)
+    g.m_sigma = np.where(g.m_type == 0, 0.004, np.where(np.isin(g.m_type, (2, 3)), 0.01, 0.008))
+    o = Oracle(g)
+    g.z = o.evaluate(g.v_true, g.theta_true, np.zeros(g.n_meas))["hx"]
+    o.close()
+    return g

@@ -273,3 +273,27 @@ def test_current_magnitude_rows_solve_matches_oracle():
     assert state_err(v, th, ov, oth) < STATE_TOL
     assert np.array_equal(e.bad_data(3.0), o.bad_data(orr, 3.0))
     e.close()
+
+
+def test_huber_stall_option_matches_oracle():
+    """Robust (Huber) solves with the reference's reweighting creep when gross
+    errors sit on critical measurement pairs; the huber_stall option also
+    stops when an iteration lowers the Huber objective by no more than that
+    fraction.  Same stopping iteration and state as the oracle with the same
+    rule; without it both run to the iteration cap."""
+    g = SyntheticGrid(600, 840, 0x5E02, gross=0.02)
+    e, o = engine(g, huber_stall=1e-5), Oracle(g)
+    rc, res = e.solve_with(max_iterations=100, tolerance=1e-6, flat_start=True, robust=True, huber_gamma=1.5)
+    v, th = e.voltages()
+    ov, oth, ores, orr = o.wls(g.z, g.v_setpoint, np.zeros(g.n_bus), max_iterations=100, tolerance=1e-6,
+                               robust=True, gamma=1.5, huber_stall=1e-5)
+    assert res.status == ores.status == 0
+    assert res.iterations == ores.iterations < 100
+    assert state_err(v, th, ov, oth) < STATE_TOL
+    assert np.array_equal(e.bad_data(3.0), o.bad_data(orr, 3.0))
+    e.set_option("huber_stall", 0.0)
+    rc, res = e.solve_with(max_iterations=100, tolerance=1e-6, flat_start=True, robust=True, huber_gamma=1.5)
+    ov, oth, ores, _ = o.wls(g.z, g.v_setpoint, np.zeros(g.n_bus), max_iterations=100, tolerance=1e-6, robust=True,
+                             gamma=1.5)
+    assert res.status == ores.status == 1 and res.iterations == ores.iterations == 100
+    e.close()
