@@ -76,7 +76,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20, help="timed steps (windows of %d requests)" % STEP_REQUESTS)
     ap.add_argument("--warmup", type=int, default=5, help="warm-up steps")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bounded CPU-baseline sample of the stream")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="bounded CPU-baseline sample of the stream")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid10k-steps", type=int, default=100, help="hot-start updates of the grid10k leg")
     ap.add_argument("--skip-extra", action="store_true", help="headline legs only")

@@ -63,6 +63,9 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
  *                           with SLE_ERROR_CUDA_FAILURE and the message
  *                           "factorisation dataflow wait timed out" instead
  *                           of the GPU hanging (default 4194304)
+ *   "gain_accumulate"       mixed pipeline: bits of the accumulator of each
+ *                           gain entry's sum of FP32 products, 32 (default)
+ *                           or 64 (re-uploads)
  *   "huber_stall"           robust (Huber) solves on one grid: also stop, as
  *                           converged, when an iteration lowers the Huber
  *                           objective by no more than this fraction of its

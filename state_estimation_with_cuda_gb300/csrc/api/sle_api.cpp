@@ -1181,7 +1181,11 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* k
     else if (k == "dataflow") { c.dataflow = value != 0.0 ? 1 : 0; E(handle)->model.structure_dirty = true; }
     else if (k == "flow_small_f") { c.flow_small_f = static_cast<int32_t>(value); E(handle)->model.structure_dirty = true; }
     else if (k == "warp_fronts") { c.warp_fronts = value < 0.0 ? -1 : (value != 0.0 ? 1 : 0); E(handle)->model.structure_dirty = true; }
-    else if (k == "huber_stall") {
+    else if (k == "gain_accumulate") {
+        if (value != 32.0 && value != 64.0) return fail(SLE_ERROR_INVALID_ARGUMENT, "gain_accumulate is 32 or 64");
+        c.gain_acc32 = value == 32.0 ? 1 : 0;
+        E(handle)->model.structure_dirty = true;  // taken at the next upload
+    } else if (k == "huber_stall") {
         if (!(value >= 0.0 && value < 1.0)) return fail(SLE_ERROR_INVALID_ARGUMENT, "huber_stall must be in [0, 1)");
         c.huber_stall = value;
     } else if (k == "spin_limit" || k == "hold_front") {

@@ -320,7 +320,10 @@ void Engine::build_schedule() {
         for (int32_t s : bigs) {
             const int32_t f = P.sn_f[s], nc = P.sn_c0[s + 1] - P.sn_c0[s];
             const int32_t tiles = (f + kTile - 1) / kTile;
-            for (int32_t tj = 0; tj < tiles; ++tj) sch_asm_.push_back(make_int4(s, tj, 0, 0));
+            for (int32_t tj = 0; tj < tiles; ++tj) {
+                const int32_t rows = f - tj * kTile;  // the tile column's lower part
+                for (int32_t rb = 0; rb * kAsmRows < rows; ++rb) sch_asm_.push_back(make_int4(s, tj, rb, 0));
+            }
             panels = std::max(panels, (nc + kTile - 1) / kTile);
         }
         sch_panels_[l] = panels;
@@ -790,6 +793,7 @@ int32_t Engine::upload() {
 
     sched_.n_levels = P.n_levels;
     sched_.n_tgt = static_cast<int32_t>(P.tgt_local.size());
+    sched_.gain_acc32 = mixed_ && cfg.gain_acc32 ? 1 : 0;
     sched_.h_small_ptr = sch_small_ptr_.data();
     sched_.d_small = d_small_;
     sched_.h_small_maxf = sch_small_maxf_.data();

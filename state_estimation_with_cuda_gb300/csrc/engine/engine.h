@@ -48,6 +48,7 @@ struct EngineConfig {
                                      // 1 on, 0 off, -1 per grid with at least kWarpPhaseMinFronts of them
     int32_t stream_priority = 0;     // CUDA stream priority of the engine's stream (lower = more urgent)
     long long spin_limit = kSpinLimitDefault;  // polls before a dataflow wait gives up (FLAG_TIMEOUT)
+    int32_t gain_acc32 = 1;          // mixed pipeline: gain entries summed in FP32 (1, default) or FP64 (0)
     double huber_stall = 0.0;        // robust solves: also stop when the Huber objective falls by no more
                                      // than this fraction in an iteration (0: the reference's test only)
     int32_t hold_front = -1;         // test hook: front whose backward-sweep completion is withheld

@@ -98,8 +98,8 @@ int32_t segen_renoise(SEGrid* g, int32_t update, double frac, double* out);
 void segen_set_status(SEGrid* g, int32_t k, int32_t status);
 
 /* Index of a seeded switchable branch, chosen by `draw`: closed, not a
- * bridge (removing it keeps the grid connected) and without flow or current
- * rows; -1 if none is found. */
+ * bridge (removing it keeps the grid connected), without flow or current
+ * rows, between buses of at least three branches; -1 if none is found. */
 int32_t segen_pick_nonbridge(const SEGrid* g, uint64_t draw);
 
 /* Fleet helpers: grid size draws used by the batched (log-uniform) and

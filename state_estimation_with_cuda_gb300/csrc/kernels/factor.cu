@@ -18,7 +18,8 @@
 // panel kernel (each CTA factors the 32 x 32 diagonal tile and solves one row
 // tile against it) and a trailing-update kernel (one CTA per 32 x 32 tile).
 // The factor type T is double for the FP64 pipeline and float for the
-// mixed-precision one; sums of the gain entries are always formed in double.
+// mixed-precision one; the mixed pipeline forms the gain entries' sums in
+// float (gain_acc32, the default) or in double.
 #include "kernels.cuh"
 
 #include <algorithm>
@@ -30,14 +31,15 @@ namespace {
 constexpr int kThreads = 256;
 
 // G entry = sum over its pairs (a, b) of (w h_a) h_b, the weighted entry
-// hw[a] written by the evaluation (FP64: the same product, so the same sum).
-template <typename HV>
-__device__ __forceinline__ double gain_entry(const DevFactor& F, const HV* hval, const HV* hw, int tg) {
-    double acc = 0.0;
+// hw[a] written by the evaluation (FP64: the same product, so the same sum),
+// accumulated in ACC.
+template <typename HV, typename ACC>
+__device__ __forceinline__ ACC gain_entry(const DevFactor& F, const HV* hval, const HV* hw, int tg) {
+    ACC acc = ACC(0);
     const int64_t p1 = F.tgt_pair_ptr[tg + 1];
     for (int64_t p = F.tgt_pair_ptr[tg]; p < p1; ++p) {
         const int a = F.pair_a[p], b = F.pair_b[p];
-        acc += static_cast<double>(hw[a]) * static_cast<double>(hval[b]);
+        acc += static_cast<ACC>(hw[a]) * static_cast<ACC>(hval[b]);
     }
     return acc;
 }
@@ -45,11 +47,11 @@ __device__ __forceinline__ double gain_entry(const DevFactor& F, const HV* hval,
 // All gain entries of the factorisation at once: fully parallel, so the
 // dependent gathers are hidden by occupancy instead of sitting on the
 // elimination tree's critical path.
-template <typename T, typename HV>
+template <typename T, typename HV, typename ACC = double>
 __global__ void k_gain_values(DevFactor F, DevWork W, const HV* hval, const HV* hw, T* gv, int n_tgt) {
     for (int tg = blockIdx.x * blockDim.x + threadIdx.x; tg < n_tgt; tg += gridDim.x * blockDim.x) {
         if (F.tgt_grid && (W.grid_flags[F.tgt_grid[tg]] & FLAG_FROZEN)) continue;
-        gv[tg] = static_cast<T>(gain_entry(F, hval, hw, tg));
+        gv[tg] = static_cast<T>(gain_entry<HV, ACC>(F, hval, hw, tg));
     }
 }
 
@@ -696,25 +698,35 @@ __device__ __forceinline__ int lower_bound_i32(const int* a, int lo, int hi, int
     return lo;
 }
 
+// Assembly of a tiled front, one CTA per (tile column tj, block rb of
+// kAsmRows rows from the tile's first column down): zero the block's lower
+// part, write its G entries, then add the children's update-matrix entries
+// that land in it, child by child (a barrier between children keeps every
+// entry's sum in child order, as in the single-CTA fronts).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_big_assemble(DevFactor F, DevWork W, const T* gv, T* lx, T* ub,
                                                            const int4* work) {
     const int4 wk = work[blockIdx.x];
-    const int s = wk.x, tj = wk.y;
+    const int s = wk.x, tj = wk.y, rb = wk.z;
     if (front_frozen(F, W, s)) return;  // the whole CTA, before any barrier
     const int f = F.sn_f[s];
     T* B = lx + F.sn_lx_off[s];
     const int c0 = tj * kTile, c1 = min(c0 + kTile, f);
+    const int R0 = c0 + rb * kAsmRows, R1 = min(R0 + kAsmRows, f);
     const int tid = threadIdx.x, nth = blockDim.x;
-    for (int x = tid; x < (c1 - c0) * f; x += nth) {
-        const int c = c0 + x / f, r = x % f;
+    for (int x = tid; x < (c1 - c0) * (R1 - R0); x += nth) {
+        const int c = c0 + x / (R1 - R0), r = R0 + x % (R1 - R0);
         if (r >= c) B[r + (int64_t)c * f] = T(0);
     }
     __syncthreads();
     // tgt_local = row + col * f is sorted, so a tile column is a contiguous range
     const int lo = lower_bound_i32(F.tgt_local, F.sn_tgt_ptr[s], F.sn_tgt_ptr[s + 1], c0 * f);
     const int hi = lower_bound_i32(F.tgt_local, lo, F.sn_tgt_ptr[s + 1], c1 * f);
-    for (int tg = lo + tid; tg < hi; tg += nth) B[F.tgt_local[tg]] = gv[tg];
+    for (int tg = lo + tid; tg < hi; tg += nth) {
+        const int l = F.tgt_local[tg];
+        const int r = l % f;
+        if (r >= R0 && r < R1) B[l] = gv[tg];
+    }
     __syncthreads();
     for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) {
         const int c = F.sn_child[ci];
@@ -722,24 +734,26 @@ __global__ void __launch_bounds__(kThreads) k_big_assemble(DevFactor F, DevWork 
         const int* rel = F.sn_relmap + F.sn_su_off[c];
         const int j0 = lower_bound_i32(rel, 0, m, c0);  // rel is increasing
         const int j1 = lower_bound_i32(rel, j0, m, c1);
+        const int ilo = lower_bound_i32(rel, 0, m, R0);  // child rows landing in [R0, R1)
+        const int ihi = lower_bound_i32(rel, ilo, m, R1);
         const T* U = update_of<T>(F, lx, ub, c);
         const int uld = F.sn_u_ld[c];
         const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
         for (int j = j0 + warp; j < j1; j += nwarp) {
             const int64_t pj = (int64_t)rel[j] * f;
             const T* Uj = U + (int64_t)j * uld;
-            for (int i0 = j + lane; i0 < m; i0 += 128) {
+            for (int i0 = max(j, ilo) + lane; i0 < ihi; i0 += 128) {
                 T u[4];
                 int r[4];
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
                     const int i = i0 + 32 * t;
-                    u[t] = (i < m) ? Uj[i] : T(0);
-                    r[t] = (i < m) ? rel[i] : 0;
+                    u[t] = (i < ihi) ? Uj[i] : T(0);
+                    r[t] = (i < ihi) ? rel[i] : 0;
                 }
 #pragma unroll
                 for (int t = 0; t < 4; ++t)
-                    if (i0 + 32 * t < m) B[r[t] + pj] += u[t];
+                    if (i0 + 32 * t < ihi) B[r[t] + pj] += u[t];
             }
         }
         __syncthreads();
@@ -850,6 +864,10 @@ __global__ void __launch_bounds__(kThreads) k_big_panel32(DevFactor F, DevWork W
     const int r0 = p0 + pb + chunk * kPanelRows;    // first row of the chunk
     const int nr = max(0, min(kPanelRows, f - r0));  // its rows
     const int tid = threadIdx.x;
+    // From the second step on, the previous step's trailing update has already
+    // factored and inverted this diagonal block (look-ahead in k_big_update):
+    // its slot holds L_dd^-1, the pivots are checked and rdiag is written.
+    const bool pre = p > 0;
     {
         // all staging loads in flight before the first shared-memory store:
         // thread (j, i) with i = tid % 32 reads column j = tid / 32 + 8 q of
@@ -871,15 +889,15 @@ __global__ void __launch_bounds__(kThreads) k_big_panel32(DevFactor F, DevWork W
 #pragma unroll
         for (int q = 0; q < kQ; ++q) {
             const int j = j0 + q * (kThreads / 32);
-            D[i + j * ld] = dv[q];
-            Lt[j * lt_ld + i] = 0.f;
+            D[i + j * ld] = pre ? 0.f : dv[q];
+            Lt[j * lt_ld + i] = pre ? dv[q] : 0.f;  // Lt[j][i] = L_dd^-1[i][j]
 #pragma unroll
             for (int u = 0; u < kPanelRows / 32; ++u) As[j * as_ld + i + 32 * u] = av[q][u];
         }
     }
     __syncthreads();
-    if (tid == 0) last = (atomicAdd(step_cnt + pair, 1) == nchunk - 1);  // this CTA's tile reads are done
-    if (tid < 32) {
+    if (tid == 0) last = !pre && (atomicAdd(step_cnt + pair, 1) == nchunk - 1);  // this CTA's tile reads are done
+    if (tid < 32 && !pre) {
         const int i = tid;
         float a[kTile];
 #pragma unroll
@@ -1029,6 +1047,46 @@ __global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, DevWork W,
         for (int u = 0; u < 2; ++u) {
             const int gr = R0 + tr + 16 * u;
             if (gr >= gc && gr < f) dst[gr] -= acc[u][v];
+        }
+    }
+    if constexpr (sizeof(T) == 4) {
+        // Look-ahead (FP32 tiled fronts): the tile that is the next step's
+        // diagonal block comes first in the step's work list; after its own
+        // update its CTA factors the block (L_dd) and inverts it in warp 0
+        // while the step's other tiles are still updating, and leaves L_dd^-1
+        // in the block's slot, the pivots' reciprocals in rdiag and the pivot
+        // check done, so that the next panel step only applies L_dd^-1.  The
+        // arithmetic is that of the panel kernel's own factorisation.
+        if (ti == tj && R0 == q0 && q0 < nc) {
+            constexpr int dld = kTile + 1, lt_ld = kTile + 4;
+            __shared__ float D[kTile * dld];
+            __shared__ float rdiag[kTile];
+            __shared__ float Lt[kTile * lt_ld];
+            __syncthreads();  // every update of this tile is written
+            const int pb2 = min(kTile, nc - q0);
+            if (threadIdx.x < 32) {
+                const int i = threadIdx.x;
+                float a[kTile];
+#pragma unroll
+                for (int j = 0; j < kTile; ++j)
+                    a[j] = (i < pb2 && j <= i) ? B[(q0 + i) + (int64_t)(q0 + j) * f] : 0.f;
+                float inv;
+                const bool bad = warp_potrf<float, kTile>(a, pb2, i, &inv);
+                if (bad && i == 0) atomicOr(singular_flags(F, W, s), FLAG_SINGULAR);
+#pragma unroll
+                for (int j = 0; j < kTile; ++j) D[i + j * dld] = (i < pb2 && j <= i) ? a[j] : 0.f;
+                if (i < pb2) {
+                    rdiag[i] = inv;
+                    reinterpret_cast<float*>(W.rdiag)[F.sn_c0[s] + q0 + i] = inv;
+                }
+                __syncwarp();
+                warp_trinv<float, kTile, dld>(reinterpret_cast<const float (*)[dld]>(D), rdiag, pb2, i, Lt, lt_ld);
+                __syncwarp();
+                for (int x = i; x < pb2 * pb2; x += 32) {
+                    const int r = x % pb2, c = x / pb2;
+                    if (r >= c) B[(q0 + r) + (int64_t)(q0 + c) * f] = Lt[c * lt_ld + r];
+                }
+            }
         }
     }
 }
@@ -1539,7 +1597,7 @@ __global__ void __launch_bounds__(kCompactThreads) k_ready_compact(DevFactor F, 
 template <typename HV>
 __global__ void k_gain_export(DevFactor F, const HV* hval, const HV* hw, int n_tgt, double* out) {
     for (int tg = blockIdx.x * blockDim.x + threadIdx.x; tg < n_tgt; tg += gridDim.x * blockDim.x)
-        out[tg] = gain_entry(F, hval, hw, tg);
+        out[tg] = gain_entry<HV, double>(F, hval, hw, tg);
 }
 
 inline int grid_for(int64_t n, int threads) {
@@ -1581,7 +1639,10 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
                         T* lx, T* ub, cudaStream_t st) {
     T* gv = reinterpret_cast<T*>(W.gvals);
     if (ls.n_tgt > 0) {
-        k_gain_values<T, HV><<<grid_for(ls.n_tgt, 256), 256, 0, st>>>(F, W, hval, hw, gv, ls.n_tgt);
+        if (sizeof(T) == 4 && ls.gain_acc32)
+            k_gain_values<T, HV, float><<<grid_for(ls.n_tgt, 256), 256, 0, st>>>(F, W, hval, hw, gv, ls.n_tgt);
+        else
+            k_gain_values<T, HV, double><<<grid_for(ls.n_tgt, 256), 256, 0, st>>>(F, W, hval, hw, gv, ls.n_tgt);
         count_launches(1);
     }
     if (ls.flow_a_n + ls.flow_b_n + ls.flow_w_n > 0) {

@@ -239,6 +239,7 @@ cudaError_t launch_results(const DevNet& net, const DevWork& w, cudaStream_t st)
 struct LevelSchedule {
     int32_t n_levels = 0;
     int32_t n_tgt = 0;                      // gain entries (targets)
+    int32_t gain_acc32 = 0;                 // mixed pipeline: sum the gain entries in FP32 (else FP64)
     const int32_t* h_small_ptr = nullptr;   // [n_levels+1] offsets into d_small
     const int32_t* d_small = nullptr;       // single-CTA fronts, per level
     const int32_t* h_small_maxf = nullptr;  // [n_levels] largest single-CTA front
@@ -372,6 +373,8 @@ cudaError_t launch_factor_solve_noalloc(const DevNet& net, const DevFactor& F, c
 constexpr int kTile = 32;
 // Rows per CTA of the FP32 panel solve of a tiled front.
 constexpr int kPanelRows = 128;
+// Rows per CTA of a tiled front's assembly (one CTA per tile column and row block).
+constexpr int kAsmRows = 128;
 // Edge of the trailing-update tiles of a tiled front (one CTA each; 64 left a
 // single grid's step on too few SMs: grid200k FP64 179 -> 203 ms).
 constexpr int kUpdTile = 32;

@@ -157,7 +157,7 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         for (size_t a = 0; a < hashes.size();) {
             size_t b = a;
             while (b < hashes.size() && hashes[b].first == hashes[a].first) ++b;
-            for (size_t x = a; x < b; ++x) {
+            for (size_t x = a; x + 1 < b; ++x) {  // a variable alone in its hash group has no twin
                 const int32_t i = hashes[x].second;
                 if (status[i] != VAR) continue;
                 si.assign(E[i].begin(), E[i].end());

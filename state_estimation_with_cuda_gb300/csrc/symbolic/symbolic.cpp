@@ -5,6 +5,7 @@
 #include <cstring>
 #include <numeric>
 #include <functional>
+#include <thread>
 
 namespace sle_gb300 {
 
@@ -263,36 +264,49 @@ int64_t trapezoid(int64_t nc, int64_t f) { return nc * f - nc * (nc - 1) / 2; }
 
 void bus_graph(const Topology& t, const std::vector<int32_t>& y_ptr, const std::vector<int32_t>& y_col,
                std::vector<int32_t>& adj_ptr, std::vector<int32_t>& adj) {
-    std::vector<std::pair<int32_t, int32_t>> edges;
-    std::vector<int32_t> buses;
-    for (int32_t q = 0; q < t.n_meas; ++q) {
-        if (t.m_active && !t.m_active[q]) continue;
-        const int32_t ty = t.m_type[q], loc = t.m_loc[q];
+    // Two passes over the active rows: an upper bound of each bus's
+    // neighbour count, then the neighbours themselves; each bus's list is
+    // then sorted and made unique on its own (short lists instead of one
+    // sort of every ordered pair).
+    const int32_t n = t.n_bus;
+    auto row_buses = [&](int32_t q, std::vector<int32_t>& buses) {
         buses.clear();
+        if (t.m_active && !t.m_active[q]) return;
+        const int32_t ty = t.m_type[q], loc = t.m_loc[q];
         if (is_inj_type(ty)) {
             buses.push_back(loc);
             for (int32_t e = y_ptr[loc]; e < y_ptr[loc + 1]; ++e) buses.push_back(y_col[e]);
         } else if (ty == 4 || ty == 5 || ty == 6) {
             buses.push_back(t.br_from[loc]);
             buses.push_back(t.br_to[loc]);
-        } else {
-            continue;
         }
-        std::sort(buses.begin(), buses.end());
-        buses.erase(std::unique(buses.begin(), buses.end()), buses.end());
-        for (size_t a = 0; a < buses.size(); ++a)
-            for (size_t b = a + 1; b < buses.size(); ++b) {
-                edges.emplace_back(buses[a], buses[b]);
-                edges.emplace_back(buses[b], buses[a]);
-            }
+    };
+    std::vector<int64_t> bound(static_cast<size_t>(n) + 1, 0);
+    std::vector<int32_t> buses;
+    for (int32_t q = 0; q < t.n_meas; ++q) {
+        row_buses(q, buses);
+        for (int32_t b : buses) bound[b + 1] += static_cast<int64_t>(buses.size()) - 1;
     }
-    std::sort(edges.begin(), edges.end());
-    edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
-    adj_ptr.assign(t.n_bus + 1, 0);
-    for (auto& e : edges) ++adj_ptr[e.first + 1];
-    for (int32_t i = 0; i < t.n_bus; ++i) adj_ptr[i + 1] += adj_ptr[i];
-    adj.resize(edges.size());
-    for (size_t k = 0; k < edges.size(); ++k) adj[k] = edges[k].second;
+    for (int32_t i = 0; i < n; ++i) bound[i + 1] += bound[i];
+    std::vector<int32_t> tmp(static_cast<size_t>(bound[n]));
+    std::vector<int64_t> fill(bound.begin(), bound.end() - 1);
+    for (int32_t q = 0; q < t.n_meas; ++q) {
+        row_buses(q, buses);
+        for (int32_t a : buses)
+            for (int32_t b : buses)
+                if (b != a) tmp[fill[a]++] = b;
+    }
+    adj_ptr.assign(static_cast<size_t>(n) + 1, 0);
+    adj.clear();
+    adj.reserve(tmp.size());
+    for (int32_t i = 0; i < n; ++i) {
+        int32_t* b0 = tmp.data() + bound[i];
+        int32_t* b1 = tmp.data() + fill[i];
+        std::sort(b0, b1);
+        int32_t* e = std::unique(b0, b1);
+        adj.insert(adj.end(), b0, e);
+        adj_ptr[i + 1] = static_cast<int32_t>(adj.size());
+    }
 }
 
 bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::string& err) {
@@ -686,45 +700,120 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     }
 
     // --- gain assembly targets --------------------------------------------------------
+    // Every pair (x, y), x <= y, of H entries of one row contributes to the G
+    // entry (lo, hi) of the front owning column lo.  Records are collected in
+    // row order per front, stably sorted by the entry's local index, and each
+    // run of equal indices becomes one target with its pair list.  Rows are
+    // cut into chunks and fronts into ranges, one host thread each; chunk
+    // offsets per front keep the row order, so the plan is the same for any
+    // thread count.
     {
         struct PairRec { int32_t local; int32_t a; int32_t b; };
-        std::vector<std::vector<PairRec>> per_sn(ns);
-        for (int32_t q = 0; q < m; ++q) {
-            for (int32_t x = P.h_ptr[q]; x < P.h_ptr[q + 1]; ++x) {
-                const int32_t px = ps_of_state[P.h_col[x]];
-                for (int32_t y = x; y < P.h_ptr[q + 1]; ++y) {
-                    const int32_t py = ps_of_state[P.h_col[y]];
-                    const int32_t lo = std::min(px, py), hi = std::max(px, py);
-                    const int32_t k = sn_of_ps[lo];
-                    const int32_t* rows = P.sn_rows.data() + P.sn_rows_off[k];
-                    const int32_t f = P.sn_f[k];
-                    const int32_t* it = std::lower_bound(rows, rows + f, hi);
-                    if (it == rows + f || *it != hi) { err = "gain entry outside the front structure"; return false; }
-                    const int32_t lr = static_cast<int32_t>(it - rows);
-                    const int32_t lc = lo - P.sn_c0[k];
-                    per_sn[k].push_back({lr + lc * f, x, y});
-                }
+        const int32_t nthr = std::max(1, std::min<int32_t>(static_cast<int32_t>(std::thread::hardware_concurrency()),
+                                                           std::max(1, m / 4096)));
+        auto parallel = [&](int32_t parts, const std::function<void(int32_t)>& fn) {
+            std::vector<std::thread> pool;
+            for (int32_t t = 1; t < parts; ++t) pool.emplace_back(fn, t);
+            fn(0);
+            for (auto& th : pool) th.join();
+        };
+        auto chunk = [&](int32_t t, int32_t total) {
+            return std::make_pair(static_cast<int32_t>((static_cast<int64_t>(total) * t) / nthr),
+                                  static_cast<int32_t>((static_cast<int64_t>(total) * (t + 1)) / nthr));
+        };
+        std::vector<std::vector<int64_t>> cnt(nthr, std::vector<int64_t>(ns + 1, 0));
+        std::vector<uint8_t> bad(nthr, 0);
+        // the front and local index of pair (x, y); false if outside the structure
+        auto locate = [&](int32_t x, int32_t y, int32_t& k, int32_t& local) {
+            const int32_t px = ps_of_state[P.h_col[x]], py = ps_of_state[P.h_col[y]];
+            const int32_t lo = std::min(px, py), hi = std::max(px, py);
+            k = sn_of_ps[lo];
+            const int32_t* rows = P.sn_rows.data() + P.sn_rows_off[k];
+            const int32_t f = P.sn_f[k];
+            const int32_t* it = std::lower_bound(rows, rows + f, hi);
+            if (it == rows + f || *it != hi) return false;
+            local = static_cast<int32_t>(it - rows) + (lo - P.sn_c0[k]) * f;
+            return true;
+        };
+        parallel(nthr, [&](int32_t t) {
+            const auto r = chunk(t, m);
+            auto& c = cnt[t];
+            for (int32_t q = r.first; q < r.second; ++q)
+                for (int32_t x = P.h_ptr[q]; x < P.h_ptr[q + 1]; ++x)
+                    for (int32_t y = x; y < P.h_ptr[q + 1]; ++y) {
+                        int32_t k, local;
+                        if (!locate(x, y, k, local)) {
+                            bad[t] = 1;
+                            return;
+                        }
+                        ++c[k];
+                    }
+        });
+        for (uint8_t b : bad)
+            if (b) {
+                err = "gain entry outside the front structure";
+                return false;
             }
-        }
-        P.sn_tgt_ptr.assign(ns + 1, 0);
-        P.tgt_pair_ptr.assign(1, 0);
+        // offsets: front-major, chunk-minor
+        std::vector<int64_t> sn_rec(ns + 1, 0);
+        std::vector<std::vector<int64_t>> off(nthr, std::vector<int64_t>(ns, 0));
+        int64_t run = 0;
         for (int32_t k = 0; k < ns; ++k) {
-            auto& v = per_sn[k];
-            std::stable_sort(v.begin(), v.end(), [](const PairRec& u, const PairRec& w) { return u.local < w.local; });
-            for (size_t i = 0; i < v.size();) {
-                size_t j = i;
-                while (j < v.size() && v[j].local == v[i].local) {
-                    P.pair_a.push_back(v[j].a);
-                    P.pair_b.push_back(v[j].b);
-                    ++j;
-                }
-                P.tgt_local.push_back(v[i].local);
-                P.tgt_pair_ptr.push_back(static_cast<int64_t>(P.pair_a.size()));
-                i = j;
+            sn_rec[k] = run;
+            for (int32_t t = 0; t < nthr; ++t) {
+                off[t][k] = run;
+                run += cnt[t][k];
             }
-            P.sn_tgt_ptr[k + 1] = static_cast<int32_t>(P.tgt_local.size());
-            std::vector<PairRec>().swap(v);
         }
+        sn_rec[ns] = run;
+        std::vector<PairRec> rec(static_cast<size_t>(run));
+        parallel(nthr, [&](int32_t t) {
+            const auto r = chunk(t, m);
+            auto& o = off[t];
+            for (int32_t q = r.first; q < r.second; ++q)
+                for (int32_t x = P.h_ptr[q]; x < P.h_ptr[q + 1]; ++x)
+                    for (int32_t y = x; y < P.h_ptr[q + 1]; ++y) {
+                        int32_t k, local;
+                        locate(x, y, k, local);
+                        rec[o[k]++] = {local, x, y};
+                    }
+        });
+        // per front: stable sort by local index, count the targets
+        std::vector<int32_t> ntg(ns + 1, 0);
+        parallel(nthr, [&](int32_t t) {
+            const auto r = chunk(t, ns);
+            for (int32_t k = r.first; k < r.second; ++k) {
+                PairRec* b = rec.data() + sn_rec[k];
+                PairRec* e = rec.data() + sn_rec[k + 1];
+                std::stable_sort(b, e, [](const PairRec& u, const PairRec& w) { return u.local < w.local; });
+                int32_t c = 0;
+                for (PairRec* it = b; it < e; ++it) c += (it == b || it->local != (it - 1)->local) ? 1 : 0;
+                ntg[k] = c;
+            }
+        });
+        P.sn_tgt_ptr.assign(ns + 1, 0);
+        for (int32_t k = 0; k < ns; ++k) P.sn_tgt_ptr[k + 1] = P.sn_tgt_ptr[k] + ntg[k];
+        const int32_t n_tgt = P.sn_tgt_ptr[ns];
+        P.tgt_local.assign(n_tgt, 0);
+        P.tgt_pair_ptr.assign(static_cast<size_t>(n_tgt) + 1, 0);
+        P.pair_a.assign(static_cast<size_t>(run), 0);
+        P.pair_b.assign(static_cast<size_t>(run), 0);
+        P.tgt_pair_ptr[n_tgt] = run;
+        parallel(nthr, [&](int32_t t) {
+            const auto r = chunk(t, ns);
+            for (int32_t k = r.first; k < r.second; ++k) {
+                int32_t tg = P.sn_tgt_ptr[k];
+                for (int64_t i = sn_rec[k]; i < sn_rec[k + 1]; ++i) {
+                    if (i == sn_rec[k] || rec[i].local != rec[i - 1].local) {
+                        P.tgt_local[tg] = rec[i].local;
+                        P.tgt_pair_ptr[tg] = i;
+                        ++tg;
+                    }
+                    P.pair_a[i] = rec[i].a;
+                    P.pair_b[i] = rec[i].b;
+                }
+            }
+        });
     }
 
     // --- RHS gather ------------------------------------------------------------------------

@@ -43,7 +43,7 @@ def switched_branches(g, count):
     out = []
     for d in range(5000):
         k = int(g._lib.segen_pick_nonbridge(g._h, d))
-        if k < 0 or k in out or k in metered:  # (the picker already skips metered branches)
+        if k < 0 or k in out or k in metered:
             continue
         trial = copy_grid(g)
         trial.br_status[out + [k]] = 0
