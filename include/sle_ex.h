@@ -56,8 +56,8 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
  *                           re-uploads)
  *   "warp_fronts"           fronts whose whole subtree is at most 32 wide are
  *                           factorised and solved one per warp: 1 on, 0 off,
- *                           -1 (default) for each grid with at least 4096 of
- *                           them (re-uploads)
+ *                           -1 (default) for each grid that has such fronts
+ *                           (re-uploads)
  *   "spin_limit"            polls (about 64 ns each) after which a dataflow
  *                           wait of the solves gives up; the call then fails
  *                           with SLE_ERROR_CUDA_FAILURE and the message
@@ -74,6 +74,12 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
  *                           reweighting creeps when gross errors sit on
  *                           critical measurement pairs, whose Huber objective
  *                           is nearly flat along the states they alone fix
+ *   "device_loop"           batch solves: 1 (default) runs the Gauss-Newton
+ *                           loop on the device, as a CUDA graph whose
+ *                           conditional while node repeats one step while
+ *                           grids are still iterating (one host wait per
+ *                           solve); 0: the host decides after every step.
+ *                           Needs use_cuda_graphs and enable_profiling = 0
  *   "hold_front"            failure-path test hook: the backward sweep never
  *                           publishes this front's completion, so the waits
  *                           of its children run out (-1, the default: none) */
@@ -177,6 +183,8 @@ typedef struct SLE_ExStats {
     int64_t analyses;       /* symbolic analyses of this handle */
     int64_t uploads;        /* device arenas built for this handle */
     int64_t branch_edits;   /* breaker / branch-parameter edits applied on the device */
+    int64_t step_waits;     /* Gauss-Newton steps after which the host waited for the device before
+                               issuing the next (none in a batch solve whose loop runs on the device) */
 } SLE_ExStats;
 
 SLE_API SLE_StatusCode SLE_CALL sle_ExGetStats(SLE_Handle handle, SLE_ExStats* stats);

@@ -236,6 +236,9 @@ class Estimator:
         self._check(self.lib.sle_ExGetStats(self.h, ctypes.byref(st)))
         return st
 
+    def reset_stats(self):
+        self._check(self.lib.sle_ExResetStats(self.h))
+
     # -- stage-level access (sle_ex.h) ------------------------------------------------------
     def schedule_info(self):
         """Kernel schedule of the current model and options (host-only before

@@ -1188,6 +1188,8 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* k
     } else if (k == "huber_stall") {
         if (!(value >= 0.0 && value < 1.0)) return fail(SLE_ERROR_INVALID_ARGUMENT, "huber_stall must be in [0, 1)");
         c.huber_stall = value;
+    } else if (k == "device_loop") {
+        c.device_loop = value != 0.0 ? 1 : 0;
     } else if (k == "spin_limit" || k == "hold_front") {
         if (k == "spin_limit") {
             if (!(value >= 1.0 && value <= 9.0e15)) return fail(SLE_ERROR_INVALID_ARGUMENT, "spin_limit must be >= 1");
@@ -1383,6 +1385,7 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExGetStats(SLE_Handle handle, SLE_ExStats* s
     st->analyses = s.analyses;
     st->uploads = s.uploads;
     st->branch_edits = s.branch_edits;
+    st->step_waits = s.step_waits;
     return SLE_OK;
 }
 

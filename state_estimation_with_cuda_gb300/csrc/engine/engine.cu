@@ -529,6 +529,7 @@ int32_t Engine::upload() {
             batch_.flat = af + G;
             batch_.retire = af + 2 * static_cast<size_t>(G);
             batch_.running = c.take<int32_t>(1);
+            batch_.loop = c.take<int32_t>(4);
             // items of kBatchChunk buses / rows, a grid's items adjacent
             auto items = [&](bool rows, std::vector<int2>& it, std::vector<int32_t>& ptr) {
                 it.clear();
@@ -735,7 +736,9 @@ int32_t Engine::upload() {
         chk(put(const_cast<int32_t*>(batch_.bus_item_ptr), bus_item_ptr_, st_));
         chk(put(const_cast<int2*>(batch_.row_items), row_items_, st_));
         chk(put(const_cast<int32_t*>(batch_.row_item_ptr), row_item_ptr_, st_));
-        const size_t out_bytes = static_cast<size_t>(G) * (4 + 4 + 8 + 8) + 8;
+        // flags, iterations, mismatch, objective per grid; running count (+4
+        // spare); the device loop's four words
+        const size_t out_bytes = static_cast<size_t>(G) * (4 + 4 + 8 + 8) + 8 + 16;
         if (h_batch_cap_ < static_cast<size_t>(G)) {
             if (h_batch_in_) cudaFreeHost(h_batch_in_);
             if (h_batch_out_) cudaFreeHost(h_batch_out_);
@@ -971,7 +974,7 @@ void Engine::collect_stage_times() {
     ev_used_ = 0;
 }
 
-int32_t Engine::enqueue_iteration(const SolveParams& sp, bool refactor, int64_t* per_stage) {
+int32_t Engine::enqueue_iteration(const SolveParams& sp, bool refactor, int64_t* per_stage, bool host_copies) {
     cudaError_t e = cudaMemsetAsync(&work_.status->flags, 0, sizeof(uint32_t), st_);
     if (e == cudaSuccess && batch_mode()) e = cudaMemsetAsync(batch_.running, 0, sizeof(int32_t), st_);
     auto update = [&](const double* step) {
@@ -1009,8 +1012,9 @@ int32_t Engine::enqueue_iteration(const SolveParams& sp, bool refactor, int64_t*
         });
         stage(ST_UPDATE, [&] { return update(work_.dx); });
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h_status_, work_.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st_);
-    if (e == cudaSuccess && batch_mode()) {
+    if (e == cudaSuccess && host_copies)
+        e = cudaMemcpyAsync(h_status_, work_.status, sizeof(DevStatus), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess && host_copies && batch_mode()) {
         const int32_t G = batch_.n_grids;
         int32_t* h_running = reinterpret_cast<int32_t*>(static_cast<char*>(h_batch_out_) + static_cast<size_t>(G) * 24);
         e = cudaMemcpyAsync(h_running, batch_.running, sizeof(int32_t), cudaMemcpyDeviceToHost, st_);
@@ -1033,6 +1037,78 @@ void Engine::drop_graphs() {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g = IterGraph();
     }
+    if (loop_graph_.exec) cudaGraphExecDestroy(loop_graph_.exec);
+    loop_graph_ = IterGraph();
+}
+
+int32_t Engine::run_device_loop(const SolveParams& sp, int32_t max_iter, int32_t& steps) {
+    steps = 0;
+    if (!cfg.device_loop || !cfg.use_cuda_graphs || cfg.enable_profiling) return -1;
+    IterGraph& g = loop_graph_;
+    if (!g.exec || std::memcmp(&g.sp, &sp, sizeof(sp)) != 0) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = IterGraph();
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaGraphCreate(&graph, 0);
+        if (e != cudaSuccess) return set_cuda_error(e, "loop graph");
+        cudaGraphConditionalHandle h{};
+        // the node's condition starts at 1 on every launch: the first step
+        // always runs (max_iter >= 1)
+        e = cudaGraphConditionalHandleCreate(&h, graph, 1u, cudaGraphCondAssignDefault);
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node = nullptr;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
+        int32_t rc = 0;
+        const int64_t before = t_kernel_launches;
+        if (e == cudaSuccess) {
+            cudaGraph_t body = np.conditional.phGraph_out[0];
+            e = cudaStreamBeginCaptureToGraph(st_, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                rc = enqueue_iteration(sp, true, g.launches, false);
+                cudaError_t ek = rc == 0 ? launch_gn_loop_next(h, batch_, work_, st_) : cudaSuccess;
+                g.launches[ST_OTHER] += 1;
+                e = cudaStreamEndCapture(st_, &body);
+                if (e == cudaSuccess) e = ek;
+            }
+        }
+        g.total = t_kernel_launches - before;
+        g_kernel_launches -= g.total;  // counted per step run
+        t_kernel_launches -= g.total;
+        if (e == cudaSuccess && rc == 0) e = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (rc) {
+            g = IterGraph();
+            return rc;
+        }
+        if (e != cudaSuccess) {
+            g = IterGraph();
+            return set_cuda_error(e, "loop graph");
+        }
+        g.sp = sp;
+    }
+    cudaError_t e = launch_gn_loop_init(batch_, max_iter, st_);
+    if (e == cudaSuccess) e = cudaGraphLaunch(g.exec, st_);
+    int32_t* h_loop = reinterpret_cast<int32_t*>(static_cast<char*>(h_batch_out_) + static_cast<size_t>(batch_.n_grids) * 24 + 8);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_loop, batch_.loop, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, st_);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return set_cuda_error(e, "device loop");
+    steps = h_loop[0];
+    g_kernel_launches += g.total * steps;
+    t_kernel_launches += g.total * steps;
+    for (int i = 0; i < ST_COUNT; ++i) {
+        stats.launches[i] += g.launches[i] * steps;
+        if (i != ST_OTHER) stats.calls[i] += steps;
+    }
+    stats.iterations += steps;
+    if (h_loop[2]) {
+        last_error = "factorisation dataflow wait timed out";
+        return -3;
+    }
+    return 0;
 }
 
 int32_t Engine::run_iteration(const SolveParams& sp, bool refactor) {
@@ -1080,6 +1156,7 @@ int32_t Engine::run_iteration(const SolveParams& sp, bool refactor) {
     }
     cudaError_t e = cudaStreamSynchronize(st_);
     ++stats.iterations;
+    ++stats.step_waits;
     if (e != cudaSuccess) {
         set_cuda_error(e, "iteration");
         return -3;
@@ -1707,7 +1784,10 @@ int32_t Engine::batch_solve(int32_t n, const int32_t* ids, const uint8_t* flat, 
     double* h_mis = reinterpret_cast<double*>(ob + 8 * static_cast<size_t>(G));
     double* h_obj = reinterpret_cast<double*>(ob + 16 * static_cast<size_t>(G));
     int32_t* h_running = reinterpret_cast<int32_t*>(ob + 24 * static_cast<size_t>(G));
-    for (int32_t it = 0; it < rq.max_iterations; ++it) {
+    int32_t steps = 0;
+    const int32_t lrc = rq.max_iterations > 0 ? run_device_loop(sp, rq.max_iterations, steps) : 0;
+    if (lrc != 0 && lrc != -1) return -3;
+    for (int32_t it = 0; lrc == -1 && it < rq.max_iterations; ++it) {
         if (run_iteration(sp, true) != 0) return -3;
         if (h_status_->flags & FLAG_TIMEOUT) {
             last_error = "factorisation dataflow wait timed out";

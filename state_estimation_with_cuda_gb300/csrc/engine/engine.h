@@ -52,6 +52,8 @@ struct EngineConfig {
     double huber_stall = 0.0;        // robust solves: also stop when the Huber objective falls by no more
                                      // than this fraction in an iteration (0: the reference's test only)
     int32_t hold_front = -1;         // test hook: front whose backward-sweep completion is withheld
+    int32_t device_loop = 1;         // batch solves: Gauss-Newton loop in a conditional graph node (needs
+                                     // use_cuda_graphs and no profiling); 0: one host round trip per step
 };
 
 // Makes `dev` the calling thread's current device for the lifetime of the
@@ -107,6 +109,9 @@ struct StageStats {
     int64_t calls[ST_COUNT] = {0, 0, 0, 0, 0, 0};
     int64_t iterations = 0, solves = 0;
     int64_t analyses = 0, uploads = 0, branch_edits = 0;
+    // Gauss-Newton steps after which the host waited for the device before
+    // issuing the next (none inside a batch solve whose loop runs on the device)
+    int64_t step_waits = 0;
 };
 
 class Engine {
@@ -321,8 +326,16 @@ private:
         int64_t total = 0;
     };
     IterGraph graphs_[2];
+    // Batch solve's whole Gauss-Newton loop: a conditional while node whose
+    // body is one step (with refactorisation) and the loop-control kernel.
+    IterGraph loop_graph_;
     void drop_graphs();
-    int32_t enqueue_iteration(const SolveParams& sp, bool refactor, int64_t* per_stage);
+    // host_copies: end the step with the status and running-count copies the
+    // host loop reads (left out of the device loop's body).
+    int32_t enqueue_iteration(const SolveParams& sp, bool refactor, int64_t* per_stage, bool host_copies = true);
+    // Runs up to max_iter steps of a batch solve on the device; `steps` gets
+    // the number run.  -1: the graph path is off (use the host loop).
+    int32_t run_device_loop(const SolveParams& sp, int32_t max_iter, int32_t& steps);
     SolveResult last_{};
     double* d_slots_ = nullptr;
     int32_t n_slots_ = 0;

@@ -176,6 +176,9 @@ struct DevBatch {
     const uint8_t* active;    // [n_grids] 1 = solve this grid
     const uint8_t* flat;      // [n_grids] 1 = flat start first
     int32_t* running;         // [1] grids still iterating after this step
+    // [4] Gauss-Newton loop run on the device by a graph's conditional while
+    // node: [0] steps run, [1] step limit, [2] 1 = a dataflow wait timed out
+    int32_t* loop;
     const uint8_t* retire;    // [n_grids] 1 = leave the running batch (stream mode)
     // Per-grid reductions spread over many CTAs: a grid's buses (rows) are cut
     // into items of kBatchChunk consecutive entries, items of a grid adjacent;
@@ -335,6 +338,12 @@ cudaError_t launch_islands(const DevNet& net, int32_t* parent, int32_t* out, int
 // others as they are; retire the grids with retire[g] = 1 (frozen, inactive).
 cudaError_t launch_batch_activate(const DevNet& net, const DevWork& w, const DevBatch& b, cudaStream_t st);
 cudaError_t launch_batch_retire(const DevBatch& b, cudaStream_t st);
+// Device Gauss-Newton loop of a batch solve: the host captures one step and
+// launch_gn_loop_next into the body of a conditional while node; the node
+// repeats the body while grids are running, no wait has timed out and fewer
+// than `limit` steps have run (launch_gn_loop_init, before each launch).
+cudaError_t launch_gn_loop_init(const DevBatch& b, int32_t limit, cudaStream_t st);
+cudaError_t launch_gn_loop_next(cudaGraphConditionalHandle h, const DevBatch& b, const DevWork& w, cudaStream_t st);
 
 // Largest front the high-occupancy dataflow phase may hold (its kernel keeps
 // 16-column panels and a register budget for several CTAs per SM).
@@ -342,11 +351,15 @@ constexpr int32_t kFlowSmallFMax = 128;
 // Panel width of the high-occupancy phase's fronts (all others use 32).
 constexpr int32_t kPanelFlowA = 16;
 // Fronts whose whole subtree is at most this wide are factorised and solved
-// one front per warp (the warp phase, dataflow phase id 3).  The phase adds a
-// phase boundary to the factorisation and to each sweep, so by default a
-// grid uses it when it has at least kWarpPhaseMinFronts such fronts.
+// one front per warp (the warp phase, dataflow phase id 3).  By default a grid
+// uses it as soon as it has kWarpPhaseMinFronts such fronts.  The phase adds
+// a boundary to the factorisation and to each sweep, which a lone mid-size
+// grid pays for (grid10k hot starts about 6 % slower), but a batch pays once
+// for all its grids, and there the warp fronts' 8-fronts-a-CTA occupancy
+// wins: on the 512-grid batch's loaded pass the factorisation falls from
+// 3.78 to 1.62 ms and the solves from 1.97 to 0.69 ms.
 constexpr int32_t kWarpFrontMax = 32;
-constexpr int32_t kWarpPhaseMinFronts = 4096;
+constexpr int32_t kWarpPhaseMinFronts = 1;
 
 // Resident-CTA grid sizes of the persistent dataflow kernels (0 = cannot run).
 struct FlowGrids {

@@ -749,6 +749,21 @@ __global__ void k_batch_mark_final(DevBatch b) {
     if (g < b.n_grids && b.retire[g]) b.flags[g] |= FLAG_FINAL;
 }
 
+__global__ void k_gn_loop_init(DevBatch b, int32_t limit) {
+    b.loop[0] = 0;
+    b.loop[1] = limit;
+    b.loop[2] = 0;
+}
+
+// One thread, after the step's last kernel: the step's flags and the running
+// count are final.  Same decision as the host loop of Engine::batch_solve.
+__global__ void k_gn_loop_next(cudaGraphConditionalHandle h, DevBatch b, const DevStatus* st) {
+    const int32_t steps = b.loop[0] + 1;
+    b.loop[0] = steps;
+    const bool timed_out = (st->flags & FLAG_TIMEOUT) != 0u;
+    if (timed_out) b.loop[2] = 1;
+    cudaGraphSetConditional(h, (!timed_out && *b.running > 0 && steps < b.loop[1]) ? 1u : 0u);
+}
 
 inline int nblocks(int n) { return (n + kBlock - 1) / kBlock; }
 
@@ -813,6 +828,18 @@ cudaError_t launch_batch_activate(const DevNet& net, const DevWork& w, const Dev
 cudaError_t launch_batch_retire(const DevBatch& b, cudaStream_t st) {
     if (b.n_grids <= 0) return cudaSuccess;
     k_batch_retire<<<(b.n_grids + kBlock - 1) / kBlock, kBlock, 0, st>>>(b);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gn_loop_init(const DevBatch& b, int32_t limit, cudaStream_t st) {
+    k_gn_loop_init<<<1, 1, 0, st>>>(b, limit);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gn_loop_next(cudaGraphConditionalHandle h, const DevBatch& b, const DevWork& w, cudaStream_t st) {
+    k_gn_loop_next<<<1, 1, 0, st>>>(h, b, w.status);
     count_launches(1);
     return cudaGetLastError();
 }

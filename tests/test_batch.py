@@ -2,14 +2,16 @@
 
 Each grid's result must equal solving it alone (same iteration count; states
 within 1e-12, same arithmetic in both), and the FP64 batch must match the
-oracle (states within 1e-8, same iteration counts).
+oracle (states within 1e-8, same iteration counts).  The Gauss-Newton loop
+runs on the device (a CUDA graph's conditional while node) and gives the same
+bits as the host loop it replaces.
 """
 import numpy as np
 import pytest
 
 from conftest import gpu_available
 from oracle.binding import Oracle
-from state_estimation_with_cuda_gb300 import BatchEstimator, Estimator
+from state_estimation_with_cuda_gb300 import BatchEstimator, Estimator, SLEError
 from state_estimation_with_cuda_gb300.workloads import SyntheticGrid, batch_sizes, grid_seed
 
 pytestmark = pytest.mark.gpu
@@ -122,4 +124,72 @@ def test_breaker_edit_changes_values_only():
     bv, bth = b.state(gid)
     assert res[0].status == st == 0 and res[0].iterations == its
     assert max(np.abs(bv - v).max(), np.abs(bth - th).max()) < 1e-9
+    b.close()
+
+
+# ------------------------------------------- Gauss-Newton loop on the device
+def run_batch(grids, mixed, device_loop, max_iterations=20, hot=None):
+    b = BatchEstimator(mixed=mixed)
+    b.set_option("device_loop", device_loop)
+    for g in grids:
+        b.add_grid(g)
+    b.solve(flat_start=True, max_iterations=max_iterations)
+    if hot is not None:
+        for i, z in hot.items():
+            b.set_telemetry(i, z)
+    b.reset_stats()
+    res = b.solve(flat_start=hot is None, max_iterations=max_iterations)
+    st = b.stats()
+    out = ([(r.status, r.iterations, r.max_mismatch, r.objective) for r in res],
+           [np.concatenate(b.state(i)) for i in range(len(grids))], st.iterations, st.step_waits)
+    b.close()
+    return out
+
+
+@pytest.mark.parametrize("mixed", [True, False])
+def test_device_loop_equals_host_loop(mixed):
+    """The conditional-node loop runs the same steps as the host loop and
+    stops on the same test: identical per-grid results, bit for bit, with no
+    host wait between steps."""
+    grids = small_batch(12, hi=1200)
+    hot = {i: grids[i].renoise(0).copy() for i in (0, 3, 5, 8)}
+    for kw in ({}, {"hot": hot}, {"max_iterations": 2}):
+        r_dev, s_dev, it_dev, w_dev = run_batch(grids, mixed, 1, **kw)
+        r_host, s_host, it_host, w_host = run_batch(grids, mixed, 0, **kw)
+        assert r_dev == r_host, kw
+        assert all(np.array_equal(a, b) for a, b in zip(s_dev, s_host)), kw
+        assert it_dev == it_host == max(r[1] for r in r_dev)
+        assert w_dev == 0 and w_host == it_host
+    # the step limit holds: every grid stops after two steps, none converged
+    r2 = run_batch(grids, mixed, 1, max_iterations=2)[0]
+    assert all(r[0] == 1 and r[1] == 2 for r in r2)
+
+
+def test_device_loop_stops_on_a_timed_out_wait():
+    """A dataflow wait that runs out inside the device loop ends the loop
+    after that step and the solve reports it; the handle then solves again."""
+    grids = small_batch(6, hi=1500)
+    b = BatchEstimator(mixed=True)
+    for g in grids:
+        b.add_grid(g)
+    par = b.symbolic()["sn_parent"]
+    roots = np.nonzero(par < 0)[0]
+    nchild = np.bincount(par[par >= 0], minlength=len(par))
+    root = int(roots[np.argmax(nchild[roots])])
+    assert nchild[root] > 0
+    b.set_option("spin_limit", 1000)
+    b.set_option("hold_front", root)
+    b.reset_stats()
+    with pytest.raises(SLEError) as err:
+        b.solve(flat_start=True)
+    assert "timed out" in str(err.value)
+    assert b.stats().iterations == 1 and b.stats().step_waits == 0
+    b.set_option("hold_front", -1)
+    b.set_option("spin_limit", 1 << 22)
+    res = b.solve(flat_start=True)
+    for i, g in enumerate(grids):
+        st, its, v, th = alone(g, True)
+        bv, bth = b.state(i)
+        assert res[i].status == st == 0 and res[i].iterations == its
+        assert max(np.abs(bv - v).max(), np.abs(bth - th).max()) <= SAME
     b.close()

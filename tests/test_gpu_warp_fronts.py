@@ -1,6 +1,6 @@
 """Warp phase: fronts whose whole subtree is at most 32 wide are factorised
-and solved one front per warp.  By default a grid uses it from 4096 such
-fronts on; here it is forced on and off on grids below that threshold.
+and solved one front per warp.  By default every grid with such fronts
+uses it; here it is forced on and off.
 
 * FP64 with the warp phase matches the oracle with the parity tolerances
   (G x = b within 1e-9, same iteration counts, states within 1e-8);

@@ -3,8 +3,9 @@ takes, the per-grid warp-phase decision, and the order of the
 level-synchronous part.  sle_ExGetScheduleInfo builds the schedule on the
 host before the first upload.
 
-* A grid uses the warp phase (one front per warp for subtrees at most 32 wide)
-  from 4096 such fronts on; the option forces it on or off.
+* By default every grid with fronts whose subtree is at most 32 wide runs
+  them in the warp phase (one front per warp); the option forces it on or
+  off.
 * In a batch the decision is per grid: the batch's warp fronts are exactly
   those of its grids that use the phase alone (each grid runs the kernels it
   runs alone).
@@ -17,9 +18,6 @@ import pytest
 
 from state_estimation_with_cuda_gb300 import BatchEstimator, Estimator
 from state_estimation_with_cuda_gb300.workloads import SyntheticGrid, grid_seed
-
-WARP_MIN = 4096
-
 
 def schedule(grids, warp=None, mixed=True):
     if len(grids) == 1:
@@ -53,20 +51,23 @@ def grids():
     return small, big
 
 
-def test_warp_phase_threshold_and_option(grids):
+def test_warp_phase_default_and_option(grids):
     small, big = grids
     s0, sp = schedule([small])
     b0, bp = schedule([big])
     for si, pi in ((s0, sp), (b0, bp)):
         check_partition(si, pi)
-    assert s0.n_warp == 0  # below the threshold
-    assert b0.n_warp >= WARP_MIN
+    # on by default for any grid with warp-able fronts
+    assert s0.n_warp > 0 and s0.warp_ready > 0
+    assert b0.n_warp > s0.n_warp
     s1, _ = schedule([small], warp=1)
+    s_off, _ = schedule([small], warp=0)
     b_off, _ = schedule([big], warp=0)
-    assert s1.n_warp > 0 and s1.warp_ready > 0
+    assert s1.n_warp == s0.n_warp and s1.warp_ready == s0.warp_ready
+    assert s_off.n_warp == 0 and s_off.n_phase_a > s0.n_phase_a
     assert b_off.n_warp == 0 and b_off.n_phase_a > b0.n_phase_a
-    # forcing the phase moves fronts between the dataflow phases only
-    assert s1.n_sync == s0.n_sync and b_off.n_sync == b0.n_sync
+    # switching the phase moves fronts between the dataflow phases only
+    assert s_off.n_sync == s0.n_sync and b_off.n_sync == b0.n_sync
 
 
 def test_batch_decides_the_warp_phase_per_grid(grids):
@@ -78,11 +79,12 @@ def test_batch_decides_the_warp_phase_per_grid(grids):
     assert u.n_warp == b0.n_warp + s0.n_warp
     assert u.n_phase_a == b0.n_phase_a + s0.n_phase_a
     assert u.warp_ready == b0.warp_ready + s0.warp_ready
-    # forced on, the small grid's fronts join too
-    s1, _ = schedule([small], warp=1)
-    b1, _ = schedule([big], warp=1)
-    u1, _ = schedule([small, big], warp=1)
-    assert u1.n_warp == s1.n_warp + b1.n_warp
+    # forced off, no grid's fronts join
+    s_off, _ = schedule([small], warp=0)
+    b_off, _ = schedule([big], warp=0)
+    u_off, _ = schedule([small, big], warp=0)
+    assert u_off.n_warp == 0
+    assert u_off.n_phase_a == s_off.n_phase_a + b_off.n_phase_a
 
 
 def test_synchronous_order_is_the_cheaper_and_aligns_a_batch():
