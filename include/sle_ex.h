@@ -74,6 +74,13 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
  *                           reweighting creeps when gross errors sit on
  *                           critical measurement pairs, whose Huber objective
  *                           is nearly flat along the states they alone fix
+ *   "tile_flow"             mixed pipeline: 1 factorises the tiled fronts
+ *                           of each synchronous level in one persistent
+ *                           dataflow launch (panel chunks and update tiles
+ *                           as items that wait, bounded, for their inputs);
+ *                           0 (default): a panel launch and an update launch
+ *                           per 32-column step.  Same arithmetic, same bits
+ *                           (re-uploads)
  *   "device_loop"           batch solves: 1 (default) runs the Gauss-Newton
  *                           loop on the device, as a CUDA graph whose
  *                           conditional while node repeats one step while
@@ -103,7 +110,8 @@ typedef struct SLE_ExScheduleInfo {
     int32_t warp_ready, a_ready, b_ready;         /* initially ready fronts of the dataflow phases */
     int32_t up_ready, down_n, down_warp_n;        /* forward-sweep leaves; backward-sweep fronts (CTA, warp) */
     int32_t sync_levels, panel_steps;             /* non-empty synchronous levels; tiled-front panel steps */
-    int32_t by_depth, pad;                        /* 1: synchronous levels ordered by depth from the root */
+    int32_t by_depth;                             /* 1: synchronous levels ordered by depth from the root */
+    int32_t tile_tasks;                           /* FP32 tiled-front dataflow items (0: per-step launches) */
     int64_t launches_by_height, launches_by_depth; /* cost of the synchronous part under either order */
 } SLE_ExScheduleInfo;
 

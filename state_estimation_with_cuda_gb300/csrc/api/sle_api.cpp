@@ -1188,6 +1188,9 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* k
     } else if (k == "huber_stall") {
         if (!(value >= 0.0 && value < 1.0)) return fail(SLE_ERROR_INVALID_ARGUMENT, "huber_stall must be in [0, 1)");
         c.huber_stall = value;
+    } else if (k == "tile_flow") {
+        c.tile_flow = value != 0.0 ? 1 : 0;
+        E(handle)->model.structure_dirty = true;  // taken at the next upload
     } else if (k == "device_loop") {
         c.device_loop = value != 0.0 ? 1 : 0;
     } else if (k == "spin_limit" || k == "hold_front") {
@@ -1220,6 +1223,7 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExGetScheduleInfo(SLE_Handle handle, SLE_ExS
     info->sync_levels = si.sync_levels;
     info->panel_steps = si.panel_steps;
     info->by_depth = si.by_depth;
+    info->tile_tasks = si.tile_tasks;
     info->launches_by_height = si.launches_by_height;
     info->launches_by_depth = si.launches_by_depth;
     return SLE_OK;

@@ -144,6 +144,117 @@ int32_t Engine::analyze() {
 // flops than cfg.big_front_flops, or too large for shared memory), lays out
 // the factor storage (big fronts in place in an f x f region) and builds the
 // tile work lists of the big-front kernels.
+// The FP32 tiled fronts of one synchronous level as dataflow items.  Items:
+// P(p, k), the panel solve of chunk k of step p, and U(p, ti, tj), the step-p
+// update of tile (ti, tj).  P(p, k) waits for U(p - 1) of its column-p tiles
+// and of the diagonal tile (whose item also factors the block: look-ahead);
+// U(p, ti, tj) waits for the panel chunks of step p that hold its rows and
+// columns and for its own step p - 1 update.  Claim order: the panel items
+// of step 0, then per step p the update tiles of the next step's panel
+// column (its diagonal tile first), the panel items of step p + 1, and the
+// rest of step p's update tiles (one step of look-ahead).  Every dependency
+// comes earlier in the order, so a waiting CTA only waits for items that
+// running CTAs hold, and a tile's successive updates are a step apart.
+void Engine::build_tile_tasks(const std::vector<int32_t>& bigs,
+                              const std::unordered_map<int64_t, int32_t>& pair_of) {
+    const Plan& P = plan_;
+    struct Front {
+        int32_t s, f, nc, steps, ut;
+        std::vector<int32_t> pid0;  // [steps] first panel item
+        std::vector<int32_t> uid;   // [steps][ut][ut] update items
+    };
+    const int32_t base = static_cast<int32_t>(sch_tt_.size());  // item ids are level-local
+    std::vector<Front> fr;
+    for (int32_t s : bigs) {
+        Front b;
+        b.s = s;
+        b.f = P.sn_f[s];
+        b.nc = P.sn_c0[s + 1] - P.sn_c0[s];
+        b.steps = (b.nc + kTile - 1) / kTile;
+        b.ut = (b.f + kUpdTile - 1) / kUpdTile;
+        b.pid0.assign(b.steps, -1);
+        b.uid.assign(static_cast<size_t>(b.steps) * b.ut * b.ut, -1);
+        fr.push_back(std::move(b));
+    }
+    auto q0_of = [](const Front& b, int32_t p) { return p * kTile + std::min(kTile, b.nc - p * kTile); };
+    auto uid = [](Front& b, int32_t p, int32_t ti, int32_t tj) -> int32_t& {
+        return b.uid[(static_cast<size_t>(p) * b.ut + ti) * b.ut + tj];
+    };
+    std::vector<int32_t> deps;
+    auto add = [&](TileTask t) {
+        const int32_t id = static_cast<int32_t>(sch_tt_.size()) - base;
+        if (deps.size() > static_cast<size_t>(kTileDeps)) tile_tasks_bad_ = true;  // never for 32-row tiles
+        t.ndep = static_cast<int32_t>(std::min<size_t>(deps.size(), kTileDeps));
+        t.pad = 0;
+        for (int32_t i = 0; i < kTileDeps; ++i) t.dep[i] = i < t.ndep ? deps[i] : 0;
+        for (int32_t d : deps)
+            if (d < 0 || d >= id) tile_tasks_bad_ = true;  // never by construction
+        sch_tt_.push_back(t);
+        return id;
+    };
+    auto push_dep = [&](int32_t d) {
+        if (std::find(deps.begin(), deps.end(), d) == deps.end()) deps.push_back(d);
+    };
+    auto emit_panel = [&](Front& b, int32_t p) {
+        const int32_t q0 = q0_of(b, p);
+        const int32_t nch = std::max(1, (b.f - q0 + kPanelRows - 1) / kPanelRows);
+        const auto it = pair_of.find((static_cast<int64_t>(b.s) << 20) | p);
+        const int32_t pair = it == pair_of.end() ? 0 : it->second;
+        for (int32_t k = 0; k < nch; ++k) {
+            deps.clear();
+            if (p > 0) {
+                push_dep(uid(b, p - 1, p, p));
+                const int32_t r0 = q0 + k * kPanelRows, r1 = std::min(r0 + kPanelRows, b.f);
+                for (int32_t ti = r0 / kUpdTile; r0 < r1 && ti <= (r1 - 1) / kUpdTile; ++ti)
+                    push_dep(uid(b, p - 1, ti, p));
+            }
+            TileTask t{};
+            t.kind = 0, t.s = b.s, t.p = p, t.a = k, t.b = nch, t.aux = pair;
+            const int32_t id = add(t);
+            if (k == 0) b.pid0[p] = id;
+        }
+    };
+    // U(p, ti, tj) for every ti >= tj in tile column tj
+    auto emit_update_column = [&](Front& b, int32_t p, int32_t tj) {
+        const int32_t q0 = q0_of(b, p);
+        for (int32_t ti = tj; ti < b.ut; ++ti) {
+            deps.clear();
+            for (int32_t t : {ti, tj}) {
+                const int32_t r0 = std::max(t * kUpdTile, q0), r1 = std::min(t * kUpdTile + kUpdTile, b.f);
+                for (int32_t k = (r0 - q0) / kPanelRows; r0 < r1 && k <= (r1 - 1 - q0) / kPanelRows; ++k)
+                    push_dep(b.pid0[p] + k);
+            }
+            if (p > 0) push_dep(uid(b, p - 1, ti, tj));
+            TileTask t{};
+            t.kind = 1, t.s = b.s, t.p = p, t.a = ti, t.b = tj;
+            uid(b, p, ti, tj) = add(t);
+        }
+    };
+    // step p updates tile columns q0(p) / 32 .. ut - 1; the first is the next
+    // step's panel column (or, for a last step narrower than a tile, its own)
+    auto emit_update = [&](Front& b, int32_t p, bool next_column) {
+        const int32_t q0 = q0_of(b, p);
+        if (q0 >= b.f) return;
+        const int32_t tj0 = q0 / kUpdTile;
+        if (next_column)
+            emit_update_column(b, p, tj0);
+        else
+            for (int32_t tj = tj0 + 1; tj < b.ut; ++tj) emit_update_column(b, p, tj);
+    };
+    int32_t max_steps = 0;
+    for (Front& b : fr) max_steps = std::max(max_steps, b.steps);
+    for (Front& b : fr)
+        if (b.steps > 0) emit_panel(b, 0);
+    for (int32_t p = 0; p < max_steps; ++p) {
+        for (Front& b : fr)
+            if (p < b.steps) emit_update(b, p, true);
+        for (Front& b : fr)
+            if (p + 1 < b.steps) emit_panel(b, p + 1);
+        for (Front& b : fr)
+            if (p < b.steps) emit_update(b, p, false);
+    }
+}
+
 void Engine::build_schedule() {
     const Plan& P = plan_;
     const int32_t ns = P.n_super, nl = P.n_levels;
@@ -165,6 +276,9 @@ void Engine::build_schedule() {
     sch_pan_ptr_.assign(1, 0);
     sch_pan_.clear();
     sch_upd_ptr_.assign(1, 0);
+    sch_tt_.clear();
+    sch_tt_ptr_.assign(nl + 1, 0);
+    tile_tasks_bad_ = false;
     sch_flow_a_.clear();
     sch_flow_w_.clear();
     sch_flow_b_.clear();
@@ -317,6 +431,7 @@ void Engine::build_schedule() {
             }
         }
         int32_t panels = 0;
+        std::unordered_map<int64_t, int32_t> pair_of;  // (front, step) -> step-0 tile-reader counter
         for (int32_t s : bigs) {
             const int32_t f = P.sn_f[s], nc = P.sn_c0[s + 1] - P.sn_c0[s];
             const int32_t tiles = (f + kTile - 1) / kTile;
@@ -339,6 +454,7 @@ void Engine::build_schedule() {
                     // one CTA per kPanelRows rows below the diagonal block
                     const int32_t nch = std::max(1, (f - q0 + kPanelRows - 1) / kPanelRows);
                     for (int32_t k = 0; k < nch; ++k) sch_pot_.push_back(make_int4(s, k, nch, n_pot_pairs_));
+                    pair_of[(static_cast<int64_t>(s) << 20) | p] = n_pot_pairs_;
                     ++n_pot_pairs_;
                 } else {
                     sch_pot_.push_back(make_int4(s, p, 0, 0));
@@ -355,6 +471,8 @@ void Engine::build_schedule() {
             sch_pan_ptr_.push_back(static_cast<int32_t>(sch_pan_.size()));
             sch_upd_ptr_.push_back(static_cast<int32_t>(sch_upd_.size()));
         }
+        if (mixed_ && cfg.tile_flow && !bigs.empty()) build_tile_tasks(bigs, pair_of);
+        sch_tt_ptr_[l + 1] = static_cast<int32_t>(sch_tt_.size());
         sch_small_ptr_[l + 1] = static_cast<int32_t>(sch_small_.size());
         sch_asm_ptr_[l + 1] = static_cast<int32_t>(sch_asm_.size());
     }
@@ -422,6 +540,7 @@ int32_t Engine::schedule_info(ScheduleInfo& out) {
     for (size_t l = 0; l + 1 < sch_small_ptr_.size(); ++l)
         out.sync_levels += (sch_small_ptr_[l + 1] > sch_small_ptr_[l] || sch_asm_ptr_[l + 1] > sch_asm_ptr_[l]) ? 1 : 0;
     for (int32_t p : sch_panels_) out.panel_steps += p;
+    out.tile_tasks = tile_tasks_bad_ ? -1 : static_cast<int32_t>(sch_tt_.size());
     out.by_depth = sync_by_depth_;
     out.launches_by_height = sync_cost_height_;
     out.launches_by_depth = sync_cost_depth_;
@@ -561,6 +680,8 @@ int32_t Engine::upload() {
         d_pot_cnt_ = c.take<int32_t>(std::max(1, n_pot_pairs_));
         d_pan_ = c.take<int4>(sch_pan_.size());
         d_upd_ = c.take<int4>(sch_upd_.size());
+        d_tt_ = c.take<TileTask>(sch_tt_.size());
+        d_tt_done_ = c.take<int32_t>(sch_tt_.size() + static_cast<size_t>(P.n_levels));
         d_flow_a_ = c.take<int32_t>(sch_flow_a_.size());
         d_flow_b_ = c.take<int32_t>(sch_flow_b_.size());
         d_down_ = c.take<int32_t>(sch_down_.size());
@@ -756,6 +877,7 @@ int32_t Engine::upload() {
     chk(put(d_pot_, sch_pot_, st_));
     chk(put(d_pan_, sch_pan_, st_));
     chk(put(d_upd_, sch_upd_, st_));
+    chk(put(d_tt_, sch_tt_, st_));
     chk(put(d_flow_a_, sch_flow_a_, st_));
     chk(put(d_flow_b_, sch_flow_b_, st_));
     chk(put(d_down_, sch_down_, st_));
@@ -819,6 +941,12 @@ int32_t Engine::upload() {
     {
         const int32_t ms = max_solve_front();
         FlowGrids g = flow_grids(mixed_, flow_a_maxf_, flow_b_maxf_, ms);
+        const bool tt = mixed_ && !sch_tt_.empty() && !tile_tasks_bad_ && g.tile > 0;
+        sched_.h_tt_ptr = sch_tt_ptr_.data();
+        sched_.d_tt = d_tt_;
+        sched_.d_tt_done = d_tt_done_;
+        sched_.n_tt = tt ? static_cast<int32_t>(sch_tt_.size()) : 0;
+        sched_.tt_grid = g.tile;
         sched_.d_flow_w = d_flow_w_;
         sched_.flow_w_n = static_cast<int32_t>(sch_flow_w_.size());
         sched_.flow_w_grid = std::max(1, std::min(g.w, sched_.flow_w_n));

@@ -7,6 +7,7 @@
 
 #include <cstdint>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../kernels/kernels.cuh"
@@ -52,6 +53,8 @@ struct EngineConfig {
     double huber_stall = 0.0;        // robust solves: also stop when the Huber objective falls by no more
                                      // than this fraction in an iteration (0: the reference's test only)
     int32_t hold_front = -1;         // test hook: front whose backward-sweep completion is withheld
+    int32_t tile_flow = 0;           // FP32 tiled fronts: 1 = one dataflow launch per level; 0 = a panel and
+                                     // an update launch per step (faster on the measured grids)
     int32_t device_loop = 1;         // batch solves: Gauss-Newton loop in a conditional graph node (needs
                                      // use_cuda_graphs and no profiling); 0: one host round trip per step
 };
@@ -132,7 +135,7 @@ public:
     struct ScheduleInfo {
         int32_t n_warp = 0, n_phase_a = 0, n_phase_b = 0, n_sync = 0;
         int32_t warp_ready = 0, a_ready = 0, b_ready = 0, up_ready = 0, down_n = 0, down_warp_n = 0;
-        int32_t sync_levels = 0, panel_steps = 0, by_depth = 0;
+        int32_t sync_levels = 0, panel_steps = 0, by_depth = 0, tile_tasks = 0;
         int64_t launches_by_height = 0, launches_by_depth = 0;
     };
     int32_t schedule_info(ScheduleInfo& out);
@@ -260,6 +263,9 @@ private:
     std::vector<int32_t> sch_small_ptr_, sch_small_, sch_small_maxf_, sch_asm_ptr_, sch_panels_, sch_step_ptr_,
         sch_pot_ptr_, sch_pan_ptr_, sch_upd_ptr_, sch_all_ptr_, sch_all_, sch_maxf_;
     std::vector<int4> sch_asm_, sch_pot_, sch_pan_, sch_upd_;
+    // FP32 tiled fronts as dataflow items (TileTask), per level
+    std::vector<TileTask> sch_tt_;
+    std::vector<int32_t> sch_tt_ptr_;
     std::vector<int64_t> sch_maxpanel_;
     std::vector<int32_t> sch_flow_a_, sch_flow_b_, sch_down_, sch_up_, sch_flow_w_, sch_down_w_, phase_nchild_, nchild_;
     std::vector<char> flow_phase_;
@@ -287,6 +293,8 @@ private:
     int32_t* d_nchild_ = nullptr;
     int32_t* d_ready_n_ = nullptr;               // [4] claim-list lengths
     int32_t* d_pot_cnt_ = nullptr;               // FP32 tiled fronts: per (front, step) tile readers
+    TileTask* d_tt_ = nullptr;
+    int32_t* d_tt_done_ = nullptr;
     int32_t n_pot_pairs_ = 0;
     int32_t* d_cmp_[kReadyLists] = {};  // batch: compacted claim lists
     int32_t* d_chunk_cnt_ = nullptr;             // batch: compaction scratch
@@ -317,6 +325,8 @@ private:
     int4* d_pan_ = nullptr;
     int4* d_upd_ = nullptr;
     void build_schedule();
+    void build_tile_tasks(const std::vector<int32_t>& bigs, const std::unordered_map<int64_t, int32_t>& pair_of);
+    bool tile_tasks_bad_ = false;  // a dependency not earlier in claim order (never by construction)
     // CUDA graphs of one Gauss-Newton iteration, [0] without and [1] with
     // the refactorisation; re-captured when the solve parameters change.
     struct IterGraph {

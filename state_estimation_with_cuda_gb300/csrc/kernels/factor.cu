@@ -296,6 +296,80 @@ __device__ __forceinline__ void warp_trinv(const T (*lt)[LTLD], const T* rinv, i
     }
 }
 
+// FP32 forms of warp_potrf / warp_trinv for one warp that owns a 16-byte
+// aligned shared buffer, used on the tiled fronts' critical path (the 32 x 32
+// diagonal blocks).  Every entry on or below the diagonal gets the same
+// operations in the same order as in warp_potrf / warp_trinv, so the results
+// are identical; only the data movement differs: pivot column k is written
+// to col[] once and read back four entries per broadcast load instead of by
+// 31 - k shuffles, and the entries above the diagonal are left unmasked (a
+// lane reads col[j] only for j > k, written by lane j, whose value there is
+// an entry of L; the entries above the diagonal are never written out).
+template <int KP>
+__device__ __forceinline__ bool warp_potrf_bcast(float (&a)[KP], int kb, int lane, float* inv_out, float* col) {
+    static_assert(KP % 4 == 0, "whole float4 groups");
+    bool bad = false;
+    float my_inv = 0.f;
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+        if (k < kb) {
+            float d = __shfl_sync(0xffffffffu, a[k], k);
+            bad |= !(d > 0.f) || !isfinite(d);
+            d = (d > 0.f && isfinite(d)) ? d : 1.f;
+            float sq, inv;
+            pivot_value(d, &sq, &inv);
+            const float lk = (lane == k) ? sq : (lane > k ? a[k] * inv : a[k]);
+            a[k] = lk;
+            my_inv = (lane == k) ? inv : my_inv;
+            if (k + 1 < KP) {
+                col[lane] = lk;
+                __syncwarp();
+#pragma unroll
+                for (int g = (k + 1) / 4; g < KP / 4; ++g) {
+                    const float4 v = reinterpret_cast<const float4*>(col)[g];
+                    const float w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        if (4 * g + q > k) a[4 * g + q] = a[4 * g + q] - lk * w[q];
+                }
+                __syncwarp();
+            }
+        }
+    }
+    *inv_out = my_inv;
+    return bad;
+}
+
+// lt rows 16-byte aligned (LTLD % 4 == 0): each row of L is read four
+// entries per broadcast load.
+template <int KP, int LTLD>
+__device__ __forceinline__ void warp_trinv_v4(const float (*lt)[LTLD], const float* rinv, int kb, int lane, float* dst,
+                                              int ld) {
+    static_assert(KP % 4 == 0 && LTLD % 4 == 0, "whole, aligned float4 groups");
+    float x[KP];
+#pragma unroll
+    for (int i = 0; i < KP; ++i) x[i] = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+    for (int c = 0; c < KP; ++c) {
+        if (c < kb) {
+            x[c] *= rinv[c];
+#pragma unroll
+            for (int g = (c + 1) / 4; g < KP / 4; ++g) {
+                const float4 v = reinterpret_cast<const float4*>(lt[c])[g];
+                const float w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (4 * g + q > c) x[4 * g + q] -= x[c] * w[q];
+            }
+        }
+    }
+    if (lane < kb) {
+#pragma unroll
+        for (int i = 0; i < KP; ++i)
+            if (i >= lane && i < kb) dst[i + lane * ld] = x[i];
+    }
+}
+
 constexpr int kWarpsPerCta = kThreads / 32;
 constexpr int kWtLd = kWarpFrontMax + 1;
 
@@ -444,8 +518,9 @@ __device__ void warp_front_factor(const DevFactor& F, const DevWork& W, const T*
 // Shared-memory scratch of one front besides the front itself.
 template <typename T>
 struct FrontSmem {
-    T lt[kPanel][kPanel + 1];  // lt[c][r] = L11[r][c] of the current panel
-    T rinv[kPanel];            // 1 / L11[c][c]
+    __align__(16) T lt[kPanel][kPanel + 4];  // lt[c][r] = L11[r][c] of the current panel (16-byte aligned rows)
+    __align__(16) T col[kPanel];             // FP32: pivot column broadcast of warp_potrf_bcast
+    T rinv[kPanel];                          // 1 / L11[c][c]
 };
 
 // Assembles and partially factorises front s in shared memory (Fm holds
@@ -486,7 +561,11 @@ __device__ void front_factor(const DevFactor& F, const DevWork& W, const T* gv, 
 #pragma unroll
             for (int j = 0; j < KP; ++j) a[j] = (lane < kb && j <= lane) ? Fm[i + (k0 + j) * ldf] : T(0);
             T my_inv;
-            const bool bad = warp_potrf<T, KP>(a, kb, lane, &my_inv);
+            bool bad;
+            if constexpr (sizeof(T) == 4)
+                bad = warp_potrf_bcast<KP>(a, kb, lane, &my_inv, sm.col);
+            else
+                bad = warp_potrf<T, KP>(a, kb, lane, &my_inv);
             if (lane < kb) {
                 sm.rinv[lane] = my_inv;
                 rdg[k0 + lane] = my_inv;
@@ -506,7 +585,8 @@ __device__ void front_factor(const DevFactor& F, const DevWork& W, const T* gv, 
         const int q0 = k0 + kb;
         constexpr int kInvThreads = kInvDiag<T> ? 32 : 0;
         if (kInvDiag<T> && warp == 0) {
-            warp_trinv<T, KP, kPanel + 1>(sm.lt, sm.rinv, kb, lane, Fm + k0 + k0 * ldf, ldf);
+            if constexpr (sizeof(T) == 4)
+                warp_trinv_v4<KP, kPanel + 4>(sm.lt, sm.rinv, kb, lane, Fm + k0 + k0 * ldf, ldf);
         } else {
             const int r = q0 + tid - kInvThreads;
             if (r < f) {
@@ -834,28 +914,36 @@ __global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, 
     }
 }
 
-// FP32 panel step p of the tiled fronts in one launch.  The rows below the
-// diagonal block are cut into chunks of kPanelRows, one CTA each.  Every CTA
+// Loads of front entries in the tiled-front kernels.  kL2: the entry may have
+// been written by another CTA of the same launch (the dataflow kernel), so
+// the load bypasses L1.
+template <bool kL2, typename T>
+__device__ __forceinline__ T ld_entry(const T* p) {
+    if constexpr (kL2) return __ldcg(p);
+    else return *p;
+}
+
+// FP32 panel step p of the tiled fronts.  The rows below the diagonal block
+// are cut into chunks of kPanelRows, one CTA each.  Every CTA
 // factors the 32 x 32 diagonal block itself (warp 0, in registers) and
 // inverts it while the other warps stage the chunk's rows of the panel; then
 // it solves the chunk as X = A L_dd^-T = A (L_dd^-1)^T, a register-tiled
 // product with 4 x 4 outputs per thread.  The CTA that reads the diagonal
 // tile last (a counter per front and step) writes L_dd^-1 into it for the
 // solves: no CTA reads an overwritten tile, and none waits for another.
-__global__ void __launch_bounds__(kThreads) k_big_panel32(DevFactor F, DevWork W, float* lx, const int4* work, int p,
-                                                          int* step_cnt) {
+template <bool kL2>
+__device__ __forceinline__ void big_panel32_item(const DevFactor& F, const DevWork& W, float* lx, int s, int p,
+                                                 int chunk, int nchunk, int pair, int* step_cnt) {
     static_assert(kThreads == 256 && kPanelRows == 128 && kTile == 32, "thread tiling below");
-    constexpr int ld = kTile + 1;
+    constexpr int ld = kTile + 4;          // 16-byte aligned rows
     constexpr int lt_ld = kTile + 4;       // 16-byte aligned rows
     constexpr int as_ld = kPanelRows + 4;  // 16-byte aligned rows
-    __shared__ float D[kTile * ld];        // D[i + j * ld] = L_dd[i][j]
+    __shared__ __align__(16) float D[kTile * ld];  // D[i + j * ld] = L_dd[i][j]
+    __shared__ __align__(16) float colbuf[kTile];
     __shared__ float rdiag[kTile];
     __shared__ __align__(16) float Lt[kTile * lt_ld];  // Lt[k][c] = L_dd^-1[c][k]
     __shared__ __align__(16) float As[kTile * as_ld];  // As[k][r] = A[r0 + r][k], then X
     __shared__ int last;
-    const int4 wk = work[blockIdx.x];
-    const int s = wk.x, chunk = wk.y, nchunk = wk.z, pair = wk.w;
-    if (front_frozen(F, W, s)) return;  // the whole CTA, before any barrier
     const int f = F.sn_f[s];
     const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
     float* B = lx + F.sn_lx_off[s];
@@ -879,11 +967,11 @@ __global__ void __launch_bounds__(kThreads) k_big_panel32(DevFactor F, DevWork W
         for (int q = 0; q < kQ; ++q) {
             const int j = j0 + q * (kThreads / 32);
             const float* col = B + (int64_t)(p0 + j) * f;
-            dv[q] = (j < pb && i < pb && i >= j) ? col[p0 + i] : 0.f;
+            dv[q] = (j < pb && i < pb && i >= j) ? ld_entry<kL2>(col + p0 + i) : 0.f;
 #pragma unroll
             for (int u = 0; u < kPanelRows / 32; ++u) {
                 const int r = i + 32 * u;
-                av[q][u] = (j < pb && r < nr) ? col[r0 + r] : 0.f;
+                av[q][u] = (j < pb && r < nr) ? ld_entry<kL2>(col + r0 + r) : 0.f;
             }
         }
 #pragma unroll
@@ -903,7 +991,7 @@ __global__ void __launch_bounds__(kThreads) k_big_panel32(DevFactor F, DevWork W
 #pragma unroll
         for (int j = 0; j < kTile; ++j) a[j] = (i < pb && j <= i) ? D[i + j * ld] : 0.f;
         float inv;
-        const bool bad = warp_potrf<float, kTile>(a, pb, i, &inv);
+        const bool bad = warp_potrf_bcast<kTile>(a, pb, i, &inv, colbuf);
         if (bad && i == 0 && chunk == 0) atomicOr(singular_flags(F, W, s), FLAG_SINGULAR);
 #pragma unroll
         for (int j = 0; j < kTile; ++j)
@@ -911,7 +999,7 @@ __global__ void __launch_bounds__(kThreads) k_big_panel32(DevFactor F, DevWork W
         if (i < pb) rdiag[i] = inv;
         if (chunk == 0 && i < pb) reinterpret_cast<float*>(W.rdiag)[F.sn_c0[s] + p0 + i] = inv;
         __syncwarp();
-        warp_trinv<float, kTile, ld>(reinterpret_cast<const float (*)[ld]>(D), rdiag, pb, i, Lt, lt_ld);
+        warp_trinv_v4<kTile, ld>(reinterpret_cast<const float (*)[ld]>(D), rdiag, pb, i, Lt, lt_ld);
     }
     __syncthreads();
     {
@@ -944,11 +1032,18 @@ __global__ void __launch_bounds__(kThreads) k_big_panel32(DevFactor F, DevWork W
         if (r < nr && k < pb) B[(r0 + r) + (int64_t)(p0 + k) * f] = As[k * as_ld + r];
     }
     if (last) {
-        for (int x = tid; x < pb * pb; x += kThreads) {
-            const int i = x % pb, j = x / pb;
-            if (i >= j) B[(p0 + i) + (int64_t)(p0 + j) * f] = Lt[j * lt_ld + i];
+        for (int x = tid; x < kTile * kTile; x += kThreads) {
+            const int i = x % kTile, j = x / kTile;
+            if (i < pb && j <= i) B[(p0 + i) + (int64_t)(p0 + j) * f] = Lt[j * lt_ld + i];
         }
     }
+}
+
+__global__ void __launch_bounds__(kThreads) k_big_panel32(DevFactor F, DevWork W, float* lx, const int4* work, int p,
+                                                          int* step_cnt) {
+    const int4 wk = work[blockIdx.x];
+    if (front_frozen(F, W, wk.x)) return;  // the whole CTA, before any barrier
+    big_panel32_item<false>(F, W, lx, wk.x, p, wk.y, wk.z, wk.w, step_cnt);
 }
 
 // FP64 panel step p, part 2: X = A L_dd^-T for the row tiles ti > p, spread
@@ -1004,15 +1099,13 @@ __global__ void __launch_bounds__(32 * kTrsmWarps<T>) k_big_trsm(DevFactor F, De
 // registers, four shared loads per four FMAs (a thread per output needed
 // two per FMA), and its read-modify-writes of a column touch 16 consecutive
 // rows per half warp.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, DevWork W, T* lx, const int4* work, int p) {
+template <typename T, bool kL2>
+__device__ __forceinline__ void big_update_item(const DevFactor& F, const DevWork& W, T* lx, int s, int p, int ti,
+                                                int tj) {
     static_assert(kThreads == 256 && kUpdTile == 32, "thread tiling below");
     constexpr int ld = kUpdTile + 1;
     __shared__ T Ai[kTile * ld];  // Ai[k * ld + r] = A(R0 + r, p0 + k)
     __shared__ T Aj[kTile * ld];
-    const int4 wk = work[blockIdx.x];
-    const int s = wk.x, ti = wk.y, tj = wk.z;
-    if (front_frozen(F, W, s)) return;  // the whole CTA, before any barrier
     const int f = F.sn_f[s];
     const int nc = F.sn_c0[s + 1] - F.sn_c0[s];
     T* B = lx + F.sn_lx_off[s];
@@ -1023,8 +1116,8 @@ __global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, DevWork W,
     for (int x = threadIdx.x; x < kUpdTile * kTile; x += kThreads) {
         const int r = x % kUpdTile, k = x / kUpdTile;
         const T* col = B + (int64_t)(p0 + k) * f;
-        Ai[k * ld + r] = (k < pb && R0 + r < f) ? col[R0 + r] : T(0);
-        Aj[k * ld + r] = (k < pb && C0 + r < f) ? col[C0 + r] : T(0);
+        Ai[k * ld + r] = (k < pb && R0 + r < f) ? ld_entry<kL2>(col + R0 + r) : T(0);
+        Aj[k * ld + r] = (k < pb && C0 + r < f) ? ld_entry<kL2>(col + C0 + r) : T(0);
     }
     __syncthreads();
     const int tr = threadIdx.x & 15, tc = threadIdx.x >> 4;
@@ -1046,7 +1139,7 @@ __global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, DevWork W,
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
             const int gr = R0 + tr + 16 * u;
-            if (gr >= gc && gr < f) dst[gr] -= acc[u][v];
+            if (gr >= gc && gr < f) dst[gr] = ld_entry<kL2>(dst + gr) - acc[u][v];
         }
     }
     if constexpr (sizeof(T) == 4) {
@@ -1058,10 +1151,11 @@ __global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, DevWork W,
         // check done, so that the next panel step only applies L_dd^-1.  The
         // arithmetic is that of the panel kernel's own factorisation.
         if (ti == tj && R0 == q0 && q0 < nc) {
-            constexpr int dld = kTile + 1, lt_ld = kTile + 4;
-            __shared__ float D[kTile * dld];
+            constexpr int dld = kTile + 4, lt_ld = kTile + 4;  // 16-byte aligned rows
+            __shared__ __align__(16) float D[kTile * dld];
             __shared__ float rdiag[kTile];
             __shared__ float Lt[kTile * lt_ld];
+            __shared__ __align__(16) float colbuf[kTile];
             __syncthreads();  // every update of this tile is written
             const int pb2 = min(kTile, nc - q0);
             if (threadIdx.x < 32) {
@@ -1069,9 +1163,9 @@ __global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, DevWork W,
                 float a[kTile];
 #pragma unroll
                 for (int j = 0; j < kTile; ++j)
-                    a[j] = (i < pb2 && j <= i) ? B[(q0 + i) + (int64_t)(q0 + j) * f] : 0.f;
+                    a[j] = (i < pb2 && j <= i) ? ld_entry<kL2>(B + (q0 + i) + (int64_t)(q0 + j) * f) : 0.f;
                 float inv;
-                const bool bad = warp_potrf<float, kTile>(a, pb2, i, &inv);
+                const bool bad = warp_potrf_bcast<kTile>(a, pb2, i, &inv, colbuf);
                 if (bad && i == 0) atomicOr(singular_flags(F, W, s), FLAG_SINGULAR);
 #pragma unroll
                 for (int j = 0; j < kTile; ++j) D[i + j * dld] = (i < pb2 && j <= i) ? a[j] : 0.f;
@@ -1080,14 +1174,105 @@ __global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, DevWork W,
                     reinterpret_cast<float*>(W.rdiag)[F.sn_c0[s] + q0 + i] = inv;
                 }
                 __syncwarp();
-                warp_trinv<float, kTile, dld>(reinterpret_cast<const float (*)[dld]>(D), rdiag, pb2, i, Lt, lt_ld);
+                warp_trinv_v4<kTile, dld>(reinterpret_cast<const float (*)[dld]>(D), rdiag, pb2, i, Lt, lt_ld);
                 __syncwarp();
-                for (int x = i; x < pb2 * pb2; x += 32) {
-                    const int r = x % pb2, c = x / pb2;
-                    if (r >= c) B[(q0 + r) + (int64_t)(q0 + c) * f] = Lt[c * lt_ld + r];
-                }
+                for (int c = 0; c < pb2; ++c)
+                    if (i >= c && i < pb2) B[(q0 + i) + (int64_t)(q0 + c) * f] = Lt[c * lt_ld + i];
             }
         }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_big_update(DevFactor F, DevWork W, T* lx, const int4* work, int p) {
+    const int4 wk = work[blockIdx.x];
+    if (front_frozen(F, W, wk.x)) return;  // the whole CTA, before any barrier
+    big_update_item<T, false>(F, W, lx, wk.x, p, wk.y, wk.z);
+}
+
+// Bounded wait of the tiled-front dataflow (one lane per dependency): true
+// once the flag is set; false when the wait runs out (it then raises
+// FLAG_TIMEOUT) or when another wait of the pass has run out, so that a
+// failed pass ends in about one spin limit instead of one per item.
+__device__ __forceinline__ bool wait_tile(const int* flag, uint32_t* status, long long limit) {
+    long long spins = 0;
+    for (;;) {
+        int v;
+        asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
+        if (v != 0) return true;
+        if (++spins > limit) {
+            atomicOr(status, FLAG_TIMEOUT);
+            return false;
+        }
+        if ((spins & 63) == 0 && (atomicOr(status, 0u) & FLAG_TIMEOUT)) return false;
+        __nanosleep(32);
+    }
+}
+
+// FP32 tiled fronts of one synchronous level in one launch: a persistent grid
+// claims the level's TileTask items in order, waits (bounded) for each
+// item's dependencies and publishes its completion; the items run the same
+// arithmetic as the per-step kernels.  Dependencies are always claimed
+// earlier, so the smallest unfinished item is always running and progress
+// never depends on CTAs that have not started (the grid need not be
+// co-resident; a CTA holds at most the item it runs and the next one it has
+// claimed).  Per item: the next claim and its 64-byte task load are issued
+// while the current item runs, and warp 0 polls the dependencies in
+// parallel, one lane each.  Entries written during the launch are read past
+// L1 (ld_entry<true>).  Items of frozen grids, and every item once a wait has
+// timed out, publish without computing.
+constexpr int kTileFlowBlocks = 3;
+__global__ void __launch_bounds__(kThreads, kTileFlowBlocks)
+    k_big_flow32(DevFactor F, DevWork W, float* lx, const TileTask* tasks, int n, int* done, int* counter,
+                 int* step_cnt) {
+    constexpr int kWords = sizeof(TileTask) / sizeof(int);
+    static_assert(kWords <= 32, "one lane per task word");
+    __shared__ TileTask task[2];
+    __shared__ int next[2];
+    __shared__ int skip;
+    const int tid = threadIdx.x, lane = tid & 31;
+    uint32_t* status = &W.status->flags;
+    int buf = 0;
+    if (tid < 32) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(counter, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (lane == 0) next[0] = item;
+        if (item < n && lane < kWords)
+            reinterpret_cast<int*>(&task[0])[lane] = __ldg(reinterpret_cast<const int*>(tasks + item) + lane);
+    }
+    __syncthreads();
+    for (;;) {
+        const int item = next[buf];
+        if (item >= n) break;
+        // warp 1 claims and loads the next item; warp 0 waits for this one's inputs
+        if (tid >= 32 && tid < 64) {
+            int nx = 0;
+            if (lane == 0) nx = atomicAdd(counter, 1);
+            nx = __shfl_sync(0xffffffffu, nx, 0);
+            if (lane == 0) next[buf ^ 1] = nx;
+            if (nx < n && lane < kWords)
+                reinterpret_cast<int*>(&task[buf ^ 1])[lane] =
+                    __ldg(reinterpret_cast<const int*>(tasks + nx) + lane);
+        }
+        const TileTask& t = task[buf];
+        if (tid < 32) {
+            const bool ok = lane < t.ndep ? wait_tile(done + t.dep[lane], status, W.spin_limit) : true;
+            const bool all = __all_sync(0xffffffffu, ok);
+            if (lane == 0) skip = !all || front_frozen(F, W, t.s) || (atomicOr(status, 0u) & FLAG_TIMEOUT) != 0u;
+            __syncwarp();
+        }
+        __syncthreads();
+        if (!skip) {
+            if (t.kind == 0)
+                big_panel32_item<true>(F, W, lx, t.s, t.p, t.a, t.b, t.aux, step_cnt);
+            else
+                big_update_item<float, true>(F, W, lx, t.s, t.p, t.a, t.b);
+        }
+        __syncthreads();
+        if (tid == 0) publish_done(done + item);
+        __syncwarp();
+        buf ^= 1;
     }
 }
 
@@ -1672,6 +1857,11 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
         cudaError_t e = cudaMemsetAsync(ls.d_pot_cnt, 0, sizeof(int) * (size_t)ls.n_pot_pairs, st);
         if (e != cudaSuccess) return e;
     }
+    const bool tile_flow = sizeof(T) == 4 && ls.n_tt > 0;
+    if (tile_flow) {
+        cudaError_t e = cudaMemsetAsync(ls.d_tt_done, 0, sizeof(int) * (size_t)(ls.n_tt + ls.n_levels), st);
+        if (e != cudaSuccess) return e;
+    }
     for (int l = 0; l < ls.n_levels; ++l) {
         const int ns = ls.h_small_ptr[l + 1] - ls.h_small_ptr[l];
         if (ns > 0) {
@@ -1684,7 +1874,16 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
         if (na > 0) {
             k_big_assemble<T><<<na, kThreads, 0, st>>>(F, W, gv, lx, ub, ls.d_asm + ls.h_asm_ptr[l]);
             count_launches(1);
-            for (int p = 0; p < ls.h_lvl_panels[l]; ++p) {
+            const int nt = tile_flow ? ls.h_tt_ptr[l + 1] - ls.h_tt_ptr[l] : 0;
+            if constexpr (sizeof(T) == 4) {
+                if (nt > 0) {
+                    k_big_flow32<<<std::min(nt, ls.tt_grid), kThreads, 0, st>>>(
+                        F, W, lx, ls.d_tt + ls.h_tt_ptr[l], nt, ls.d_tt_done + ls.h_tt_ptr[l],
+                        ls.d_tt_done + ls.n_tt + l, ls.d_pot_cnt);
+                    count_launches(1);
+                }
+            }
+            for (int p = 0; nt == 0 && p < ls.h_lvl_panels[l]; ++p) {
                 const int slot = ls.h_step_ptr[l] + p;
                 const int npot = ls.h_pot_ptr[slot + 1] - ls.h_pot_ptr[slot];
                 const int nupd = ls.h_upd_ptr[slot + 1] - ls.h_upd_ptr[slot];
@@ -1768,7 +1967,7 @@ cudaError_t solve_impl(const DevFactor& F, const DevWork& W, const LevelSchedule
 
 template <typename T>
 FlowGrids flow_grids_impl(int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf) {
-    FlowGrids g{0, 0, 0, 0, 0};
+    FlowGrids g{0, 0, 0, 0, 0, 0};
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return g;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return g;
@@ -1782,6 +1981,7 @@ FlowGrids flow_grids_impl(int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf) {
     if (solve_maxf <= 16384) g.solve = resident((const void*)k_fwd_flow<T, T>, solve_smem<T>(solve_maxf));
     g.w = resident((const void*)k_front_warp<T>, sizeof(WarpTile<T>) * kWarpsPerCta);
     g.wsolve = std::min(resident((const void*)k_fwd_warp<T, T>, 0), resident((const void*)k_bwd_warp<T, T>, 0));
+    g.tile = sizeof(T) == 4 ? resident((const void*)k_big_flow32, 0) : 0;
     cudaGetLastError();
     return g;
 }

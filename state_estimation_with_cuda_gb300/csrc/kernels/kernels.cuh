@@ -236,6 +236,19 @@ cudaError_t launch_flat_start(const DevNet& net, const DevWork& w, cudaStream_t 
 // Injections and branch flows at the current state (result download).
 cudaError_t launch_results(const DevNet& net, const DevWork& w, cudaStream_t st);
 
+// One work item of the FP32 tiled fronts' dataflow factorisation (one
+// persistent launch per synchronous level).  kind 0: the panel solve of
+// chunk a (of b chunks) of step p, aux = the (front, step) pair of the
+// step-0 tile-reader counter; kind 1: the trailing update of tile (a, b) at
+// step p.  The item waits for the items dep[0, ndep) (level-local indices,
+// all earlier in claim order) to publish their completion.  64 bytes: one
+// load per item.
+constexpr int kTileDeps = 8;
+struct __align__(16) TileTask {
+    int32_t kind, s, p, a, b, aux, ndep, pad;
+    int32_t dep[kTileDeps];
+};
+
 // Level-scheduled multifrontal factorisation and solves.  Host-side copies
 // of the schedule size the launches; device copies are read by kernels.
 // Work-list entries are int4 (front, a, b, 0).
@@ -258,6 +271,12 @@ struct LevelSchedule {
     const int4* d_pan = nullptr;            // (big front, row tile below the panel)
     const int32_t* h_upd_ptr = nullptr;     // [n_slots+1] offsets into d_upd
     const int4* d_upd = nullptr;            // (big front, row tile, column tile)
+    // FP32 tiled fronts as dataflow items, one persistent launch per level
+    // (n_tt = 0: the per-step panel and update launches above)
+    const int32_t* h_tt_ptr = nullptr;      // [n_levels+1] offsets into d_tt
+    const TileTask* d_tt = nullptr;
+    int32_t* d_tt_done = nullptr;           // [n_tt] completion flags, then [n_levels] claim counters
+    int32_t n_tt = 0, tt_grid = 0;
     const int32_t* h_all_ptr = nullptr;     // [n_levels+1] offsets into d_all
     const int32_t* d_all = nullptr;         // every front, per level (solves)
     const int32_t* h_lvl_maxf = nullptr;    // [n_levels] largest front per level
@@ -363,7 +382,7 @@ constexpr int32_t kWarpPhaseMinFronts = 1;
 
 // Resident-CTA grid sizes of the persistent dataflow kernels (0 = cannot run).
 struct FlowGrids {
-    int32_t a, b, solve, w, wsolve;
+    int32_t a, b, solve, w, wsolve, tile;
 };
 FlowGrids flow_grids(bool mixed, int32_t maxf_a, int32_t maxf_b, int32_t solve_maxf);
 

@@ -142,7 +142,7 @@ class SLE_ExPlanInfo(ctypes.Structure):
 class SLE_ExScheduleInfo(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "n_warp", "n_phase_a", "n_phase_b", "n_sync", "warp_ready", "a_ready", "b_ready", "up_ready", "down_n",
-        "down_warp_n", "sync_levels", "panel_steps", "by_depth", "pad")] + [
+        "down_warp_n", "sync_levels", "panel_steps", "by_depth", "tile_tasks")] + [
         ("launches_by_height", ctypes.c_int64), ("launches_by_depth", ctypes.c_int64)]
 
 

@@ -10,6 +10,9 @@ host before the first upload.
   those of its grids that use the phase alone (each grid runs the kernels it
   runs alone).
 * Every front belongs to exactly one phase and one backward sweep.
+* The mixed pipeline's tiled fronts (wider than 224) become dataflow items:
+  per 32-column step, one panel item per 128 rows below the diagonal block
+  and one update item per 32 x 32 tile of the trailing lower triangle.
 * The synchronous levels are ordered by depth or by height, whichever needs
   fewer launches; in a batch, depth lines up the grids' tiled fronts so the
   union needs far fewer panel steps than its grids one after another.
@@ -19,17 +22,19 @@ import pytest
 from state_estimation_with_cuda_gb300 import BatchEstimator, Estimator
 from state_estimation_with_cuda_gb300.workloads import SyntheticGrid, grid_seed
 
-def schedule(grids, warp=None, mixed=True):
+def schedule(grids, warp=None, mixed=True, **options):
     if len(grids) == 1:
         e = Estimator()
         e.set_option("use_double_precision", 0 if mixed else 1)
-        if warp is not None:
-            e.set_option("warp_fronts", warp)
-        e.load_network(grids[0])
     else:
         e = BatchEstimator(mixed=mixed)
-        if warp is not None:
-            e.set_option("warp_fronts", warp)
+    if warp is not None:
+        e.set_option("warp_fronts", warp)
+    for k, v in options.items():
+        e.set_option(k, v)
+    if len(grids) == 1:
+        e.load_network(grids[0])
+    else:
         for g in grids:
             e.add_grid(g)
     si, pi = e.schedule_info(), e.plan_info()
@@ -103,3 +108,38 @@ def test_synchronous_order_is_the_cheaper_and_aligns_a_batch():
     assert u.by_depth == 1
     assert u.panel_steps < a.panel_steps + b.panel_steps
     assert u.panel_steps <= max(a.panel_steps, b.panel_steps) + min(a.panel_steps, b.panel_steps) // 2
+
+
+def expected_tile_tasks(est):
+    """Panel chunks and update tiles of every front wider than 224."""
+    sym = est.symbolic()
+    c0, off = sym["sn_c0"], sym["sn_rows_off"]
+    n = 0
+    for s in range(len(c0) - 1):
+        f, nc = int(off[s + 1] - off[s]), int(c0[s + 1] - c0[s])
+        if f <= 224:
+            continue
+        ut = (f + 31) // 32
+        for p in range((nc + 31) // 32):
+            q0 = 32 * p + min(32, nc - 32 * p)
+            n += max(1, (f - q0 + 127) // 128)
+            if q0 < f:
+                n += sum(ut - tj for tj in range(q0 // 32, ut))
+    return n
+
+
+def test_tiled_fronts_as_dataflow_items(grids):
+    _, big = grids
+    e = Estimator()
+    e.set_option("use_double_precision", 0)
+    e.set_option("tile_flow", 1)
+    e.load_network(big)
+    want = expected_tile_tasks(e)
+    si = e.schedule_info()
+    e.close()
+    assert want > 0 and si.tile_tasks == want  # -1 would mean an out-of-order dependency
+    off, _ = schedule([big])  # the default: per-step launches
+    fp64, _ = schedule([big], mixed=False, tile_flow=1)
+    assert off.tile_tasks == 0 and fp64.tile_tasks == 0
+    # the same fronts, the same steps: only how they are launched changes
+    assert off.panel_steps == si.panel_steps
