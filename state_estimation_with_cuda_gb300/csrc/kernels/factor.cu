@@ -1498,6 +1498,10 @@ __device__ __forceinline__ V warp_sum_v(V v) {
     return v;
 }
 
+// Column entries a lane of the backward CTA sweep loads ahead of their use.
+template <typename T>
+constexpr int kSolveBatch = sizeof(T) == 4 ? 16 : 8;
+
 template <typename T, typename V>
 __device__ void front_bwd(const DevFactor& F, const T* lx, const T* rdiag, const SolveVecs& sv, int s, V* x, T* D) {
     V* sol = reinterpret_cast<V*>(sv.sol);
@@ -1515,9 +1519,21 @@ __device__ void front_bwd(const DevFactor& F, const T* lx, const T* rdiag, const
     const int nblk = (nc + bw - 1) / bw;
     for (int b = nblk - 1; b >= 0; --b) {
         const int k0 = b * bw, kb = min(bw, nc - k0);
+        // t_k = x_k - sum over the rows below of L[r][k] x_r, rows in order;
+        // long columns load kSolveBatch entries per lane ahead of their use
+        // (the same additions, a load latency per batch instead of per entry)
         for (int k = k0 + warp; k < k0 + kb; k += nwarp) {
             V acc = V(0);
-            for (int r = k0 + kb + lane; r < f; r += 32) acc += static_cast<V>(L[r + (int64_t)k * f]) * x[r];
+            const T* Lk = L + (int64_t)k * f;
+            int r = k0 + kb + lane;
+            for (; r + 32 * (kSolveBatch<T> - 1) < f; r += 32 * kSolveBatch<T>) {
+                T l[kSolveBatch<T>];
+#pragma unroll
+                for (int u = 0; u < kSolveBatch<T>; ++u) l[u] = Lk[r + 32 * u];
+#pragma unroll
+                for (int u = 0; u < kSolveBatch<T>; ++u) acc += static_cast<V>(l[u]) * x[r + 32 * u];
+            }
+            for (; r < f; r += 32) acc += static_cast<V>(Lk[r]) * x[r];
             acc = warp_sum_v(acc);
             if (lane == 0) x[k] -= acc;
         }
