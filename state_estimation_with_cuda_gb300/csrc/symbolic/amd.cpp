@@ -6,8 +6,14 @@
 //   min(n - k, d_old + |Lp \ i|, |A_i \ i| + |Lp \ i| + sum_e |Le \ Lp|),
 // indistinguishable variables are merged into supervariables (mass
 // elimination) and elements whose variables are all in the new element are
-// absorbed.  Written with explicit per-node lists rather than AMD's in-place
-// workspace; ties are broken by bucket order, so the result is deterministic.
+// absorbed.  Ties are broken by bucket order, so the result is deterministic.
+//
+// Storage is flat: a variable's remaining neighbours are a shrinking range of
+// one copy of the adjacency; element lists (Le) are ranges of a bump pool,
+// compacted in place; a variable's element list (Ei) is a range of a second
+// pool that moves to the pool's end when it outgrows its capacity; the
+// members of a supervariable are a linked chain.  Every list keeps the order
+// the list-per-node form had, so the ordering is the same.
 #include <algorithm>
 #include <cstdint>
 #include <vector>
@@ -18,13 +24,43 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
     enum : uint8_t { VAR = 0, ELEM = 1, DEAD = 2 };
     std::vector<uint8_t> status(n, VAR);
     std::vector<int32_t> nv(n, 1), deg(n, 0);
-    std::vector<std::vector<int32_t>> A(n), E(n), L(n), members(n);
+    // A: [a_beg, a_beg + a_len) of a_pool (self loops dropped)
+    std::vector<int32_t> a_pool;
+    a_pool.reserve(adj.size());
+    std::vector<int64_t> a_beg(n);
+    std::vector<int32_t> a_len(n);
     for (int32_t i = 0; i < n; ++i) {
-        A[i].assign(adj.begin() + ptr[i], adj.begin() + ptr[i + 1]);
-        A[i].erase(std::remove(A[i].begin(), A[i].end(), i), A[i].end());
-        deg[i] = static_cast<int32_t>(A[i].size());
-        members[i].push_back(i);
+        a_beg[i] = static_cast<int64_t>(a_pool.size());
+        for (int32_t e = ptr[i]; e < ptr[i + 1]; ++e)
+            if (adj[e] != i) a_pool.push_back(adj[e]);
+        a_len[i] = static_cast<int32_t>(a_pool.size() - a_beg[i]);
+        deg[i] = a_len[i];
     }
+    // L (elements): [l_beg, l_beg + l_len) of l_pool
+    std::vector<int32_t> l_pool;
+    l_pool.reserve(adj.size() + static_cast<size_t>(n));
+    std::vector<int64_t> l_beg(n, 0);
+    std::vector<int32_t> l_len(n, 0);
+    // E (variables' elements): [e_beg, e_beg + e_len) of e_pool, capacity e_cap
+    std::vector<int32_t> e_pool;
+    e_pool.reserve(4 * static_cast<size_t>(n));
+    std::vector<int64_t> e_beg(n, 0);
+    std::vector<int32_t> e_len(n, 0), e_cap(n, 0);
+    auto e_push = [&](int32_t i, int32_t v) {
+        if (e_len[i] == e_cap[i]) {
+            const int32_t cap = std::max(4, 2 * e_cap[i]);
+            const int64_t nb = static_cast<int64_t>(e_pool.size());
+            e_pool.resize(e_pool.size() + cap);
+            std::copy(e_pool.begin() + e_beg[i], e_pool.begin() + e_beg[i] + e_len[i], e_pool.begin() + nb);
+            e_beg[i] = nb;
+            e_cap[i] = cap;
+        }
+        e_pool[e_beg[i] + e_len[i]++] = v;
+    };
+    // members of supervariable i: chain from m_head[i] to m_tail[i] through m_next
+    std::vector<int32_t> m_head(n), m_tail(n), m_next(n, -1);
+    for (int32_t i = 0; i < n; ++i) m_head[i] = m_tail[i] = i;
+
     // Degree buckets (doubly linked lists).
     std::vector<int32_t> head(n + 1, -1), nxt(n, -1), prv(n, -1);
     auto bucket_insert = [&](int32_t i) {
@@ -49,6 +85,7 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
     int32_t tag = 0, mindeg = 0, eliminated = 0;
     std::vector<int32_t> Lp;
     std::vector<std::pair<uint64_t, int32_t>> hashes;
+    std::vector<int32_t> si, sj, ai, aj, ai2, aj2;
 
     while (eliminated < n) {
         while (mindeg <= n && head[mindeg] < 0) ++mindeg;
@@ -59,29 +96,31 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         // --- new element Lp -------------------------------------------------------
         Lp.clear();
         flag[p] = tag;
-        for (int32_t e : E[p]) {
+        for (int32_t x = 0; x < e_len[p]; ++x) {
+            const int32_t e = e_pool[e_beg[p] + x];
             if (status[e] != ELEM) continue;
-            for (int32_t i : L[e]) {
+            for (int32_t y = 0; y < l_len[e]; ++y) {
+                const int32_t i = l_pool[l_beg[e] + y];
                 if (status[i] == VAR && flag[i] != tag) {
                     flag[i] = tag;
                     Lp.push_back(i);
                 }
             }
             status[e] = DEAD;  // absorbed into p
-            std::vector<int32_t>().swap(L[e]);
+            l_len[e] = 0;
         }
-        for (int32_t i : A[p]) {
+        for (int32_t x = 0; x < a_len[p]; ++x) {
+            const int32_t i = a_pool[a_beg[p] + x];
             if (status[i] == VAR && flag[i] != tag) {
                 flag[i] = tag;
                 Lp.push_back(i);
             }
         }
-        std::vector<int32_t>().swap(A[p]);
-        std::vector<int32_t>().swap(E[p]);
+        a_len[p] = 0;
+        e_len[p] = 0;
         status[p] = ELEM;
-        for (int32_t m : members[p]) order.push_back(m);
+        for (int32_t mb = m_head[p]; mb >= 0; mb = m_next[mb]) order.push_back(mb);
         eliminated += nv[p];
-        std::vector<int32_t>().swap(members[p]);
         int32_t lp_w = 0;
         for (int32_t i : Lp) {
             bucket_remove(i);
@@ -91,19 +130,21 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         ++tag;  // second tag for w
         const int32_t wt = tag;
         for (int32_t i : Lp) {
-            for (int32_t e : E[i]) {
+            for (int32_t x = 0; x < e_len[i]; ++x) {
+                const int32_t e = e_pool[e_beg[i] + x];
                 if (status[e] != ELEM) continue;
                 if (wtag[e] != wt) {
                     // weighted size of L[e], compacting dead entries
-                    int32_t sz = 0;
-                    auto& le = L[e];
-                    size_t k2 = 0;
-                    for (int32_t v : le)
+                    int32_t sz = 0, k2 = 0;
+                    int32_t* le = l_pool.data() + l_beg[e];
+                    for (int32_t y = 0; y < l_len[e]; ++y) {
+                        const int32_t v = le[y];
                         if (status[v] == VAR) {
                             le[k2++] = v;
                             sz += nv[v];
                         }
-                    le.resize(k2);
+                    }
+                    l_len[e] = k2;
                     w[e] = sz;
                     wtag[e] = wt;
                 }
@@ -114,30 +155,31 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         // flag[] == tag - 1 marks membership in Lp.
         const int32_t lp_tag = tag - 1;
         for (int32_t i : Lp) {
-            auto& ei = E[i];
-            size_t k2 = 0;
-            int32_t ext = 0;
-            for (int32_t e : ei) {
+            int32_t* ei = e_pool.data() + e_beg[i];
+            int32_t k2 = 0, ext = 0;
+            for (int32_t x = 0; x < e_len[i]; ++x) {
+                const int32_t e = ei[x];
                 if (status[e] != ELEM || e == p) continue;
                 if (wtag[e] == wt && w[e] <= 0) {  // Le subset of Lp: absorb into p
                     status[e] = DEAD;
-                    std::vector<int32_t>().swap(L[e]);
+                    l_len[e] = 0;
                     continue;
                 }
                 ei[k2++] = e;
                 ext += (wtag[e] == wt) ? w[e] : 0;
             }
-            ei.resize(k2);
-            ei.push_back(p);
-            auto& ai = A[i];
-            k2 = 0;
+            e_len[i] = k2;
+            e_push(i, p);
+            int32_t* ap = a_pool.data() + a_beg[i];
             int32_t aw = 0;
-            for (int32_t v : ai) {
+            k2 = 0;
+            for (int32_t x = 0; x < a_len[i]; ++x) {
+                const int32_t v = ap[x];
                 if (status[v] != VAR || v == p || flag[v] == lp_tag) continue;
-                ai[k2++] = v;
+                ap[k2++] = v;
                 aw += nv[v];
             }
-            ai.resize(k2);
+            a_len[i] = k2;
             const int32_t remaining = n - eliminated;
             const int32_t d1 = deg[i] + lp_w - nv[i];
             const int32_t d2 = aw + (lp_w - nv[i]) + ext;
@@ -148,32 +190,34 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         for (int32_t i : Lp) {
             if (status[i] != VAR) continue;
             uint64_t h = 0;
-            for (int32_t e : E[i]) h += static_cast<uint64_t>(e) * 0x9E3779B97F4A7C15ULL + 1;
-            for (int32_t v : A[i]) h += static_cast<uint64_t>(v) * 0xC2B2AE3D27D4EB4FULL + 7;
+            for (int32_t x = 0; x < e_len[i]; ++x)
+                h += static_cast<uint64_t>(e_pool[e_beg[i] + x]) * 0x9E3779B97F4A7C15ULL + 1;
+            for (int32_t x = 0; x < a_len[i]; ++x)
+                h += static_cast<uint64_t>(a_pool[a_beg[i] + x]) * 0xC2B2AE3D27D4EB4FULL + 7;
             hashes.emplace_back(h, i);
         }
         std::sort(hashes.begin(), hashes.end());
-        std::vector<int32_t> si, sj;
         for (size_t a = 0; a < hashes.size();) {
             size_t b = a;
             while (b < hashes.size() && hashes[b].first == hashes[a].first) ++b;
             for (size_t x = a; x + 1 < b; ++x) {  // a variable alone in its hash group has no twin
                 const int32_t i = hashes[x].second;
                 if (status[i] != VAR) continue;
-                si.assign(E[i].begin(), E[i].end());
+                si.assign(e_pool.begin() + e_beg[i], e_pool.begin() + e_beg[i] + e_len[i]);
                 std::sort(si.begin(), si.end());
-                std::vector<int32_t> ai(A[i].begin(), A[i].end());
+                ai.assign(a_pool.begin() + a_beg[i], a_pool.begin() + a_beg[i] + a_len[i]);
                 std::sort(ai.begin(), ai.end());
                 for (size_t y = x + 1; y < b; ++y) {
                     const int32_t j = hashes[y].second;
                     if (status[j] != VAR) continue;
-                    if (E[j].size() != E[i].size()) continue;
-                    sj.assign(E[j].begin(), E[j].end());
+                    if (e_len[j] != e_len[i]) continue;
+                    sj.assign(e_pool.begin() + e_beg[j], e_pool.begin() + e_beg[j] + e_len[j]);
                     std::sort(sj.begin(), sj.end());
                     if (si != sj) continue;
-                    std::vector<int32_t> aj(A[j].begin(), A[j].end());
+                    aj.assign(a_pool.begin() + a_beg[j], a_pool.begin() + a_beg[j] + a_len[j]);
                     std::sort(aj.begin(), aj.end());
-                    std::vector<int32_t> ai2, aj2;
+                    ai2.clear();
+                    aj2.clear();
                     for (int32_t v : ai) if (v != j) ai2.push_back(v);
                     for (int32_t v : aj) if (v != i) aj2.push_back(v);
                     if (ai2 != aj2) continue;
@@ -182,25 +226,26 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
                     deg[i] = std::max(0, deg[i] - nv[j]);
                     nv[j] = 0;
                     status[j] = DEAD;
-                    members[i].insert(members[i].end(), members[j].begin(), members[j].end());
-                    std::vector<int32_t>().swap(members[j]);
-                    std::vector<int32_t>().swap(A[j]);
-                    std::vector<int32_t>().swap(E[j]);
+                    m_next[m_tail[i]] = m_head[j];
+                    m_tail[i] = m_tail[j];
+                    a_len[j] = 0;
+                    e_len[j] = 0;
                     ai.erase(std::remove(ai.begin(), ai.end(), j), ai.end());
-                    A[i].erase(std::remove(A[i].begin(), A[i].end(), j), A[i].end());
+                    int32_t* ap = a_pool.data() + a_beg[i];
+                    a_len[i] = static_cast<int32_t>(std::remove(ap, ap + a_len[i], j) - ap);
                 }
             }
             a = b;
         }
         // --- finalise element p and reinsert variables ------------------------------------
-        auto& lpe = L[p];
-        lpe.clear();
+        l_beg[p] = static_cast<int64_t>(l_pool.size());
         for (int32_t i : Lp) {
             if (status[i] != VAR) continue;
-            lpe.push_back(i);
+            l_pool.push_back(i);
             bucket_insert(i);
             mindeg = std::min(mindeg, std::min(deg[i], n));
         }
+        l_len[p] = static_cast<int32_t>(l_pool.size() - l_beg[p]);
     }
     return order;
 }

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <memory>
 #include <numeric>
 #include <functional>
 #include <thread>
@@ -15,6 +16,54 @@ namespace {
 
 inline bool is_bus_type(int32_t t) { return t == 0 || t == 1 || t == 2 || t == 3 || t == 7 || t == 8; }
 inline bool is_inj_type(int32_t t) { return t == 2 || t == 3 || t == 7 || t == 8; }
+
+// Host threads for the analysis: at most the hardware's, and few enough that
+// each gets at least `grain` items.
+int32_t host_threads(int64_t items, int64_t grain) {
+    const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
+    return static_cast<int32_t>(std::max<int64_t>(1, std::min<int64_t>(hw, items / std::max<int64_t>(1, grain))));
+}
+
+// fn(t, begin, end) on `parts` contiguous ranges of [0, n), one thread each;
+// range t is the same for any machine, so results merged in t order are too.
+template <typename Fn>
+void parallel_ranges(int64_t n, int32_t parts, Fn&& fn) {
+    auto range = [&](int32_t t) {
+        return std::make_pair(n * t / parts, n * (t + 1) / parts);
+    };
+    std::vector<std::thread> pool;
+    for (int32_t t = 1; t < parts; ++t)
+        pool.emplace_back([&, t] {
+            const auto r = range(t);
+            fn(t, r.first, r.second);
+        });
+    const auto r0 = range(0);
+    fn(0, r0.first, r0.second);
+    for (auto& th : pool) th.join();
+}
+
+// Per-range output lists of a parallel pass, concatenated in range order
+// into a CSR structure (ptr[i + 1] - ptr[i] = length of item i's list).
+struct RangeLists {
+    std::vector<std::vector<int32_t>> data, len;
+    explicit RangeLists(int32_t parts) : data(parts), len(parts) {}
+    void gather(int64_t n, std::vector<int32_t>& ptr, std::vector<int32_t>& out) const {
+        ptr.assign(static_cast<size_t>(n) + 1, 0);
+        size_t total = 0;
+        for (auto& d : data) total += d.size();
+        out.resize(total);
+        int64_t i = 0;
+        size_t o = 0;
+        for (size_t t = 0; t < data.size(); ++t) {
+            std::copy(data[t].begin(), data[t].end(), out.begin() + o);
+            o += data[t].size();
+            for (int32_t l : len[t]) {
+                ptr[i + 1] = ptr[i] + l;
+                ++i;
+            }
+        }
+    }
+};
 
 // ---------------------------------------------------------------------------
 // Nested dissection on the bus graph.
@@ -264,49 +313,73 @@ int64_t trapezoid(int64_t nc, int64_t f) { return nc * f - nc * (nc - 1) / 2; }
 
 void bus_graph(const Topology& t, const std::vector<int32_t>& y_ptr, const std::vector<int32_t>& y_col,
                std::vector<int32_t>& adj_ptr, std::vector<int32_t>& adj) {
-    // Two passes over the active rows: an upper bound of each bus's
-    // neighbour count, then the neighbours themselves; each bus's list is
-    // then sorted and made unique on its own (short lists instead of one
-    // sort of every ordered pair).
+    // Buses a and b are adjacent when an active row couples them: an
+    // injection row at c couples every pair of {c} and c's Ybus neighbours,
+    // a flow or current row couples the branch's two ends.  Bus a's list is
+    // therefore the Ybus rows of the injection-measured buses of a's own Ybus
+    // row, plus a's flow partners; each list is built on its own (sorted,
+    // unique), buses in parallel ranges.
     const int32_t n = t.n_bus;
-    auto row_buses = [&](int32_t q, std::vector<int32_t>& buses) {
-        buses.clear();
-        if (t.m_active && !t.m_active[q]) return;
-        const int32_t ty = t.m_type[q], loc = t.m_loc[q];
-        if (is_inj_type(ty)) {
-            buses.push_back(loc);
-            for (int32_t e = y_ptr[loc]; e < y_ptr[loc + 1]; ++e) buses.push_back(y_col[e]);
-        } else if (ty == 4 || ty == 5 || ty == 6) {
-            buses.push_back(t.br_from[loc]);
-            buses.push_back(t.br_to[loc]);
-        }
+    std::vector<uint8_t> has_inj(n, 0);
+    std::vector<int32_t> fptr(static_cast<size_t>(n) + 1, 0), fpart;
+    auto flow_row = [&](int32_t q) {
+        const int32_t ty = t.m_type[q];
+        return (!t.m_active || t.m_active[q]) && (ty == 4 || ty == 5 || ty == 6) &&
+               t.br_from[t.m_loc[q]] != t.br_to[t.m_loc[q]];
     };
-    std::vector<int64_t> bound(static_cast<size_t>(n) + 1, 0);
-    std::vector<int32_t> buses;
     for (int32_t q = 0; q < t.n_meas; ++q) {
-        row_buses(q, buses);
-        for (int32_t b : buses) bound[b + 1] += static_cast<int64_t>(buses.size()) - 1;
+        if (t.m_active && !t.m_active[q]) continue;
+        if (is_inj_type(t.m_type[q])) has_inj[t.m_loc[q]] = 1;
+        if (flow_row(q)) {
+            ++fptr[t.br_from[t.m_loc[q]] + 1];
+            ++fptr[t.br_to[t.m_loc[q]] + 1];
+        }
     }
-    for (int32_t i = 0; i < n; ++i) bound[i + 1] += bound[i];
-    std::vector<int32_t> tmp(static_cast<size_t>(bound[n]));
-    std::vector<int64_t> fill(bound.begin(), bound.end() - 1);
-    for (int32_t q = 0; q < t.n_meas; ++q) {
-        row_buses(q, buses);
-        for (int32_t a : buses)
-            for (int32_t b : buses)
-                if (b != a) tmp[fill[a]++] = b;
+    for (int32_t i = 0; i < n; ++i) fptr[i + 1] += fptr[i];
+    fpart.resize(fptr[n]);
+    {
+        std::vector<int32_t> fill(fptr.begin(), fptr.end() - 1);
+        for (int32_t q = 0; q < t.n_meas; ++q)
+            if (flow_row(q)) {
+                const int32_t i = t.br_from[t.m_loc[q]], j = t.br_to[t.m_loc[q]];
+                fpart[fill[i]++] = j;
+                fpart[fill[j]++] = i;
+            }
     }
-    adj_ptr.assign(static_cast<size_t>(n) + 1, 0);
-    adj.clear();
-    adj.reserve(tmp.size());
-    for (int32_t i = 0; i < n; ++i) {
-        int32_t* b0 = tmp.data() + bound[i];
-        int32_t* b1 = tmp.data() + fill[i];
-        std::sort(b0, b1);
-        int32_t* e = std::unique(b0, b1);
-        adj.insert(adj.end(), b0, e);
-        adj_ptr[i + 1] = static_cast<int32_t>(adj.size());
-    }
+    const int32_t parts = host_threads(n, 4096);
+    RangeLists out(parts);
+    parallel_ranges(n, parts, [&](int32_t th, int64_t b0, int64_t b1) {
+        std::vector<int32_t> mark(n, -1), list;
+        auto& d = out.data[th];
+        auto& len = out.len[th];
+        for (int64_t a64 = b0; a64 < b1; ++a64) {
+            const int32_t a = static_cast<int32_t>(a64);
+            list.clear();
+            mark[a] = a;
+            for (int32_t e = y_ptr[a]; e < y_ptr[a + 1]; ++e) {
+                const int32_t c = y_col[e];
+                if (!has_inj[c]) continue;
+                for (int32_t f = y_ptr[c]; f < y_ptr[c + 1]; ++f) {
+                    const int32_t b = y_col[f];
+                    if (mark[b] != a) {
+                        mark[b] = a;
+                        list.push_back(b);
+                    }
+                }
+            }
+            for (int32_t f = fptr[a]; f < fptr[a + 1]; ++f) {
+                const int32_t b = fpart[f];
+                if (mark[b] != a) {
+                    mark[b] = a;
+                    list.push_back(b);
+                }
+            }
+            std::sort(list.begin(), list.end());
+            d.insert(d.end(), list.begin(), list.end());
+            len.push_back(static_cast<int32_t>(list.size()));
+        }
+    });
+    out.gather(n, adj_ptr, adj);
 }
 
 bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::string& err) {
@@ -333,94 +406,146 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     auto col_v = [&](int32_t i) { return n - 1 + i; };
 
     // --- Ybus pattern -----------------------------------------------------------
+    // Row i: the diagonal, then (column, 2k + end) of each closed branch k at
+    // bus i, sorted.
     {
-        std::vector<std::vector<std::pair<int32_t, int32_t>>> rows(n);  // (col, src)
+        std::vector<int32_t> cnt(static_cast<size_t>(n) + 1, 0);
         for (int32_t k = 0; k < nbr; ++k) {
             if (!t.br_closed[k]) continue;
-            rows[t.br_from[k]].emplace_back(t.br_to[k], (k << 1) | 0);
-            rows[t.br_to[k]].emplace_back(t.br_from[k], (k << 1) | 1);
+            ++cnt[t.br_from[k] + 1];
+            ++cnt[t.br_to[k] + 1];
         }
-        P.y_ptr.assign(n + 1, 0);
+        P.y_ptr.assign(static_cast<size_t>(n) + 1, 0);
         for (int32_t i = 0; i < n; ++i) {
-            auto& r = rows[i];
-            std::sort(r.begin(), r.end());
-            P.y_col.push_back(i);
-            P.y_src.push_back(-1);
-            for (auto& e : r) {
-                P.y_col.push_back(e.first);
-                P.y_src.push_back(e.second);
-            }
-            P.y_ptr[i + 1] = static_cast<int32_t>(P.y_col.size());
+            P.y_ptr[i + 1] = P.y_ptr[i] + 1 + cnt[i + 1];
+            cnt[i + 1] += cnt[i];
         }
+        std::vector<std::pair<int32_t, int32_t>> ent(static_cast<size_t>(cnt[n]));
+        {
+            std::vector<int32_t> fill(cnt.begin(), cnt.end() - 1);
+            for (int32_t k = 0; k < nbr; ++k) {
+                if (!t.br_closed[k]) continue;
+                ent[fill[t.br_from[k]]++] = {t.br_to[k], (k << 1) | 0};
+                ent[fill[t.br_to[k]]++] = {t.br_from[k], (k << 1) | 1};
+            }
+        }
+        P.y_col.resize(P.y_ptr[n]);
+        P.y_src.resize(P.y_ptr[n]);
+        parallel_ranges(n, host_threads(n, 8192), [&](int32_t, int64_t i0, int64_t i1) {
+            for (int64_t i = i0; i < i1; ++i) {
+                auto* r0 = ent.data() + cnt[i];
+                auto* r1 = ent.data() + cnt[i + 1];
+                std::sort(r0, r1);
+                int32_t o = P.y_ptr[i];
+                P.y_col[o] = static_cast<int32_t>(i);
+                P.y_src[o] = -1;
+                for (auto* e = r0; e < r1; ++e) {
+                    ++o;
+                    P.y_col[o] = e->first;
+                    P.y_src[o] = e->second;
+                }
+            }
+        });
     }
 
     // --- H pattern ------------------------------------------------------------------
     {
-        // Injection-row column lists per bus (computed once per bus).
-        std::vector<int32_t> inj_cols_ptr(n + 1, 0), inj_cols;
+        // Injection-row column lists per bus (computed once per bus, in
+        // parallel ranges): the angle and magnitude columns of the bus's Ybus
+        // row, sorted and unique, with each Ybus entry's positions in it.
+        std::vector<int32_t> inj_cols_ptr, inj_cols;
         P.y_hpos_t.assign(P.y_col.size(), -1);
         P.y_hpos_v.assign(P.y_col.size(), -1);
-        std::vector<int32_t> cols;
-        for (int32_t i = 0; i < n; ++i) {
-            cols.clear();
-            for (int32_t e = P.y_ptr[i]; e < P.y_ptr[i + 1]; ++e) {
-                const int32_t j = P.y_col[e];
-                if (col_t(j) >= 0) cols.push_back(col_t(j));
-                cols.push_back(col_v(j));
-            }
-            std::sort(cols.begin(), cols.end());
-            cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
-            for (int32_t e = P.y_ptr[i]; e < P.y_ptr[i + 1]; ++e) {
-                const int32_t j = P.y_col[e];
-                if (col_t(j) >= 0)
-                    P.y_hpos_t[e] = static_cast<int32_t>(std::lower_bound(cols.begin(), cols.end(), col_t(j)) - cols.begin());
-                P.y_hpos_v[e] = static_cast<int32_t>(std::lower_bound(cols.begin(), cols.end(), col_v(j)) - cols.begin());
-            }
-            inj_cols.insert(inj_cols.end(), cols.begin(), cols.end());
-            inj_cols_ptr[i + 1] = static_cast<int32_t>(inj_cols.size());
-        }
-        P.h_ptr.assign(m + 1, 0);
-        P.m_kind.assign(m, ROW_NONE);
-        P.m_fpos.assign(m, -1);
-        for (int32_t q = 0; q < m; ++q) {
-            const int32_t ty = t.m_type[q], loc = t.m_loc[q];
-            const bool active = !t.m_active || t.m_active[q];
-            if (active) {
-                if (ty == 0) {
-                    P.m_kind[q] = ROW_VMAG;
-                    P.h_col.push_back(col_v(loc));
-                } else if (ty == 1) {
-                    P.m_kind[q] = ROW_VANG;
-                    if (col_t(loc) >= 0) P.h_col.push_back(col_t(loc));
-                } else if (is_inj_type(ty)) {
-                    P.m_kind[q] = ROW_INJ;
-                    P.h_col.insert(P.h_col.end(), inj_cols.begin() + inj_cols_ptr[loc],
-                                   inj_cols.begin() + inj_cols_ptr[loc + 1]);
-                } else {
-                    P.m_kind[q] = (ty == 6) ? ROW_IMAG : ROW_FLOW;
-                    const int32_t i = t.br_from[loc], j = t.br_to[loc];
-                    const int32_t c4[4] = {col_t(i), col_v(i), col_t(j), col_v(j)};
+        {
+            const int32_t parts = host_threads(n, 8192);
+            RangeLists out(parts);
+            parallel_ranges(n, parts, [&](int32_t th, int64_t i0, int64_t i1) {
+                std::vector<int32_t> cols;
+                for (int64_t i = i0; i < i1; ++i) {
                     cols.clear();
-                    for (int32_t c : c4)
-                        if (c >= 0) cols.push_back(c);
+                    for (int32_t e = P.y_ptr[i]; e < P.y_ptr[i + 1]; ++e) {
+                        const int32_t j = P.y_col[e];
+                        if (col_t(j) >= 0) cols.push_back(col_t(j));
+                        cols.push_back(col_v(j));
+                    }
                     std::sort(cols.begin(), cols.end());
                     cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
-                    uint32_t packed = 0;
-                    for (int x = 0; x < 4; ++x) {
-                        uint32_t pos = 0xFF;
-                        if (c4[x] >= 0)
-                            pos = static_cast<uint32_t>(std::lower_bound(cols.begin(), cols.end(), c4[x]) - cols.begin());
-                        packed |= pos << (8 * x);
+                    for (int32_t e = P.y_ptr[i]; e < P.y_ptr[i + 1]; ++e) {
+                        const int32_t j = P.y_col[e];
+                        if (col_t(j) >= 0)
+                            P.y_hpos_t[e] =
+                                static_cast<int32_t>(std::lower_bound(cols.begin(), cols.end(), col_t(j)) - cols.begin());
+                        P.y_hpos_v[e] =
+                            static_cast<int32_t>(std::lower_bound(cols.begin(), cols.end(), col_v(j)) - cols.begin());
                     }
-                    P.m_fpos[q] = static_cast<int32_t>(packed);
-                    P.h_col.insert(P.h_col.end(), cols.begin(), cols.end());
+                    out.data[th].insert(out.data[th].end(), cols.begin(), cols.end());
+                    out.len[th].push_back(static_cast<int32_t>(cols.size()));
                 }
-            }
-            P.h_ptr[q + 1] = static_cast<int32_t>(P.h_col.size());
+            });
+            out.gather(n, inj_cols_ptr, inj_cols);
         }
-        P.h_row.resize(P.h_col.size());
-        for (int32_t q = 0; q < m; ++q)
-            for (int32_t h = P.h_ptr[q]; h < P.h_ptr[q + 1]; ++h) P.h_row[h] = q;
+        // Rows: the columns of each active row (a pass of lengths, then each
+        // row written at its offset, rows in parallel ranges).
+        P.m_kind.assign(m, ROW_NONE);
+        P.m_fpos.assign(m, -1);
+        auto row_cols = [&](int32_t q, int32_t* dst, int32_t& kind, int32_t& fpos) {
+            const int32_t ty = t.m_type[q], loc = t.m_loc[q];
+            if (t.m_active && !t.m_active[q]) return 0;
+            if (ty == 0) {
+                kind = ROW_VMAG;
+                if (dst) dst[0] = col_v(loc);
+                return 1;
+            }
+            if (ty == 1) {
+                kind = ROW_VANG;
+                if (col_t(loc) < 0) return 0;
+                if (dst) dst[0] = col_t(loc);
+                return 1;
+            }
+            if (is_inj_type(ty)) {
+                kind = ROW_INJ;
+                const int32_t c0 = inj_cols_ptr[loc], c1 = inj_cols_ptr[loc + 1];
+                if (dst) std::copy(inj_cols.begin() + c0, inj_cols.begin() + c1, dst);
+                return c1 - c0;
+            }
+            kind = (ty == 6) ? ROW_IMAG : ROW_FLOW;
+            const int32_t i = t.br_from[loc], j = t.br_to[loc];
+            const int32_t c4[4] = {col_t(i), col_v(i), col_t(j), col_v(j)};
+            int32_t cols[4], nc = 0;
+            for (int32_t c : c4)
+                if (c >= 0) cols[nc++] = c;
+            std::sort(cols, cols + nc);
+            nc = static_cast<int32_t>(std::unique(cols, cols + nc) - cols);
+            uint32_t packed = 0;
+            for (int x = 0; x < 4; ++x) {
+                uint32_t pos = 0xFF;
+                if (c4[x] >= 0) pos = static_cast<uint32_t>(std::lower_bound(cols, cols + nc, c4[x]) - cols);
+                packed |= pos << (8 * x);
+            }
+            fpos = static_cast<int32_t>(packed);
+            if (dst) std::copy(cols, cols + nc, dst);
+            return nc;
+        };
+        P.h_ptr.assign(static_cast<size_t>(m) + 1, 0);
+        const int32_t parts = host_threads(m, 16384);
+        parallel_ranges(m, parts, [&](int32_t, int64_t q0, int64_t q1) {
+            for (int64_t q = q0; q < q1; ++q) {
+                int32_t kind = ROW_NONE, fpos = -1;
+                P.h_ptr[q + 1] = row_cols(static_cast<int32_t>(q), nullptr, kind, fpos);
+                P.m_kind[q] = kind;
+                P.m_fpos[q] = fpos;
+            }
+        });
+        for (int32_t q = 0; q < m; ++q) P.h_ptr[q + 1] += P.h_ptr[q];
+        P.h_col.resize(P.h_ptr[m]);
+        P.h_row.resize(P.h_ptr[m]);
+        parallel_ranges(m, parts, [&](int32_t, int64_t q0, int64_t q1) {
+            for (int64_t q = q0; q < q1; ++q) {
+                int32_t kind = ROW_NONE, fpos = -1;
+                row_cols(static_cast<int32_t>(q), P.h_col.data() + P.h_ptr[q], kind, fpos);
+                for (int32_t h = P.h_ptr[q]; h < P.h_ptr[q + 1]; ++h) P.h_row[h] = static_cast<int32_t>(q);
+            }
+        });
     }
 
     // --- ordering on the bus graph -----------------------------------------------------
@@ -709,8 +834,7 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     // thread count.
     {
         struct PairRec { int32_t local; int32_t a; int32_t b; };
-        const int32_t nthr = std::max(1, std::min<int32_t>(static_cast<int32_t>(std::thread::hardware_concurrency()),
-                                                           std::max(1, m / 4096)));
+        const int32_t nthr = host_threads(m, 4096);
         auto parallel = [&](int32_t parts, const std::function<void(int32_t)>& fn) {
             std::vector<std::thread> pool;
             for (int32_t t = 1; t < parts; ++t) pool.emplace_back(fn, t);
@@ -721,87 +845,135 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
             return std::make_pair(static_cast<int32_t>((static_cast<int64_t>(total) * t) / nthr),
                                   static_cast<int32_t>((static_cast<int64_t>(total) * (t + 1)) / nthr));
         };
+        // pairs of row q start at pair_off[q] (x-major, y >= x)
+        std::vector<int64_t> pair_off(static_cast<size_t>(m) + 1, 0);
+        for (int32_t q = 0; q < m; ++q) {
+            const int64_t L = P.h_ptr[q + 1] - P.h_ptr[q];
+            pair_off[q + 1] = pair_off[q] + L * (L + 1) / 2;
+        }
+        const int64_t run = pair_off[m];
+        // the output arrays are zero-filled (page faults) on a thread of their
+        // own while the passes below run
+        std::thread alloc_out([&] {
+            P.pair_a.resize(static_cast<size_t>(run));
+            P.pair_b.resize(static_cast<size_t>(run));
+        });
+        std::unique_ptr<int32_t[]> pk(new int32_t[std::max<int64_t>(run, 1)]);
+        std::unique_ptr<int32_t[]> pl(new int32_t[std::max<int64_t>(run, 1)]);
         std::vector<std::vector<int64_t>> cnt(nthr, std::vector<int64_t>(ns + 1, 0));
         std::vector<uint8_t> bad(nthr, 0);
-        // the front and local index of pair (x, y); false if outside the structure
-        auto locate = [&](int32_t x, int32_t y, int32_t& k, int32_t& local) {
-            const int32_t px = ps_of_state[P.h_col[x]], py = ps_of_state[P.h_col[y]];
+        // the front and local index of a pair of H entries in permuted
+        // columns px, py; false if outside the structure.  A front's own
+        // columns lead its row list in order, so a row there is found without
+        // a search.
+        auto locate = [&](int32_t px, int32_t py, int32_t& k, int32_t& local) {
             const int32_t lo = std::min(px, py), hi = std::max(px, py);
             k = sn_of_ps[lo];
-            const int32_t* rows = P.sn_rows.data() + P.sn_rows_off[k];
-            const int32_t f = P.sn_f[k];
-            const int32_t* it = std::lower_bound(rows, rows + f, hi);
-            if (it == rows + f || *it != hi) return false;
-            local = static_cast<int32_t>(it - rows) + (lo - P.sn_c0[k]) * f;
+            const int32_t f = P.sn_f[k], c0 = P.sn_c0[k], nc = P.sn_c0[k + 1] - c0;
+            int32_t r;
+            if (hi - c0 < nc) {
+                r = hi - c0;
+            } else {
+                const int32_t* rows = P.sn_rows.data() + P.sn_rows_off[k];
+                const int32_t* it = std::lower_bound(rows + nc, rows + f, hi);
+                if (it == rows + f || *it != hi) return false;
+                r = static_cast<int32_t>(it - rows);
+            }
+            local = r + (lo - c0) * f;
             return true;
         };
         parallel(nthr, [&](int32_t t) {
             const auto r = chunk(t, m);
             auto& c = cnt[t];
-            for (int32_t q = r.first; q < r.second; ++q)
-                for (int32_t x = P.h_ptr[q]; x < P.h_ptr[q + 1]; ++x)
-                    for (int32_t y = x; y < P.h_ptr[q + 1]; ++y) {
+            std::vector<int32_t> ps;
+            for (int32_t q = r.first; q < r.second; ++q) {
+                int64_t o = pair_off[q];
+                const int32_t h0 = P.h_ptr[q], L = P.h_ptr[q + 1] - h0;
+                ps.resize(L);
+                for (int32_t x = 0; x < L; ++x) ps[x] = ps_of_state[P.h_col[h0 + x]];
+                for (int32_t x = 0; x < L; ++x)
+                    for (int32_t y = x; y < L; ++y, ++o) {
                         int32_t k, local;
-                        if (!locate(x, y, k, local)) {
+                        if (!locate(ps[x], ps[y], k, local)) {
                             bad[t] = 1;
                             return;
                         }
+                        pk[o] = k;
+                        pl[o] = local;
                         ++c[k];
                     }
+            }
         });
         for (uint8_t b : bad)
             if (b) {
+                alloc_out.join();
                 err = "gain entry outside the front structure";
                 return false;
             }
         // offsets: front-major, chunk-minor
         std::vector<int64_t> sn_rec(ns + 1, 0);
         std::vector<std::vector<int64_t>> off(nthr, std::vector<int64_t>(ns, 0));
-        int64_t run = 0;
+        int64_t acc = 0;
         for (int32_t k = 0; k < ns; ++k) {
-            sn_rec[k] = run;
+            sn_rec[k] = acc;
             for (int32_t t = 0; t < nthr; ++t) {
-                off[t][k] = run;
-                run += cnt[t][k];
+                off[t][k] = acc;
+                acc += cnt[t][k];
             }
         }
-        sn_rec[ns] = run;
-        std::vector<PairRec> rec(static_cast<size_t>(run));
+        sn_rec[ns] = acc;
+        std::unique_ptr<PairRec[]> rec(new PairRec[std::max<int64_t>(run, 1)]);
         parallel(nthr, [&](int32_t t) {
             const auto r = chunk(t, m);
             auto& o = off[t];
-            for (int32_t q = r.first; q < r.second; ++q)
+            for (int32_t q = r.first; q < r.second; ++q) {
+                int64_t i = pair_off[q];
                 for (int32_t x = P.h_ptr[q]; x < P.h_ptr[q + 1]; ++x)
-                    for (int32_t y = x; y < P.h_ptr[q + 1]; ++y) {
-                        int32_t k, local;
-                        locate(x, y, k, local);
-                        rec[o[k]++] = {local, x, y};
-                    }
+                    for (int32_t y = x; y < P.h_ptr[q + 1]; ++y, ++i) rec[o[pk[i]]++] = {pl[i], x, y};
+            }
         });
-        // per front: stable sort by local index, count the targets
+        pk.reset();
+        pl.reset();
+        // fronts cut into nthr ranges of about equal record counts
+        std::vector<int32_t> fr_cut(nthr + 1, ns);
+        fr_cut[0] = 0;
+        for (int32_t t = 1, k = 0; t < nthr; ++t) {
+            const int64_t goal = run * t / nthr;
+            while (k < ns && sn_rec[k] < goal) ++k;
+            fr_cut[t] = k;
+        }
+        // per front: stable counting sort by local index (local < f * nc),
+        // count the targets
         std::vector<int32_t> ntg(ns + 1, 0);
         parallel(nthr, [&](int32_t t) {
-            const auto r = chunk(t, ns);
-            for (int32_t k = r.first; k < r.second; ++k) {
-                PairRec* b = rec.data() + sn_rec[k];
-                PairRec* e = rec.data() + sn_rec[k + 1];
-                std::stable_sort(b, e, [](const PairRec& u, const PairRec& w) { return u.local < w.local; });
+            std::vector<int32_t> hist;
+            std::vector<PairRec> tmp;
+            for (int32_t k = fr_cut[t]; k < fr_cut[t + 1]; ++k) {
+                PairRec* b = rec.get() + sn_rec[k];
+                const int64_t cntk = sn_rec[k + 1] - sn_rec[k];
+                const int32_t range = P.sn_f[k] * (P.sn_c0[k + 1] - P.sn_c0[k]);
+                hist.assign(static_cast<size_t>(range) + 1, 0);
+                for (int64_t i = 0; i < cntk; ++i) ++hist[b[i].local + 1];
                 int32_t c = 0;
-                for (PairRec* it = b; it < e; ++it) c += (it == b || it->local != (it - 1)->local) ? 1 : 0;
+                for (int32_t v = 0; v < range; ++v) {
+                    c += hist[v + 1] > 0 ? 1 : 0;
+                    hist[v + 1] += hist[v];
+                }
+                tmp.resize(static_cast<size_t>(cntk));
+                for (int64_t i = 0; i < cntk; ++i) tmp[hist[b[i].local]++] = b[i];
+                std::copy(tmp.begin(), tmp.end(), b);
                 ntg[k] = c;
             }
         });
         P.sn_tgt_ptr.assign(ns + 1, 0);
         for (int32_t k = 0; k < ns; ++k) P.sn_tgt_ptr[k + 1] = P.sn_tgt_ptr[k] + ntg[k];
         const int32_t n_tgt = P.sn_tgt_ptr[ns];
-        P.tgt_local.assign(n_tgt, 0);
-        P.tgt_pair_ptr.assign(static_cast<size_t>(n_tgt) + 1, 0);
-        P.pair_a.assign(static_cast<size_t>(run), 0);
-        P.pair_b.assign(static_cast<size_t>(run), 0);
+        P.tgt_local.resize(n_tgt);
+        P.tgt_pair_ptr.resize(static_cast<size_t>(n_tgt) + 1);
+        alloc_out.join();
         P.tgt_pair_ptr[n_tgt] = run;
         parallel(nthr, [&](int32_t t) {
-            const auto r = chunk(t, ns);
-            for (int32_t k = r.first; k < r.second; ++k) {
+            for (int32_t k = fr_cut[t]; k < fr_cut[t + 1]; ++k) {
                 int32_t tg = P.sn_tgt_ptr[k];
                 for (int64_t i = sn_rec[k]; i < sn_rec[k + 1]; ++i) {
                     if (i == sn_rec[k] || rec[i].local != rec[i - 1].local) {
