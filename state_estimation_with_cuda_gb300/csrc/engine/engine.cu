@@ -269,6 +269,7 @@ void Engine::build_schedule() {
     sch_small_.clear();
     sch_all_.clear();
     sch_asm_.clear();
+    sch_asm_child_.clear();
     sch_pot_.clear();
     n_pot_pairs_ = 0;
     sch_upd_.clear();
@@ -437,7 +438,30 @@ void Engine::build_schedule() {
             const int32_t tiles = (f + kTile - 1) / kTile;
             for (int32_t tj = 0; tj < tiles; ++tj) {
                 const int32_t rows = f - tj * kTile;  // the tile column's lower part
-                for (int32_t rb = 0; rb * kAsmRows < rows; ++rb) sch_asm_.push_back(make_int4(s, tj, rb, 0));
+                const int32_t c0 = tj * kTile, c1 = std::min(c0 + kTile, f);
+                const int32_t* tl = P.tgt_local.data();
+                const int32_t tg_lo = static_cast<int32_t>(
+                    std::lower_bound(tl + P.sn_tgt_ptr[s], tl + P.sn_tgt_ptr[s + 1], c0 * f) - tl);
+                const int32_t tg_hi = static_cast<int32_t>(
+                    std::lower_bound(tl + tg_lo, tl + P.sn_tgt_ptr[s + 1], c1 * f) - tl);
+                for (int32_t rb = 0; rb * kAsmRows < rows; ++rb) {
+                    const int32_t R0 = c0 + rb * kAsmRows, R1 = std::min(R0 + kAsmRows, f);
+                    AsmItem it{s, tj, rb, tg_lo, tg_hi, static_cast<int32_t>(sch_asm_child_.size()), 0, 0};
+                    // the children that add entries to rows [R0, R1) of columns [c0, c1), in order
+                    for (int32_t ci = P.sn_child_ptr[s]; ci < P.sn_child_ptr[s + 1]; ++ci) {
+                        const int32_t c = P.sn_child[ci];
+                        const int32_t m = P.sn_f[c] - (P.sn_c0[c + 1] - P.sn_c0[c]);
+                        const int32_t* rel = P.sn_relmap.data() + P.sn_su_off[c];
+                        const int32_t j0 = static_cast<int32_t>(std::lower_bound(rel, rel + m, c0) - rel);
+                        const int32_t j1 = static_cast<int32_t>(std::lower_bound(rel + j0, rel + m, c1) - rel);
+                        const int32_t ilo = static_cast<int32_t>(std::lower_bound(rel, rel + m, R0) - rel);
+                        const int32_t ihi = static_cast<int32_t>(std::lower_bound(rel + ilo, rel + m, R1) - rel);
+                        if (j0 < j1 && std::max(j0, ilo) < ihi)
+                            sch_asm_child_.push_back(AsmChild{c, j0, j1, ilo, ihi, 0, 0, 0});
+                    }
+                    it.ch_hi = static_cast<int32_t>(sch_asm_child_.size());
+                    sch_asm_.push_back(it);
+                }
             }
             panels = std::max(panels, (nc + kTile - 1) / kTile);
         }
@@ -675,7 +699,8 @@ int32_t Engine::upload() {
         }
         d_small_ = c.take<int32_t>(sch_small_.size());
         d_all_ = c.take<int32_t>(sch_all_.size());
-        d_asm_ = c.take<int4>(sch_asm_.size());
+        d_asm_ = c.take<AsmItem>(sch_asm_.size());
+        d_asm_child_ = c.take<AsmChild>(sch_asm_child_.size());
         d_pot_ = c.take<int4>(sch_pot_.size());
         d_pot_cnt_ = c.take<int32_t>(std::max(1, n_pot_pairs_));
         d_pan_ = c.take<int4>(sch_pan_.size());
@@ -874,6 +899,7 @@ int32_t Engine::upload() {
     chk(put(d_small_, sch_small_, st_));
     chk(put(d_all_, sch_all_, st_));
     chk(put(d_asm_, sch_asm_, st_));
+    chk(put(d_asm_child_, sch_asm_child_, st_));
     chk(put(d_pot_, sch_pot_, st_));
     chk(put(d_pan_, sch_pan_, st_));
     chk(put(d_upd_, sch_upd_, st_));
@@ -924,6 +950,7 @@ int32_t Engine::upload() {
     sched_.h_small_maxf = sch_small_maxf_.data();
     sched_.h_asm_ptr = sch_asm_ptr_.data();
     sched_.d_asm = d_asm_;
+    sched_.d_asm_child = d_asm_child_;
     sched_.h_lvl_panels = sch_panels_.data();
     sched_.h_step_ptr = sch_step_ptr_.data();
     sched_.h_pot_ptr = sch_pot_ptr_.data();

@@ -262,7 +262,9 @@ private:
     // level schedule (host copies) and in-place storage layout
     std::vector<int32_t> sch_small_ptr_, sch_small_, sch_small_maxf_, sch_asm_ptr_, sch_panels_, sch_step_ptr_,
         sch_pot_ptr_, sch_pan_ptr_, sch_upd_ptr_, sch_all_ptr_, sch_all_, sch_maxf_;
-    std::vector<int4> sch_asm_, sch_pot_, sch_pan_, sch_upd_;
+    std::vector<int4> sch_pot_, sch_pan_, sch_upd_;
+    std::vector<AsmItem> sch_asm_;
+    std::vector<AsmChild> sch_asm_child_;
     // FP32 tiled fronts as dataflow items (TileTask), per level
     std::vector<TileTask> sch_tt_;
     std::vector<int32_t> sch_tt_ptr_;
@@ -320,7 +322,8 @@ private:
     int64_t lay_lx_size_ = 0, lay_u_size_ = 0;
     int32_t* d_small_ = nullptr;
     int32_t* d_all_ = nullptr;
-    int4* d_asm_ = nullptr;
+    AsmItem* d_asm_ = nullptr;
+    AsmChild* d_asm_child_ = nullptr;
     int4* d_pot_ = nullptr;
     int4* d_pan_ = nullptr;
     int4* d_upd_ = nullptr;

@@ -780,14 +780,16 @@ __device__ __forceinline__ int lower_bound_i32(const int* a, int lo, int hi, int
 
 // Assembly of a tiled front, one CTA per (tile column tj, block rb of
 // kAsmRows rows from the tile's first column down): zero the block's lower
-// part, write its G entries, then add the children's update-matrix entries
-// that land in it, child by child (a barrier between children keeps every
-// entry's sum in child order, as in the single-CTA fronts).
+// part, write its G entries, then add the update-matrix entries of the
+// children that land in it, child by child (a barrier between children keeps
+// every entry's sum in child order, as in the single-CTA fronts).  The
+// block's target range and its contributing children with their column and
+// row ranges come from the host schedule (AsmItem / AsmChild).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_big_assemble(DevFactor F, DevWork W, const T* gv, T* lx, T* ub,
-                                                           const int4* work) {
-    const int4 wk = work[blockIdx.x];
-    const int s = wk.x, tj = wk.y, rb = wk.z;
+                                                           const AsmItem* work, const AsmChild* kids) {
+    const AsmItem wk = work[blockIdx.x];
+    const int s = wk.s, tj = wk.tj, rb = wk.rb;
     if (front_frozen(F, W, s)) return;  // the whole CTA, before any barrier
     const int f = F.sn_f[s];
     T* B = lx + F.sn_lx_off[s];
@@ -799,41 +801,34 @@ __global__ void __launch_bounds__(kThreads) k_big_assemble(DevFactor F, DevWork 
         if (r >= c) B[r + (int64_t)c * f] = T(0);
     }
     __syncthreads();
-    // tgt_local = row + col * f is sorted, so a tile column is a contiguous range
-    const int lo = lower_bound_i32(F.tgt_local, F.sn_tgt_ptr[s], F.sn_tgt_ptr[s + 1], c0 * f);
-    const int hi = lower_bound_i32(F.tgt_local, lo, F.sn_tgt_ptr[s + 1], c1 * f);
-    for (int tg = lo + tid; tg < hi; tg += nth) {
+    for (int tg = wk.tg_lo + tid; tg < wk.tg_hi; tg += nth) {
         const int l = F.tgt_local[tg];
         const int r = l % f;
         if (r >= R0 && r < R1) B[l] = gv[tg];
     }
     __syncthreads();
-    for (int ci = F.sn_child_ptr[s]; ci < F.sn_child_ptr[s + 1]; ++ci) {
-        const int c = F.sn_child[ci];
-        const int m = F.sn_f[c] - (F.sn_c0[c + 1] - F.sn_c0[c]);
+    for (int ci = wk.ch_lo; ci < wk.ch_hi; ++ci) {
+        const AsmChild ch = kids[ci];
+        const int c = ch.c;
         const int* rel = F.sn_relmap + F.sn_su_off[c];
-        const int j0 = lower_bound_i32(rel, 0, m, c0);  // rel is increasing
-        const int j1 = lower_bound_i32(rel, j0, m, c1);
-        const int ilo = lower_bound_i32(rel, 0, m, R0);  // child rows landing in [R0, R1)
-        const int ihi = lower_bound_i32(rel, ilo, m, R1);
         const T* U = update_of<T>(F, lx, ub, c);
         const int uld = F.sn_u_ld[c];
         const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
-        for (int j = j0 + warp; j < j1; j += nwarp) {
+        for (int j = ch.j0 + warp; j < ch.j1; j += nwarp) {
             const int64_t pj = (int64_t)rel[j] * f;
             const T* Uj = U + (int64_t)j * uld;
-            for (int i0 = max(j, ilo) + lane; i0 < ihi; i0 += 128) {
+            for (int i0 = max(j, ch.ilo) + lane; i0 < ch.ihi; i0 += 128) {
                 T u[4];
                 int r[4];
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
                     const int i = i0 + 32 * t;
-                    u[t] = (i < ihi) ? Uj[i] : T(0);
-                    r[t] = (i < ihi) ? rel[i] : 0;
+                    u[t] = (i < ch.ihi) ? Uj[i] : T(0);
+                    r[t] = (i < ch.ihi) ? rel[i] : 0;
                 }
 #pragma unroll
                 for (int t = 0; t < 4; ++t)
-                    if (i0 + 32 * t < ihi) B[r[t] + pj] += u[t];
+                    if (i0 + 32 * t < ch.ihi) B[r[t] + pj] += u[t];
             }
         }
         __syncthreads();
@@ -1888,7 +1883,7 @@ cudaError_t factor_impl(const DevNet& net, const DevFactor& F, const DevWork& W,
         }
         const int na = ls.h_asm_ptr[l + 1] - ls.h_asm_ptr[l];
         if (na > 0) {
-            k_big_assemble<T><<<na, kThreads, 0, st>>>(F, W, gv, lx, ub, ls.d_asm + ls.h_asm_ptr[l]);
+            k_big_assemble<T><<<na, kThreads, 0, st>>>(F, W, gv, lx, ub, ls.d_asm + ls.h_asm_ptr[l], ls.d_asm_child);
             count_launches(1);
             const int nt = tile_flow ? ls.h_tt_ptr[l + 1] - ls.h_tt_ptr[l] : 0;
             if constexpr (sizeof(T) == 4) {

@@ -236,6 +236,20 @@ cudaError_t launch_flat_start(const DevNet& net, const DevWork& w, cudaStream_t 
 // Injections and branch flows at the current state (result download).
 cudaError_t launch_results(const DevNet& net, const DevWork& w, cudaStream_t st);
 
+// A tiled front's assembly block (one CTA): tile column tj and row block rb
+// (kAsmRows rows from the column's first row), the front's gain targets that
+// land in the tile column, [tg_lo, tg_hi), and the children that add entries
+// to the block, [ch_lo, ch_hi) of the AsmChild list, in child order.
+struct AsmItem {
+    int32_t s, tj, rb, tg_lo, tg_hi, ch_lo, ch_hi, pad;
+};
+// One child's part of an assembly block: its update-matrix columns [j0, j1)
+// that land in the tile column and rows [ilo, ihi) that land in the row
+// block (positions in the child's relative map).
+struct AsmChild {
+    int32_t c, j0, j1, ilo, ihi, pad0, pad1, pad2;
+};
+
 // One work item of the FP32 tiled fronts' dataflow factorisation (one
 // persistent launch per synchronous level).  kind 0: the panel solve of
 // chunk a (of b chunks) of step p, aux = the (front, step) pair of the
@@ -260,7 +274,8 @@ struct LevelSchedule {
     const int32_t* d_small = nullptr;       // single-CTA fronts, per level
     const int32_t* h_small_maxf = nullptr;  // [n_levels] largest single-CTA front
     const int32_t* h_asm_ptr = nullptr;     // [n_levels+1] offsets into d_asm
-    const int4* d_asm = nullptr;            // (big front, tile column)
+    const AsmItem* d_asm = nullptr;         // assembly blocks of the big fronts
+    const AsmChild* d_asm_child = nullptr;  // their contributing children
     const int32_t* h_lvl_panels = nullptr;  // [n_levels] panel steps of the level
     const int32_t* h_step_ptr = nullptr;    // [n_levels+1] first step slot of a level
     const int32_t* h_pot_ptr = nullptr;     // [n_slots+1] offsets into d_pot
