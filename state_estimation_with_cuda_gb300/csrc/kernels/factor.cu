@@ -370,6 +370,47 @@ __device__ __forceinline__ void warp_trinv_v4(const float (*lt)[LTLD], const flo
     }
 }
 
+// FP64 form of warp_potrf_bcast for the tiled fronts' diagonal blocks: lane i
+// holds row i in registers, the pivot comes by shuffle and each pivot column
+// goes through the shared buffer, read back two entries per 16-byte load.
+// Every entry on or below the diagonal gets the operations of the FP64
+// shared-memory elimination it replaces (scale by 1 / L_kk, then
+// a_ij -= l_ik l_jk in k order), so the results are the same.
+template <int KP>
+__device__ __forceinline__ bool warp_potrf_bcast(double (&a)[KP], int kb, int lane, double* inv_out, double* col) {
+    static_assert(KP % 2 == 0, "whole double2 groups");
+    bool bad = false;
+    double my_inv = 0.0;
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+        if (k < kb) {
+            double d = __shfl_sync(0xffffffffu, a[k], k);
+            bad |= !(d > 0.0) || !isfinite(d);
+            d = (d > 0.0 && isfinite(d)) ? d : 1.0;
+            double sq, inv;
+            pivot_value(d, &sq, &inv);
+            const double lk = (lane == k) ? sq : (lane > k ? a[k] * inv : a[k]);
+            a[k] = lk;
+            my_inv = (lane == k) ? inv : my_inv;
+            if (k + 1 < KP) {
+                col[lane] = lk;
+                __syncwarp();
+#pragma unroll
+                for (int g = (k + 1) / 2; g < KP / 2; ++g) {
+                    const double2 v = reinterpret_cast<const double2*>(col)[g];
+                    const double w[2] = {v.x, v.y};
+#pragma unroll
+                    for (int q = 0; q < 2; ++q)
+                        if (2 * g + q > k) a[2 * g + q] = a[2 * g + q] - lk * w[q];
+                }
+                __syncwarp();
+            }
+        }
+    }
+    *inv_out = my_inv;
+    return bad;
+}
+
 constexpr int kWarpsPerCta = kThreads / 32;
 constexpr int kWtLd = kWarpFrontMax + 1;
 
@@ -835,19 +876,20 @@ __global__ void __launch_bounds__(kThreads) k_big_assemble(DevFactor F, DevWork 
     }
 }
 
-// FP64 panel step p, part 1 (one CTA per front): one warp factors the
-// diagonal tile through shared memory (a shuffle moves half a double, so the
-// register form is slower for FP64) and writes L_dd back; the other warps
-// solve the rows of tile p below the block (x = a L_dd^-T by forward
-// substitution in registers; volatile reads keep the compiler from hoisting
-// the factor into registers across rows).  k_big_trsm takes the row tiles
-// below on many CTAs; then the trailing update.
+// FP64 panel step p, part 1 (one CTA per front): warp 0 factors the diagonal
+// tile with a row per lane in registers (warp_potrf_bcast) and writes L_dd
+// back; the other warps solve the rows of tile p below the block (only a last
+// block narrower than a tile has any: x = a L_dd^-T by forward substitution in
+// registers; volatile reads keep the compiler from hoisting the factor into
+// registers across rows).  k_big_trsm takes the row tiles below on many CTAs;
+// then the trailing update.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, T* lx, const int4* work, int p) {
     static_assert(sizeof(T) == 8, "FP32 panels use k_big_panel32");
     constexpr int ld = kTile + 1;
     __shared__ T D[kTile * ld];
     __shared__ T rdiag[kTile];
+    __shared__ __align__(16) T colbuf[kTile];
     const int s = work[blockIdx.x].x;
     if (front_frozen(F, W, s)) return;  // the whole CTA, before any barrier
     const int f = F.sn_f[s];
@@ -855,38 +897,30 @@ __global__ void __launch_bounds__(kThreads) k_big_potrf(DevFactor F, DevWork W, 
     T* B = lx + F.sn_lx_off[s];
     const int p0 = p * kTile;
     const int pb = min(kTile, nc - p0);
-    for (int x = threadIdx.x; x < pb * pb; x += blockDim.x) {
-        const int i = x % pb, j = x / pb;
-        D[i + j * ld] = (i >= j) ? B[(p0 + i) + (int64_t)(p0 + j) * f] : T(0);
-    }
-    __syncthreads();
     if (threadIdx.x < 32) {
+        // warp 0: the diagonal block, row i in lane i's registers
         const int i = threadIdx.x;
-        for (int k = 0; k < pb; ++k) {
-            if (i == k) {
-                T sq, inv;
-                pivot(D[k + k * ld], &sq, &inv, singular_flags(F, W, s));
-                D[k + k * ld] = sq;
-                rdiag[k] = inv;
-                reinterpret_cast<T*>(W.rdiag)[F.sn_c0[s] + p0 + k] = inv;
+        T a[kTile];
+#pragma unroll
+        for (int j = 0; j < kTile; ++j) a[j] = (i < pb && j <= i) ? B[(p0 + i) + (int64_t)(p0 + j) * f] : T(0);
+        T inv;
+        const bool bad = warp_potrf_bcast<kTile>(a, pb, i, &inv, colbuf);
+        if (bad && i == 0) atomicOr(singular_flags(F, W, s), FLAG_SINGULAR);
+#pragma unroll
+        for (int j = 0; j < kTile; ++j)
+            if (i < pb && j <= i) {
+                D[i + j * ld] = a[j];
+                B[(p0 + i) + (int64_t)(p0 + j) * f] = a[j];
             }
-            __syncwarp();
-            const T inv = rdiag[k];
-            if (i > k && i < pb) D[i + k * ld] *= inv;
-            __syncwarp();
-            if (i > k && i < pb) {
-                const T lik = D[i + k * ld];
-                for (int j = k + 1; j <= i; ++j) D[i + j * ld] -= lik * D[j + k * ld];
-            }
-            __syncwarp();
+        if (i < pb) {
+            rdiag[i] = inv;
+            reinterpret_cast<T*>(W.rdiag)[F.sn_c0[s] + p0 + i] = inv;
         }
     }
     __syncthreads();
-    if (threadIdx.x < 32) {
-        const int i = threadIdx.x;
-        for (int j = 0; j < pb; ++j)
-            if (i >= j && i < pb) B[(p0 + i) + (int64_t)(p0 + j) * f] = D[i + j * ld];
-    } else {
+    if (threadIdx.x >= 32) {
+        // the rows of tile p below the block (a last block narrower than a
+        // tile): x = a L_dd^-T by forward substitution in registers
         const volatile T* Dv = D;
         const int r_end = min(p0 + kTile, f);
 #pragma unroll 1
