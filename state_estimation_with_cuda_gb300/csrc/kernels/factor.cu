@@ -560,7 +560,7 @@ __device__ void warp_front_factor(const DevFactor& F, const DevWork& W, const T*
 template <typename T>
 struct FrontSmem {
     __align__(16) T lt[kPanel][kPanel + 4];  // lt[c][r] = L11[r][c] of the current panel (16-byte aligned rows)
-    __align__(16) T col[kPanel];             // FP32: pivot column broadcast of warp_potrf_bcast
+    __align__(16) T col[kPanel];             // pivot column broadcast of warp_potrf_bcast
     T rinv[kPanel];                          // 1 / L11[c][c]
 };
 
@@ -602,11 +602,7 @@ __device__ void front_factor(const DevFactor& F, const DevWork& W, const T* gv, 
 #pragma unroll
             for (int j = 0; j < KP; ++j) a[j] = (lane < kb && j <= lane) ? Fm[i + (k0 + j) * ldf] : T(0);
             T my_inv;
-            bool bad;
-            if constexpr (sizeof(T) == 4)
-                bad = warp_potrf_bcast<KP>(a, kb, lane, &my_inv, sm.col);
-            else
-                bad = warp_potrf<T, KP>(a, kb, lane, &my_inv);
+            const bool bad = warp_potrf_bcast<KP>(a, kb, lane, &my_inv, sm.col);
             if (lane < kb) {
                 sm.rinv[lane] = my_inv;
                 rdg[k0 + lane] = my_inv;
