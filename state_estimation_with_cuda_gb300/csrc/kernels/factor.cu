@@ -55,37 +55,6 @@ __global__ void k_gain_values(DevFactor F, DevWork W, const HV* hval, const HV* 
     }
 }
 
-// Pivot: L_kk = sqrt(d) and its reciprocal.  Non-positive or non-finite d
-// flags the gain matrix as not positive definite and continues with 1.
-// FP64: a reciprocal square root seeded in FP32 and refined by two
-// Newton-Raphson steps y <- y (3 - d y^2) / 2 (each step doubles the correct
-// bits: ~24 -> 48 -> 96), which keeps serial FP64 work short on a GPU with
-// few FP64 units; the library routines are used outside the FP32 range.
-__device__ __forceinline__ void pivot(float d, float* sq, float* inv, uint32_t* flags) {
-    if (!(d > 0.f) || !isfinite(d)) {
-        atomicOr(flags, FLAG_SINGULAR);
-        d = 1.f;
-    }
-    *sq = sqrtf(d);
-    *inv = 1.f / *sq;
-}
-__device__ __forceinline__ void pivot(double d, double* sq, double* inv, uint32_t* flags) {
-    if (!(d > 0.0) || !isfinite(d)) {
-        atomicOr(flags, FLAG_SINGULAR);
-        d = 1.0;
-    }
-    if (d > 1e-30 && d < 1e30) {
-        double y = static_cast<double>(rsqrtf(static_cast<float>(d)));
-        y = y * (1.5 - 0.5 * d * y * y);
-        y = y * (1.5 - 0.5 * d * y * y);
-        *sq = d * y;
-        *inv = y;
-    } else {
-        *sq = sqrt(d);
-        *inv = 1.0 / *sq;
-    }
-}
-
 // Where a non-positive pivot of front s is reported: the grid's own flags in
 // a batch, the engine status otherwise.
 __device__ __forceinline__ uint32_t* singular_flags(const DevFactor& F, const DevWork& W, int s) {
@@ -96,7 +65,13 @@ __device__ __forceinline__ bool front_frozen(const DevFactor& F, const DevWork& 
     return W.grid_flags && (W.grid_flags[F.sn_grid[s]] & FLAG_FROZEN);
 }
 
-// L_kk = sqrt(d) and 1 / L_kk for a positive finite d (the caller checks).
+// Pivot: L_kk = sqrt(d) and 1 / L_kk for a positive finite d (the callers
+// flag a non-positive or non-finite d as a matrix that is not positive
+// definite and go on with 1).  FP64: a reciprocal square root seeded in FP32
+// and refined by two Newton-Raphson steps y <- y (3 - d y^2) / 2 (each step
+// doubles the correct bits: ~24 -> 48 -> 96), which keeps serial FP64 work
+// short on a GPU with few FP64 units; the library routines are used outside
+// the FP32 range.
 __device__ __forceinline__ void pivot_value(float d, float* sq, float* inv) {
     const float y = rsqrtf(d);  // the FP32 factor is a preconditioner of FP64 steps
     *sq = d * y;
@@ -228,42 +203,6 @@ __device__ __forceinline__ void store4<double>(double* p, const double (&v)[4]) 
     reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
 }
 
-// Eliminates the first kb columns of the rows held by one warp in registers:
-// lane i owns row i in a[] (entries j <= i, zeros elsewhere); the remaining
-// columns receive the Schur complement update.  Fully unrolled and
-// branch-free (a branch per column, even one always taken, keeps the next
-// step's shuffles from overlapping the pivot chain): the chain from one pivot
-// to the next is a shuffle, a reciprocal square root and two FMAs, and the
-// remaining shuffles and updates of a step overlap with it.  On return a[] is
-// row i of L and *inv_out = 1 / L_ii; returns true if a pivot was not
-// positive and finite (then replaced by 1).
-template <typename T, int KP>
-__device__ __forceinline__ bool warp_potrf(T (&a)[KP], int kb, int lane, T* inv_out) {
-    bool bad = false;
-    T my_inv = T(0);
-#pragma unroll
-    for (int k = 0; k < KP; ++k) {
-        if (k < kb) {
-            T d = __shfl_sync(0xffffffffu, a[k], k);
-            bad |= !(d > T(0)) || !isfinite(d);
-            d = (d > T(0) && isfinite(d)) ? d : T(1);
-            T sq, inv;
-            pivot_value(d, &sq, &inv);
-            const T lk = (lane == k) ? sq : (lane > k ? a[k] * inv : a[k]);
-            a[k] = lk;
-            my_inv = (lane == k) ? inv : my_inv;
-#pragma unroll
-            for (int j = k + 1; j < KP; ++j) {
-                const T ljk = __shfl_sync(0xffffffffu, lk, j);
-                a[j] = (lane >= j) ? a[j] - lk * ljk : a[j];
-            }
-            __syncwarp();
-        }
-    }
-    *inv_out = my_inv;
-    return bad;
-}
-
 // FP32 factors store L11^-1 in each diagonal block's slot, so that the solves
 // multiply by it (independent dot products) instead of sweeping the triangle
 // one column at a time.  FP64 keeps L11 there: at this GPU's FP64 rate the
@@ -271,40 +210,22 @@ __device__ __forceinline__ bool warp_potrf(T (&a)[KP], int kb, int lane, T* inv_
 template <typename T>
 constexpr bool kInvDiag = sizeof(T) == 4;
 
-// Inverse of a kb x kb lower-triangular block held in shared memory as
-// lt[c][r] = L[r][c] (r > c) with reciprocal diagonal rinv: lane j forms
-// column j of L^-1 = L^-1 e_j by the same right-looking substitution as the
-// panel's row solve (a chain of kb multiply/FMA steps; the updates of a step
-// are independent) and writes rows i >= j to dst[i + j * ld].
-template <typename T, int KP, int LTLD>
-__device__ __forceinline__ void warp_trinv(const T (*lt)[LTLD], const T* rinv, int kb, int lane, T* dst, int ld) {
-    T x[KP];
-#pragma unroll
-    for (int i = 0; i < KP; ++i) x[i] = (i == lane) ? T(1) : T(0);
-#pragma unroll
-    for (int c = 0; c < KP; ++c) {
-        if (c < kb) {
-            x[c] *= rinv[c];
-#pragma unroll
-            for (int c2 = c + 1; c2 < KP; ++c2) x[c2] -= x[c] * lt[c][c2];
-        }
-    }
-    if (lane < kb) {
-#pragma unroll
-        for (int i = 0; i < KP; ++i)
-            if (i >= lane && i < kb) dst[i + lane * ld] = x[i];
-    }
-}
-
-// FP32 forms of warp_potrf / warp_trinv for one warp that owns a 16-byte
-// aligned shared buffer, used on the tiled fronts' critical path (the 32 x 32
-// diagonal blocks).  Every entry on or below the diagonal gets the same
-// operations in the same order as in warp_potrf / warp_trinv, so the results
-// are identical; only the data movement differs: pivot column k is written
-// to col[] once and read back four entries per broadcast load instead of by
-// 31 - k shuffles, and the entries above the diagonal are left unmasked (a
-// lane reads col[j] only for j > k, written by lane j, whose value there is
-// an entry of L; the entries above the diagonal are never written out).
+// Diagonal blocks in one warp's registers.  warp_potrf_bcast eliminates the
+// first kb columns of the rows the warp holds: lane i owns row i in a[]
+// (entries j <= i; zeros elsewhere); the remaining columns receive the Schur
+// complement update.  Per pivot k the pivot comes by shuffle, lanes below
+// scale their entry by 1 / L_kk, and every entry a_ij, k < j <= i, gets
+// a_ij -= l_ik l_jk, the column l_jk broadcast through the 16-byte-aligned
+// shared buffer col[] (four FP32 or two FP64 entries per load).  Entries
+// above the diagonal are left unmasked: a lane reads col[j] only for j > k,
+// written by lane j, whose value there is an entry of L, and the entries
+// above the diagonal are never written out.  Fully unrolled and branch-free
+// (a branch per column, even one always taken, keeps the next step's loads
+// from overlapping the pivot chain).  On return a[] is row i of L and
+// *inv_out = 1 / L_ii; returns true if a pivot was not positive and finite
+// (then replaced by 1).  warp_trinv_v4 forms L^-1 one column per lane
+// (L^-1 e_j by right-looking substitution, its rows read four at a time) and
+// writes rows i >= j to dst[i + j * ld].
 template <int KP>
 __device__ __forceinline__ bool warp_potrf_bcast(float (&a)[KP], int kb, int lane, float* inv_out, float* col) {
     static_assert(KP % 4 == 0, "whole float4 groups");
@@ -370,12 +291,7 @@ __device__ __forceinline__ void warp_trinv_v4(const float (*lt)[LTLD], const flo
     }
 }
 
-// FP64 form of warp_potrf_bcast for the tiled fronts' diagonal blocks: lane i
-// holds row i in registers, the pivot comes by shuffle and each pivot column
-// goes through the shared buffer, read back two entries per 16-byte load.
-// Every entry on or below the diagonal gets the operations of the FP64
-// shared-memory elimination it replaces (scale by 1 / L_kk, then
-// a_ij -= l_ik l_jk in k order), so the results are the same.
+// FP64 form of warp_potrf_bcast (two entries per 16-byte load).
 template <int KP>
 __device__ __forceinline__ bool warp_potrf_bcast(double (&a)[KP], int kb, int lane, double* inv_out, double* col) {
     static_assert(KP % 2 == 0, "whole double2 groups");
