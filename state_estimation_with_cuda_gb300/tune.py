@@ -30,12 +30,14 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 TUNED = os.path.join(HERE, "tuned.json")
 
-BATCH_WIDTHS = (32, 64, 96)
+BATCH_WIDTHS = (32, 64, 96, 128)
 SERVE_CANDIDATES = (
     {"bucket_bus": (300, 2000, 20000, 0), "own_unit_bus": 1 << 30},
     {"bucket_bus": (300, 2000, 0, 0), "own_unit_bus": 1 << 30},
     {"bucket_bus": (300, 2000, 20000, 80000), "own_unit_bus": 1 << 30},
     {"bucket_bus": (500, 5000, 50000, 0), "own_unit_bus": 1 << 30},
+    {"bucket_bus": (500, 5000, 0, 0), "own_unit_bus": 1 << 30},
+    {"bucket_bus": (300, 2000, 10000, 50000), "own_unit_bus": 1 << 30},
     {"bucket_bus": (300, 2000, 20000, 0), "own_unit_bus": 100000},
 )
 
