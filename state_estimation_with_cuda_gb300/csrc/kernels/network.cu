@@ -200,9 +200,32 @@ __device__ __forceinline__ void put_flow(double* hrow, int fpos, const double d[
 }
 
 // a3/a6/a7/a8/a9 fused: one thread per measurement row.
+// H entries of a warp's 32 consecutive rows (a contiguous range of the CSR
+// values) staged in shared memory by k_evaluate.
+constexpr int kEvalSpan = 512;
+
 __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, SolveParams sp) {
     __shared__ double sh[32];
+    // A warp's rows own the contiguous H range [hw0, hw1).  When it fits,
+    // each row is built in shared memory and the warp writes the range out
+    // coalesced (H in FP64, FP32 and weighted), skipping rows it did not
+    // evaluate; otherwise each thread writes its own row in place.
+    __shared__ double hs[kBlock / 32][kEvalSpan];
+    __shared__ uint16_t hlane[kBlock / 32][kEvalSpan];
+    __shared__ double wes[kBlock / 32][32];
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int qw0 = q - lane;
+    const int hw0 = qw0 < net.n_meas ? net.h_ptr[qw0] : 0;
+    const int hw1 = qw0 < net.n_meas ? net.h_ptr[min(qw0 + 32, net.n_meas)] : 0;
+    const bool staged = hw1 - hw0 <= kEvalSpan;  // warp-uniform
+    if (staged) {
+        for (int x = lane; x < hw1 - hw0; x += 32) {
+            hs[warp][x] = 0.0;
+            hlane[warp][x] = 0xFFFF;  // not evaluated: left as it is
+        }
+        __syncwarp();
+    }
     double obj = 0.0, hub = 0.0;
     bool skip = false;
     if (q < net.n_meas && net.meas_grid) {
@@ -216,8 +239,12 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
         const bool exact = sp.exact_jacobian != 0;
         const int base = net.h_ptr[q];
         const int nh = net.h_ptr[q + 1] - base;
-        double* hrow = w.hval + base;
-        for (int x = 0; x < nh; ++x) hrow[x] = 0.0;
+        double* hrow = staged ? &hs[warp][base - hw0] : w.hval + base;
+        if (staged) {
+            for (int x = 0; x < nh; ++x) hlane[warp][base - hw0 + x] = static_cast<uint16_t>(lane);
+        } else {
+            for (int x = 0; x < nh; ++x) hrow[x] = 0.0;
+        }
         double hv = 0.0;
         if (kind == 0) {  // V_MAG
             hv = w.v[loc];
@@ -299,7 +326,7 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
             }
             put_flow(hrow, net.m_fpos[q], d);
         }
-        if (sp.mixed)
+        if (sp.mixed && !staged)
             for (int x = 0; x < nh; ++x) w.hval32[base + x] = static_cast<float>(hrow[x]);
         double rr = 0.0, we = 0.0;
         if (kind != 5) {
@@ -324,10 +351,27 @@ __global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, Solv
         w.w_eff[q] = we;
         w.wr[q] = we * rr;
         // weighted H entries for the gain sums G_ij = sum (w h_a) h_b
-        if (sp.mixed && w.hw32) {
+        if (staged) {
+            wes[warp][lane] = we;
+        } else if (sp.mixed && w.hw32) {
             for (int x = 0; x < nh; ++x) w.hw32[base + x] = static_cast<float>(we * hrow[x]);
         } else if (!sp.mixed && w.hw) {
             for (int x = 0; x < nh; ++x) w.hw[base + x] = we * hrow[x];
+        }
+    }
+    if (staged) {
+        __syncwarp();
+        for (int x = lane; x < hw1 - hw0; x += 32) {
+            const int r = hlane[warp][x];
+            if (r == 0xFFFF) continue;
+            const double v = hs[warp][x];
+            w.hval[hw0 + x] = v;
+            if (sp.mixed) {
+                w.hval32[hw0 + x] = static_cast<float>(v);
+                if (w.hw32) w.hw32[hw0 + x] = static_cast<float>(wes[warp][r] * v);
+            } else if (w.hw) {
+                w.hw[hw0 + x] = wes[warp][r] * v;
+            }
         }
     }
     const double s = block_sum(obj, sh);
