@@ -611,6 +611,8 @@ int32_t Engine::upload() {
         net_.br_b = c.take<double>(nbr);
         net_.br_bsf = c.take<double>(nbr);
         net_.br_bst = c.take<double>(nbr);
+        net_.br_itap = c.take<double>(nbr);
+        net_.br_itap2 = c.take<double>(nbr);
         net_.y_ptr = c.take<int32_t>(n + 1);
         net_.y_col = c.take<int32_t>(nnz_y);
         net_.y_src = c.take<int32_t>(nnz_y);

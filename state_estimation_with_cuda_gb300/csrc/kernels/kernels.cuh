@@ -50,6 +50,8 @@ struct DevNet {
     double* br_b;
     double* br_bsf;
     double* br_bst;
+    double* br_itap;  // 1 / max(tap, eps) and its square, for the flow rows (no FP64 division per row)
+    double* br_itap2;
     // Ybus
     const int32_t* y_ptr;
     const int32_t* y_col;

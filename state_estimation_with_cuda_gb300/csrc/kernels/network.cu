@@ -54,6 +54,9 @@ __global__ void k_admittance(DevNet net) {
     net.br_b[k] = -x / den;
     net.br_bsf[k] = bt / (2.0 * a * a);
     net.br_bst[k] = bt / 2.0;
+    const double A = fmax(a, kEps), ia = 1.0 / A;
+    net.br_itap[k] = ia;
+    net.br_itap2[k] = 1.0 / (A * A);
 }
 
 // a2: Ybus values on the canonical pattern, one thread per bus row; the
@@ -104,22 +107,23 @@ __device__ FlowTerms flow_terms_sc(const DevNet& net, const double* v, int k, bo
     const int i = net.br_from[k], j = net.br_to[k];
     const double Vi = v[i], Vj = v[j];
     const double g = net.br_g[k], b = net.br_b[k];
-    const double A = fmax(net.br_tap[k], kEps);
-    const double inv = 1.0 / A, a2 = A * A;
+    // 1 / a and 1 / a^2 of the tap a (clamped as the reference clamps it),
+    // computed once per branch: the rows multiply instead of dividing
+    const double inv = net.br_itap[k], ia2 = net.br_itap2[k];
     const double on = net.br_closed[k] ? 1.0 : 0.0;
     const double vv = Vi * Vj * inv;
     FlowTerms f;
     if (!is_q && !to_end) {
-        f.val = Vi * Vi / a2 * g - vv * (g * c + b * s);
+        f.val = Vi * Vi * ia2 * g - vv * (g * c + b * s);
         f.d[0] = vv * (g * s - b * c);
-        f.d[1] = 2.0 * Vi / a2 * g - Vj * inv * (g * c + b * s);
+        f.d[1] = 2.0 * Vi * ia2 * g - Vj * inv * (g * c + b * s);
         f.d[2] = -f.d[0];
         f.d[3] = -Vi * inv * (g * c + b * s);
     } else if (is_q && !to_end) {
         const double bsf = net.br_bsf[k];
-        f.val = -(Vi * Vi / a2) * (b + bsf) - vv * (g * s - b * c);
+        f.val = -(Vi * Vi * ia2) * (b + bsf) - vv * (g * s - b * c);
         f.d[0] = -vv * (g * c + b * s);
-        f.d[1] = (exact ? -2.0 * Vi * (b + bsf) / a2 : -2.0 * Vi * b / a2) - Vj * inv * (g * s - b * c);
+        f.d[1] = (exact ? -2.0 * Vi * (b + bsf) * ia2 : -2.0 * Vi * b * ia2) - Vj * inv * (g * s - b * c);
         f.d[2] = -f.d[0];
         f.d[3] = -Vi * inv * (g * s - b * c);
     } else if (!is_q && to_end) {
