@@ -74,6 +74,12 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
  *                           reweighting creeps when gross errors sit on
  *                           critical measurement pairs, whose Huber objective
  *                           is nearly flat along the states they alone fix
+ *   "eval_pair_rows"        evaluation: from this many measurement rows on
+ *                           (default 262144), a P injection or flow row and
+ *                           its Q twin (same bus, or same branch end) are
+ *                           evaluated by one thread, sharing their angle and
+ *                           admittance terms; below it every row has its own
+ *                           thread (re-uploads)
  *   "tile_flow"             mixed pipeline: 1 factorises the tiled fronts
  *                           of each synchronous level in one persistent
  *                           dataflow launch (panel chunks and update tiles

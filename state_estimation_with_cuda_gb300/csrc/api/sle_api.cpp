@@ -1188,6 +1188,10 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExSetOption(SLE_Handle handle, const char* k
     } else if (k == "huber_stall") {
         if (!(value >= 0.0 && value < 1.0)) return fail(SLE_ERROR_INVALID_ARGUMENT, "huber_stall must be in [0, 1)");
         c.huber_stall = value;
+    } else if (k == "eval_pair_rows") {
+        if (!(value >= 0.0 && value <= 2.0e9)) return fail(SLE_ERROR_INVALID_ARGUMENT, "eval_pair_rows must be >= 0");
+        c.eval_pair_rows = static_cast<int32_t>(value);
+        E(handle)->model.structure_dirty = true;  // taken at the next upload
     } else if (k == "tile_flow") {
         c.tile_flow = value != 0.0 ? 1 : 0;
         E(handle)->model.structure_dirty = true;  // taken at the next upload

@@ -53,6 +53,7 @@ struct EngineConfig {
     double huber_stall = 0.0;        // robust solves: also stop when the Huber objective falls by no more
                                      // than this fraction in an iteration (0: the reference's test only)
     int32_t hold_front = -1;         // test hook: front whose backward-sweep completion is withheld
+    int32_t eval_pair_rows = 1 << 18;  // evaluation: a P row and its Q twin share one thread from this many rows
     int32_t tile_flow = 0;           // FP32 tiled fronts: 1 = one dataflow launch per level; 0 = a panel and
                                      // an update launch per step (faster on the measured grids)
     int32_t device_loop = 1;         // batch solves: Gauss-Newton loop in a conditional graph node (needs
@@ -264,6 +265,8 @@ private:
         sch_pot_ptr_, sch_pan_ptr_, sch_upd_ptr_, sch_all_ptr_, sch_all_, sch_maxf_;
     std::vector<int4> sch_pot_, sch_pan_, sch_upd_;
     std::vector<AsmItem> sch_asm_;
+    std::vector<int2> ev_unit_, ev_grp_;  // evaluation units (DevNet::ev_unit / ev_grp)
+    void build_eval_units();
     std::vector<AsmChild> sch_asm_child_;
     // FP32 tiled fronts as dataflow items (TileTask), per level
     std::vector<TileTask> sch_tt_;

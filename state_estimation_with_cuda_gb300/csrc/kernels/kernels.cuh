@@ -75,6 +75,13 @@ struct DevNet {
     const int32_t* h_pcol;   // column of each H entry in the permuted state order
     const int32_t* meas_grid;  // batch: grid of each measurement row (nullptr for one grid)
     const int32_t* bus_grid;   // batch: grid of each bus (nullptr for one grid)
+    // Evaluation units: a row alone, or a P row with its Q twin (same bus,
+    // or same branch end), (first row, twin or -1), in row order; per 32
+    // units the row range [lo, hi) they cover when it is contiguous
+    // (lo = -1 otherwise).
+    const int2* ev_unit;
+    const int2* ev_grp;
+    int32_t n_units;
 };
 
 // Factorisation plan (device).

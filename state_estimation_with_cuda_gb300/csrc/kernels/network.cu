@@ -204,11 +204,282 @@ __device__ __forceinline__ void put_flow(double* hrow, int fpos, const double d[
 }
 
 // a3/a6/a7/a8/a9 fused: one thread per measurement row.
-// H entries of a warp's 32 consecutive rows (a contiguous range of the CSR
-// values) staged in shared memory by k_evaluate.
+// P and Q flow at one end of branch k from the same angle difference: the
+// two rows' values and derivatives with the expressions of flow_terms_sc.
+__device__ __forceinline__ void flow_terms_pq(const DevNet& net, const double* v, int k, bool to_end, bool exact,
+                                              double s, double c, FlowTerms& P, FlowTerms& Q) {
+    const int i = net.br_from[k], j = net.br_to[k];
+    const double Vi = v[i], Vj = v[j];
+    const double g = net.br_g[k], b = net.br_b[k];
+    const double inv = net.br_itap[k], ia2 = net.br_itap2[k];
+    const double on = net.br_closed[k] ? 1.0 : 0.0;
+    const double vv = Vi * Vj * inv;
+    if (!to_end) {
+        P.val = Vi * Vi * ia2 * g - vv * (g * c + b * s);
+        P.d[0] = vv * (g * s - b * c);
+        P.d[1] = 2.0 * Vi * ia2 * g - Vj * inv * (g * c + b * s);
+        P.d[2] = -P.d[0];
+        P.d[3] = -Vi * inv * (g * c + b * s);
+        const double bsf = net.br_bsf[k];
+        Q.val = -(Vi * Vi * ia2) * (b + bsf) - vv * (g * s - b * c);
+        Q.d[0] = -vv * (g * c + b * s);
+        Q.d[1] = (exact ? -2.0 * Vi * (b + bsf) * ia2 : -2.0 * Vi * b * ia2) - Vj * inv * (g * s - b * c);
+        Q.d[2] = -Q.d[0];
+        Q.d[3] = -Vi * inv * (g * s - b * c);
+    } else {
+        P.val = Vj * Vj * g - vv * (g * c - b * s);
+        P.d[0] = exact ? vv * (g * s + b * c) : vv * (-g * s - b * c);
+        P.d[1] = -Vj * inv * (g * c - b * s);
+        P.d[2] = -P.d[0];
+        P.d[3] = 2.0 * Vj * g - Vi * inv * (g * c - b * s);
+        const double bst = net.br_bst[k];
+        Q.val = -Vj * Vj * (b + bst) + vv * (g * s + b * c);
+        Q.d[0] = vv * (g * c - b * s);
+        Q.d[1] = Vj * inv * (g * s + b * c);
+        Q.d[2] = -Q.d[0];
+        Q.d[3] = (exact ? -2.0 * Vj * (b + bst) : -2.0 * Vj * b) + Vi * inv * (g * s + b * c);
+    }
+    P.val *= on;
+    Q.val *= on;
+    if (exact) {
+        for (int x = 0; x < 4; ++x) {
+            P.d[x] *= on;
+            Q.d[x] *= on;
+        }
+    }
+}
+
+// H entries of a warp's rows (a contiguous range of the CSR values) staged
+// in shared memory by k_evaluate.
 constexpr int kEvalSpan = 512;
 
-__global__ void __launch_bounds__(kBlock) k_evaluate(DevNet net, DevWork w, SolveParams sp) {
+// a3/a6/a7/a8/a9 fused, one thread per evaluation unit (one row, or a P row
+// and its Q twin): h(x), the H row values, the residual, the (Huber) weight,
+// the FP32 and weighted copies of the H row, and per-block partials of the
+// objective.  A warp's 32 units cover a contiguous range of rows whenever
+// the rows come in order (the usual case); their H entries are then built in
+// shared memory and the warp writes the range out coalesced, skipping rows
+// it does not evaluate.  Otherwise each thread writes its rows in place.
+__global__ void __launch_bounds__(kBlock) k_evaluate_pairs(DevNet net, DevWork w, SolveParams sp) {
+    __shared__ double sh[32];
+    __shared__ double hs[kBlock / 32][kEvalSpan];
+    __shared__ uint8_t hrow_id[kBlock / 32][kEvalSpan];  // row - lo of each entry; 0xFF = not evaluated
+    __shared__ double wes[kBlock / 32][64];
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gidx = u >> 5;
+    const int2 grp = (u - lane) < net.n_units ? net.ev_grp[gidx] : make_int2(-1, -1);
+    const int hw0 = grp.x >= 0 ? net.h_ptr[grp.x] : 0;
+    const int hw1 = grp.x >= 0 ? net.h_ptr[grp.y] : 0;
+    const bool staged = grp.x >= 0 && hw1 - hw0 <= kEvalSpan && grp.y - grp.x <= 64;  // warp-uniform
+    if (staged) {
+        for (int x = lane; x < hw1 - hw0; x += 32) {
+            hs[warp][x] = 0.0;
+            hrow_id[warp][x] = 0xFF;
+        }
+        __syncwarp();
+    }
+    double obj = 0.0, hub = 0.0;
+    const int2 un = u < net.n_units ? net.ev_unit[u] : make_int2(-1, -1);
+    bool skip = un.x < 0;
+    if (!skip && net.meas_grid) {
+        const uint32_t gf = w.grid_flags[net.meas_grid[un.x]];
+        skip = (gf & sp.skip_flags) || (gf & sp.need_flags) != sp.need_flags;
+    }
+    const bool exact = sp.exact_jacobian != 0;
+    // the H row of row q: in the warp's staged range or in place (zeroed)
+    auto row_of = [&](int q) -> double* {
+        const int base = net.h_ptr[q], nh = net.h_ptr[q + 1] - base;
+        if (staged) {
+            for (int x = 0; x < nh; ++x) hrow_id[warp][base - hw0 + x] = static_cast<uint8_t>(q - grp.x);
+            return &hs[warp][base - hw0];
+        }
+        double* hrow = w.hval + base;
+        for (int x = 0; x < nh; ++x) hrow[x] = 0.0;
+        return hrow;
+    };
+    // residual, weight, outputs and objective of row q with value hv
+    auto finish = [&](int q, int kind, double hv, const double* hrow) {
+        const int base = net.h_ptr[q], nh = net.h_ptr[q + 1] - base;
+        if (sp.mixed && !staged)
+            for (int x = 0; x < nh; ++x) w.hval32[base + x] = static_cast<float>(hrow[x]);
+        double rr = 0.0, we = 0.0;
+        if (kind != 5) {
+            rr = w.z[q] - hv;
+            const double wb = net.m_w[q];
+            we = wb;
+            if (sp.robust) {  // kernels.cu:634-671
+                const double sg = net.m_sigma[q];
+                const double rn = fabs(rr / sg);
+                if (!(rn <= sp.huber_gamma)) we = sp.huber_gamma / (sg * fabs(rr) + kEps);
+            }
+            obj += wb * rr * rr;
+            if (sp.huber_objective) {  // rho(u) = u^2 / 2 inside gamma, gamma |u| - gamma^2 / 2 outside
+                const double uu = fabs(rr) / fmax(net.m_sigma[q], kEps);
+                hub += (uu <= sp.huber_gamma) ? 0.5 * uu * uu
+                                              : sp.huber_gamma * uu - 0.5 * sp.huber_gamma * sp.huber_gamma;
+            }
+        } else {
+            hv = 0.0;
+        }
+        w.h[q] = hv;
+        w.r[q] = rr;
+        w.w_eff[q] = we;
+        w.wr[q] = we * rr;
+        // weighted H entries for the gain sums G_ij = sum (w h_a) h_b
+        if (staged) {
+            wes[warp][q - grp.x] = we;
+        } else if (sp.mixed && w.hw32) {
+            for (int x = 0; x < nh; ++x) w.hw32[base + x] = static_cast<float>(we * hrow[x]);
+        } else if (!sp.mixed && w.hw) {
+            for (int x = 0; x < nh; ++x) w.hw[base + x] = we * hrow[x];
+        }
+    };
+    if (!skip) {
+        const int qa = un.x, qb = un.y;
+        const int kind = net.m_kind[qa];
+        const int ty = net.m_type[qa];
+        const int loc = net.m_loc[qa];
+        if (kind == 0) {  // V_MAG
+            double* hrow = row_of(qa);
+            hrow[0] = 1.0;
+            finish(qa, kind, w.v[loc], hrow);
+        } else if (kind == 1) {  // V_ANGLE
+            double* hrow = row_of(qa);
+            if (net.h_ptr[qa + 1] > net.h_ptr[qa]) hrow[0] = 1.0;
+            finish(qa, kind, w.th[loc], hrow);
+        } else if (kind == 2) {  // P/Q injection or pseudo; with its twin when qb >= 0
+            // slot 0: the P row, slot 1: the Q row (either may be absent)
+            const bool a_is_q = (ty == 3 || ty == 8);
+            const int qp = a_is_q ? qb : qa, qq = a_is_q ? qa : qb;
+            double* hp = qp >= 0 ? row_of(qp) : nullptr;
+            double* hq = qq >= 0 ? row_of(qq) : nullptr;
+            const double Vi = w.v[loc];
+            const double2 cs_i = w.bus_cs[loc];
+            double hvp = 0.0, dVip = 0.0, dTip = 0.0, hvq = 0.0, dViq = 0.0, dTiq = 0.0;
+            const int e0 = net.y_ptr[loc], e1 = net.y_ptr[loc + 1];
+            for (int e = e0; e < e1; ++e) {
+                const int j = net.y_col[e];
+                const double G = net.y_g[e], B = net.y_b[e];
+                if (j == loc) {
+                    hvp += Vi * Vi * G;
+                    dVip += 2.0 * Vi * G;
+                    if (!exact) dTip += Vi * Vi * B;
+                    hvq -= Vi * Vi * B;
+                    dViq -= 2.0 * Vi * B;
+                    if (!exact) dTiq += Vi * Vi * G;
+                } else {
+                    const double Vj = w.v[j];
+                    double sn, cn;
+                    angle_diff(cs_i, w.bus_cs[j], &sn, &cn);
+                    const double gcbs = G * cn + B * sn, gsbc = G * sn - B * cn;
+                    const int pt = net.y_hpos_t[e], pv = net.y_hpos_v[e];
+                    if (hp) {
+                        hvp += Vi * Vj * gcbs;
+                        dVip += Vj * gcbs;
+                        dTip -= Vi * Vj * gsbc;
+                        if (pt >= 0) hp[pt] += Vi * Vj * gsbc;
+                        hp[pv] += Vi * gcbs;
+                    }
+                    if (hq) {
+                        hvq += Vi * Vj * gsbc;
+                        dViq += Vj * gsbc;
+                        dTiq += Vi * Vj * gcbs;
+                        if (pt >= 0) hq[pt] += -Vi * Vj * gcbs;
+                        hq[pv] += Vi * gsbc;
+                    }
+                }
+            }
+            const int pt = net.y_hpos_t[e0], pv = net.y_hpos_v[e0];
+            if (hp) {
+                if (pt >= 0) hp[pt] += dTip;
+                hp[pv] += dVip;
+                finish(qp, kind, hvp, hp);
+            }
+            if (hq) {
+                if (pt >= 0) hq[pt] += dTiq;
+                hq[pv] += dViq;
+                finish(qq, kind, hvq, hq);
+            }
+        } else if (kind == 3) {  // P/Q flow; with its twin at the same end when qb >= 0
+            const bool to_end = net.m_end[qa] != 0;
+            if (qb < 0) {
+                double* hrow = row_of(qa);
+                const FlowTerms f = flow_terms_cs(net, w.v, w.bus_cs, loc, ty == 5, to_end, exact);
+                put_flow(hrow, net.m_fpos[qa], f.d);
+                finish(qa, kind, f.val, hrow);
+            } else {
+                const bool a_is_q = ty == 5;
+                const int qp = a_is_q ? qb : qa, qq = a_is_q ? qa : qb;
+                double sn, cn;
+                branch_angle(net, w.bus_cs, loc, &sn, &cn);
+                FlowTerms fp, fq;
+                flow_terms_pq(net, w.v, loc, to_end, exact, sn, cn, fp, fq);
+                double* hp = row_of(qp);
+                put_flow(hp, net.m_fpos[qp], fp.d);
+                finish(qp, kind, fp.val, hp);
+                double* hq = row_of(qq);
+                put_flow(hq, net.m_fpos[qq], fq.d);
+                finish(qq, kind, fq.val, hq);
+            }
+        } else if (kind == 4) {  // current magnitude
+            double* hrow = row_of(qa);
+            const bool to_end = net.m_end[qa] != 0;
+            const FlowTerms fp = flow_terms_cs(net, w.v, w.bus_cs, loc, false, to_end, exact);
+            const int ib = to_end ? net.br_to[loc] : net.br_from[loc];
+            const double ve = w.v[ib];
+            const double vs = fmax(ve, kEps);
+            const double on = net.br_closed[loc] ? 1.0 : 0.0;
+            double d[4];
+            double hv;
+            if (!exact) {  // the reference reuses the P-flow derivatives
+                const FlowTerms fq = flow_terms_cs(net, w.v, w.bus_cs, loc, true, to_end, exact);
+                hv = sqrt(fp.val * fp.val + fq.val * fq.val) / vs * on;
+                for (int x = 0; x < 4; ++x) d[x] = fp.d[x];
+            } else {
+                const FlowTerms fq = flow_terms_cs(net, w.v, w.bus_cs, loc, true, to_end, exact);
+                const double S = sqrt(fp.val * fp.val + fq.val * fq.val);
+                hv = S / vs * on;
+                for (int x = 0; x < 4; ++x)
+                    d[x] = (S > 0.0) ? (fp.val * fp.d[x] + fq.val * fq.d[x]) / (S * vs) * on : 0.0;
+                if (ve > kEps) d[to_end ? 3 : 1] -= S / (vs * vs) * on;
+            }
+            put_flow(hrow, net.m_fpos[qa], d);
+            finish(qa, kind, hv, hrow);
+        } else {
+            double* hrow = row_of(qa);
+            finish(qa, kind, 0.0, hrow);
+        }
+    }
+    if (staged) {
+        __syncwarp();
+        for (int x = lane; x < hw1 - hw0; x += 32) {
+            const int r = hrow_id[warp][x];
+            if (r == 0xFF) continue;
+            const double v = hs[warp][x];
+            w.hval[hw0 + x] = v;
+            if (sp.mixed) {
+                w.hval32[hw0 + x] = static_cast<float>(v);
+                if (w.hw32) w.hw32[hw0 + x] = static_cast<float>(wes[warp][r] * v);
+            } else if (w.hw) {
+                w.hw[hw0 + x] = wes[warp][r] * v;
+            }
+        }
+    }
+    const double s = block_sum(obj, sh);
+    if (threadIdx.x == 0) w.part[blockIdx.x] = s;
+    if (sp.huber_objective) {
+        __syncthreads();  // sh is reused
+        const double hs2 = block_sum(hub, sh);
+        if (threadIdx.x == 0) w.hpart[blockIdx.x] = hs2;
+    }
+}
+
+// a3/a6/a7/a8/a9 fused, one thread per measurement row (the form for
+// evaluations with no paired rows: twice the threads of k_evaluate_pairs,
+// which a small grid needs to fill the GPU).
+
+__global__ void __launch_bounds__(kBlock) k_evaluate_rows(DevNet net, DevWork w, SolveParams sp) {
     __shared__ double sh[32];
     // A warp's rows own the contiguous H range [hw0, hw1).  When it fits,
     // each row is built in shared memory and the warp writes the range out
@@ -491,13 +762,15 @@ __global__ void __launch_bounds__(kBlock) k_objective_part(DevNet net, DevWork w
     }
 }
 
-__global__ void k_objective(DevNet net, DevWork w, int nblk) {
+// nblk: blocks of k_objective_part (rows); nblk_eval: blocks of the last
+// k_evaluate (evaluation units), whose objective partials are summed.
+__global__ void k_objective(DevNet net, DevWork w, int nblk, int nblk_eval) {
     __shared__ double sh[32];
     __shared__ double sb[1024];
     __shared__ int si[1024];
     __shared__ int sc[1024];
     double acc = 0.0;
-    for (int b = threadIdx.x; b < nblk; b += blockDim.x) acc += w.part[b];
+    for (int b = threadIdx.x; b < nblk_eval; b += blockDim.x) acc += w.part[b];
     const double tot = block_sum(acc, sh);
     double best = -1.0;
     int bidx = 0x7fffffff, cnt = 0;
@@ -927,10 +1200,14 @@ cudaError_t launch_admittance_and_ybus(const DevNet& net, cudaStream_t st) {
 cudaError_t launch_evaluate(const DevNet& net, const DevWork& w, const SolveParams& sp, cudaStream_t st) {
     if (net.n_meas <= 0) return cudaSuccess;
     k_bus_trig<<<nblocks(net.n_bus), kBlock, 0, st>>>(net, w, sp);
-    k_evaluate<<<nblocks(net.n_meas), kBlock, 0, st>>>(net, w, sp);
+    // the unit list has as many units as rows when no row is paired
+    if (net.n_units < net.n_meas)
+        k_evaluate_pairs<<<nblocks(net.n_units), kBlock, 0, st>>>(net, w, sp);
+    else
+        k_evaluate_rows<<<nblocks(net.n_meas), kBlock, 0, st>>>(net, w, sp);
     count_launches(2);
     if (sp.huber_objective) {
-        k_huber_objective<<<1, 1024, 0, st>>>(w, nblocks(net.n_meas));
+        k_huber_objective<<<1, 1024, 0, st>>>(w, nblocks(net.n_units));
         count_launches(1);
     }
     return cudaGetLastError();
@@ -942,7 +1219,7 @@ cudaError_t launch_objective(const DevNet& net, const DevWork& w, double bad_thr
         k_objective_part<<<nb, kBlock, 0, st>>>(net, w, bad_threshold);
         count_launches(1);
     }
-    k_objective<<<1, 1024, 0, st>>>(net, w, nb);
+    k_objective<<<1, 1024, 0, st>>>(net, w, nb, net.n_units > 0 ? nblocks(net.n_units) : 0);
     count_launches(1);
     return cudaGetLastError();
 }

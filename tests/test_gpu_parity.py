@@ -42,8 +42,10 @@ def grid(name):
     return workloads.make(name)
 
 
-def engine(g):
+def engine(g, **options):
     e = Estimator()
+    for k, v in options.items():
+        e.set_option(k, v)
     e.load_network(g)
     e.upload_model()
     return e
@@ -74,6 +76,35 @@ def test_measurement_function_and_jacobian(name, exact):
     assert np.allclose(got["h_val"], ref["h_val"], rtol=1e-12, atol=1e-12 * scale)
     rs = np.abs(ref["rhs"]).max()
     assert np.allclose(got["rhs"], ref["rhs"], rtol=1e-10, atol=1e-10 * rs)
+
+
+@pytest.mark.parametrize("name", ["grid14", "grid2k"])
+@pytest.mark.parametrize("exact", [True, False])
+def test_paired_evaluation_matches_oracle(name, exact):
+    """P rows evaluated with their Q twins (one thread per pair, shared angle
+    and admittance terms; the default from 2^18 rows on), forced here on small
+    grids: the same h(x), H and gradient as the oracle, and as the row-per-
+    thread evaluation within rounding."""
+    g = grid(name)
+    e, e1, o = engine(g, eval_pair_rows=0), engine(g), Oracle(g)
+    v, th = synthetic_state(g)
+    got = e.evaluate_at(v, th, exact=exact)
+    single = e1.evaluate_at(v, th, exact=exact)
+    ref = o.evaluate(v, th, g.z, exact=exact)
+    assert np.array_equal(got["h_ptr"], ref["h_ptr"]) and np.array_equal(got["h_col"], ref["h_col"])
+    assert np.allclose(got["hx"], ref["hx"], rtol=1e-12, atol=1e-12)
+    scale = np.abs(ref["h_val"]).max()
+    assert np.allclose(got["h_val"], ref["h_val"], rtol=1e-12, atol=1e-12 * scale)
+    assert np.allclose(got["h_val"], single["h_val"], rtol=1e-14, atol=1e-14 * scale)
+    rs = np.abs(ref["rhs"]).max()
+    assert np.allclose(got["rhs"], ref["rhs"], rtol=1e-10, atol=1e-10 * rs)
+    rc, res = e.solve_with(max_iterations=20, tolerance=1e-6, flat_start=True)
+    ov, oth, ores, _ = o.wls(g.z, g.v_setpoint, np.zeros(g.n_bus), max_iterations=20, tolerance=1e-6)
+    v2, th2 = e.voltages()
+    assert rc == 0 and res.status == ores.status == 0 and res.iterations == ores.iterations
+    assert max(np.abs(v2 - ov).max(), np.abs(th2 - oth).max()) < 1e-8
+    e.close()
+    e1.close()
 
 
 @pytest.mark.parametrize("name", ["grid14", "grid2k", "grid10k"])
