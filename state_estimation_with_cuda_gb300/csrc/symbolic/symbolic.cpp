@@ -618,7 +618,15 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
         for (int32_t k = 0; k < n; ++k) order2[k] = order[post[k]];
         order.swap(order2);
         for (int32_t k = 0; k < n; ++k) pos[order[k]] = k;
-        etree_of(order, pos, parent);
+        // a postorder is an equivalent ordering: its elimination tree is the
+        // same tree, renumbered
+        std::vector<int32_t> new_of(n), parent2(n, -1);
+        for (int32_t k = 0; k < n; ++k) new_of[post[k]] = k;
+        for (int32_t k = 0; k < n; ++k) {
+            const int32_t pa = parent[post[k]];
+            parent2[k] = pa < 0 ? -1 : new_of[pa];
+        }
+        parent.swap(parent2);
     }
 
     // --- column structures (bus level, strictly below the diagonal) ----------------------
@@ -989,14 +997,33 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     }
 
     // --- RHS gather ------------------------------------------------------------------------
+    // H entries by permuted state (a CSR transpose): ranges of entries count
+    // per thread, the offsets run state-major then range-minor, so each
+    // state's entries stay in ascending order.
     {
         const int64_t nnz = static_cast<int64_t>(P.h_col.size());
-        P.rhs_ptr.assign(P.n_state + 1, 0);
-        for (int64_t h = 0; h < nnz; ++h) ++P.rhs_ptr[ps_of_state[P.h_col[h]] + 1];
-        for (int32_t p = 0; p < P.n_state; ++p) P.rhs_ptr[p + 1] += P.rhs_ptr[p];
-        P.rhs_h.assign(nnz, 0);
-        std::vector<int32_t> fill(P.rhs_ptr.begin(), P.rhs_ptr.end() - 1);
-        for (int64_t h = 0; h < nnz; ++h) P.rhs_h[fill[ps_of_state[P.h_col[h]]]++] = static_cast<int32_t>(h);
+        const int32_t ns_ = P.n_state;
+        const int32_t parts = host_threads(nnz, 1 << 18);
+        std::vector<std::vector<int32_t>> cnt(parts, std::vector<int32_t>(ns_, 0));
+        parallel_ranges(nnz, parts, [&](int32_t t, int64_t h0, int64_t h1) {
+            auto& c = cnt[t];
+            for (int64_t h = h0; h < h1; ++h) ++c[ps_of_state[P.h_col[h]]];
+        });
+        P.rhs_ptr.assign(static_cast<size_t>(ns_) + 1, 0);
+        for (int32_t p = 0; p < ns_; ++p) {
+            int32_t run = P.rhs_ptr[p];
+            for (int32_t t = 0; t < parts; ++t) {
+                const int32_t c = cnt[t][p];
+                cnt[t][p] = run;  // this range's first slot of state p
+                run += c;
+            }
+            P.rhs_ptr[p + 1] = run;
+        }
+        P.rhs_h.resize(nnz);
+        parallel_ranges(nnz, parts, [&](int32_t t, int64_t h0, int64_t h1) {
+            auto& o = cnt[t];
+            for (int64_t h = h0; h < h1; ++h) P.rhs_h[o[ps_of_state[P.h_col[h]]]++] = static_cast<int32_t>(h);
+        });
     }
     return true;
 }
