@@ -142,3 +142,37 @@ def test_removal_compacts_indices():
     assert e.lib.sle_RemoveBus(e.h, b"Bus14") == 0
     assert e.counts()[0] == 13
     e.close()
+
+
+def test_extension_options_validate_and_apply():
+    """sle_ExSetOption keys (host side): every documented key is accepted with a
+    valid value, out-of-range values are refused with INVALID_ARGUMENT, and an
+    unknown key is refused."""
+    e = Estimator()
+    valid = {"exact_jacobian": 0, "gain_policy": 1, "ordering": 0, "use_double_precision": 0,
+             "refine_steps": 1, "big_front_flops": 1e6, "dataflow": 1, "flow_small_f": 64, "warp_fronts": -1,
+             "gain_accumulate": 64, "huber_stall": 1e-5, "spin_limit": 1 << 20, "hold_front": -1,
+             "device_loop": 0, "tile_flow": 1, "eval_pair_rows": 0}
+    for k, v in valid.items():
+        e.set_option(k, v)
+    for k, v in (("gain_accumulate", 16), ("huber_stall", 1.5), ("spin_limit", 0), ("eval_pair_rows", -1)):
+        with pytest.raises(SLEError) as err:
+            e.set_option(k, v)
+        assert err.value.code == api.ERROR_INVALID_ARGUMENT
+    with pytest.raises(SLEError):
+        e.set_option("no_such_option", 1)
+    e.close()
+
+
+def test_stats_layout_matches_header():
+    """SLE_ExStats as the header declares it: six stage arrays, then the
+    counters, step_waits last."""
+    st = native.SLE_ExStats()
+    names = [f[0] for f in st._fields_]
+    assert names[-1] == "step_waits" and names[:3] == ["launches", "ms", "calls"]
+    assert ctypes.sizeof(st) == 6 * 8 * 3 + 7 * 8
+    e = Estimator()
+    e.reset_stats()
+    s = e.stats()
+    assert s.step_waits == 0 and s.iterations == 0
+    e.close()
