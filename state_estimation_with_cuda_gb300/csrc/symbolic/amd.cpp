@@ -9,53 +9,74 @@
 // absorbed.  Ties are broken by bucket order, so the result is deterministic.
 //
 // Storage is flat: a variable's remaining neighbours are a shrinking range of
-// one copy of the adjacency; element lists (Le) are ranges of a bump pool,
-// compacted in place; a variable's element list (Ei) is a range of a second
+// one copy of the adjacency; element lists (Le) are ranges of a bump pool;
+// a variable's element list (Ei) is a range of a second
 // pool that moves to the pool's end when it outgrows its capacity; the
 // members of a supervariable are a linked chain.  Every list keeps the order
 // the list-per-node form had, so the ordering is the same.
+//
+// The new element Lp of a pivot is the exact set of variables adjacent to it
+// in the elimination graph, so, expanded to the members of its
+// supervariables, it is the below-diagonal structure of the L column of the
+// pivot's last member (and, with the later members, of every member).  The
+// optional trace keeps it, which gives the elimination tree and the column
+// counts without a second symbolic pass.
+#include "amd.h"
+
 #include <algorithm>
-#include <cstdint>
-#include <vector>
 
 namespace sle_gb300 {
 
-std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const std::vector<int32_t>& adj) {
+std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const std::vector<int32_t>& adj,
+                               AmdTrace* trace) {
+    if (trace) {
+        trace->piv_end.clear();
+        trace->lp_ptr.assign(1, 0);
+        trace->lp.clear();
+        trace->lp.reserve(adj.size());
+    }
     enum : uint8_t { VAR = 0, ELEM = 1, DEAD = 2 };
     std::vector<uint8_t> status(n, VAR);
-    std::vector<int32_t> nv(n, 1), deg(n, 0);
+    // The per-variable (and per-element) fields the elimination loop reads
+    // together share one cache line: bus numbers carry no locality, so every
+    // list entry visited is a random access.
+    struct Node {
+        int64_t a_beg, e_beg, l_beg;     // list starts in a_pool, e_pool, l_pool
+        int32_t a_len, e_len, e_cap, l_len;
+        int32_t nv, deg, flag, wtag;
+        int32_t w, l_w;
+    };
+    static_assert(sizeof(Node) == 64, "one cache line per node");
+    std::vector<Node> nd(n, Node{0, 0, 0, 0, 0, 0, 0, 1, 0, -1, -1, 0, 0});
     // A: [a_beg, a_beg + a_len) of a_pool (self loops dropped)
     std::vector<int32_t> a_pool;
     a_pool.reserve(adj.size());
-    std::vector<int64_t> a_beg(n);
-    std::vector<int32_t> a_len(n);
     for (int32_t i = 0; i < n; ++i) {
-        a_beg[i] = static_cast<int64_t>(a_pool.size());
+        nd[i].a_beg = static_cast<int64_t>(a_pool.size());
         for (int32_t e = ptr[i]; e < ptr[i + 1]; ++e)
             if (adj[e] != i) a_pool.push_back(adj[e]);
-        a_len[i] = static_cast<int32_t>(a_pool.size() - a_beg[i]);
-        deg[i] = a_len[i];
+        nd[i].a_len = static_cast<int32_t>(a_pool.size() - nd[i].a_beg);
+        nd[i].deg = nd[i].a_len;
     }
     // L (elements): [l_beg, l_beg + l_len) of l_pool
     std::vector<int32_t> l_pool;
     l_pool.reserve(adj.size() + static_cast<size_t>(n));
-    std::vector<int64_t> l_beg(n, 0);
-    std::vector<int32_t> l_len(n, 0);
+    // l_w of element e = sum of nv over its live variables.  It holds while e lives: a
+    // variable leaves Le only by elimination, which absorbs e, or by merging
+    // into a twin that is in Le too.  Dead entries stay in Le until e dies.
     // E (variables' elements): [e_beg, e_beg + e_len) of e_pool, capacity e_cap
     std::vector<int32_t> e_pool;
     e_pool.reserve(4 * static_cast<size_t>(n));
-    std::vector<int64_t> e_beg(n, 0);
-    std::vector<int32_t> e_len(n, 0), e_cap(n, 0);
     auto e_push = [&](int32_t i, int32_t v) {
-        if (e_len[i] == e_cap[i]) {
-            const int32_t cap = std::max(4, 2 * e_cap[i]);
+        if (nd[i].e_len == nd[i].e_cap) {
+            const int32_t cap = std::max(4, 2 * nd[i].e_cap);
             const int64_t nb = static_cast<int64_t>(e_pool.size());
             e_pool.resize(e_pool.size() + cap);
-            std::copy(e_pool.begin() + e_beg[i], e_pool.begin() + e_beg[i] + e_len[i], e_pool.begin() + nb);
-            e_beg[i] = nb;
-            e_cap[i] = cap;
+            std::copy(e_pool.begin() + nd[i].e_beg, e_pool.begin() + nd[i].e_beg + nd[i].e_len, e_pool.begin() + nb);
+            nd[i].e_beg = nb;
+            nd[i].e_cap = cap;
         }
-        e_pool[e_beg[i] + e_len[i]++] = v;
+        e_pool[nd[i].e_beg + nd[i].e_len++] = v;
     };
     // members of supervariable i: chain from m_head[i] to m_tail[i] through m_next
     std::vector<int32_t> m_head(n), m_tail(n), m_next(n, -1);
@@ -64,14 +85,14 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
     // Degree buckets (doubly linked lists).
     std::vector<int32_t> head(n + 1, -1), nxt(n, -1), prv(n, -1);
     auto bucket_insert = [&](int32_t i) {
-        const int32_t d = std::min(deg[i], n);
+        const int32_t d = std::min(nd[i].deg, n);
         nxt[i] = head[d];
         prv[i] = -1;
         if (head[d] >= 0) prv[head[d]] = i;
         head[d] = i;
     };
     auto bucket_remove = [&](int32_t i) {
-        const int32_t d = std::min(deg[i], n);
+        const int32_t d = std::min(nd[i].deg, n);
         if (prv[i] >= 0) nxt[prv[i]] = nxt[i];
         else head[d] = nxt[i];
         if (nxt[i] >= 0) prv[nxt[i]] = prv[i];
@@ -79,7 +100,6 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
     };
     for (int32_t i = n - 1; i >= 0; --i) bucket_insert(i);
 
-    std::vector<int32_t> flag(n, -1), wtag(n, -1), w(n, 0);
     std::vector<int32_t> order;
     order.reserve(n);
     int32_t tag = 0, mindeg = 0, eliminated = 0;
@@ -95,105 +115,94 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         ++tag;
         // --- new element Lp -------------------------------------------------------
         Lp.clear();
-        flag[p] = tag;
-        for (int32_t x = 0; x < e_len[p]; ++x) {
-            const int32_t e = e_pool[e_beg[p] + x];
+        nd[p].flag = tag;
+        for (int32_t x = 0; x < nd[p].e_len; ++x) {
+            const int32_t e = e_pool[nd[p].e_beg + x];
             if (status[e] != ELEM) continue;
-            for (int32_t y = 0; y < l_len[e]; ++y) {
-                const int32_t i = l_pool[l_beg[e] + y];
-                if (status[i] == VAR && flag[i] != tag) {
-                    flag[i] = tag;
+            for (int32_t y = 0; y < nd[e].l_len; ++y) {
+                const int32_t i = l_pool[nd[e].l_beg + y];
+                if (status[i] == VAR && nd[i].flag != tag) {
+                    nd[i].flag = tag;
                     Lp.push_back(i);
                 }
             }
             status[e] = DEAD;  // absorbed into p
-            l_len[e] = 0;
+            nd[e].l_len = 0;
         }
-        for (int32_t x = 0; x < a_len[p]; ++x) {
-            const int32_t i = a_pool[a_beg[p] + x];
-            if (status[i] == VAR && flag[i] != tag) {
-                flag[i] = tag;
+        for (int32_t x = 0; x < nd[p].a_len; ++x) {
+            const int32_t i = a_pool[nd[p].a_beg + x];
+            if (status[i] == VAR && nd[i].flag != tag) {
+                nd[i].flag = tag;
                 Lp.push_back(i);
             }
         }
-        a_len[p] = 0;
-        e_len[p] = 0;
+        nd[p].a_len = 0;
+        nd[p].e_len = 0;
         status[p] = ELEM;
         for (int32_t mb = m_head[p]; mb >= 0; mb = m_next[mb]) order.push_back(mb);
-        eliminated += nv[p];
+        eliminated += nd[p].nv;
         int32_t lp_w = 0;
         for (int32_t i : Lp) {
             bucket_remove(i);
-            lp_w += nv[i];
+            lp_w += nd[i].nv;
         }
         // --- |Le \ Lp| for elements adjacent to Lp -------------------------------
         ++tag;  // second tag for w
         const int32_t wt = tag;
         for (int32_t i : Lp) {
-            for (int32_t x = 0; x < e_len[i]; ++x) {
-                const int32_t e = e_pool[e_beg[i] + x];
+            for (int32_t x = 0; x < nd[i].e_len; ++x) {
+                const int32_t e = e_pool[nd[i].e_beg + x];
                 if (status[e] != ELEM) continue;
-                if (wtag[e] != wt) {
-                    // weighted size of L[e], compacting dead entries
-                    int32_t sz = 0, k2 = 0;
-                    int32_t* le = l_pool.data() + l_beg[e];
-                    for (int32_t y = 0; y < l_len[e]; ++y) {
-                        const int32_t v = le[y];
-                        if (status[v] == VAR) {
-                            le[k2++] = v;
-                            sz += nv[v];
-                        }
-                    }
-                    l_len[e] = k2;
-                    w[e] = sz;
-                    wtag[e] = wt;
+                if (nd[e].wtag != wt) {
+                    nd[e].w = nd[e].l_w;
+                    nd[e].wtag = wt;
                 }
-                w[e] -= nv[i];
+                nd[e].w -= nd[i].nv;
             }
         }
         // --- update variables in Lp ---------------------------------------------------
-        // flag[] == tag - 1 marks membership in Lp.
+        // flag == tag - 1 marks membership in Lp.
         const int32_t lp_tag = tag - 1;
         for (int32_t i : Lp) {
-            int32_t* ei = e_pool.data() + e_beg[i];
+            int32_t* ei = e_pool.data() + nd[i].e_beg;
             int32_t k2 = 0, ext = 0;
-            for (int32_t x = 0; x < e_len[i]; ++x) {
+            for (int32_t x = 0; x < nd[i].e_len; ++x) {
                 const int32_t e = ei[x];
                 if (status[e] != ELEM || e == p) continue;
-                if (wtag[e] == wt && w[e] <= 0) {  // Le subset of Lp: absorb into p
+                if (nd[e].wtag == wt && nd[e].w <= 0) {  // Le subset of Lp: absorb into p
                     status[e] = DEAD;
-                    l_len[e] = 0;
+                    nd[e].l_len = 0;
                     continue;
                 }
                 ei[k2++] = e;
-                ext += (wtag[e] == wt) ? w[e] : 0;
+                ext += (nd[e].wtag == wt) ? nd[e].w : 0;
             }
-            e_len[i] = k2;
+            nd[i].e_len = k2;
             e_push(i, p);
-            int32_t* ap = a_pool.data() + a_beg[i];
+            int32_t* ap = a_pool.data() + nd[i].a_beg;
             int32_t aw = 0;
             k2 = 0;
-            for (int32_t x = 0; x < a_len[i]; ++x) {
+            for (int32_t x = 0; x < nd[i].a_len; ++x) {
                 const int32_t v = ap[x];
-                if (status[v] != VAR || v == p || flag[v] == lp_tag) continue;
+                if (status[v] != VAR || v == p || nd[v].flag == lp_tag) continue;
                 ap[k2++] = v;
-                aw += nv[v];
+                aw += nd[v].nv;
             }
-            a_len[i] = k2;
+            nd[i].a_len = k2;
             const int32_t remaining = n - eliminated;
-            const int32_t d1 = deg[i] + lp_w - nv[i];
-            const int32_t d2 = aw + (lp_w - nv[i]) + ext;
-            deg[i] = std::max(0, std::min(std::min(d1, d2), remaining - nv[i]));
+            const int32_t d1 = nd[i].deg + lp_w - nd[i].nv;
+            const int32_t d2 = aw + (lp_w - nd[i].nv) + ext;
+            nd[i].deg = std::max(0, std::min(std::min(d1, d2), remaining - nd[i].nv));
         }
         // --- supervariable detection among Lp ------------------------------------------
         hashes.clear();
         for (int32_t i : Lp) {
             if (status[i] != VAR) continue;
             uint64_t h = 0;
-            for (int32_t x = 0; x < e_len[i]; ++x)
-                h += static_cast<uint64_t>(e_pool[e_beg[i] + x]) * 0x9E3779B97F4A7C15ULL + 1;
-            for (int32_t x = 0; x < a_len[i]; ++x)
-                h += static_cast<uint64_t>(a_pool[a_beg[i] + x]) * 0xC2B2AE3D27D4EB4FULL + 7;
+            for (int32_t x = 0; x < nd[i].e_len; ++x)
+                h += static_cast<uint64_t>(e_pool[nd[i].e_beg + x]) * 0x9E3779B97F4A7C15ULL + 1;
+            for (int32_t x = 0; x < nd[i].a_len; ++x)
+                h += static_cast<uint64_t>(a_pool[nd[i].a_beg + x]) * 0xC2B2AE3D27D4EB4FULL + 7;
             hashes.emplace_back(h, i);
         }
         std::sort(hashes.begin(), hashes.end());
@@ -203,18 +212,18 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
             for (size_t x = a; x + 1 < b; ++x) {  // a variable alone in its hash group has no twin
                 const int32_t i = hashes[x].second;
                 if (status[i] != VAR) continue;
-                si.assign(e_pool.begin() + e_beg[i], e_pool.begin() + e_beg[i] + e_len[i]);
+                si.assign(e_pool.begin() + nd[i].e_beg, e_pool.begin() + nd[i].e_beg + nd[i].e_len);
                 std::sort(si.begin(), si.end());
-                ai.assign(a_pool.begin() + a_beg[i], a_pool.begin() + a_beg[i] + a_len[i]);
+                ai.assign(a_pool.begin() + nd[i].a_beg, a_pool.begin() + nd[i].a_beg + nd[i].a_len);
                 std::sort(ai.begin(), ai.end());
                 for (size_t y = x + 1; y < b; ++y) {
                     const int32_t j = hashes[y].second;
                     if (status[j] != VAR) continue;
-                    if (e_len[j] != e_len[i]) continue;
-                    sj.assign(e_pool.begin() + e_beg[j], e_pool.begin() + e_beg[j] + e_len[j]);
+                    if (nd[j].e_len != nd[i].e_len) continue;
+                    sj.assign(e_pool.begin() + nd[j].e_beg, e_pool.begin() + nd[j].e_beg + nd[j].e_len);
                     std::sort(sj.begin(), sj.end());
                     if (si != sj) continue;
-                    aj.assign(a_pool.begin() + a_beg[j], a_pool.begin() + a_beg[j] + a_len[j]);
+                    aj.assign(a_pool.begin() + nd[j].a_beg, a_pool.begin() + nd[j].a_beg + nd[j].a_len);
                     std::sort(aj.begin(), aj.end());
                     ai2.clear();
                     aj2.clear();
@@ -222,30 +231,37 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
                     for (int32_t v : aj) if (v != i) aj2.push_back(v);
                     if (ai2 != aj2) continue;
                     // merge j into i
-                    nv[i] += nv[j];
-                    deg[i] = std::max(0, deg[i] - nv[j]);
-                    nv[j] = 0;
+                    nd[i].nv += nd[j].nv;
+                    nd[i].deg = std::max(0, nd[i].deg - nd[j].nv);
+                    nd[j].nv = 0;
                     status[j] = DEAD;
                     m_next[m_tail[i]] = m_head[j];
                     m_tail[i] = m_tail[j];
-                    a_len[j] = 0;
-                    e_len[j] = 0;
+                    nd[j].a_len = 0;
+                    nd[j].e_len = 0;
                     ai.erase(std::remove(ai.begin(), ai.end(), j), ai.end());
-                    int32_t* ap = a_pool.data() + a_beg[i];
-                    a_len[i] = static_cast<int32_t>(std::remove(ap, ap + a_len[i], j) - ap);
+                    int32_t* ap = a_pool.data() + nd[i].a_beg;
+                    nd[i].a_len = static_cast<int32_t>(std::remove(ap, ap + nd[i].a_len, j) - ap);
                 }
             }
             a = b;
         }
         // --- finalise element p and reinsert variables ------------------------------------
-        l_beg[p] = static_cast<int64_t>(l_pool.size());
+        nd[p].l_beg = static_cast<int64_t>(l_pool.size());
         for (int32_t i : Lp) {
             if (status[i] != VAR) continue;
             l_pool.push_back(i);
+            nd[p].l_w += nd[i].nv;
             bucket_insert(i);
-            mindeg = std::min(mindeg, std::min(deg[i], n));
+            mindeg = std::min(mindeg, std::min(nd[i].deg, n));
         }
-        l_len[p] = static_cast<int32_t>(l_pool.size() - l_beg[p]);
+        nd[p].l_len = static_cast<int32_t>(l_pool.size() - nd[p].l_beg);
+        if (trace) {
+            trace->piv_end.push_back(eliminated);
+            for (int64_t y = nd[p].l_beg; y < nd[p].l_beg + nd[p].l_len; ++y)
+                for (int32_t mb = m_head[l_pool[y]]; mb >= 0; mb = m_next[mb]) trace->lp.push_back(mb);
+            trace->lp_ptr.push_back(static_cast<int64_t>(trace->lp.size()));
+        }
     }
     return order;
 }

@@ -1,6 +1,8 @@
 // Symbolic analysis for the GPU WLS pipeline (definitions in symbolic.h).
 #include "symbolic.h"
 
+#include "amd.h"
+
 #include <algorithm>
 #include <cstring>
 #include <memory>
@@ -9,8 +11,6 @@
 #include <thread>
 
 namespace sle_gb300 {
-
-std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const std::vector<int32_t>& adj);
 
 namespace {
 
@@ -552,6 +552,8 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     std::vector<int32_t> gptr, gadj;
     bus_graph(t, P.y_ptr, P.y_col, gptr, gadj);
     std::vector<int32_t> order;
+    AmdTrace trace;
+    const bool traced = prm.ordering != 1 && prm.ordering != 2;
     if (prm.ordering == 1) {
         order.resize(n);
         std::iota(order.begin(), order.end(), 0);
@@ -559,20 +561,35 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
         NestedDissection nd(n, gptr, gadj, prm.leaf_size);
         order = nd.run();
     } else {
-        order = amd_order(n, gptr, gadj);
+        order = amd_order(n, gptr, gadj, &trace);
     }
     if (static_cast<int32_t>(order.size()) != n) { err = "ordering failed"; return false; }
     std::vector<int32_t> pos(n, -1);
     for (int32_t k = 0; k < n; ++k) pos[order[k]] = k;
+    const int32_t n_piv = static_cast<int32_t>(trace.piv_end.size());
+    const int32_t piv_parts = host_threads(n_piv, 4096);
 
-    // --- elimination tree (Liu) and postorder ---------------------------------------------
-    auto etree_of = [&](const std::vector<int32_t>& ord, const std::vector<int32_t>& ps, std::vector<int32_t>& parent) {
-        parent.assign(n, -1);
+    // --- elimination tree and postorder -----------------------------------------------------
+    // From the ordering's trace: a supervariable's members form a chain, and
+    // the last one's parent is the first vertex of its column structure.
+    // Otherwise Liu's algorithm on the bus graph.
+    std::vector<int32_t> parent(n, -1);
+    if (traced) {
+        parallel_ranges(n_piv, piv_parts, [&](int32_t, int64_t k0, int64_t k1) {
+            for (int64_t k = k0; k < k1; ++k) {
+                const int32_t b0 = k ? trace.piv_end[k - 1] : 0, b1 = trace.piv_end[k];
+                for (int32_t q = b0; q + 1 < b1; ++q) parent[q] = q + 1;
+                int32_t first = n;
+                for (int64_t y = trace.lp_ptr[k]; y < trace.lp_ptr[k + 1]; ++y) first = std::min(first, pos[trace.lp[y]]);
+                parent[b1 - 1] = first < n ? first : -1;
+            }
+        });
+    } else {
         std::vector<int32_t> anc(n, -1);
         for (int32_t j = 0; j < n; ++j) {
-            const int32_t b = ord[j];
+            const int32_t b = order[j];
             for (int32_t e = gptr[b]; e < gptr[b + 1]; ++e) {
-                int32_t i = ps[gadj[e]];
+                int32_t i = pos[gadj[e]];
                 if (i >= j) continue;
                 while (anc[i] != -1 && anc[i] != j) {
                     const int32_t nx = anc[i];
@@ -585,9 +602,9 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
                 }
             }
         }
-    };
-    std::vector<int32_t> parent;
-    etree_of(order, pos, parent);
+    }
+    std::vector<int32_t> post, new_of(n);  // new position -> old, old -> new
+    post.reserve(n);
     {
         std::vector<int32_t> head(n, -1), next(n, -1);
         for (int32_t j = n - 1; j >= 0; --j) {
@@ -596,8 +613,6 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
                 head[parent[j]] = j;
             }
         }
-        std::vector<int32_t> post;
-        post.reserve(n);
         std::vector<int32_t> stack;
         for (int32_t r = 0; r < n; ++r) {
             if (parent[r] != -1) continue;
@@ -620,7 +635,7 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
         for (int32_t k = 0; k < n; ++k) pos[order[k]] = k;
         // a postorder is an equivalent ordering: its elimination tree is the
         // same tree, renumbered
-        std::vector<int32_t> new_of(n), parent2(n, -1);
+        std::vector<int32_t> parent2(n, -1);
         for (int32_t k = 0; k < n; ++k) new_of[post[k]] = k;
         for (int32_t k = 0; k < n; ++k) {
             const int32_t pa = parent[post[k]];
@@ -630,8 +645,27 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     }
 
     // --- column structures (bus level, strictly below the diagonal) ----------------------
-    std::vector<std::vector<int32_t>> cstruct(n);
-    {
+    // csize[j] = |struct(L(:, j))|; col_struct(j, out) writes the sorted
+    // structure.  A postorder keeps the structures as vertex sets, so from
+    // the trace column j is the later members of its supervariable plus the
+    // supervariable's element, renumbered.  Otherwise the structures are
+    // merged up the tree from the bus graph.
+    std::vector<int32_t> csize(n);
+    std::vector<std::vector<int32_t>> cstruct;
+    std::vector<int32_t> piv_of_old;
+    if (traced) {
+        piv_of_old.resize(n);
+        parallel_ranges(n_piv, piv_parts, [&](int32_t, int64_t k0, int64_t k1) {
+            for (int64_t k = k0; k < k1; ++k)
+                for (int32_t q = k ? trace.piv_end[k - 1] : 0; q < trace.piv_end[k]; ++q)
+                    piv_of_old[q] = static_cast<int32_t>(k);
+        });
+        for (int32_t j = 0; j < n; ++j) {
+            const int32_t q = post[j], k = piv_of_old[q];
+            csize[j] = trace.piv_end[k] - 1 - q + static_cast<int32_t>(trace.lp_ptr[k + 1] - trace.lp_ptr[k]);
+        }
+    } else {
+        cstruct.resize(n);
         std::vector<std::vector<int32_t>> kids(n);
         for (int32_t j = 0; j < n; ++j)
             if (parent[j] >= 0) kids[parent[j]].push_back(j);
@@ -652,8 +686,20 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
                 tmp.swap(merged);
             }
             cstruct[j] = tmp;
+            csize[j] = static_cast<int32_t>(tmp.size());
         }
     }
+    auto col_struct = [&](int32_t j, int32_t* out) {
+        if (!traced) {
+            std::copy(cstruct[j].begin(), cstruct[j].end(), out);
+            return;
+        }
+        const int32_t q = post[j], k = piv_of_old[q];
+        int32_t o = 0;
+        for (int32_t q2 = q + 1; q2 < trace.piv_end[k]; ++q2) out[o++] = new_of[q2];
+        for (int64_t y = trace.lp_ptr[k]; y < trace.lp_ptr[k + 1]; ++y) out[o++] = pos[trace.lp[y]];
+        std::sort(out, out + o);
+    };
 
     // --- fundamental supernodes + relaxed amalgamation (bus level) ------------------------
     std::vector<int32_t> nkids(n, 0);
@@ -662,7 +708,7 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     std::vector<int32_t> fs_start;  // fundamental supernode starts
     for (int32_t j = 0; j < n; ++j) {
         const bool joins_prev = j > 0 && parent[j - 1] == j && nkids[j] == 1 &&
-                                cstruct[j - 1].size() == cstruct[j].size() + 1;
+                                csize[j - 1] == csize[j] + 1;
         if (!joins_prev) fs_start.push_back(j);
     }
     const int32_t nfs = static_cast<int32_t>(fs_start.size());
@@ -677,7 +723,7 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
         const int32_t last = fs_start[f + 1] - 1;
         g_start[f] = fs_start[f];
         g_nc[f] = fs_start[f + 1] - fs_start[f];
-        g_f[f] = g_nc[f] + static_cast<int32_t>(cstruct[last].size());
+        g_f[f] = g_nc[f] + csize[last];
         g_true[f] = trapezoid(g_nc[f], g_f[f]);
     }
     for (int32_t f = 0; f < nfs; ++f) {
@@ -745,21 +791,36 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     P.sn_u_off.assign(ns + 1, 0);
     P.sn_su_off.assign(ns + 1, 0);
     std::vector<int32_t> sn_of_ps(P.n_state);
-    for (int32_t k = 0; k < ns; ++k) {
-        P.sn_c0[k] = ps0[sn_b0[k]];
-        const int32_t lastpos = sn_b1[k] - 1;
-        // rows: own columns then structure of the last column
-        for (int32_t j = sn_b0[k]; j < sn_b1[k]; ++j)
-            for (int32_t x = ps0[j]; x < ps0[j + 1]; ++x) P.sn_rows.push_back(x);
-        for (int32_t r : cstruct[lastpos])
-            for (int32_t x = ps0[r]; x < ps0[r + 1]; ++x) P.sn_rows.push_back(x);
-        P.sn_rows_off[k + 1] = static_cast<int64_t>(P.sn_rows.size());
-        const int64_t f = P.sn_rows_off[k + 1] - P.sn_rows_off[k];
-        P.sn_f[k] = static_cast<int32_t>(f);
-        const int32_t pj = parent[lastpos];
-        P.sn_parent[k] = pj >= 0 ? sn_of_pos[pj] : -1;
-        for (int32_t x = ps0[sn_b0[k]]; x < ps0[sn_b1[k]]; ++x) sn_of_ps[x] = k;
-    }
+    // Rows of front k: its own columns, then the structure of its last column,
+    // each bus expanded to its states.
+    std::vector<int64_t> sb_off(ns + 1, 0);
+    for (int32_t k = 0; k < ns; ++k) sb_off[k + 1] = sb_off[k] + csize[sn_b1[k] - 1];
+    std::vector<int32_t> sb(static_cast<size_t>(sb_off[ns]));
+    const int32_t sn_parts = host_threads(ns, 2048);
+    parallel_ranges(ns, sn_parts, [&](int32_t, int64_t k0, int64_t k1) {
+        for (int64_t k = k0; k < k1; ++k) {
+            col_struct(sn_b1[k] - 1, sb.data() + sb_off[k]);
+            int32_t f = ps0[sn_b1[k]] - ps0[sn_b0[k]];
+            for (int64_t y = sb_off[k]; y < sb_off[k + 1]; ++y) f += ps0[sb[y] + 1] - ps0[sb[y]];
+            P.sn_f[k] = f;
+        }
+    });
+    for (int32_t k = 0; k < ns; ++k) P.sn_rows_off[k + 1] = P.sn_rows_off[k] + P.sn_f[k];
+    P.sn_rows.resize(static_cast<size_t>(P.sn_rows_off[ns]));
+    parallel_ranges(ns, sn_parts, [&](int32_t, int64_t k0, int64_t k1) {
+        for (int64_t k = k0; k < k1; ++k) {
+            P.sn_c0[k] = ps0[sn_b0[k]];
+            int32_t* row = P.sn_rows.data() + P.sn_rows_off[k];
+            for (int32_t x = ps0[sn_b0[k]]; x < ps0[sn_b1[k]]; ++x) {
+                *row++ = x;
+                sn_of_ps[x] = static_cast<int32_t>(k);
+            }
+            for (int64_t y = sb_off[k]; y < sb_off[k + 1]; ++y)
+                for (int32_t x = ps0[sb[y]]; x < ps0[sb[y] + 1]; ++x) *row++ = x;
+            const int32_t pj = parent[sn_b1[k] - 1];
+            P.sn_parent[k] = pj >= 0 ? sn_of_pos[pj] : -1;
+        }
+    });
     P.sn_c0[ns] = P.n_state;
     int64_t lx = 0, uu = 0, su = 0;
     P.nnz_l = 0;
