@@ -27,8 +27,8 @@ struct Carver {
     }
 };
 
-template <typename T>
-cudaError_t put(T* dst, const std::vector<T>& src, cudaStream_t st) {
+template <typename T, typename A>
+cudaError_t put(T* dst, const std::vector<T, A>& src, cudaStream_t st) {
     if (src.empty()) return cudaSuccess;
     return cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, st);
 }

@@ -861,19 +861,32 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
             if (P.sn_parent[k] >= 0) P.sn_child[fill[P.sn_parent[k]]++] = k;
     }
     P.sn_relmap.assign(su, 0);
-    for (int32_t k = 0; k < ns; ++k) {
-        const int32_t p = P.sn_parent[k];
-        const int64_t nc = P.sn_c0[k + 1] - P.sn_c0[k];
-        const int64_t f = P.sn_f[k];
-        if (f > nc && p < 0) { err = "front has below rows but no parent"; return false; }
-        if (p < 0) continue;
-        const int32_t* pr = P.sn_rows.data() + P.sn_rows_off[p];
-        const int32_t pf = P.sn_f[p];
-        for (int64_t r = nc; r < f; ++r) {
-            const int32_t row = P.sn_rows[P.sn_rows_off[k] + r];
-            const int32_t* it = std::lower_bound(pr, pr + pf, row);
-            if (it == pr + pf || *it != row) { err = "child row missing from parent front"; return false; }
-            P.sn_relmap[P.sn_su_off[k] + (r - nc)] = static_cast<int32_t>(it - pr);
+    {
+        // 1: a front with below rows has no parent; 2: a row missing from the parent
+        std::vector<uint8_t> bad(sn_parts, 0);
+        parallel_ranges(ns, sn_parts, [&](int32_t t, int64_t k0, int64_t k1) {
+            for (int64_t k = k0; k < k1 && !bad[t]; ++k) {
+                const int32_t p = P.sn_parent[k];
+                const int64_t nc = P.sn_c0[k + 1] - P.sn_c0[k];
+                const int64_t f = P.sn_f[k];
+                if (f > nc && p < 0) bad[t] = 1;
+                if (p < 0) continue;
+                const int32_t* pr = P.sn_rows.data() + P.sn_rows_off[p];
+                const int32_t pf = P.sn_f[p];
+                for (int64_t r = nc; r < f; ++r) {
+                    const int32_t row = P.sn_rows[P.sn_rows_off[k] + r];
+                    const int32_t* it = std::lower_bound(pr, pr + pf, row);
+                    if (it == pr + pf || *it != row) {
+                        bad[t] = 2;
+                        break;
+                    }
+                    P.sn_relmap[P.sn_su_off[k] + (r - nc)] = static_cast<int32_t>(it - pr);
+                }
+            }
+        });
+        for (uint8_t b : bad) {  // the first failing range names the error
+            if (b == 1) { err = "front has below rows but no parent"; return false; }
+            if (b == 2) { err = "child row missing from parent front"; return false; }
         }
     }
     {
@@ -891,170 +904,6 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
         P.lvl_sn.assign(ns, 0);
         std::vector<int32_t> fill(P.lvl_ptr.begin(), P.lvl_ptr.end() - 1);
         for (int32_t k = 0; k < ns; ++k) P.lvl_sn[fill[lvl[k]]++] = k;
-    }
-
-    // --- gain assembly targets --------------------------------------------------------
-    // Every pair (x, y), x <= y, of H entries of one row contributes to the G
-    // entry (lo, hi) of the front owning column lo.  Records are collected in
-    // row order per front, stably sorted by the entry's local index, and each
-    // run of equal indices becomes one target with its pair list.  Rows are
-    // cut into chunks and fronts into ranges, one host thread each; chunk
-    // offsets per front keep the row order, so the plan is the same for any
-    // thread count.
-    {
-        struct PairRec { int32_t local; int32_t a; int32_t b; };
-        const int32_t nthr = host_threads(m, 4096);
-        auto parallel = [&](int32_t parts, const std::function<void(int32_t)>& fn) {
-            std::vector<std::thread> pool;
-            for (int32_t t = 1; t < parts; ++t) pool.emplace_back(fn, t);
-            fn(0);
-            for (auto& th : pool) th.join();
-        };
-        auto chunk = [&](int32_t t, int32_t total) {
-            return std::make_pair(static_cast<int32_t>((static_cast<int64_t>(total) * t) / nthr),
-                                  static_cast<int32_t>((static_cast<int64_t>(total) * (t + 1)) / nthr));
-        };
-        // pairs of row q start at pair_off[q] (x-major, y >= x)
-        std::vector<int64_t> pair_off(static_cast<size_t>(m) + 1, 0);
-        for (int32_t q = 0; q < m; ++q) {
-            const int64_t L = P.h_ptr[q + 1] - P.h_ptr[q];
-            pair_off[q + 1] = pair_off[q] + L * (L + 1) / 2;
-        }
-        const int64_t run = pair_off[m];
-        // the output arrays are zero-filled (page faults) on a thread of their
-        // own while the passes below run
-        std::thread alloc_out([&] {
-            P.pair_a.resize(static_cast<size_t>(run));
-            P.pair_b.resize(static_cast<size_t>(run));
-        });
-        std::unique_ptr<int32_t[]> pk(new int32_t[std::max<int64_t>(run, 1)]);
-        std::unique_ptr<int32_t[]> pl(new int32_t[std::max<int64_t>(run, 1)]);
-        std::vector<std::vector<int64_t>> cnt(nthr, std::vector<int64_t>(ns + 1, 0));
-        std::vector<uint8_t> bad(nthr, 0);
-        // the front and local index of a pair of H entries in permuted
-        // columns px, py; false if outside the structure.  A front's own
-        // columns lead its row list in order, so a row there is found without
-        // a search.
-        auto locate = [&](int32_t px, int32_t py, int32_t& k, int32_t& local) {
-            const int32_t lo = std::min(px, py), hi = std::max(px, py);
-            k = sn_of_ps[lo];
-            const int32_t f = P.sn_f[k], c0 = P.sn_c0[k], nc = P.sn_c0[k + 1] - c0;
-            int32_t r;
-            if (hi - c0 < nc) {
-                r = hi - c0;
-            } else {
-                const int32_t* rows = P.sn_rows.data() + P.sn_rows_off[k];
-                const int32_t* it = std::lower_bound(rows + nc, rows + f, hi);
-                if (it == rows + f || *it != hi) return false;
-                r = static_cast<int32_t>(it - rows);
-            }
-            local = r + (lo - c0) * f;
-            return true;
-        };
-        parallel(nthr, [&](int32_t t) {
-            const auto r = chunk(t, m);
-            auto& c = cnt[t];
-            std::vector<int32_t> ps;
-            for (int32_t q = r.first; q < r.second; ++q) {
-                int64_t o = pair_off[q];
-                const int32_t h0 = P.h_ptr[q], L = P.h_ptr[q + 1] - h0;
-                ps.resize(L);
-                for (int32_t x = 0; x < L; ++x) ps[x] = ps_of_state[P.h_col[h0 + x]];
-                for (int32_t x = 0; x < L; ++x)
-                    for (int32_t y = x; y < L; ++y, ++o) {
-                        int32_t k, local;
-                        if (!locate(ps[x], ps[y], k, local)) {
-                            bad[t] = 1;
-                            return;
-                        }
-                        pk[o] = k;
-                        pl[o] = local;
-                        ++c[k];
-                    }
-            }
-        });
-        for (uint8_t b : bad)
-            if (b) {
-                alloc_out.join();
-                err = "gain entry outside the front structure";
-                return false;
-            }
-        // offsets: front-major, chunk-minor
-        std::vector<int64_t> sn_rec(ns + 1, 0);
-        std::vector<std::vector<int64_t>> off(nthr, std::vector<int64_t>(ns, 0));
-        int64_t acc = 0;
-        for (int32_t k = 0; k < ns; ++k) {
-            sn_rec[k] = acc;
-            for (int32_t t = 0; t < nthr; ++t) {
-                off[t][k] = acc;
-                acc += cnt[t][k];
-            }
-        }
-        sn_rec[ns] = acc;
-        std::unique_ptr<PairRec[]> rec(new PairRec[std::max<int64_t>(run, 1)]);
-        parallel(nthr, [&](int32_t t) {
-            const auto r = chunk(t, m);
-            auto& o = off[t];
-            for (int32_t q = r.first; q < r.second; ++q) {
-                int64_t i = pair_off[q];
-                for (int32_t x = P.h_ptr[q]; x < P.h_ptr[q + 1]; ++x)
-                    for (int32_t y = x; y < P.h_ptr[q + 1]; ++y, ++i) rec[o[pk[i]]++] = {pl[i], x, y};
-            }
-        });
-        pk.reset();
-        pl.reset();
-        // fronts cut into nthr ranges of about equal record counts
-        std::vector<int32_t> fr_cut(nthr + 1, ns);
-        fr_cut[0] = 0;
-        for (int32_t t = 1, k = 0; t < nthr; ++t) {
-            const int64_t goal = run * t / nthr;
-            while (k < ns && sn_rec[k] < goal) ++k;
-            fr_cut[t] = k;
-        }
-        // per front: stable counting sort by local index (local < f * nc),
-        // count the targets
-        std::vector<int32_t> ntg(ns + 1, 0);
-        parallel(nthr, [&](int32_t t) {
-            std::vector<int32_t> hist;
-            std::vector<PairRec> tmp;
-            for (int32_t k = fr_cut[t]; k < fr_cut[t + 1]; ++k) {
-                PairRec* b = rec.get() + sn_rec[k];
-                const int64_t cntk = sn_rec[k + 1] - sn_rec[k];
-                const int32_t range = P.sn_f[k] * (P.sn_c0[k + 1] - P.sn_c0[k]);
-                hist.assign(static_cast<size_t>(range) + 1, 0);
-                for (int64_t i = 0; i < cntk; ++i) ++hist[b[i].local + 1];
-                int32_t c = 0;
-                for (int32_t v = 0; v < range; ++v) {
-                    c += hist[v + 1] > 0 ? 1 : 0;
-                    hist[v + 1] += hist[v];
-                }
-                tmp.resize(static_cast<size_t>(cntk));
-                for (int64_t i = 0; i < cntk; ++i) tmp[hist[b[i].local]++] = b[i];
-                std::copy(tmp.begin(), tmp.end(), b);
-                ntg[k] = c;
-            }
-        });
-        P.sn_tgt_ptr.assign(ns + 1, 0);
-        for (int32_t k = 0; k < ns; ++k) P.sn_tgt_ptr[k + 1] = P.sn_tgt_ptr[k] + ntg[k];
-        const int32_t n_tgt = P.sn_tgt_ptr[ns];
-        P.tgt_local.resize(n_tgt);
-        P.tgt_pair_ptr.resize(static_cast<size_t>(n_tgt) + 1);
-        alloc_out.join();
-        P.tgt_pair_ptr[n_tgt] = run;
-        parallel(nthr, [&](int32_t t) {
-            for (int32_t k = fr_cut[t]; k < fr_cut[t + 1]; ++k) {
-                int32_t tg = P.sn_tgt_ptr[k];
-                for (int64_t i = sn_rec[k]; i < sn_rec[k + 1]; ++i) {
-                    if (i == sn_rec[k] || rec[i].local != rec[i - 1].local) {
-                        P.tgt_local[tg] = rec[i].local;
-                        P.tgt_pair_ptr[tg] = i;
-                        ++tg;
-                    }
-                    P.pair_a[i] = rec[i].a;
-                    P.pair_b[i] = rec[i].b;
-                }
-            }
-        });
     }
 
     // --- RHS gather ------------------------------------------------------------------------
@@ -1086,18 +935,137 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
             for (int64_t h = h0; h < h1; ++h) P.rhs_h[o[ps_of_state[P.h_col[h]]]++] = static_cast<int32_t>(h);
         });
     }
+    // --- gain assembly targets --------------------------------------------------------
+    // Every pair (x, y), x <= y, of H entries of one row contributes to the G
+    // entry (lo, hi), lo <= hi their permuted columns, of the front owning
+    // column lo.  A front's pairs are generated column by column from the
+    // column lists of H (the RHS gather): for each entry of column lo, in
+    // ascending row order, the entries of its row at columns >= lo.  They are
+    // stably sorted by the entry's local index (row + col * f in the front's
+    // panel), and each run of equal indices becomes one target with its pair
+    // list; a target gets at most one pair per row, so its pairs are in row
+    // order.  Fronts are cut into ranges of about equal pair counts, one host
+    // thread each, so the plan is the same for any thread count.
+    {
+        struct PairRec { int32_t local; int32_t a; int32_t b; };
+        const int64_t nnz = static_cast<int64_t>(P.h_col.size());
+        int64_t run = 0;
+        for (int32_t q = 0; q < m; ++q) {
+            const int64_t L = P.h_ptr[q + 1] - P.h_ptr[q];
+            run += L * (L + 1) / 2;
+        }
+        P.pair_a.resize(static_cast<size_t>(run));  // written (first touched) by the workers below
+        P.pair_b.resize(static_cast<size_t>(run));
+        // hps[h] = permuted column of entry h; ge[h] = entries of h's row at
+        // permuted columns >= h's, h included
+        std::vector<int32_t> hps(static_cast<size_t>(nnz)), ge(static_cast<size_t>(nnz));
+        parallel_ranges(m, host_threads(m, 4096), [&](int32_t, int64_t q0, int64_t q1) {
+            for (int64_t q = q0; q < q1; ++q) {
+                const int32_t h0 = P.h_ptr[q], h1 = P.h_ptr[q + 1];
+                for (int32_t x = h0; x < h1; ++x) hps[x] = ps_of_state[P.h_col[x]];
+                for (int32_t x = h0; x < h1; ++x) {
+                    int32_t c = 0;
+                    for (int32_t y = h0; y < h1; ++y) c += hps[y] >= hps[x];
+                    ge[x] = c;
+                }
+            }
+        });
+        std::vector<int64_t> fr_off(ns + 1, 0);
+        parallel_ranges(ns, sn_parts, [&](int32_t, int64_t k0, int64_t k1) {
+            for (int64_t k = k0; k < k1; ++k) {
+                int64_t c = 0;
+                for (int32_t i = P.rhs_ptr[P.sn_c0[k]]; i < P.rhs_ptr[P.sn_c0[k + 1]]; ++i) c += ge[P.rhs_h[i]];
+                fr_off[k + 1] = c;
+            }
+        });
+        for (int32_t k = 0; k < ns; ++k) fr_off[k + 1] += fr_off[k];
+        const int32_t nthr = host_threads(run, 1 << 16);
+        std::vector<int32_t> fr_cut(nthr + 1, ns);
+        fr_cut[0] = 0;
+        for (int32_t t = 1, k = 0; t < nthr; ++t) {
+            const int64_t goal = run * t / nthr;
+            while (k < ns && fr_off[k] < goal) ++k;
+            fr_cut[t] = k;
+        }
+        std::vector<int32_t> ntg(ns, 0);
+        std::vector<std::vector<int32_t>> t_local(nthr);
+        std::vector<std::vector<int64_t>> t_start(nthr);
+        std::vector<uint8_t> bad(nthr, 0);
+        parallel_ranges(nthr, nthr, [&](int32_t t, int64_t, int64_t) {
+            std::vector<PairRec> rec, tmp;
+            std::vector<int32_t> hist;
+            for (int32_t k = fr_cut[t]; k < fr_cut[t + 1]; ++k) {
+                const int32_t f = P.sn_f[k], c0 = P.sn_c0[k], nc = P.sn_c0[k + 1] - c0;
+                const int32_t* rows = P.sn_rows.data() + P.sn_rows_off[k];
+                rec.clear();
+                for (int32_t lo = c0; lo < c0 + nc; ++lo)
+                    for (int32_t i = P.rhs_ptr[lo]; i < P.rhs_ptr[lo + 1]; ++i) {
+                        const int32_t h = P.rhs_h[i], q = P.h_row[h];
+                        for (int32_t h2 = P.h_ptr[q]; h2 < P.h_ptr[q + 1]; ++h2) {
+                            const int32_t hi = hps[h2];
+                            if (hi < lo) continue;
+                            int32_t r = hi - c0;
+                            if (r >= nc) {  // below the front's own columns
+                                const int32_t* it = std::lower_bound(rows + nc, rows + f, hi);
+                                if (it == rows + f || *it != hi) {
+                                    bad[t] = 1;
+                                    return;
+                                }
+                                r = static_cast<int32_t>(it - rows);
+                            }
+                            rec.push_back({r + (lo - c0) * f, std::min(h, h2), std::max(h, h2)});
+                        }
+                    }
+                // stable counting sort by local index (local < f * nc)
+                const int32_t range = f * nc;
+                hist.assign(static_cast<size_t>(range) + 1, 0);
+                for (const PairRec& x : rec) ++hist[x.local + 1];
+                for (int32_t v = 0; v < range; ++v) hist[v + 1] += hist[v];
+                tmp.resize(rec.size());
+                for (const PairRec& x : rec) tmp[hist[x.local]++] = x;
+                const int64_t o = fr_off[k];
+                int32_t c = 0;
+                for (size_t i = 0; i < tmp.size(); ++i) {
+                    if (i == 0 || tmp[i].local != tmp[i - 1].local) {
+                        t_local[t].push_back(tmp[i].local);
+                        t_start[t].push_back(o + static_cast<int64_t>(i));
+                        ++c;
+                    }
+                    P.pair_a[o + i] = tmp[i].a;
+                    P.pair_b[o + i] = tmp[i].b;
+                }
+                ntg[k] = c;
+            }
+        });
+        for (uint8_t b : bad)
+            if (b) {
+                err = "gain entry outside the front structure";
+                return false;
+            }
+        P.sn_tgt_ptr.assign(ns + 1, 0);
+        for (int32_t k = 0; k < ns; ++k) P.sn_tgt_ptr[k + 1] = P.sn_tgt_ptr[k] + ntg[k];
+        const int32_t n_tgt = P.sn_tgt_ptr[ns];
+        P.tgt_local.resize(n_tgt);
+        P.tgt_pair_ptr.resize(static_cast<size_t>(n_tgt) + 1);
+        P.tgt_pair_ptr[n_tgt] = run;
+        parallel_ranges(nthr, nthr, [&](int32_t t, int64_t, int64_t) {
+            const int32_t g0 = P.sn_tgt_ptr[fr_cut[t]];
+            std::copy(t_local[t].begin(), t_local[t].end(), P.tgt_local.begin() + g0);
+            std::copy(t_start[t].begin(), t_start[t].end(), P.tgt_pair_ptr.begin() + g0);
+        });
+    }
     return true;
 }
 
 
 namespace {
-template <typename T>
-void append_shift(std::vector<T>& dst, const std::vector<T>& src, T shift, bool keep_negative = false) {
+template <typename T, typename A, typename B>
+void append_shift(std::vector<T, A>& dst, const std::vector<T, B>& src, T shift, bool keep_negative = false) {
     for (T v : src) dst.push_back((keep_negative && v < 0) ? v : static_cast<T>(v + shift));
 }
 // CSR row pointers: drop the leading 0 of every part after the first.
-template <typename T>
-void append_ptr(std::vector<T>& dst, const std::vector<T>& src, T shift) {
+template <typename T, typename A, typename B>
+void append_ptr(std::vector<T, A>& dst, const std::vector<T, B>& src, T shift) {
     if (dst.empty()) dst.push_back(0);
     for (size_t i = 1; i < src.size(); ++i) dst.push_back(static_cast<T>(src[i] + shift));
 }

@@ -33,10 +33,31 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
+#include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace sle_gb300 {
+
+// Allocator that leaves new elements of trivial types uninitialised.  The
+// analysis writes every element of its largest arrays from several threads,
+// so their pages are first touched by the writers instead of a serial fill.
+template <typename T>
+struct UninitAlloc : std::allocator<T> {
+    template <typename U>
+    struct rebind { using other = UninitAlloc<U>; };
+    UninitAlloc() = default;
+    template <typename U>
+    UninitAlloc(const UninitAlloc<U>&) noexcept {}
+    template <typename U>
+    void construct(U* p) noexcept { ::new (static_cast<void*>(p)) U; }
+    template <typename U, typename... A>
+    void construct(U* p, A&&... a) { ::new (static_cast<void*>(p)) U(std::forward<A>(a)...); }
+};
+template <typename T>
+using BigVec = std::vector<T, UninitAlloc<T>>;
 
 struct Topology {
     int32_t n_bus = 0, n_branch = 0, n_meas = 0, slack = 0;
@@ -98,9 +119,9 @@ struct Plan {
     // Gain assembly: targets sorted by (front, local index); local index =
     // row + col * f within the front's L panel.  Pairs are H entry indices.
     std::vector<int32_t> sn_tgt_ptr;   // [n_super+1]
-    std::vector<int32_t> tgt_local;    // [n_tgt]
-    std::vector<int64_t> tgt_pair_ptr; // [n_tgt+1]
-    std::vector<int32_t> pair_a, pair_b;
+    BigVec<int32_t> tgt_local;         // [n_tgt]
+    BigVec<int64_t> tgt_pair_ptr;      // [n_tgt+1]
+    BigVec<int32_t> pair_a, pair_b;
 
     // RHS gather: per permuted state, the H entries in that column.
     std::vector<int32_t> rhs_ptr, rhs_h;
