@@ -199,6 +199,9 @@ typedef struct SLE_ExStats {
     int64_t branch_edits;   /* breaker / branch-parameter edits applied on the device */
     int64_t step_waits;     /* Gauss-Newton steps after which the host waited for the device before
                                issuing the next (none in a batch solve whose loop runs on the device) */
+    /* host wall time in ms, summed since load or reset: symbolic analyses, schedule builds, device
+     * arena builds with their host-to-device copies, CUDA graph captures with instantiation */
+    double analysis_ms, schedule_ms, upload_ms, capture_ms;
 } SLE_ExStats;
 
 SLE_API SLE_StatusCode SLE_CALL sle_ExGetStats(SLE_Handle handle, SLE_ExStats* stats);

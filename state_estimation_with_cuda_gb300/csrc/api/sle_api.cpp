@@ -1394,6 +1394,10 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExGetStats(SLE_Handle handle, SLE_ExStats* s
     st->uploads = s.uploads;
     st->branch_edits = s.branch_edits;
     st->step_waits = s.step_waits;
+    st->analysis_ms = s.analysis_ms;
+    st->schedule_ms = s.schedule_ms;
+    st->upload_ms = s.upload_ms;
+    st->capture_ms = s.capture_ms;
     return SLE_OK;
 }
 

@@ -4,6 +4,7 @@
 #include <thread>
 
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 
 namespace sle_gb300 {
@@ -34,6 +35,14 @@ cudaError_t put(T* dst, const std::vector<T, A>& src, cudaStream_t st) {
 }
 
 inline int nblk(int n) { return (n + 255) / 256; }
+
+// Adds the wall time of its scope to *acc, in milliseconds.
+struct HostTimer {
+    double* acc;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    explicit HostTimer(double* a) : acc(a) {}
+    ~HostTimer() { *acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); }
+};
 
 }  // namespace
 
@@ -130,6 +139,7 @@ int32_t Engine::analyze() {
     t.m_active = model.m_active.data();
     SymbolicParams sp;
     sp.ordering = cfg.ordering;
+    const HostTimer timer(&stats.analysis_ms);
     if (!build_plan(t, sp, plan_, err)) {
         last_error = "symbolic analysis: " + err;
         analyzed_ = false;
@@ -631,14 +641,16 @@ int32_t Engine::upload() {
     const int32_t n = model.n_bus(), nbr = model.n_branch(), m = model.n_meas();
     const Plan& P = plan_;
     mixed_ = cfg.use_double_precision == 0;
-    build_schedule();
-    build_eval_units();
     {
+        const HostTimer timer(&stats.schedule_ms);
+        build_schedule();
+        build_eval_units();
         std::vector<int32_t> ps_of_state(P.n_state);
         for (int32_t p = 0; p < P.n_state; ++p) ps_of_state[P.state_of_ps[p]] = p;
         h_pcol_.resize(P.h_col.size());
         for (size_t h = 0; h < P.h_col.size(); ++h) h_pcol_[h] = ps_of_state[P.h_col[h]];
     }
+    const HostTimer upload_timer(&stats.upload_ms);
     const int64_t nnz_h = static_cast<int64_t>(P.h_col.size());
     const int64_t nnz_y = static_cast<int64_t>(P.y_col.size());
     const int32_t ns = P.n_super;
@@ -1257,6 +1269,7 @@ int32_t Engine::run_device_loop(const SolveParams& sp, int32_t max_iter, int32_t
     if (!cfg.device_loop || !cfg.use_cuda_graphs || cfg.enable_profiling) return -1;
     IterGraph& g = loop_graph_;
     if (!g.exec || std::memcmp(&g.sp, &sp, sizeof(sp)) != 0) {
+        const HostTimer timer(&stats.capture_ms);
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g = IterGraph();
         cudaGraph_t graph = nullptr;
@@ -1331,6 +1344,7 @@ int32_t Engine::run_iteration(const SolveParams& sp, bool refactor) {
     } else {
         IterGraph& g = graphs_[refactor ? 1 : 0];
         if (!g.exec || std::memcmp(&g.sp, &sp, sizeof(sp)) != 0) {
+            const HostTimer timer(&stats.capture_ms);
             if (g.exec) cudaGraphExecDestroy(g.exec);
             g = IterGraph();
             cudaGraph_t graph = nullptr;
@@ -1898,6 +1912,7 @@ int32_t Engine::batch_add_grid(int32_t nb, const int32_t* btype, const double* v
 }
 
 int32_t Engine::analyze_batch() {
+    const HostTimer timer(&stats.analysis_ms);
     const int32_t G = static_cast<int32_t>(grids_.size());
     grid_plans_.assign(G, Plan());
     std::vector<std::string> errs(G);

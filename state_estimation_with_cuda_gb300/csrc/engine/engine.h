@@ -116,6 +116,9 @@ struct StageStats {
     // Gauss-Newton steps after which the host waited for the device before
     // issuing the next (none inside a batch solve whose loop runs on the device)
     int64_t step_waits = 0;
+    // host wall time: symbolic analyses, schedule builds, device arena builds
+    // with their copies, CUDA graph captures with instantiation
+    double analysis_ms = 0, schedule_ms = 0, upload_ms = 0, capture_ms = 0;
 };
 
 class Engine {

@@ -150,7 +150,8 @@ class SLE_ExStats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_int64 * 6), ("ms", ctypes.c_double * 6), ("calls", ctypes.c_int64 * 6),
                 ("iterations", ctypes.c_int64), ("solves", ctypes.c_int64), ("total_launches", ctypes.c_int64),
                 ("analyses", ctypes.c_int64), ("uploads", ctypes.c_int64), ("branch_edits", ctypes.c_int64),
-                ("step_waits", ctypes.c_int64)]
+                ("step_waits", ctypes.c_int64), ("analysis_ms", ctypes.c_double), ("schedule_ms", ctypes.c_double),
+                ("upload_ms", ctypes.c_double), ("capture_ms", ctypes.c_double)]
 
 
 H = ctypes.c_void_p

@@ -165,12 +165,13 @@ def test_extension_options_validate_and_apply():
 
 
 def test_stats_layout_matches_header():
-    """SLE_ExStats as the header declares it: six stage arrays, then the
-    counters, step_waits last."""
+    """SLE_ExStats as the header declares it: six stage arrays, the
+    counters up to step_waits, then the four host phase times."""
     st = native.SLE_ExStats()
     names = [f[0] for f in st._fields_]
-    assert names[-1] == "step_waits" and names[:3] == ["launches", "ms", "calls"]
-    assert ctypes.sizeof(st) == 6 * 8 * 3 + 7 * 8
+    assert names[:3] == ["launches", "ms", "calls"]
+    assert names[-5:] == ["step_waits", "analysis_ms", "schedule_ms", "upload_ms", "capture_ms"]
+    assert ctypes.sizeof(st) == 6 * 8 * 3 + 7 * 8 + 4 * 8
     e = Estimator()
     e.reset_stats()
     s = e.stats()

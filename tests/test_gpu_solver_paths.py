@@ -297,3 +297,21 @@ def test_huber_stall_option_matches_oracle():
                              gamma=1.5)
     assert res.status == ores.status == 1 and res.iterations == ores.iterations == 100
     e.close()
+
+
+def test_host_phase_times_in_stats():
+    """SLE_ExStats carries the host time of the analysis, the schedule, the
+    arena build with its copies and the graph captures (taken by the first
+    solve); a reset clears them."""
+    g = grid2k()
+    e = engine(g)
+    s = e.stats()
+    assert s.analyses == 1 and s.analysis_ms > 0 and s.schedule_ms > 0 and s.upload_ms > 0
+    assert s.capture_ms == 0
+    e.solve_with(max_iterations=10, tolerance=1e-6, flat_start=True)
+    s2 = e.stats()
+    assert s2.capture_ms > 0 and s2.analysis_ms == s.analysis_ms
+    e.reset_stats()
+    s3 = e.stats()
+    assert s3.analysis_ms == s3.schedule_ms == s3.upload_ms == s3.capture_ms == 0
+    e.close()
