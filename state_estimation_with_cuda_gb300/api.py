@@ -121,11 +121,12 @@ class Estimator:
     def load_network(self, grid, z=None):
         """Bulk-load a SyntheticGrid (or any object with the same arrays)."""
         L = self.lib
-        self._arrays = [np.ascontiguousarray(a) for a in (
-            grid.bus_type.astype(np.int32), grid.v_setpoint.astype(np.float64), grid.br_from.astype(np.int32),
-            grid.br_to.astype(np.int32), grid.br_r, grid.br_x, grid.br_b, grid.br_tap, grid.br_shift,
-            grid.br_status.astype(np.int32), grid.m_type.astype(np.int32), grid.m_loc.astype(np.int32),
-            grid.m_end.astype(np.int32), grid.m_sigma, np.asarray(grid.z if z is None else z, np.float64))]
+        i32, f64 = np.int32, np.float64
+        self._arrays = [np.ascontiguousarray(a, dt) for a, dt in (  # no copy when already contiguous and typed
+            (grid.bus_type, i32), (grid.v_setpoint, f64), (grid.br_from, i32), (grid.br_to, i32), (grid.br_r, f64),
+            (grid.br_x, f64), (grid.br_b, f64), (grid.br_tap, f64), (grid.br_shift, f64), (grid.br_status, i32),
+            (grid.m_type, i32), (grid.m_loc, i32), (grid.m_end, i32), (grid.m_sigma, f64),
+            (grid.z if z is None else z, f64))]
         a = self._arrays
         self._check(L.sle_ExLoadNetwork(self.h, grid.n_bus, _ip(a[0]), _dp(a[1]), grid.n_branch, _ip(a[2]), _ip(a[3]),
                                         _dp(a[4]), _dp(a[5]), _dp(a[6]), _dp(a[7]), _dp(a[8]), _ip(a[9]), grid.n_meas,

@@ -279,22 +279,29 @@ void Engine::build_eval_units() {
     const Plan& P = plan_;
     const int32_t m = model.n_meas();
     std::vector<int32_t> twin(m, -1);
-    std::unordered_map<int64_t, int32_t> wait;
-    for (int32_t q = 0; q < m && m >= kEvalPairRows; ++q) {
-        if (P.m_kind[q] != ROW_INJ && P.m_kind[q] != ROW_FLOW) continue;
-        const int32_t ty = model.m_type[q];
-        const int32_t grp = (ty == 2 || ty == 3) ? 0 : (ty == 7 || ty == 8) ? 1 : (ty == 4 || ty == 5) ? 2 : -1;
-        if (grp < 0) continue;
-        const int32_t is_q = (ty == 3 || ty == 8 || ty == 5) ? 1 : 0;
-        const int32_t end = grp == 2 ? (model.m_end[q] != 0 ? 1 : 0) : 0;
-        const int64_t key = ((static_cast<int64_t>(model.m_loc[q]) * 8 + grp * 2 + end) << 1) | is_q;
-        const auto it = wait.find(key ^ 1);
-        if (it != wait.end()) {
-            twin[it->second] = q;
-            twin[q] = -2;
-            wait.erase(it);
-        } else {
-            wait[key] = q;
+    if (m >= kEvalPairRows) {
+        // A row waits in the slot of its (location, group, end), by P or Q,
+        // until the opposite kind arrives there; a later row of the same kind
+        // takes the slot over.  Slots: injections (groups 0, 1) per bus,
+        // flows (group 2) per branch end.
+        const int32_t nb = model.n_bus(), nbr = model.n_branch();
+        std::vector<int32_t> wait(2 * (2 * static_cast<size_t>(nb) + 2 * static_cast<size_t>(nbr)), -1);
+        for (int32_t q = 0; q < m; ++q) {
+            if (P.m_kind[q] != ROW_INJ && P.m_kind[q] != ROW_FLOW) continue;
+            const int32_t ty = model.m_type[q];
+            const int32_t grp = (ty == 2 || ty == 3) ? 0 : (ty == 7 || ty == 8) ? 1 : (ty == 4 || ty == 5) ? 2 : -1;
+            if (grp < 0) continue;
+            const int32_t is_q = (ty == 3 || ty == 8 || ty == 5) ? 1 : 0;
+            const int64_t loc = model.m_loc[q];
+            const int64_t slot = grp < 2 ? loc * 2 + grp : 2 * static_cast<int64_t>(nb) + loc * 2 + (model.m_end[q] != 0 ? 1 : 0);
+            int32_t& other = wait[slot * 2 + (is_q ^ 1)];
+            if (other >= 0) {
+                twin[other] = q;
+                twin[q] = -2;
+                other = -1;
+            } else {
+                wait[slot * 2 + is_q] = q;
+            }
         }
     }
     ev_unit_.clear();

@@ -448,8 +448,14 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
         });
     }
 
+    // --- bus graph -------------------------------------------------------------------
+    std::vector<int32_t> gptr, gadj;
+    bus_graph(t, P.y_ptr, P.y_col, gptr, gadj);
+
     // --- H pattern ------------------------------------------------------------------
-    {
+    // Built on a thread of its own while the bus graph is ordered (the ordering
+    // does not read it); joined before anything else returns or reads it.
+    std::thread h_pattern([&] {
         // Injection-row column lists per bus (computed once per bus, in
         // parallel ranges): the angle and magnitude columns of the bus's Ybus
         // row, sorted and unique, with each Ybus entry's positions in it.
@@ -546,11 +552,9 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
                 for (int32_t h = P.h_ptr[q]; h < P.h_ptr[q + 1]; ++h) P.h_row[h] = static_cast<int32_t>(q);
             }
         });
-    }
+    });
 
     // --- ordering on the bus graph -----------------------------------------------------
-    std::vector<int32_t> gptr, gadj;
-    bus_graph(t, P.y_ptr, P.y_col, gptr, gadj);
     std::vector<int32_t> order;
     AmdTrace trace;
     const bool traced = prm.ordering != 1 && prm.ordering != 2;
@@ -563,6 +567,7 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     } else {
         order = amd_order(n, gptr, gadj, &trace);
     }
+    h_pattern.join();
     if (static_cast<int32_t>(order.size()) != n) { err = "ordering failed"; return false; }
     std::vector<int32_t> pos(n, -1);
     for (int32_t k = 0; k < n; ++k) pos[order[k]] = k;
