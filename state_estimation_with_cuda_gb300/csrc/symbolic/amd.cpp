@@ -78,25 +78,29 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         }
         e_pool[nd[i].e_beg + nd[i].e_len++] = v;
     };
-    // members of supervariable i: chain from m_head[i] to m_tail[i] through m_next
-    std::vector<int32_t> m_head(n), m_tail(n), m_next(n, -1);
-    for (int32_t i = 0; i < n; ++i) m_head[i] = m_tail[i] = i;
+    // members of supervariable i: chain from mc[i].head to mc[i].tail through .next
+    struct Chain { int32_t head, tail, next; };
+    std::vector<Chain> mc(n);
+    for (int32_t i = 0; i < n; ++i) mc[i] = Chain{i, i, -1};
 
     // Degree buckets (doubly linked lists).
-    std::vector<int32_t> head(n + 1, -1), nxt(n, -1), prv(n, -1);
+    struct Link { int32_t nxt, prv; };  // one line per node for both neighbours
+    std::vector<int32_t> head(n + 1, -1);
+    std::vector<Link> lk(n, Link{-1, -1});
     auto bucket_insert = [&](int32_t i) {
         const int32_t d = std::min(nd[i].deg, n);
-        nxt[i] = head[d];
-        prv[i] = -1;
-        if (head[d] >= 0) prv[head[d]] = i;
+        lk[i].nxt = head[d];
+        lk[i].prv = -1;
+        if (head[d] >= 0) lk[head[d]].prv = i;
         head[d] = i;
     };
     auto bucket_remove = [&](int32_t i) {
         const int32_t d = std::min(nd[i].deg, n);
-        if (prv[i] >= 0) nxt[prv[i]] = nxt[i];
-        else head[d] = nxt[i];
-        if (nxt[i] >= 0) prv[nxt[i]] = prv[i];
-        nxt[i] = prv[i] = -1;
+        const Link l = lk[i];
+        if (l.prv >= 0) lk[l.prv].nxt = l.nxt;
+        else head[d] = l.nxt;
+        if (l.nxt >= 0) lk[l.nxt].prv = l.prv;
+        lk[i] = Link{-1, -1};
     };
     for (int32_t i = n - 1; i >= 0; --i) bucket_insert(i);
 
@@ -139,12 +143,14 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         nd[p].a_len = 0;
         nd[p].e_len = 0;
         status[p] = ELEM;
-        for (int32_t mb = m_head[p]; mb >= 0; mb = m_next[mb]) order.push_back(mb);
+        for (int32_t mb = mc[p].head; mb >= 0; mb = mc[mb].next) order.push_back(mb);
         eliminated += nd[p].nv;
         int32_t lp_w = 0;
         for (int32_t i : Lp) {
             bucket_remove(i);
             lp_w += nd[i].nv;
+            __builtin_prefetch(&e_pool[nd[i].e_beg]);
+            __builtin_prefetch(&a_pool[nd[i].a_beg]);
         }
         // --- |Le \ Lp| for elements adjacent to Lp -------------------------------
         ++tag;  // second tag for w
@@ -159,6 +165,9 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
                 }
                 nd[e].w -= nd[i].nv;
             }
+            // the next pass reads the nodes of i's remaining neighbours
+            const int32_t* ap = a_pool.data() + nd[i].a_beg;
+            for (int32_t x = 0; x < nd[i].a_len; ++x) __builtin_prefetch(&nd[ap[x]]);
         }
         // --- update variables in Lp ---------------------------------------------------
         // flag == tag - 1 marks membership in Lp.
@@ -235,8 +244,8 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
                     nd[i].deg = std::max(0, nd[i].deg - nd[j].nv);
                     nd[j].nv = 0;
                     status[j] = DEAD;
-                    m_next[m_tail[i]] = m_head[j];
-                    m_tail[i] = m_tail[j];
+                    mc[mc[i].tail].next = mc[j].head;
+                    mc[i].tail = mc[j].tail;
                     nd[j].a_len = 0;
                     nd[j].e_len = 0;
                     ai.erase(std::remove(ai.begin(), ai.end(), j), ai.end());
@@ -259,7 +268,7 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         if (trace) {
             trace->piv_end.push_back(eliminated);
             for (int64_t y = nd[p].l_beg; y < nd[p].l_beg + nd[p].l_len; ++y)
-                for (int32_t mb = m_head[l_pool[y]]; mb >= 0; mb = m_next[mb]) trace->lp.push_back(mb);
+                for (int32_t mb = mc[l_pool[y]].head; mb >= 0; mb = mc[mb].next) trace->lp.push_back(mb);
             trace->lp_ptr.push_back(static_cast<int64_t>(trace->lp.size()));
         }
     }
