@@ -652,10 +652,6 @@ int32_t Engine::upload() {
         const HostTimer timer(&stats.schedule_ms);
         build_schedule();
         build_eval_units();
-        std::vector<int32_t> ps_of_state(P.n_state);
-        for (int32_t p = 0; p < P.n_state; ++p) ps_of_state[P.state_of_ps[p]] = p;
-        h_pcol_.resize(P.h_col.size());
-        for (size_t h = 0; h < P.h_col.size(); ++h) h_pcol_[h] = ps_of_state[P.h_col[h]];
     }
     const HostTimer upload_timer(&stats.upload_ms);
     const int64_t nnz_h = static_cast<int64_t>(P.h_col.size());
@@ -902,7 +898,7 @@ int32_t Engine::upload() {
     chk(put(const_cast<double*>(net_.m_w), model.m_w, st_));
     chk(put(const_cast<int32_t*>(net_.h_ptr), P.h_ptr, st_));
     chk(put(const_cast<int32_t*>(net_.h_row), P.h_row, st_));
-    chk(put(const_cast<int32_t*>(net_.h_pcol), h_pcol_, st_));
+    chk(put(const_cast<int32_t*>(net_.h_pcol), P.h_pcol, st_));
     chk(put(const_cast<int32_t*>(fac_.sn_c0), P.sn_c0, st_));
     chk(put(const_cast<int32_t*>(fac_.sn_f), P.sn_f, st_));
     chk(put(const_cast<int32_t*>(fac_.sn_parent), P.sn_parent, st_));

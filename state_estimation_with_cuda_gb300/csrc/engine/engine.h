@@ -323,7 +323,7 @@ private:
     std::vector<int32_t> stream_iters_;
     int32_t analyze_batch();
     std::vector<int64_t> lay_lx_off_, lay_u_off_;
-    std::vector<int32_t> lay_u_ld_, h_pcol_;
+    std::vector<int32_t> lay_u_ld_;
     std::vector<uint8_t> lay_u_big_;
     int64_t lay_lx_size_ = 0, lay_u_size_ = 0;
     int32_t* d_small_ = nullptr;

@@ -912,32 +912,46 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     }
 
     // --- RHS gather ------------------------------------------------------------------------
-    // H entries by permuted state (a CSR transpose): ranges of entries count
-    // per thread, the offsets run state-major then range-minor, so each
-    // state's entries stay in ascending order.
+    // Each H entry's permuted column, then the entries by permuted state (a
+    // CSR transpose): ranges of entries count per thread, the offsets run
+    // state-major then range-minor, so each state's entries stay in
+    // ascending order.
     {
         const int64_t nnz = static_cast<int64_t>(P.h_col.size());
         const int32_t ns_ = P.n_state;
         const int32_t parts = host_threads(nnz, 1 << 18);
-        std::vector<std::vector<int32_t>> cnt(parts, std::vector<int32_t>(ns_, 0));
+        P.h_pcol.resize(static_cast<size_t>(nnz));
+        std::vector<std::vector<int32_t>> cnt(parts);
         parallel_ranges(nnz, parts, [&](int32_t t, int64_t h0, int64_t h1) {
             auto& c = cnt[t];
-            for (int64_t h = h0; h < h1; ++h) ++c[ps_of_state[P.h_col[h]]];
-        });
-        P.rhs_ptr.assign(static_cast<size_t>(ns_) + 1, 0);
-        for (int32_t p = 0; p < ns_; ++p) {
-            int32_t run = P.rhs_ptr[p];
-            for (int32_t t = 0; t < parts; ++t) {
-                const int32_t c = cnt[t][p];
-                cnt[t][p] = run;  // this range's first slot of state p
-                run += c;
+            c.assign(static_cast<size_t>(ns_), 0);
+            for (int64_t h = h0; h < h1; ++h) {
+                const int32_t pc = ps_of_state[P.h_col[h]];
+                P.h_pcol[h] = pc;
+                ++c[pc];
             }
-            P.rhs_ptr[p + 1] = run;
-        }
+        });
+        // per state: the ranges' first slots relative to the state's start
+        P.rhs_ptr.assign(static_cast<size_t>(ns_) + 1, 0);
+        parallel_ranges(ns_, host_threads(ns_, 1 << 15), [&](int32_t, int64_t p0, int64_t p1) {
+            for (int64_t p = p0; p < p1; ++p) {
+                int32_t run = 0;
+                for (int32_t t = 0; t < parts; ++t) {
+                    const int32_t c = cnt[t][p];
+                    cnt[t][p] = run;
+                    run += c;
+                }
+                P.rhs_ptr[p + 1] = run;
+            }
+        });
+        for (int32_t p = 0; p < ns_; ++p) P.rhs_ptr[p + 1] += P.rhs_ptr[p];
         P.rhs_h.resize(nnz);
         parallel_ranges(nnz, parts, [&](int32_t t, int64_t h0, int64_t h1) {
             auto& o = cnt[t];
-            for (int64_t h = h0; h < h1; ++h) P.rhs_h[o[ps_of_state[P.h_col[h]]]++] = static_cast<int32_t>(h);
+            for (int64_t h = h0; h < h1; ++h) {
+                const int32_t pc = P.h_pcol[h];
+                P.rhs_h[P.rhs_ptr[pc] + o[pc]++] = static_cast<int32_t>(h);
+            }
         });
     }
     // --- gain assembly targets --------------------------------------------------------
@@ -961,17 +975,20 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
         }
         P.pair_a.resize(static_cast<size_t>(run));  // written (first touched) by the workers below
         P.pair_b.resize(static_cast<size_t>(run));
-        // hps[h] = permuted column of entry h; ge[h] = entries of h's row at
-        // permuted columns >= h's, h included
-        std::vector<int32_t> hps(static_cast<size_t>(nnz)), ge(static_cast<size_t>(nnz));
+        // ge[h] = entries of h's row at permuted columns >= h's, h included;
+        // hrow[h] = h's row range
+        const BigVec<int32_t>& hps = P.h_pcol;
+        BigVec<int32_t> ge(static_cast<size_t>(nnz));
+        struct RowRange { int32_t beg, end; };
+        BigVec<RowRange> hrow(static_cast<size_t>(nnz));
         parallel_ranges(m, host_threads(m, 4096), [&](int32_t, int64_t q0, int64_t q1) {
             for (int64_t q = q0; q < q1; ++q) {
                 const int32_t h0 = P.h_ptr[q], h1 = P.h_ptr[q + 1];
-                for (int32_t x = h0; x < h1; ++x) hps[x] = ps_of_state[P.h_col[x]];
                 for (int32_t x = h0; x < h1; ++x) {
                     int32_t c = 0;
                     for (int32_t y = h0; y < h1; ++y) c += hps[y] >= hps[x];
                     ge[x] = c;
+                    hrow[x] = RowRange{h0, h1};
                 }
             }
         });
@@ -997,47 +1014,50 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
         std::vector<std::vector<int64_t>> t_start(nthr);
         std::vector<uint8_t> bad(nthr, 0);
         parallel_ranges(nthr, nthr, [&](int32_t t, int64_t, int64_t) {
-            std::vector<PairRec> rec, tmp;
+            std::vector<PairRec> rec;
             std::vector<int32_t> hist;
+            std::vector<int32_t> where(static_cast<size_t>(P.n_state), -1);  // state -> row in the front
             for (int32_t k = fr_cut[t]; k < fr_cut[t + 1]; ++k) {
                 const int32_t f = P.sn_f[k], c0 = P.sn_c0[k], nc = P.sn_c0[k + 1] - c0;
                 const int32_t* rows = P.sn_rows.data() + P.sn_rows_off[k];
-                rec.clear();
+                for (int32_t r = 0; r < f; ++r) where[rows[r]] = r;
+                rec.resize(static_cast<size_t>(fr_off[k + 1] - fr_off[k]));
+                size_t nr = 0;
                 for (int32_t lo = c0; lo < c0 + nc; ++lo)
                     for (int32_t i = P.rhs_ptr[lo]; i < P.rhs_ptr[lo + 1]; ++i) {
-                        const int32_t h = P.rhs_h[i], q = P.h_row[h];
-                        for (int32_t h2 = P.h_ptr[q]; h2 < P.h_ptr[q + 1]; ++h2) {
+                        const int32_t h = P.rhs_h[i];
+                        for (int32_t h2 = hrow[h].beg; h2 < hrow[h].end; ++h2) {
                             const int32_t hi = hps[h2];
                             if (hi < lo) continue;
-                            int32_t r = hi - c0;
-                            if (r >= nc) {  // below the front's own columns
-                                const int32_t* it = std::lower_bound(rows + nc, rows + f, hi);
-                                if (it == rows + f || *it != hi) {
-                                    bad[t] = 1;
-                                    return;
-                                }
-                                r = static_cast<int32_t>(it - rows);
+                            const int32_t r = where[hi];
+                            if (r < 0) {  // outside the front's structure
+                                bad[t] = 1;
+                                return;
                             }
-                            rec.push_back({r + (lo - c0) * f, std::min(h, h2), std::max(h, h2)});
+                            rec[nr++] = {r + (lo - c0) * f, std::min(h, h2), std::max(h, h2)};
                         }
                     }
-                // stable counting sort by local index (local < f * nc)
+                for (int32_t r = 0; r < f; ++r) where[rows[r]] = -1;
+                // stable counting sort by local index (local < f * nc), the
+                // targets found in the prefix pass, the pairs scattered into
+                // place
                 const int32_t range = f * nc;
+                const int64_t o = fr_off[k];
                 hist.assign(static_cast<size_t>(range) + 1, 0);
                 for (const PairRec& x : rec) ++hist[x.local + 1];
-                for (int32_t v = 0; v < range; ++v) hist[v + 1] += hist[v];
-                tmp.resize(rec.size());
-                for (const PairRec& x : rec) tmp[hist[x.local]++] = x;
-                const int64_t o = fr_off[k];
                 int32_t c = 0;
-                for (size_t i = 0; i < tmp.size(); ++i) {
-                    if (i == 0 || tmp[i].local != tmp[i - 1].local) {
-                        t_local[t].push_back(tmp[i].local);
-                        t_start[t].push_back(o + static_cast<int64_t>(i));
+                for (int32_t v = 0; v < range; ++v) {
+                    if (hist[v + 1] > 0) {
+                        t_local[t].push_back(v);
+                        t_start[t].push_back(o + hist[v]);
                         ++c;
                     }
-                    P.pair_a[o + i] = tmp[i].a;
-                    P.pair_b[o + i] = tmp[i].b;
+                    hist[v + 1] += hist[v];
+                }
+                for (const PairRec& x : rec) {
+                    const int64_t at = o + hist[x.local]++;
+                    P.pair_a[at] = x.a;
+                    P.pair_b[at] = x.b;
                 }
                 ntg[k] = c;
             }
@@ -1118,6 +1138,7 @@ void merge_plans(const std::vector<const Plan*>& parts, const std::vector<int32_
         append_shift(M.pair_b, P.pair_b, h0);
         append_ptr(M.rhs_ptr, P.rhs_ptr, static_cast<int32_t>(M.rhs_h.size()));
         append_shift(M.rhs_h, P.rhs_h, h0);
+        append_shift(M.h_pcol, P.h_pcol, st0);
         M.nnz_l += P.nnz_l;
         M.flops += P.flops;
         M.max_front = std::max(M.max_front, P.max_front);

@@ -125,6 +125,8 @@ struct Plan {
 
     // RHS gather: per permuted state, the H entries in that column.
     std::vector<int32_t> rhs_ptr, rhs_h;
+    // Permuted state index of each H entry (the entry's column).
+    BigVec<int32_t> h_pcol;
 
     // Statistics.
     int64_t nnz_l = 0;        // stored entries of L (lower trapezoids of the panels)
