@@ -19,6 +19,7 @@ void Model::ensure_names() {
         bus_map[bus_id[i]] = i;
     }
     br_id.resize(n_branch());
+    br_sd.resize(n_branch());
     for (int32_t k = 0; k < n_branch(); ++k) {
         if (br_id[k].empty()) br_id[k] = "BR" + std::to_string(k);
         br_map[br_id[k]] = k;
@@ -296,7 +297,7 @@ void Model::load_soa(int32_t nb, const int32_t* btype, const double* vset, int32
     bus_q.assign(nb, 0.0);
     bus_v.assign(vset, vset + nb);
     bus_th.assign(nb, 0.0);
-    bus_id.assign(nb, std::string());
+    bus_id.clear();  // names: default ones, made by ensure_names() at the first lookup
     for (int32_t i = 0; i < nb; ++i)
         if (btype[i] == 2) slack = i;
     br_from.assign(from, from + nbr);
@@ -310,8 +311,8 @@ void Model::load_soa(int32_t nb, const int32_t* btype, const double* vset, int32
     br_xfmr.assign(nbr, 0);
     br_closed.resize(nbr);
     for (int32_t k = 0; k < nbr; ++k) br_closed[k] = status ? (status[k] ? 1 : 0) : 1;
-    br_id.assign(nbr, std::string());
-    br_sd.assign(nbr, std::string());
+    br_id.clear();
+    br_sd.clear();
     m_type.assign(mtype, mtype + nm);
     m_loc.assign(mloc, mloc + nm);
     m_end.assign(mend, mend + nm);
@@ -328,7 +329,7 @@ void Model::load_soa(int32_t nb, const int32_t* btype, const double* vset, int32
     m_active.assign(nm, 1);
     m_est.assign(nm, 0.0);
     m_res.assign(nm, 0.0);
-    m_id.assign(nm, std::string());
+    m_id.clear();
     names_ready = false;
     structure_dirty = true;
 }

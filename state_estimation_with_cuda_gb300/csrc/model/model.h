@@ -26,6 +26,9 @@ struct Meter {
 };
 
 struct Model {
+    // Names (bus_id, br_id, br_sd, m_id) may be shorter than the element
+    // arrays after a bulk load: ensure_names() sizes them and gives unnamed
+    // elements their default names; every lookup calls it first.
     // buses
     std::vector<std::string> bus_id;
     std::vector<double> bus_kv, bus_vset, bus_p, bus_q;

@@ -131,6 +131,28 @@ def test_bulk_load_validates_indices():
     e.close()
 
 
+def test_bulk_load_default_names_and_edits():
+    """A bulk-loaded model has no names until the first lookup, which gives
+    every element its default name; adding and removing elements by name
+    keep the names aligned with the element arrays."""
+    from state_estimation_with_cuda_gb300 import workloads
+
+    g = workloads.make("grid14")
+    e = Estimator()
+    e.load_network(g)
+    lib = e.lib
+    assert lib.sle_GetMeasurementIdByIndex(e.h, 0) == b"M0"
+    assert lib.sle_GetMeasurementIdByIndex(e.h, g.n_meas - 1) == b"M%d" % (g.n_meas - 1)
+    assert lib.sle_RemoveBranch(e.h, b"BR3") == 0
+    nb, nbr, nm = e.counts()
+    assert nbr == g.n_branch - 1
+    assert lib.sle_GetMeasurementIdByIndex(e.h, nm - 1) is not None
+    assert lib.sle_GetMeasurementIdByIndex(e.h, nm) is None
+    assert lib.sle_RemoveBus(e.h, b"BUS5") == 0
+    assert e.counts()[0] == nb - 1
+    e.close()
+
+
 def test_removal_compacts_indices():
     e = Estimator()
     e.load_ieee14()
