@@ -4,6 +4,7 @@
 #include "amd.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -48,20 +49,23 @@ struct RangeLists {
     std::vector<std::vector<int32_t>> data, len;
     explicit RangeLists(int32_t parts) : data(parts), len(parts) {}
     void gather(int64_t n, std::vector<int32_t>& ptr, std::vector<int32_t>& out) const {
+        const int32_t parts = static_cast<int32_t>(data.size());
         ptr.assign(static_cast<size_t>(n) + 1, 0);
-        size_t total = 0;
-        for (auto& d : data) total += d.size();
-        out.resize(total);
-        int64_t i = 0;
-        size_t o = 0;
-        for (size_t t = 0; t < data.size(); ++t) {
-            std::copy(data[t].begin(), data[t].end(), out.begin() + o);
-            o += data[t].size();
-            for (int32_t l : len[t]) {
-                ptr[i + 1] = ptr[i] + l;
-                ++i;
-            }
+        std::vector<size_t> o(parts + 1, 0);
+        std::vector<int64_t> i0(parts + 1, 0);
+        for (int32_t t = 0; t < parts; ++t) {
+            o[t + 1] = o[t] + data[t].size();
+            i0[t + 1] = i0[t] + static_cast<int64_t>(len[t].size());
         }
+        out.resize(o[parts]);
+        parallel_ranges(parts, parts, [&](int32_t t, int64_t, int64_t) {
+            std::copy(data[t].begin(), data[t].end(), out.begin() + o[t]);
+            int32_t run = static_cast<int32_t>(o[t]);
+            for (size_t x = 0; x < len[t].size(); ++x) {
+                run += len[t][x];
+                ptr[i0[t] + static_cast<int64_t>(x) + 1] = run;
+            }
+        });
     }
 };
 
@@ -317,31 +321,42 @@ void bus_graph(const Topology& t, const std::vector<int32_t>& y_ptr, const std::
     // injection row at c couples every pair of {c} and c's Ybus neighbours,
     // a flow or current row couples the branch's two ends.  Bus a's list is
     // therefore the Ybus rows of the injection-measured buses of a's own Ybus
-    // row, plus a's flow partners; each list is built on its own (sorted,
-    // unique), buses in parallel ranges.
-    const int32_t n = t.n_bus;
-    std::vector<uint8_t> has_inj(n, 0);
-    std::vector<int32_t> fptr(static_cast<size_t>(n) + 1, 0), fpart;
-    auto flow_row = [&](int32_t q) {
-        const int32_t ty = t.m_type[q];
-        return (!t.m_active || t.m_active[q]) && (ty == 4 || ty == 5 || ty == 6) &&
-               t.br_from[t.m_loc[q]] != t.br_to[t.m_loc[q]];
-    };
-    for (int32_t q = 0; q < t.n_meas; ++q) {
-        if (t.m_active && !t.m_active[q]) continue;
-        if (is_inj_type(t.m_type[q])) has_inj[t.m_loc[q]] = 1;
-        if (flow_row(q)) {
-            ++fptr[t.br_from[t.m_loc[q]] + 1];
-            ++fptr[t.br_to[t.m_loc[q]] + 1];
+    // row, plus the far ends of a's flow-measured branches; each list is
+    // built on its own (sorted, unique), buses in parallel ranges.
+    const int32_t n = t.n_bus, nbr = t.n_branch;
+    // marks: injection-measured buses, flow-measured branches (rows in
+    // parallel ranges; a mark is only ever set to 1)
+    std::unique_ptr<std::atomic<uint8_t>[]> has_inj(new std::atomic<uint8_t>[n]);
+    std::unique_ptr<std::atomic<uint8_t>[]> has_flow(new std::atomic<uint8_t>[std::max(nbr, 1)]);
+    parallel_ranges(n, host_threads(n, 1 << 16), [&](int32_t, int64_t i0, int64_t i1) {
+        for (int64_t i = i0; i < i1; ++i) has_inj[i].store(0, std::memory_order_relaxed);
+    });
+    parallel_ranges(nbr, host_threads(nbr, 1 << 16), [&](int32_t, int64_t k0, int64_t k1) {
+        for (int64_t k = k0; k < k1; ++k) has_flow[k].store(0, std::memory_order_relaxed);
+    });
+    parallel_ranges(t.n_meas, host_threads(t.n_meas, 1 << 16), [&](int32_t, int64_t q0, int64_t q1) {
+        for (int64_t q = q0; q < q1; ++q) {
+            if (t.m_active && !t.m_active[q]) continue;
+            const int32_t ty = t.m_type[q], loc = t.m_loc[q];
+            if (is_inj_type(ty)) has_inj[loc].store(1, std::memory_order_relaxed);
+            if ((ty == 4 || ty == 5 || ty == 6) && t.br_from[loc] != t.br_to[loc])
+                has_flow[loc].store(1, std::memory_order_relaxed);
         }
-    }
+    });
+    // flow-measured branches by end bus (CSR)
+    std::vector<int32_t> fptr(static_cast<size_t>(n) + 1, 0), fpart;
+    for (int32_t k = 0; k < nbr; ++k)
+        if (has_flow[k].load(std::memory_order_relaxed)) {
+            ++fptr[t.br_from[k] + 1];
+            ++fptr[t.br_to[k] + 1];
+        }
     for (int32_t i = 0; i < n; ++i) fptr[i + 1] += fptr[i];
     fpart.resize(fptr[n]);
     {
         std::vector<int32_t> fill(fptr.begin(), fptr.end() - 1);
-        for (int32_t q = 0; q < t.n_meas; ++q)
-            if (flow_row(q)) {
-                const int32_t i = t.br_from[t.m_loc[q]], j = t.br_to[t.m_loc[q]];
+        for (int32_t k = 0; k < nbr; ++k)
+            if (has_flow[k].load(std::memory_order_relaxed)) {
+                const int32_t i = t.br_from[k], j = t.br_to[k];
                 fpart[fill[i]++] = j;
                 fpart[fill[j]++] = i;
             }
@@ -358,7 +373,7 @@ void bus_graph(const Topology& t, const std::vector<int32_t>& y_ptr, const std::
             mark[a] = a;
             for (int32_t e = y_ptr[a]; e < y_ptr[a + 1]; ++e) {
                 const int32_t c = y_col[e];
-                if (!has_inj[c]) continue;
+                if (!has_inj[c].load(std::memory_order_relaxed)) continue;
                 for (int32_t f = y_ptr[c]; f < y_ptr[c + 1]; ++f) {
                     const int32_t b = y_col[f];
                     if (mark[b] != a) {
