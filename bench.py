@@ -66,6 +66,7 @@ FLEET = 200
 SNAPS_PER_GRID = 4
 BREAKER_FRAC = 0.005
 STEP_REQUESTS = 150   # requests per step (one window of the stream)
+COLD_STARTS = 3  # grid200k cold flat starts per precision (the median is reported)
 HUBER_STALL = 1e-5    # the grid200k leg's Huber stall safeguard (option huber_stall)
 REF_STEP_SECONDS = 4.0  # CPU seconds of each window the host-core reference arm spends
 
@@ -620,7 +621,10 @@ def run_grid200k(oracle_state=None):
         w.upload_model()
         w.solve_with(max_iterations=3, tolerance=1e-6, flat_start=True)
         w.close()
-    for mixed in (True, False):
+
+    def cold_flat_start(mixed):
+        """One cold flat start on a fresh handle: its wall time, its host
+        phases (upload = analysis + schedule + arena and copies) and the handle."""
         t0 = time.perf_counter()
         e = Estimator()
         e.set_option("use_double_precision", 0 if mixed else 1)
@@ -628,14 +632,25 @@ def run_grid200k(oracle_state=None):
         t_load = time.perf_counter()
         e.upload_model()
         t_up = time.perf_counter()
-        rc, rc0 = e.solve_with(max_iterations=30, tolerance=1e-6, flat_start=True)
+        e.solve_with(max_iterations=30, tolerance=1e-6, flat_start=True)
         cold = time.perf_counter() - t0
         st = e.stats()
-        # the cold flat start's host phases (upload = analysis + schedule + arena and copies)
         phases = {"handle_and_load": round((t_load - t0) * 1e3, 1), "analysis": round(st.analysis_ms, 1),
                   "schedule": round(st.schedule_ms, 1), "arena_and_copies": round(st.upload_ms, 1),
                   "upload_total": round((t_up - t_load) * 1e3, 1),
                   "first_solve": round((t0 + cold - t_up) * 1e3, 1), "graph_capture_in_solve": round(st.capture_ms, 1)}
+        return cold, phases, e
+
+    for mixed in (True, False):
+        # three cold starts, each on a fresh handle; the median one is reported
+        runs = []
+        for k in range(COLD_STARTS):
+            cold, phases, e = cold_flat_start(mixed)
+            runs.append((cold, phases))
+            if k + 1 < COLD_STARTS:
+                e.close()
+        cold_samples = [round(c * 1e3, 1) for c, _ in runs]
+        cold, phases = sorted(runs, key=lambda r: r[0])[COLD_STARTS // 2]
         e.solve_with(max_iterations=2, tolerance=1e-6, flat_start=True)  # graphs of both iteration kinds
         t0 = time.perf_counter()
         rc, r = e.solve_with(max_iterations=30, tolerance=1e-6, flat_start=True)
@@ -653,7 +668,8 @@ def run_grid200k(oracle_state=None):
                                            "ms": round((time.perf_counter() - t0) * 1e3, 1)}
         e.close()
         out["mixed" if mixed else "fp64"] = {
-            "cold_flat_start_ms": round(cold * 1e3, 1), "cold_phases_ms": phases, "flat_start_ms": round(dt * 1e3, 2),
+            "cold_flat_start_ms": round(cold * 1e3, 1), "cold_samples_ms": cold_samples, "cold_phases_ms": phases,
+            "flat_start_ms": round(dt * 1e3, 2),
             "iterations": r.iterations, "status": r.status, "huber": huber}
     out["mixed_vs_fp64_max_state_err"] = float(max(np.abs(states[True][0] - states[False][0]).max(),
                                                    np.abs(states[True][1] - states[False][1]).max()))
@@ -664,7 +680,8 @@ def run_grid200k(oracle_state=None):
             out["%s_vs_oracle_max_state_err" % ("mixed" if mixed else "fp64")] = err
         out["oracle_iterations"] = iters
     out["config"] = ("%d buses, %d branches, %d rows, 2%% gross errors on telemetry rows; flat start, "
-                     "max|dx| < 1e-6; cold = load + analysis + upload + solve" % (g.n_bus, g.n_branch, g.n_meas))
+                     "max|dx| < 1e-6; cold = load + analysis + upload + solve on a fresh handle, median of %d"
+                     % (g.n_bus, g.n_branch, g.n_meas, COLD_STARTS))
     return out
 
 
