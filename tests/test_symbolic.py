@@ -22,6 +22,7 @@ def cases():
         "grid14": workloads.make("grid14"),
         "grid2k": SyntheticGrid(2000, 2800, 0x5E01),
         "open_branches": _with_open(SyntheticGrid(300, 420, 9)),
+        "grid20k_open": _with_open(SyntheticGrid(20000, 28000, 0x5E77)),
     }
 
 
@@ -31,7 +32,7 @@ def _with_open(g):
     return g
 
 
-@pytest.fixture(scope="module", params=["ieee14", "grid14", "grid2k", "open_branches"])
+@pytest.fixture(scope="module", params=["ieee14", "grid14", "grid2k", "open_branches", "grid20k_open"])
 def case(request):
     g = cases()[request.param]
     return g, load(g), Oracle(g)
