@@ -120,11 +120,15 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         // --- new element Lp -------------------------------------------------------
         Lp.clear();
         nd[p].flag = tag;
-        for (int32_t x = 0; x < nd[p].e_len; ++x) {
-            const int32_t e = e_pool[nd[p].e_beg + x];
+        // (list lengths and starts are read once: the loops store only into
+        // other nodes)
+        const int32_t* ep = e_pool.data() + nd[p].e_beg;
+        for (int32_t x = 0, ne = nd[p].e_len; x < ne; ++x) {
+            const int32_t e = ep[x];
             if (status[e] != ELEM) continue;
-            for (int32_t y = 0; y < nd[e].l_len; ++y) {
-                const int32_t i = l_pool[nd[e].l_beg + y];
+            const int32_t* le = l_pool.data() + nd[e].l_beg;
+            for (int32_t y = 0, nl = nd[e].l_len; y < nl; ++y) {
+                const int32_t i = le[y];
                 if (status[i] == VAR && nd[i].flag != tag) {
                     nd[i].flag = tag;
                     Lp.push_back(i);
@@ -133,8 +137,9 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
             status[e] = DEAD;  // absorbed into p
             nd[e].l_len = 0;
         }
-        for (int32_t x = 0; x < nd[p].a_len; ++x) {
-            const int32_t i = a_pool[nd[p].a_beg + x];
+        const int32_t* pa = a_pool.data() + nd[p].a_beg;
+        for (int32_t x = 0, na = nd[p].a_len; x < na; ++x) {
+            const int32_t i = pa[x];
             if (status[i] == VAR && nd[i].flag != tag) {
                 nd[i].flag = tag;
                 Lp.push_back(i);
@@ -156,18 +161,20 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         ++tag;  // second tag for w
         const int32_t wt = tag;
         for (int32_t i : Lp) {
-            for (int32_t x = 0; x < nd[i].e_len; ++x) {
-                const int32_t e = e_pool[nd[i].e_beg + x];
+            const Node ni = nd[i];
+            const int32_t* ei = e_pool.data() + ni.e_beg;
+            for (int32_t x = 0; x < ni.e_len; ++x) {
+                const int32_t e = ei[x];
                 if (status[e] != ELEM) continue;
                 if (nd[e].wtag != wt) {
                     nd[e].w = nd[e].l_w;
                     nd[e].wtag = wt;
                 }
-                nd[e].w -= nd[i].nv;
+                nd[e].w -= ni.nv;
             }
             // the next pass reads the nodes of i's remaining neighbours
-            const int32_t* ap = a_pool.data() + nd[i].a_beg;
-            for (int32_t x = 0; x < nd[i].a_len; ++x) __builtin_prefetch(&nd[ap[x]]);
+            const int32_t* ap = a_pool.data() + ni.a_beg;
+            for (int32_t x = 0; x < ni.a_len; ++x) __builtin_prefetch(&nd[ap[x]]);
         }
         // --- update variables in Lp ---------------------------------------------------
         // flag == tag - 1 marks membership in Lp.
@@ -175,7 +182,7 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         for (int32_t i : Lp) {
             int32_t* ei = e_pool.data() + nd[i].e_beg;
             int32_t k2 = 0, ext = 0;
-            for (int32_t x = 0; x < nd[i].e_len; ++x) {
+            for (int32_t x = 0, ne = nd[i].e_len; x < ne; ++x) {
                 const int32_t e = ei[x];
                 if (status[e] != ELEM || e == p) continue;
                 if (nd[e].wtag == wt && nd[e].w <= 0) {  // Le subset of Lp: absorb into p
@@ -191,7 +198,7 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
             int32_t* ap = a_pool.data() + nd[i].a_beg;
             int32_t aw = 0;
             k2 = 0;
-            for (int32_t x = 0; x < nd[i].a_len; ++x) {
+            for (int32_t x = 0, na = nd[i].a_len; x < na; ++x) {
                 const int32_t v = ap[x];
                 if (status[v] != VAR || v == p || nd[v].flag == lp_tag) continue;
                 ap[k2++] = v;
