@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <functional>
 
 namespace sle_gb300 {
 
@@ -111,7 +112,8 @@ int32_t Engine::initialize() {
     return 0;
 }
 
-int32_t Engine::analyze() {
+int32_t Engine::analyze(bool* scheduled) {
+    if (scheduled) *scheduled = false;
     if (batch_mode()) return analyze_batch();
     std::string err;
     if (!model.validate(err)) {
@@ -140,10 +142,21 @@ int32_t Engine::analyze() {
     SymbolicParams sp;
     sp.ordering = cfg.ordering;
     const HostTimer timer(&stats.analysis_ms);
-    if (!build_plan(t, sp, plan_, err)) {
+    std::function<void()> alongside;
+    if (scheduled)
+        alongside = [this] {
+            const HostTimer schedule_timer(&stats.schedule_ms);
+            build_schedule(false);
+            build_eval_units();
+        };
+    if (!build_plan(t, sp, plan_, err, alongside)) {
         last_error = "symbolic analysis: " + err;
         analyzed_ = false;
         return -5;
+    }
+    if (scheduled) {
+        fill_asm_targets();
+        *scheduled = true;
     }
     analyzed_ = true;
     ++stats.analyses;
@@ -320,7 +333,21 @@ void Engine::build_eval_units() {
     }
 }
 
-void Engine::build_schedule() {
+// The gain targets of an assembly item: those of its front in its tile
+// column, [tj * kTile, tj * kTile + kTile) (targets are sorted by local index
+// row + col * f).
+void Engine::fill_asm_targets() {
+    const Plan& P = plan_;
+    const int32_t* tl = P.tgt_local.data();
+    for (AsmItem& it : sch_asm_) {
+        const int32_t s = it.s, f = P.sn_f[s];
+        const int32_t c0 = it.tj * kTile, c1 = std::min(c0 + kTile, f);
+        it.tg_lo = static_cast<int32_t>(std::lower_bound(tl + P.sn_tgt_ptr[s], tl + P.sn_tgt_ptr[s + 1], c0 * f) - tl);
+        it.tg_hi = static_cast<int32_t>(std::lower_bound(tl + it.tg_lo, tl + P.sn_tgt_ptr[s + 1], c1 * f) - tl);
+    }
+}
+
+void Engine::build_schedule(bool targets_ready) {
     const Plan& P = plan_;
     const int32_t ns = P.n_super, nl = P.n_levels;
     sch_small_ptr_.assign(nl + 1, 0);
@@ -504,14 +531,10 @@ void Engine::build_schedule() {
             for (int32_t tj = 0; tj < tiles; ++tj) {
                 const int32_t rows = f - tj * kTile;  // the tile column's lower part
                 const int32_t c0 = tj * kTile, c1 = std::min(c0 + kTile, f);
-                const int32_t* tl = P.tgt_local.data();
-                const int32_t tg_lo = static_cast<int32_t>(
-                    std::lower_bound(tl + P.sn_tgt_ptr[s], tl + P.sn_tgt_ptr[s + 1], c0 * f) - tl);
-                const int32_t tg_hi = static_cast<int32_t>(
-                    std::lower_bound(tl + tg_lo, tl + P.sn_tgt_ptr[s + 1], c1 * f) - tl);
                 for (int32_t rb = 0; rb * kAsmRows < rows; ++rb) {
                     const int32_t R0 = c0 + rb * kAsmRows, R1 = std::min(R0 + kAsmRows, f);
-                    AsmItem it{s, tj, rb, tg_lo, tg_hi, static_cast<int32_t>(sch_asm_child_.size()), 0, 0};
+                    // target range [tg_lo, tg_hi) by fill_asm_targets()
+                    AsmItem it{s, tj, rb, 0, 0, static_cast<int32_t>(sch_asm_child_.size()), 0, 0};
                     // the children that add entries to rows [R0, R1) of columns [c0, c1), in order
                     for (int32_t ci = P.sn_child_ptr[s]; ci < P.sn_child_ptr[s + 1]; ++ci) {
                         const int32_t c = P.sn_child[ci];
@@ -596,6 +619,7 @@ void Engine::build_schedule() {
     std::sort(sch_flow_a_.begin(), sch_flow_a_.end(), by_cost);
     std::sort(sch_flow_b_.begin(), sch_flow_b_.end(), by_cost);
     std::sort(sch_up_.begin(), sch_up_.end(), by_cost);
+    if (targets_ready) fill_asm_targets();
 }
 
 int32_t Engine::schedule_info(ScheduleInfo& out) {
@@ -642,13 +666,18 @@ int32_t Engine::upload() {
     if (rc) return rc;
     // keep the hot-start state across re-uploads
     if (uploaded_) download_results();
-    if (!(reuse_analysis_once && analyzed_)) rc = analyze();
+    const bool mixed_before = mixed_;
+    mixed_ = cfg.use_double_precision == 0;  // the schedule may be built during the analysis
+    bool scheduled = false;
+    if (!(reuse_analysis_once && analyzed_)) rc = analyze(&scheduled);
     reuse_analysis_once = false;
-    if (rc) return rc;
+    if (rc) {
+        mixed_ = mixed_before;
+        return rc;
+    }
     const int32_t n = model.n_bus(), nbr = model.n_branch(), m = model.n_meas();
     const Plan& P = plan_;
-    mixed_ = cfg.use_double_precision == 0;
-    {
+    if (!scheduled) {
         const HostTimer timer(&stats.schedule_ms);
         build_schedule();
         build_eval_units();

@@ -134,7 +134,10 @@ public:
     std::string last_error;
 
     int32_t initialize();
-    int32_t analyze();  // host-only symbolic analysis of the current model
+    // Host-only symbolic analysis of the current model.  With `scheduled`
+    // (one grid), the level schedule and evaluation units of the current
+    // options are built alongside, and *scheduled says whether they were.
+    int32_t analyze(bool* scheduled = nullptr);
     // Schedule summary (host-only before the first upload).
     struct ScheduleInfo {
         int32_t n_warp = 0, n_phase_a = 0, n_phase_b = 0, n_sync = 0;
@@ -333,7 +336,10 @@ private:
     int4* d_pot_ = nullptr;
     int4* d_pan_ = nullptr;
     int4* d_upd_ = nullptr;
-    void build_schedule();
+    // targets_ready = false leaves the assembly items' target ranges to
+    // fill_asm_targets(), for a schedule built before the gain targets exist.
+    void build_schedule(bool targets_ready = true);
+    void fill_asm_targets();
     void build_tile_tasks(const std::vector<int32_t>& bigs, const std::unordered_map<int64_t, int32_t>& pair_of);
     bool tile_tasks_bad_ = false;  // a dependency not earlier in claim order (never by construction)
     // CUDA graphs of one Gauss-Newton iteration, [0] without and [1] with

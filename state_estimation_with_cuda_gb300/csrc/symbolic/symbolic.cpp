@@ -397,7 +397,8 @@ void bus_graph(const Topology& t, const std::vector<int32_t>& y_ptr, const std::
     out.gather(n, adj_ptr, adj);
 }
 
-bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::string& err) {
+bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::string& err,
+                const std::function<void()>& alongside) {
     const int32_t n = t.n_bus, nbr = t.n_branch, m = t.n_meas, s = t.slack;
     if (n < 1 || s < 0 || s >= n) { err = "invalid bus count or slack index"; return false; }
     P = Plan();
@@ -925,6 +926,15 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
         std::vector<int32_t> fill(P.lvl_ptr.begin(), P.lvl_ptr.end() - 1);
         for (int32_t k = 0; k < ns; ++k) P.lvl_sn[fill[lvl[k]]++] = k;
     }
+    // the caller's work that needs only the fronts runs from here on, joined
+    // on every way out
+    struct Joiner {
+        std::thread th;
+        ~Joiner() {
+            if (th.joinable()) th.join();
+        }
+    } beside;
+    if (alongside) beside.th = std::thread(alongside);
 
     // --- RHS gather ------------------------------------------------------------------------
     // Each H entry's permuted column, then the entries by permuted state (a

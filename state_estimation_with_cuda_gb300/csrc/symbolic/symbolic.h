@@ -33,6 +33,7 @@
 #pragma once
 
 #include <cstdint>
+#include <functional>
 #include <memory>
 #include <new>
 #include <string>
@@ -136,8 +137,13 @@ struct Plan {
     int64_t lx_size = 0, u_size = 0, su_size = 0;
 };
 
-// Builds the plan; returns false and sets err on invalid input.
-bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& plan, std::string& err);
+// Builds the plan; returns false and sets err on invalid input.  alongside,
+// when given, runs on a thread of its own once the fronts are complete
+// (patterns, ordering, sn_*, children, relative maps, levels) and the
+// analysis finishes after it; it may read those fields, not the RHS gather,
+// h_pcol or the gain targets and pairs, which are built meanwhile.
+bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& plan, std::string& err,
+                const std::function<void()>& alongside = nullptr);
 
 // Block-diagonal union of independent grids' plans (a batch): every index
 // array is shifted by the preceding grids' counts (buses, branches, rows,
