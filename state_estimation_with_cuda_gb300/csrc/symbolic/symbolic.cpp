@@ -18,10 +18,12 @@ namespace {
 inline bool is_bus_type(int32_t t) { return t == 0 || t == 1 || t == 2 || t == 3 || t == 7 || t == 8; }
 inline bool is_inj_type(int32_t t) { return t == 2 || t == 3 || t == 7 || t == 8; }
 
-// Host threads for the analysis: at most the hardware's, and few enough that
-// each gets at least `grain` items.
-int32_t host_threads(int64_t items, int64_t grain) {
-    const int64_t hw = std::max(1u, std::thread::hardware_concurrency());
+// Host threads for the analysis: at most the hardware's less `reserved`
+// (cores left to other work), and few enough that each gets at least `grain`
+// items.  Ranges are split statically, so a pass is as slow as its slowest
+// thread: the threads must not outnumber the free cores.
+int32_t host_threads(int64_t items, int64_t grain, int32_t reserved = 0) {
+    const int64_t hw = std::max<int64_t>(1, static_cast<int64_t>(std::thread::hardware_concurrency()) - reserved);
     return static_cast<int32_t>(std::max<int64_t>(1, std::min<int64_t>(hw, items / std::max<int64_t>(1, grain))));
 }
 
@@ -935,6 +937,7 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
         }
     } beside;
     if (alongside) beside.th = std::thread(alongside);
+    const int32_t busy = alongside ? 1 : 0;  // cores taken from the passes below
 
     // --- RHS gather ------------------------------------------------------------------------
     // Each H entry's permuted column, then the entries by permuted state (a
@@ -944,7 +947,7 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     {
         const int64_t nnz = static_cast<int64_t>(P.h_col.size());
         const int32_t ns_ = P.n_state;
-        const int32_t parts = host_threads(nnz, 1 << 18);
+        const int32_t parts = host_threads(nnz, 1 << 18, busy);
         P.h_pcol.resize(static_cast<size_t>(nnz));
         std::vector<std::vector<int32_t>> cnt(parts);
         parallel_ranges(nnz, parts, [&](int32_t t, int64_t h0, int64_t h1) {
@@ -958,7 +961,7 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
         });
         // per state: the ranges' first slots relative to the state's start
         P.rhs_ptr.assign(static_cast<size_t>(ns_) + 1, 0);
-        parallel_ranges(ns_, host_threads(ns_, 1 << 15), [&](int32_t, int64_t p0, int64_t p1) {
+        parallel_ranges(ns_, host_threads(ns_, 1 << 15, busy), [&](int32_t, int64_t p0, int64_t p1) {
             for (int64_t p = p0; p < p1; ++p) {
                 int32_t run = 0;
                 for (int32_t t = 0; t < parts; ++t) {
@@ -1006,7 +1009,7 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
         BigVec<int32_t> ge(static_cast<size_t>(nnz));
         struct RowRange { int32_t beg, end; };
         BigVec<RowRange> hrow(static_cast<size_t>(nnz));
-        parallel_ranges(m, host_threads(m, 4096), [&](int32_t, int64_t q0, int64_t q1) {
+        parallel_ranges(m, host_threads(m, 4096, busy), [&](int32_t, int64_t q0, int64_t q1) {
             for (int64_t q = q0; q < q1; ++q) {
                 const int32_t h0 = P.h_ptr[q], h1 = P.h_ptr[q + 1];
                 for (int32_t x = h0; x < h1; ++x) {
@@ -1018,7 +1021,7 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
             }
         });
         std::vector<int64_t> fr_off(ns + 1, 0);
-        parallel_ranges(ns, sn_parts, [&](int32_t, int64_t k0, int64_t k1) {
+        parallel_ranges(ns, host_threads(ns, 2048, busy), [&](int32_t, int64_t k0, int64_t k1) {
             for (int64_t k = k0; k < k1; ++k) {
                 int64_t c = 0;
                 for (int32_t i = P.rhs_ptr[P.sn_c0[k]]; i < P.rhs_ptr[P.sn_c0[k + 1]]; ++i) c += ge[P.rhs_h[i]];
@@ -1026,7 +1029,7 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
             }
         });
         for (int32_t k = 0; k < ns; ++k) fr_off[k + 1] += fr_off[k];
-        const int32_t nthr = host_threads(run, 1 << 16);
+        const int32_t nthr = host_threads(run, 1 << 16, busy);
         std::vector<int32_t> fr_cut(nthr + 1, ns);
         fr_cut[0] = 0;
         for (int32_t t = 1, k = 0; t < nthr; ++t) {
