@@ -200,7 +200,8 @@ typedef struct SLE_ExStats {
     int64_t step_waits;     /* Gauss-Newton steps after which the host waited for the device before
                                issuing the next (none in a batch solve whose loop runs on the device) */
     /* host wall time in ms, summed since load or reset: symbolic analyses, schedule builds, device
-     * arena builds with their host-to-device copies, CUDA graph captures with instantiation */
+     * arena builds with their host-to-device copies, CUDA graph captures with instantiation.  A single
+     * grid's schedule is built beside the last passes of its analysis: that time overlaps analysis_ms. */
     double analysis_ms, schedule_ms, upload_ms, capture_ms;
 } SLE_ExStats;
 
