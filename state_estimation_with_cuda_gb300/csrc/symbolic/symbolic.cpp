@@ -992,7 +992,8 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     // panel), and each run of equal indices becomes one target with its pair
     // list; a target gets at most one pair per row, so its pairs are in row
     // order.  Fronts are cut into ranges of about equal pair counts, one host
-    // thread each, so the plan is the same for any thread count.
+    // thread each; every front is written at its own offsets, so the plan
+    // does not depend on the thread count.
     {
         struct PairRec { int32_t local; int32_t a; int32_t b; };
         const int64_t nnz = static_cast<int64_t>(P.h_col.size());
