@@ -43,15 +43,11 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
     struct Node {
         int64_t a_beg, e_beg, l_beg;     // list starts in a_pool, e_pool, l_pool
         int32_t a_len, e_len, e_cap, l_len;
-        int32_t deg, wtag, w, l_w;
-        int32_t pad[2];
+        int32_t nv, deg, flag, wtag;
+        int32_t w, l_w;
     };
     static_assert(sizeof(Node) == 64, "one cache line per node");
-    std::vector<Node> nd(n, Node{0, 0, 0, 0, 0, 0, 0, 0, -1, 0, 0, {0, 0}});
-    // What a scan of a neighbour list reads besides status: the membership
-    // tag and the weight (variables in the supervariable), in 8 bytes a node.
-    struct Var { int32_t flag, nv; };
-    std::vector<Var> vi(n, Var{-1, 1});
+    std::vector<Node> nd(n, Node{0, 0, 0, 0, 0, 0, 0, 1, 0, -1, -1, 0, 0});
     // A: [a_beg, a_beg + a_len) of a_pool (self loops dropped)
     std::vector<int32_t> a_pool;
     a_pool.reserve(adj.size());
@@ -123,7 +119,7 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         ++tag;
         // --- new element Lp -------------------------------------------------------
         Lp.clear();
-        vi[p].flag = tag;
+        nd[p].flag = tag;
         // (list lengths and starts are read once: the loops store only into
         // other nodes)
         const int32_t* ep = e_pool.data() + nd[p].e_beg;
@@ -133,8 +129,8 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
             const int32_t* le = l_pool.data() + nd[e].l_beg;
             for (int32_t y = 0, nl = nd[e].l_len; y < nl; ++y) {
                 const int32_t i = le[y];
-                if (status[i] == VAR && vi[i].flag != tag) {
-                    vi[i].flag = tag;
+                if (status[i] == VAR && nd[i].flag != tag) {
+                    nd[i].flag = tag;
                     Lp.push_back(i);
                 }
             }
@@ -144,8 +140,8 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         const int32_t* pa = a_pool.data() + nd[p].a_beg;
         for (int32_t x = 0, na = nd[p].a_len; x < na; ++x) {
             const int32_t i = pa[x];
-            if (status[i] == VAR && vi[i].flag != tag) {
-                vi[i].flag = tag;
+            if (status[i] == VAR && nd[i].flag != tag) {
+                nd[i].flag = tag;
                 Lp.push_back(i);
             }
         }
@@ -153,11 +149,11 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         nd[p].e_len = 0;
         status[p] = ELEM;
         for (int32_t mb = mc[p].head; mb >= 0; mb = mc[mb].next) order.push_back(mb);
-        eliminated += vi[p].nv;
+        eliminated += nd[p].nv;
         int32_t lp_w = 0;
         for (int32_t i : Lp) {
             bucket_remove(i);
-            lp_w += vi[i].nv;
+            lp_w += nd[i].nv;
             __builtin_prefetch(&e_pool[nd[i].e_beg]);
             __builtin_prefetch(&a_pool[nd[i].a_beg]);
         }
@@ -174,11 +170,11 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
                     nd[e].w = nd[e].l_w;
                     nd[e].wtag = wt;
                 }
-                nd[e].w -= vi[i].nv;
+                nd[e].w -= ni.nv;
             }
             // the next pass reads the nodes of i's remaining neighbours
             const int32_t* ap = a_pool.data() + ni.a_beg;
-            for (int32_t x = 0; x < ni.a_len; ++x) __builtin_prefetch(&vi[ap[x]]);
+            for (int32_t x = 0; x < ni.a_len; ++x) __builtin_prefetch(&nd[ap[x]]);
         }
         // --- update variables in Lp ---------------------------------------------------
         // flag == tag - 1 marks membership in Lp.
@@ -204,15 +200,15 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
             k2 = 0;
             for (int32_t x = 0, na = nd[i].a_len; x < na; ++x) {
                 const int32_t v = ap[x];
-                if (status[v] != VAR || v == p || vi[v].flag == lp_tag) continue;
+                if (status[v] != VAR || v == p || nd[v].flag == lp_tag) continue;
                 ap[k2++] = v;
-                aw += vi[v].nv;
+                aw += nd[v].nv;
             }
             nd[i].a_len = k2;
             const int32_t remaining = n - eliminated;
-            const int32_t d1 = nd[i].deg + lp_w - vi[i].nv;
-            const int32_t d2 = aw + (lp_w - vi[i].nv) + ext;
-            nd[i].deg = std::max(0, std::min(std::min(d1, d2), remaining - vi[i].nv));
+            const int32_t d1 = nd[i].deg + lp_w - nd[i].nv;
+            const int32_t d2 = aw + (lp_w - nd[i].nv) + ext;
+            nd[i].deg = std::max(0, std::min(std::min(d1, d2), remaining - nd[i].nv));
         }
         // --- supervariable detection among Lp ------------------------------------------
         hashes.clear();
@@ -251,9 +247,9 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
                     for (int32_t v : aj) if (v != i) aj2.push_back(v);
                     if (ai2 != aj2) continue;
                     // merge j into i
-                    vi[i].nv += vi[j].nv;
-                    nd[i].deg = std::max(0, nd[i].deg - vi[j].nv);
-                    vi[j].nv = 0;
+                    nd[i].nv += nd[j].nv;
+                    nd[i].deg = std::max(0, nd[i].deg - nd[j].nv);
+                    nd[j].nv = 0;
                     status[j] = DEAD;
                     mc[mc[i].tail].next = mc[j].head;
                     mc[i].tail = mc[j].tail;
@@ -271,7 +267,7 @@ std::vector<int32_t> amd_order(int32_t n, const std::vector<int32_t>& ptr, const
         for (int32_t i : Lp) {
             if (status[i] != VAR) continue;
             l_pool.push_back(i);
-            nd[p].l_w += vi[i].nv;
+            nd[p].l_w += nd[i].nv;
             bucket_insert(i);
             mindeg = std::min(mindeg, std::min(nd[i].deg, n));
         }
