@@ -23,7 +23,11 @@
 //                    quotient graph and expanded to states (theta, then V).
 //  Ordering          approximate minimum degree on the bus graph (default) or
 //                    nested dissection with BFS level-set separators, then an
-//                    elimination-tree postorder.
+//                    elimination-tree postorder.  With minimum degree the
+//                    elimination tree and the column structures come from the
+//                    ordering's own elimination record (each pivot's element
+//                    is its column structure); otherwise from Liu's algorithm
+//                    and a merge up the tree.
 //  Supernodes        fundamental supernodes of the bus-level etree, then
 //                    relaxed amalgamation of each supernode into its parent
 //                    when it immediately precedes it (bounded explicit zeros).

@@ -153,6 +153,22 @@ def test_bulk_load_default_names_and_edits():
     e.close()
 
 
+def test_host_analysis_time_in_stats():
+    """A host-only analysis (no device) counts itself and its host time in
+    SLE_ExStats; nothing is uploaded or captured."""
+    from state_estimation_with_cuda_gb300 import workloads
+
+    g = workloads.make("grid14")
+    e = Estimator()
+    e.load_network(g)
+    e.reset_stats()
+    e.plan_info()
+    s = e.stats()
+    assert s.analyses == 1 and s.analysis_ms > 0
+    assert s.uploads == 0 and s.upload_ms == 0 and s.capture_ms == 0
+    e.close()
+
+
 def test_removal_compacts_indices():
     e = Estimator()
     e.load_ieee14()
