@@ -23,16 +23,17 @@ def cases():
         "grid2k": SyntheticGrid(2000, 2800, 0x5E01),
         "open_branches": _with_open(SyntheticGrid(300, 420, 9)),
         "grid20k_open": _with_open(SyntheticGrid(20000, 28000, 0x5E77)),
+        "islands": _with_open(SyntheticGrid(400, 560, 21), step=3),
     }
 
 
-def _with_open(g):
+def _with_open(g, step=17):
     g.br_status = g.br_status.copy()
-    g.br_status[::17] = 0
+    g.br_status[::step] = 0
     return g
 
 
-@pytest.fixture(scope="module", params=["ieee14", "grid14", "grid2k", "open_branches", "grid20k_open"])
+@pytest.fixture(scope="module", params=["ieee14", "grid14", "grid2k", "open_branches", "grid20k_open", "islands"])
 def case(request):
     g = cases()[request.param]
     return g, load(g), Oracle(g)
