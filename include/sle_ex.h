@@ -41,7 +41,10 @@ SLE_API SLE_StatusCode SLE_CALL sle_ExLoadNetwork(SLE_Handle handle, int32_t n_b
  *                              (the reference's fixed-gain policy,
  *                              wls_solver.cu:416-419)
  *   "ordering"              0 approximate minimum degree, 1 natural,
- *                           2 nested dissection (takes effect at upload)
+ *                           2 nested dissection (takes effect at upload);
+ *                           1 and 2 are for tests and comparisons: on a
+ *                           20,000-bus synthetic grid their factors hold
+ *                           530x and 33x the entries of the default's
  *   "use_double_precision"  as SLE_Config.use_double_precision (re-uploads)
  *   "refine_steps"          mixed precision: refinement steps per Gauss-Newton
  *                           step, each b - H^T W H dx in FP64 and an FP32 solve
