@@ -18,6 +18,10 @@ namespace {
 inline bool is_bus_type(int32_t t) { return t == 0 || t == 1 || t == 2 || t == 3 || t == 7 || t == 8; }
 inline bool is_inj_type(int32_t t) { return t == 2 || t == 3 || t == 7 || t == 8; }
 
+// Buses + measurement rows from which a side task of the analysis (the H
+// pattern, the caller's work beside the last passes) gets a thread of its own.
+constexpr int64_t kOwnThreadItems = 1 << 15;
+
 // Host threads for the analysis: at most the hardware's less `reserved`
 // (cores left to other work), and few enough that each gets at least `grain`
 // items.  Ranges are split statically, so a pass is as slow as its slowest
@@ -472,8 +476,9 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
 
     // --- H pattern ------------------------------------------------------------------
     // Built on a thread of its own while the bus graph is ordered (the ordering
-    // does not read it); joined before anything else returns or reads it.
-    std::thread h_pattern([&] {
+    // does not read it), joined before anything else returns or reads it; a
+    // small grid builds it in place (a thread costs more than it hides).
+    auto h_pattern_build = [&] {
         // Injection-row column lists per bus (computed once per bus, in
         // parallel ranges): the angle and magnitude columns of the bus's Ybus
         // row, sorted and unique, with each Ybus entry's positions in it.
@@ -570,7 +575,10 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
                 for (int32_t h = P.h_ptr[q]; h < P.h_ptr[q + 1]; ++h) P.h_row[h] = static_cast<int32_t>(q);
             }
         });
-    });
+    };
+    std::thread h_pattern;
+    if (static_cast<int64_t>(n) + m >= kOwnThreadItems) h_pattern = std::thread(h_pattern_build);
+    else h_pattern_build();
 
     // --- ordering on the bus graph -----------------------------------------------------
     std::vector<int32_t> order;
@@ -585,7 +593,7 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
     } else {
         order = amd_order(n, gptr, gadj, &trace);
     }
-    h_pattern.join();
+    if (h_pattern.joinable()) h_pattern.join();
     if (static_cast<int32_t>(order.size()) != n) { err = "ordering failed"; return false; }
     std::vector<int32_t> pos(n, -1);
     for (int32_t k = 0; k < n; ++k) pos[order[k]] = k;
@@ -936,8 +944,9 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
             if (th.joinable()) th.join();
         }
     } beside;
-    if (alongside) beside.th = std::thread(alongside);
-    const int32_t busy = alongside ? 1 : 0;  // cores taken from the passes below
+    if (alongside && static_cast<int64_t>(n) + m >= kOwnThreadItems) beside.th = std::thread(alongside);
+    else if (alongside) alongside();
+    const int32_t busy = beside.th.joinable() ? 1 : 0;  // cores taken from the passes below
 
     // --- RHS gather ------------------------------------------------------------------------
     // Each H entry's permuted column, then the entries by permuted state (a

@@ -142,10 +142,11 @@ struct Plan {
 };
 
 // Builds the plan; returns false and sets err on invalid input.  alongside,
-// when given, runs on a thread of its own once the fronts are complete
-// (patterns, ordering, sn_*, children, relative maps, levels) and the
-// analysis finishes after it; it may read those fields, not the RHS gather,
-// h_pcol or the gain targets and pairs, which are built meanwhile.
+// when given, runs once the fronts are complete (patterns, ordering, sn_*,
+// children, relative maps, levels), on a thread of its own for all but small
+// grids, and the analysis finishes after it; it may read those fields, not
+// the RHS gather, h_pcol or the gain targets and pairs, which are built
+// meanwhile.
 bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& plan, std::string& err,
                 const std::function<void()>& alongside = nullptr);
 
