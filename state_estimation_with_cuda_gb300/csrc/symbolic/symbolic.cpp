@@ -660,18 +660,24 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
                 }
             }
         }
-        std::vector<int32_t> order2(n);
-        for (int32_t k = 0; k < n; ++k) order2[k] = order[post[k]];
+        // renumbering (positions in parallel ranges); a postorder is an
+        // equivalent ordering: its elimination tree is the same tree, renumbered
+        const int32_t parts = host_threads(n, 1 << 15);
+        std::vector<int32_t> order2(n), parent2(n);
+        parallel_ranges(n, parts, [&](int32_t, int64_t k0, int64_t k1) {
+            for (int64_t k = k0; k < k1; ++k) {
+                order2[k] = order[post[k]];
+                pos[order2[k]] = static_cast<int32_t>(k);
+                new_of[post[k]] = static_cast<int32_t>(k);
+            }
+        });
+        parallel_ranges(n, parts, [&](int32_t, int64_t k0, int64_t k1) {
+            for (int64_t k = k0; k < k1; ++k) {
+                const int32_t pa = parent[post[k]];
+                parent2[k] = pa < 0 ? -1 : new_of[pa];
+            }
+        });
         order.swap(order2);
-        for (int32_t k = 0; k < n; ++k) pos[order[k]] = k;
-        // a postorder is an equivalent ordering: its elimination tree is the
-        // same tree, renumbered
-        std::vector<int32_t> parent2(n, -1);
-        for (int32_t k = 0; k < n; ++k) new_of[post[k]] = k;
-        for (int32_t k = 0; k < n; ++k) {
-            const int32_t pa = parent[post[k]];
-            parent2[k] = pa < 0 ? -1 : new_of[pa];
-        }
         parent.swap(parent2);
     }
 
@@ -793,25 +799,35 @@ bool build_plan(const Topology& t, const SymbolicParams& prm, Plan& P, std::stri
         for (int32_t j = sn_b0[k]; j < sn_b1[k]; ++j) sn_of_pos[j] = k;
 
     // --- expansion to states --------------------------------------------------------------
-    std::vector<int32_t> ps0(n + 1, 0);
-    for (int32_t k = 0; k < n; ++k) ps0[k + 1] = ps0[k] + (order[k] == s ? 1 : 2);
+    // ps0[k] = first permuted state of bus position k: two states a bus, one
+    // for the slack (theta, then V); buses in parallel ranges
+    std::vector<int32_t> ps0(n + 1);
+    const int32_t pos_s = pos[s];
+    const int32_t bus_parts = host_threads(n, 1 << 15);
     P.bus_perm = order;
     P.bus_ps_theta.assign(n, -1);
     P.bus_ps_v.assign(n, -1);
     P.state_of_ps.assign(P.n_state, -1);
-    for (int32_t k = 0; k < n; ++k) {
-        const int32_t b = order[k];
-        if (b == s) {
-            P.bus_ps_v[b] = ps0[k];
-        } else {
-            P.bus_ps_theta[b] = ps0[k];
-            P.bus_ps_v[b] = ps0[k] + 1;
-            P.state_of_ps[ps0[k]] = col_t(b);
+    parallel_ranges(n + 1, bus_parts, [&](int32_t, int64_t k0, int64_t k1) {
+        for (int64_t k = k0; k < k1; ++k) ps0[k] = static_cast<int32_t>(2 * k - (k > pos_s ? 1 : 0));
+    });
+    parallel_ranges(n, bus_parts, [&](int32_t, int64_t k0, int64_t k1) {
+        for (int64_t k = k0; k < k1; ++k) {
+            const int32_t b = order[k];
+            if (b == s) {
+                P.bus_ps_v[b] = ps0[k];
+            } else {
+                P.bus_ps_theta[b] = ps0[k];
+                P.bus_ps_v[b] = ps0[k] + 1;
+                P.state_of_ps[ps0[k]] = col_t(b);
+            }
+            P.state_of_ps[P.bus_ps_v[b]] = col_v(b);
         }
-        P.state_of_ps[P.bus_ps_v[b]] = col_v(b);
-    }
+    });
     std::vector<int32_t> ps_of_state(P.n_state);
-    for (int32_t p = 0; p < P.n_state; ++p) ps_of_state[P.state_of_ps[p]] = p;
+    parallel_ranges(P.n_state, bus_parts, [&](int32_t, int64_t p0, int64_t p1) {
+        for (int64_t p = p0; p < p1; ++p) ps_of_state[P.state_of_ps[p]] = static_cast<int32_t>(p);
+    });
 
     P.n_super = ns;
     P.sn_c0.assign(ns + 1, 0);
